@@ -1,0 +1,191 @@
+/*
+ * ndtensors_gb300.h -- C ABI of libndtensors_gb300.so, the GB300 (sm_103a)
+ * implementation of the NDTensors contraction hot path.
+ *
+ * Conventions (identical to NDTensors):
+ *   - tensors are column-major (first index fastest);
+ *   - block numbers are 1-based (Julia `Block{N}`), block offsets are 0-based
+ *     element offsets into one flat data vector (`BlockOffsets`);
+ *   - labels follow ncon: a label shared by both inputs is contracted
+ *     (NDTensors uses negative labels for those), output labels list the
+ *     uncontracted labels in output order;
+ *   - permutations are 1-based (Julia `permutedims(T, perm)`);
+ *   - every function returns an nd_status; nd_last_error() gives the message.
+ *     No entry point aborts, exits or traps the GPU.
+ *
+ * All data pointers are DEVICE pointers unless a parameter says "host".
+ * Work is enqueued on the handle's stream; functions that return structure
+ * to the host (plans, SVD kept dimensions) synchronise that stream.
+ */
+#ifndef NDTENSORS_GB300_H
+#define NDTENSORS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t nd_status;
+enum {
+  ND_OK = 0,
+  ND_ERR_ARG = 1,          /* invalid argument (labels, dims, perm, sizes)      */
+  ND_ERR_OOM = 2,          /* device allocation failed                          */
+  ND_ERR_NOCONV = 3,       /* an SVD did not converge within the sweep limit    */
+  ND_ERR_TIMEOUT = 4,      /* a device-side wait ran past its iteration limit   */
+  ND_ERR_CUDA = 5,         /* a CUDA runtime/driver call failed                 */
+  ND_ERR_UNSUPPORTED = 6,  /* shape/feature outside what this build supports    */
+  ND_ERR_NONFINITE = 7     /* split-precision GEMM met Inf/NaN input            */
+};
+
+/* GEMM arithmetic for contractions. */
+enum {
+  ND_PREC_FP64 = 0,    /* FP64 tensor-core (DMMA) GEMM: the plain drop-in          */
+  ND_PREC_OZAKI = 1,   /* exact int8-range slices on tcgen05 BF16, FP64 result     */
+  ND_PREC_BF16X3 = 2   /* 3xBF16 split, FP32 accumulate, FP64 result               */
+};
+
+#define ND_MAX_RANK 8
+
+typedef struct nd_context *nd_handle;
+typedef struct nd_bs_plan_s *nd_plan;
+
+/* ---- context, memory, streams ------------------------------------------ */
+/* Replaces the storage/stream management CUDA.jl gives NDTensorsCUDAExt
+ * (NDTensors/ext/NDTensorsCUDAExt/NDTensorsCUDAExt.jl). */
+nd_status nd_create(int32_t device, nd_handle *out);
+nd_status nd_destroy(nd_handle h);
+const char *nd_last_error(nd_handle h);
+nd_status nd_set_stream(nd_handle h, void *cuda_stream);      /* NULL = library-owned stream */
+nd_status nd_get_stream(nd_handle h, void **cuda_stream);
+nd_status nd_sync(nd_handle h);
+nd_status nd_alloc(nd_handle h, size_t bytes, void **dptr);
+nd_status nd_free(nd_handle h, void *dptr);
+nd_status nd_h2d(nd_handle h, void *dst, const void *host_src, size_t bytes);
+nd_status nd_d2h(nd_handle h, void *host_dst, const void *src, size_t bytes);
+nd_status nd_memset0(nd_handle h, void *dst, size_t bytes);
+/* Number of slice digits used by ND_PREC_OZAKI (3..6, default 5). */
+nd_status nd_set_ozaki_slices(nd_handle h, int32_t slices);
+/* Count of kernel launches this handle enqueued so far (diagnostics). */
+nd_status nd_launch_count(nd_handle h, int64_t *count);
+
+/* ---- dense permutation --------------------------------------------------
+ * R = beta*R + alpha*permutedims(T, perm), with the reference's rules: beta == 0
+ * overwrites R (NaN in R does not propagate), alpha == 0 keeps only beta*R.
+ * Replaces permutedims!(::Exposed{<:Array}, ...) (NDTensors/src/array/permutedims.jl:5-24)
+ * and the fused _contract_scalar_perm! (NDTensors/src/abstractarray/tensoralgebra/contract.jl:88-113);
+ * GPU counterpart NDTensors/ext/NDTensorsCUDAExt/permutedims.jl:4-23. */
+nd_status nd_permutedims_f64(nd_handle h, double *R, const double *T, int32_t rank,
+                             const int64_t *dimsT /* host */, const int32_t *perm /* host, 1-based */,
+                             double alpha, double beta);
+
+/* ---- dense contraction --------------------------------------------------
+ * R = alpha * contract(A, B) + beta * R.  Replaces
+ * contract!(R::DenseTensor, labelsR, T1, labelsT1, T2, labelsT2, alpha, beta)
+ * (NDTensors/src/dense/tensoralgebra/contract.jl:160-216), i.e. the cuTENSOR hook
+ * NDTensors/ext/NDTensorscuTENSORExt/contract.jl:15-58 and the cuBLAS mul! of
+ * NDTensors/ext/NDTensorsCUDAExt/mul.jl:7-47.  A one-element operand takes the
+ * reference's scalar branch (contract.jl:100-150).  rel_err_estimate (nullable,
+ * host) receives the a-priori error bound of the chosen precision. */
+nd_status nd_contract_dense_f64(nd_handle h,
+                                double *R, int32_t rankR, const int64_t *dimsR, const int32_t *labelsR,
+                                const double *A, int32_t rankA, const int64_t *dimsA, const int32_t *labelsA,
+                                const double *B, int32_t rankB, const int64_t *dimsB, const int32_t *labelsB,
+                                double alpha, double beta, int32_t precision);
+
+/* ---- block-sparse structure ---------------------------------------------
+ * A block-sparse operand: per-dimension block dims plus the ordered list of
+ * nonzero blocks and their offsets (NDTensors BlockSparse + BlockOffsets,
+ * NDTensors/src/blocksparse/blocksparse.jl:5-13, blockoffsets.jl:11). Host arrays. */
+typedef struct {
+  int32_t rank;
+  const int32_t *nblocks;    /* [rank] number of blocks of each dimension                */
+  const int64_t *blockdims;  /* concatenation over dimensions of the per-block dims      */
+  int32_t nnzblocks;
+  const int32_t *blocks;     /* [nnzblocks][rank] 1-based block numbers, row per block   */
+  const int64_t *offsets;    /* [nnzblocks] 0-based element offsets                      */
+} nd_bs_desc;
+
+/* Build the contraction plan ON THE DEVICE: the list of contracted block pairs
+ * in the reference's sequential order (A-block major, B-block minor), the
+ * output block list in first-appearance order and its offsets.  Bit-exact with
+ * contract_blockoffsets(::Algorithm"sequential", ...)
+ * (NDTensors/src/blocksparse/contract_sequential.jl:1-41,
+ *  contract_utilities.jl:45-91, contract.jl:20-55). */
+nd_status nd_bs_plan_create(nd_handle h, const nd_bs_desc *A, const int32_t *labelsA,
+                            const nd_bs_desc *B, const int32_t *labelsB,
+                            int32_t rankR, const int32_t *labelsR, nd_plan *plan);
+/* Sizes of the plan's outputs. */
+nd_status nd_bs_plan_sizes(nd_plan plan, int32_t *npairs, int32_t *nnzblocksR, int64_t *nnzR);
+/* Copy the plan to host arrays: blocksR [nnzblocksR][rankR] (1-based), offsetsR,
+ * pairs [npairs][3] = (A block index, B block index, R block index), 0-based
+ * positions in the respective block lists.  Any pointer may be NULL. */
+nd_status nd_bs_plan_get(nd_plan plan, int32_t *blocksR, int64_t *offsetsR, int32_t *pairs);
+nd_status nd_bs_plan_destroy(nd_plan plan);
+
+/* R = alpha * contract(A, B) executed as ONE grouped-GEMM launch over all
+ * block pairs: pairs are grouped by output block, the first pair of a group
+ * overwrites and the rest accumulate (NDTensors/src/blocksparse/contract_generic.jl:37-129,
+ * with compute_alpha == 1, contract_utilities.jl:2-15). */
+nd_status nd_bs_contract_f64(nd_handle h, nd_plan plan, double *R, const double *A,
+                             const double *B, double alpha, int32_t precision);
+
+/* Pullback of R = contract(A, B) for the same plan (ext/ITensorsChainRulesCoreExt/itensor.jl:94-103):
+ * Abar = Rbar * B (contract over B's free labels), Bbar = A * Rbar.  Both
+ * contractions run in one grouped-GEMM launch.  Abar/Bbar have A's/B's structure. */
+nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan plan, const double *Rbar,
+                                     const double *A, const double *B,
+                                     double *Abar, double *Bbar, int32_t precision);
+
+/* Block-sparse permutedims: every block permuted; output block order = input
+ * order, offsets recomputed by the caller's layout (offsetsR, host).
+ * (NDTensors/src/blocksparse/blocksparsetensor.jl:834-881, blockoffsets.jl:103-111) */
+nd_status nd_bs_permutedims_f64(nd_handle h, const nd_bs_desc *T, const double *Tdata,
+                                const int32_t *perm, const int64_t *offsetsR, double *Rdata);
+
+/* ---- block matrix factorizations ----------------------------------------
+ * Blockwise SVD of a 2-index block matrix with truncation
+ * (NDTensors/src/blocksparse/linearalgebra.jl:45-215, truncate.jl:23-107).
+ * Blocks are dense column-major m_b x n_b at offsets[b] in A.  Outputs, for
+ * the kept blocks in input order (dropped blocks removed):
+ *   U: concatenation of m_b x k_b column-major blocks,
+ *   S: concatenation of k_b values (descending within a block),
+ *   V: concatenation of n_b x k_b column-major blocks,
+ * where k_b = kept[b] (0 = dropped).  Caller sizes U/S/V for the untruncated
+ * case (sum m_b*min, sum min, sum n_b*min).  spectrum (host, length >= sum min)
+ * receives the truncated sorted s^2; *spectrum_len its length.  Pass maxdim or
+ * cutoff < 0 to mean "nothing" (no truncation).  ND_ERR_NOCONV if a block
+ * did not converge (the reference returns `nothing`). */
+nd_status nd_bs_svd_f64(nd_handle h, int32_t nblocks, const int64_t *rows, const int64_t *cols,
+                        const int64_t *offsets, const double *A,
+                        double *U, double *S, double *V,
+                        int32_t mindim, int32_t maxdim, double cutoff,
+                        int32_t use_absolute_cutoff, int32_t use_relative_cutoff, int32_t min_blockdim,
+                        int32_t *kept, double *spectrum, int32_t *spectrum_len,
+                        double *truncerr, double *docut);
+
+/* Blockwise QR (NDTensors/src/blocksparse/linearalgebra.jl:351-415, dense qr /
+ * qr_positive NDTensors/src/linearalgebra/linearalgebra.jl:321-381).  Q blocks
+ * m_b x k_b, R blocks k_b x n_b, k_b = min(m_b, n_b), concatenated in order. */
+nd_status nd_bs_qr_f64(nd_handle h, int32_t nblocks, const int64_t *rows, const int64_t *cols,
+                       const int64_t *offsets, const double *A, double *Q, double *Rf,
+                       int32_t positive);
+
+/* truncate! on a device vector of descending weights (NDTensors/src/truncate.jl:23-107);
+ * results to host.  *newlen = kept length. */
+nd_status nd_truncate_f64(nd_handle h, const double *P, int32_t n, int32_t mindim, int32_t maxdim,
+                          double cutoff, int32_t use_absolute_cutoff, int32_t use_relative_cutoff,
+                          int32_t *newlen, double *truncerr, double *docut);
+
+/* ---- CUDA graphs ---------------------------------------------------------
+ * Capture the handle's stream into a graph (a sweep step) and replay it. */
+nd_status nd_graph_begin(nd_handle h);
+nd_status nd_graph_end(nd_handle h, void **graph_exec);
+nd_status nd_graph_launch(nd_handle h, void *graph_exec);
+nd_status nd_graph_destroy(void *graph_exec);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NDTENSORS_GB300_H */

@@ -1,0 +1,259 @@
+// Context, memory, error plumbing, label roles and CUDA-graph entry points.
+#include "nd_common.h"
+#include <cstdarg>
+#include <cstring>
+#include <algorithm>
+
+static thread_local std::string g_noctx_error;
+
+nd_status nd_fail(nd_handle h, nd_status code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->last_error = buf; else g_noctx_error = buf;
+  return code;
+}
+
+nd_status nd_cuda_check(nd_handle h, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return ND_OK;
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return nd_fail(h, ND_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+  }
+  return nd_fail(h, ND_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+nd_status nd_workspace(nd_handle h, size_t bytes, void** out) {
+  if (bytes == 0) bytes = 256;
+  if (bytes > h->ws_size) {
+    if (h->capturing)
+      return nd_fail(h, ND_ERR_ARG, "workspace must grow during graph capture: run the call once before capture");
+    if (h->ws) {
+      ND_CUDA(h, cudaStreamSynchronize(h->stream));
+      ND_CUDA(h, cudaFree(h->ws));
+      h->ws = nullptr;
+      h->ws_size = 0;
+    }
+    size_t sz = std::max(bytes, h->ws_size * 3 / 2);
+    ND_CUDA(h, cudaMalloc(&h->ws, sz));
+    h->ws_size = sz;
+  }
+  *out = h->ws;
+  return ND_OK;
+}
+
+nd_status nd_check_device_status(nd_handle h, const char* what) {
+  if (h->capturing) return ND_OK;   // read after replay via nd_sync
+  DeviceStatus st{};
+  ND_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  ND_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (st.code != ND_OK) {
+    DeviceStatus z{};
+    cudaMemcpy(h->d_status, &z, sizeof(z), cudaMemcpyHostToDevice);
+    if (st.code == ND_ERR_TIMEOUT)
+      return nd_fail(h, ND_ERR_TIMEOUT, "%s: device wait exceeded its iteration limit (site %d)", what, st.where);
+    if (st.code == ND_ERR_NONFINITE)
+      return nd_fail(h, ND_ERR_NONFINITE, "%s: Inf/NaN input cannot be split exactly; use ND_PREC_FP64", what);
+    if (st.code == ND_ERR_NOCONV)
+      return nd_fail(h, ND_ERR_NOCONV, "%s: SVD did not converge (block %d)", what, st.where);
+    return nd_fail(h, st.code, "%s: device reported error %d at site %d", what, st.code, st.where);
+  }
+  return ND_OK;
+}
+
+extern "C" {
+
+nd_status nd_create(int32_t device, nd_handle* out) {
+  if (!out) return nd_fail(nullptr, ND_ERR_ARG, "nd_create: out is NULL");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return nd_fail(nullptr, ND_ERR_CUDA, "nd_create: no CUDA device (%s)", cudaGetErrorString(e));
+  if (device < 0 || device >= n) return nd_fail(nullptr, ND_ERR_ARG, "nd_create: bad device %d", device);
+  nd_handle h = new nd_context();
+  h->device = device;
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) { delete h; return nd_fail(nullptr, ND_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e)); }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, device);
+  if (prop.major * 10 + prop.minor < 100) {
+    delete h;
+    return nd_fail(nullptr, ND_ERR_UNSUPPORTED, "nd_create: device sm_%d%d is not a Blackwell (sm_10x) GPU", prop.major, prop.minor);
+  }
+  h->num_sms = prop.multiProcessorCount;
+  e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete h; return nd_fail(nullptr, ND_ERR_CUDA, "stream: %s", cudaGetErrorString(e)); }
+  h->own_stream = true;
+  e = cudaMalloc(&h->d_status, sizeof(DeviceStatus));
+  if (e != cudaSuccess) { cudaStreamDestroy(h->stream); delete h; return nd_fail(nullptr, ND_ERR_OOM, "status word"); }
+  cudaMemset(h->d_status, 0, sizeof(DeviceStatus));
+  cudaDeviceSynchronize();
+  *out = h;
+  return ND_OK;
+}
+
+nd_status nd_destroy(nd_handle h) {
+  if (!h) return ND_OK;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  if (h->ws) cudaFree(h->ws);
+  if (h->d_status) cudaFree(h->d_status);
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return ND_OK;
+}
+
+const char* nd_last_error(nd_handle h) { return h ? h->last_error.c_str() : g_noctx_error.c_str(); }
+
+nd_status nd_set_stream(nd_handle h, void* s) {
+  if (!h) return ND_ERR_ARG;
+  if (h->own_stream && s) { cudaStreamSynchronize(h->stream); cudaStreamDestroy(h->stream); h->own_stream = false; }
+  if (s) h->stream = (cudaStream_t)s;
+  else if (!h->own_stream) {
+    ND_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->own_stream = true;
+  }
+  return ND_OK;
+}
+
+nd_status nd_get_stream(nd_handle h, void** s) {
+  if (!h || !s) return ND_ERR_ARG;
+  *s = (void*)h->stream;
+  return ND_OK;
+}
+
+nd_status nd_sync(nd_handle h) {
+  if (!h) return ND_ERR_ARG;
+  ND_CUDA(h, cudaStreamSynchronize(h->stream));
+  return nd_check_device_status(h, "nd_sync");
+}
+
+nd_status nd_alloc(nd_handle h, size_t bytes, void** dptr) {
+  if (!h || !dptr) return nd_fail(h, ND_ERR_ARG, "nd_alloc: NULL argument");
+  *dptr = nullptr;
+  if (bytes == 0) bytes = 16;
+  ND_CUDA(h, cudaMalloc(dptr, bytes));
+  return ND_OK;
+}
+
+nd_status nd_free(nd_handle h, void* p) {
+  if (!h) return ND_ERR_ARG;
+  if (p) ND_CUDA(h, cudaFree(p));
+  return ND_OK;
+}
+
+nd_status nd_h2d(nd_handle h, void* dst, const void* src, size_t bytes) {
+  if (!h || (bytes && (!dst || !src))) return nd_fail(h, ND_ERR_ARG, "nd_h2d: NULL argument");
+  if (bytes) ND_CUDA(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+  return ND_OK;
+}
+
+nd_status nd_d2h(nd_handle h, void* dst, const void* src, size_t bytes) {
+  if (!h || (bytes && (!dst || !src))) return nd_fail(h, ND_ERR_ARG, "nd_d2h: NULL argument");
+  if (bytes) {
+    ND_CUDA(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+    ND_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  return ND_OK;
+}
+
+nd_status nd_memset0(nd_handle h, void* dst, size_t bytes) {
+  if (!h || (bytes && !dst)) return nd_fail(h, ND_ERR_ARG, "nd_memset0: NULL argument");
+  if (bytes) ND_CUDA(h, cudaMemsetAsync(dst, 0, bytes, h->stream));
+  return ND_OK;
+}
+
+nd_status nd_set_ozaki_slices(nd_handle h, int32_t s) {
+  if (!h) return ND_ERR_ARG;
+  if (s < 3 || s > 6) return nd_fail(h, ND_ERR_ARG, "ozaki slices must be in 3..6 (got %d)", s);
+  h->ozaki_slices = s;
+  return ND_OK;
+}
+
+nd_status nd_launch_count(nd_handle h, int64_t* c) {
+  if (!h || !c) return ND_ERR_ARG;
+  *c = h->launches;
+  return ND_OK;
+}
+
+nd_status nd_graph_begin(nd_handle h) {
+  if (!h) return ND_ERR_ARG;
+  if (h->capturing) return nd_fail(h, ND_ERR_ARG, "nd_graph_begin: already capturing");
+  ND_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  h->capturing = true;
+  return ND_OK;
+}
+
+nd_status nd_graph_end(nd_handle h, void** exec) {
+  if (!h || !exec) return ND_ERR_ARG;
+  if (!h->capturing) return nd_fail(h, ND_ERR_ARG, "nd_graph_end: not capturing");
+  cudaGraph_t g = nullptr;
+  h->capturing = false;
+  ND_CUDA(h, cudaStreamEndCapture(h->stream, &g));
+  cudaGraphExec_t ge = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return nd_cuda_check(h, e, "cudaGraphInstantiate");
+  *exec = (void*)ge;
+  return ND_OK;
+}
+
+nd_status nd_graph_launch(nd_handle h, void* exec) {
+  if (!h || !exec) return ND_ERR_ARG;
+  ND_CUDA(h, cudaGraphLaunch((cudaGraphExec_t)exec, h->stream));
+  return ND_OK;
+}
+
+nd_status nd_graph_destroy(void* exec) {
+  if (exec) cudaGraphExecDestroy((cudaGraphExec_t)exec);
+  return ND_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Label roles: which dimensions of A and B are free / contracted and where the
+// free ones land in R (contract_labels / find_matching_positions,
+// NDTensors/src/tensoroperations/contraction_logic.jl:5-55,
+// NDTensors/src/blocksparse/contract_utilities.jl:28-55).
+// ---------------------------------------------------------------------------
+bool nd_make_roles(int rankA, const int32_t* la, int rankB, const int32_t* lb, int rankR,
+                   const int32_t* lr, Roles& ro, std::string& why) {
+  memset(&ro, 0, sizeof(ro));
+  if (rankA < 0 || rankB < 0 || rankR < 0 || rankA > ND_MAX_RANK || rankB > ND_MAX_RANK || rankR > ND_MAX_RANK) {
+    why = "rank out of range (max 8)";
+    return false;
+  }
+  ro.rankA = rankA; ro.rankB = rankB; ro.rankR = rankR;
+  for (int i = 0; i < rankA; ++i)
+    for (int j = i + 1; j < rankA; ++j)
+      if (la[i] == la[j]) { why = "repeated label in A"; return false; }
+  for (int i = 0; i < rankB; ++i)
+    for (int j = i + 1; j < rankB; ++j)
+      if (lb[i] == lb[j]) { why = "repeated label in B"; return false; }
+  for (int i = 0; i < rankR; ++i)
+    for (int j = i + 1; j < rankR; ++j)
+      if (lr[i] == lr[j]) { why = "repeated label in R"; return false; }
+  auto find = [](const int32_t* l, int n, int x) { for (int i = 0; i < n; ++i) if (l[i] == x) return i; return -1; };
+  int nfree = 0;
+  for (int i = 0; i < rankA; ++i) {
+    int j = find(lb, rankB, la[i]);
+    if (j >= 0) { ro.a_k[ro.nk] = i; ro.b_k[ro.nk] = j; ro.nk++; }
+    else nfree++;
+  }
+  for (int j = 0; j < rankB; ++j)
+    if (find(la, rankA, lb[j]) < 0) nfree++;
+  if (nfree != rankR) { why = "output labels must be exactly the uncontracted labels"; return false; }
+  // free dims ordered by their position in R
+  for (int r = 0; r < rankR; ++r) {
+    int i = find(la, rankA, lr[r]);
+    int j = find(lb, rankB, lr[r]);
+    if (i >= 0 && find(lb, rankB, lr[r]) < 0) { ro.a_free[ro.nfa] = i; ro.r_afree[ro.nfa] = r; ro.nfa++; }
+    else if (j >= 0 && find(la, rankA, lr[r]) < 0) { ro.b_free[ro.nfb] = j; ro.r_bfree[ro.nfb] = r; ro.nfb++; }
+    else { why = "output label not found among the uncontracted labels"; return false; }
+  }
+  return true;
+}

@@ -1,0 +1,171 @@
+// Internal definitions shared by the translation units of libndtensors_gb300.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <mutex>
+#include "../../include/ndtensors_gb300.h"
+
+#define ND_HOSTDEV __host__ __device__ __forceinline__
+
+// Bounded device-side waits: a spin that runs past this many polls records
+// ND_ERR_TIMEOUT in the status word and returns instead of hanging the GPU.
+#define ND_SPIN_LIMIT (1u << 26)
+
+// device status word layout (int32): [0] = first error code, [1] = where it was raised
+struct DeviceStatus {
+  int32_t code;
+  int32_t where;
+};
+
+struct nd_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int num_sms = 0;
+  int ozaki_slices = 5;
+  std::string last_error;
+  DeviceStatus* d_status = nullptr;   // device status word
+  int64_t launches = 0;
+  // grow-only scratch arena (device)
+  void* ws = nullptr;
+  size_t ws_size = 0;
+  // graph capture
+  cudaGraph_t graph = nullptr;
+  bool capturing = false;
+};
+
+// Host helpers -------------------------------------------------------------
+nd_status nd_fail(nd_handle h, nd_status code, const char* fmt, ...);
+nd_status nd_cuda_check(nd_handle h, cudaError_t e, const char* what);
+nd_status nd_workspace(nd_handle h, size_t bytes, void** out);
+nd_status nd_check_device_status(nd_handle h, const char* what);  // syncs
+
+#define ND_CUDA(h, call)                                              \
+  do {                                                                \
+    cudaError_t _e = (call);                                          \
+    if (_e != cudaSuccess) return nd_cuda_check((h), _e, #call);      \
+  } while (0)
+
+#define ND_LAUNCHED(h) do { (h)->launches++; } while (0)
+
+// Mixed-radix index decomposition ------------------------------------------
+// A GEMM row / column / reduction index enumerates several tensor dimensions,
+// first dimension fastest.  st0/st1 are the element strides of those
+// dimensions in two tensors (e.g. A and R for rows).
+struct Mixed {
+  int32_t n;
+  int32_t dim[ND_MAX_RANK];
+  int64_t st0[ND_MAX_RANK];
+  int64_t st1[ND_MAX_RANK];
+};
+
+ND_HOSTDEV void mixed_offsets(const Mixed& m, int64_t lin, int64_t& o0, int64_t& o1) {
+  int64_t a = 0, b = 0;
+  for (int d = 0; d < m.n; ++d) {
+    int64_t q = lin / m.dim[d];
+    int64_t r = lin - q * m.dim[d];
+    a += r * m.st0[d];
+    b += r * m.st1[d];
+    lin = q;
+  }
+  o0 = a;
+  o1 = b;
+}
+
+// Merge adjacent dimensions that are contiguous in both strided views.
+inline void mixed_simplify(Mixed& m) {
+  Mixed o{};
+  o.n = 0;
+  for (int d = 0; d < m.n; ++d) {
+    if (m.dim[d] == 1) continue;
+    if (o.n > 0) {
+      int k = o.n - 1;
+      if (o.st0[k] * o.dim[k] == m.st0[d] && o.st1[k] * o.dim[k] == m.st1[d]) {
+        o.dim[k] *= m.dim[d];
+        continue;
+      }
+    }
+    o.dim[o.n] = m.dim[d];
+    o.st0[o.n] = m.st0[d];
+    o.st1[o.n] = m.st1[d];
+    o.n++;
+  }
+  m = o;
+}
+
+// How the labels of one contraction map onto a GEMM (shared by all block pairs).
+struct Roles {
+  int rankA, rankB, rankR;
+  int nfa, nfb, nk;
+  int a_free[ND_MAX_RANK];   // positions in A of A-free dims, in output order
+  int r_afree[ND_MAX_RANK];  // their positions in R
+  int b_free[ND_MAX_RANK];
+  int r_bfree[ND_MAX_RANK];
+  int a_k[ND_MAX_RANK];      // positions in A of contracted dims, in A order
+  int b_k[ND_MAX_RANK];      // matching positions in B
+};
+
+// Build roles from ncon labels; returns false on invalid labels.
+bool nd_make_roles(int rankA, const int32_t* la, int rankB, const int32_t* lb, int rankR,
+                   const int32_t* lr, Roles& ro, std::string& why);
+
+// One block pair of a contraction, ready for the GEMM kernels.
+struct PairDesc {
+  int64_t a_off, b_off, r_off;   // element offsets of the three blocks
+  int32_t M, N, K, group;        // GEMM sizes, output block (group) id
+  int32_t a_op, b_op;            // operand-slot ids (packed split operands)
+  int32_t first;                 // 1 if first pair of its group (overwrite)
+  int32_t job;                   // which (A, B, R) base-pointer triple (0 or 1)
+  Mixed rows;   // st0: A strides, st1: R strides
+  Mixed cols;   // st0: B strides, st1: R strides
+  Mixed ks;     // st0: A strides, st1: B strides
+};
+
+// A split operand (one A block or one B block) for the split-precision GEMMs.
+struct OperandDesc {
+  int64_t src_off;      // element offset of the block in its tensor
+  int32_t rows, kdim;   // GEMM view: rows (M or N) x K
+  int32_t row_tiles, k_steps;
+  int64_t pack_off;     // byte offset of its packed slices
+  int64_t exp_off;      // int32 offset of its per-row exponents
+  Mixed rk;             // st0: strides of rows, st1 unused ; see pack kernel
+  Mixed kk;             // st0: strides of k
+};
+
+// Work item of the grouped GEMMs: one output tile of one group.
+struct WorkItem {
+  int32_t group;        // group id
+  int32_t pair_begin;   // first pair (pairs sorted by group)
+  int32_t pair_count;
+  int32_t mt, nt;       // tile coordinates
+};
+
+// Split-precision parameters
+#define ND_OZ_BM 128
+#define ND_OZ_BN 64
+#define ND_OZ_BK 32
+#define ND_OZ_CHUNK_STEPS 16   // 16 * 32 = 512 of K per exact chunk
+
+// Kernel launchers (defined in the .cu files) ------------------------------
+nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, const int64_t* dims,
+                            const int* perm0, double alpha, double beta, const double* scalar_dev);
+// Base pointers of up to two contractions executed by one grouped launch.
+struct JobPtrs {
+  const double* A[2];
+  const double* B[2];
+  double* R[2];
+};
+
+// Grouped execution shared by dense / block-sparse / adjoint paths.
+// pairs: sorted by (job, group); items derived inside.  Groups are numbered
+// globally across jobs.
+nd_status nd_execute_grouped(nd_handle h, const std::vector<PairDesc>& pairs, int ngroups,
+                             const JobPtrs& ptrs, double alpha, double beta, int precision);
+nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items,
+                             int nitems, const JobPtrs& ptrs, double alpha, double beta);
+nd_status nd_run_split_gemm(nd_handle h, int precision, const std::vector<PairDesc>& pairs,
+                            const std::vector<WorkItem>& items, const JobPtrs& ptrs,
+                            double alpha, double beta);

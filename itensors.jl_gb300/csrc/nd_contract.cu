@@ -1,0 +1,459 @@
+// Contraction drivers: dense contract!, block-sparse plan / contract / adjoint,
+// block-sparse permutedims.  Host-side C++; all arithmetic runs in the kernels.
+//
+// Reference behaviour reproduced here:
+//   dense contract!  NDTensors/src/dense/tensoralgebra/contract.jl:160-216
+//     - one-element operand -> scalar branch (drop singleton dims, permute, scale; :100-150)
+//     - otherwise one GEMM with the permutations folded into addressing
+//   block-sparse     NDTensors/src/blocksparse/contract.jl:3-76, contract_generic.jl:37-129
+//     - plan on device (nd_plan.cu), pairs grouped by output block in R's block order,
+//       first pair of a group overwrites, the rest accumulate
+//   adjoint          ext/ITensorsChainRulesCoreExt/itensor.jl:94-103
+#include "nd_plan.h"
+#include <algorithm>
+#include <numeric>
+#include <cstring>
+
+nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups, int precision);
+nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double alpha, double beta);
+
+void ExecCache::free_all() {
+  if (d_pairs) cudaFree(d_pairs);
+  if (d_items) cudaFree(d_items);
+  if (d_operands) cudaFree(d_operands);
+  if (d_pack) cudaFree(d_pack);
+  if (d_exp) cudaFree(d_exp);
+  if (d_pack_items) cudaFree(d_pack_items);
+  *this = ExecCache{};
+}
+
+nd_status nd_bs_import(nd_handle h, const nd_bs_desc* in, BsDesc& out, const char* name) {
+  if (!in) return nd_fail(h, ND_ERR_ARG, "%s: NULL descriptor", name);
+  if (in->rank < 0 || in->rank > ND_MAX_RANK) return nd_fail(h, ND_ERR_ARG, "%s: rank %d out of range", name, in->rank);
+  if (in->nnzblocks < 0) return nd_fail(h, ND_ERR_ARG, "%s: negative block count", name);
+  out = BsDesc{};
+  out.rank = in->rank;
+  out.nnzblocks = in->nnzblocks;
+  size_t off = 0;
+  for (int d = 0; d < in->rank; ++d) {
+    int nb = in->nblocks ? in->nblocks[d] : 0;
+    if (nb <= 0) return nd_fail(h, ND_ERR_ARG, "%s: dimension %d has no blocks", name, d);
+    out.nblocks.push_back(nb);
+    std::vector<int64_t> bd(in->blockdims + off, in->blockdims + off + nb);
+    for (auto x : bd) if (x < 0) return nd_fail(h, ND_ERR_ARG, "%s: negative block dim", name);
+    out.blockdims.push_back(bd);
+    off += nb;
+  }
+  out.blocks_store.assign(in->blocks, in->blocks + (size_t)in->nnzblocks * in->rank);
+  out.blocks = out.blocks_store.data();
+  out.offsets.assign(in->offsets, in->offsets + in->nnzblocks);
+  for (int b = 0; b < in->nnzblocks; ++b)
+    for (int d = 0; d < in->rank; ++d) {
+      int v = out.blocks_store[(size_t)b * in->rank + d];
+      if (v < 1 || v > out.nblocks[d]) return nd_fail(h, ND_ERR_ARG, "%s: block %d has block number %d out of range in dim %d", name, b, v, d);
+    }
+  return ND_OK;
+}
+
+bool nd_make_pair(const Roles& ro, const int64_t* dA, const int64_t* dB, const int64_t* dR, PairDesc& pd,
+                  std::string& why) {
+  memset(&pd, 0, sizeof(pd));
+  int64_t sA[ND_MAX_RANK + 1], sB[ND_MAX_RANK + 1], sR[ND_MAX_RANK + 1];
+  sA[0] = sB[0] = sR[0] = 1;
+  for (int k = 0; k < ro.rankA; ++k) sA[k + 1] = sA[k] * dA[k];
+  for (int k = 0; k < ro.rankB; ++k) sB[k + 1] = sB[k] * dB[k];
+  for (int k = 0; k < ro.rankR; ++k) sR[k + 1] = sR[k] * dR[k];
+  int64_t M = 1, N = 1, K = 1;
+  pd.rows.n = ro.nfa;
+  for (int t = 0; t < ro.nfa; ++t) {
+    int64_t d = dA[ro.a_free[t]];
+    if (d != dR[ro.r_afree[t]]) { why = "output dimension does not match A"; return false; }
+    pd.rows.dim[t] = (int32_t)d; pd.rows.st0[t] = sA[ro.a_free[t]]; pd.rows.st1[t] = sR[ro.r_afree[t]];
+    M *= d;
+  }
+  pd.cols.n = ro.nfb;
+  for (int t = 0; t < ro.nfb; ++t) {
+    int64_t d = dB[ro.b_free[t]];
+    if (d != dR[ro.r_bfree[t]]) { why = "output dimension does not match B"; return false; }
+    pd.cols.dim[t] = (int32_t)d; pd.cols.st0[t] = sB[ro.b_free[t]]; pd.cols.st1[t] = sR[ro.r_bfree[t]];
+    N *= d;
+  }
+  pd.ks.n = ro.nk;
+  for (int t = 0; t < ro.nk; ++t) {
+    int64_t d = dA[ro.a_k[t]];
+    if (d != dB[ro.b_k[t]]) { why = "contracted dimensions of A and B differ"; return false; }
+    pd.ks.dim[t] = (int32_t)d; pd.ks.st0[t] = sA[ro.a_k[t]]; pd.ks.st1[t] = sB[ro.b_k[t]];
+    K *= d;
+  }
+  if (M > INT32_MAX || N > INT32_MAX || K > INT32_MAX) { why = "GEMM extent exceeds 2^31"; return false; }
+  pd.M = (int32_t)M; pd.N = (int32_t)N; pd.K = (int32_t)K;
+  mixed_simplify(pd.rows);
+  mixed_simplify(pd.cols);
+  mixed_simplify(pd.ks);
+  return true;
+}
+
+static nd_status upload(nd_handle h, void** dst, const void* src, size_t bytes) {
+  if (*dst) { cudaFree(*dst); *dst = nullptr; }
+  ND_CUDA(h, cudaMalloc(dst, std::max<size_t>(bytes, 16)));
+  if (bytes) ND_CUDA(h, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+  return ND_OK;
+}
+
+// Work items for the FP64 kernel: 64x64 tiles, biggest groups first.
+static void make_items(const std::vector<PairDesc>& pairs, int bm, int bn, std::vector<WorkItem>& items) {
+  items.clear();
+  struct G { int begin, count; int64_t cost; };
+  std::vector<G> groups;
+  for (size_t i = 0; i < pairs.size();) {
+    size_t j = i;
+    int64_t ksum = 0;
+    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) { ksum += pairs[j].K; ++j; }
+    groups.push_back({(int)i, (int)(j - i), ksum});
+    i = j;
+  }
+  std::vector<std::pair<int64_t, WorkItem>> tmp;
+  for (auto& g : groups) {
+    const PairDesc& p = pairs[g.begin];
+    int mt = (p.M + bm - 1) / bm, nt = (p.N + bn - 1) / bn;
+    for (int a = 0; a < mt; ++a)
+      for (int b = 0; b < nt; ++b) {
+        int64_t mm = std::min(bm, p.M - a * bm), nn = std::min(bn, p.N - b * bn);
+        tmp.push_back({mm * nn * std::max<int64_t>(g.cost, 1), WorkItem{p.group, g.begin, g.count, a, b}});
+      }
+  }
+  std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+  for (auto& t : tmp) items.push_back(t.second);
+}
+
+nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups,
+                            const JobPtrs& ptrs, double alpha, double beta, int precision) {
+  if (pairs.empty()) return ND_OK;
+  if (precision != ND_PREC_FP64 && precision != ND_PREC_OZAKI && precision != ND_PREC_BF16X3)
+    return nd_fail(h, ND_ERR_ARG, "unknown precision %d", precision);
+  const int want_slices = precision == ND_PREC_OZAKI ? h->ozaki_slices : (precision == ND_PREC_BF16X3 ? 2 : 0);
+  if (!c.built || c.precision != precision || c.slices != want_slices) {
+    if (h->capturing) return nd_fail(h, ND_ERR_ARG, "contraction state must be built before graph capture (run once first)");
+    c.free_all();
+    c.precision = precision;
+    c.slices = want_slices;
+    nd_status s = upload(h, (void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc));
+    if (s) return s;
+    if (precision == ND_PREC_FP64) {
+      std::vector<WorkItem> items;
+      make_items(pairs, 64, 64, items);
+      c.nitems = (int)items.size();
+      s = upload(h, (void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem));
+      if (s) return s;
+    } else {
+      s = nd_split_build(h, c, pairs, ngroups, precision);
+      if (s) return s;
+    }
+    c.built = true;
+  }
+  if (precision == ND_PREC_FP64) return nd_launch_gemm_f64(h, c.d_pairs, c.d_items, c.nitems, ptrs, alpha, beta);
+  return nd_split_run(h, c, ptrs, alpha, beta);
+}
+
+// ---------------------------------------------------------------------------
+// Dense contract!
+// ---------------------------------------------------------------------------
+extern "C" nd_status nd_contract_dense_f64(nd_handle h, double* R, int32_t rankR, const int64_t* dimsR,
+                                           const int32_t* labelsR, const double* A, int32_t rankA,
+                                           const int64_t* dimsA, const int32_t* labelsA, const double* B,
+                                           int32_t rankB, const int64_t* dimsB, const int32_t* labelsB,
+                                           double alpha, double beta, int32_t precision) {
+  if (!h) return ND_ERR_ARG;
+  if (rankA < 0 || rankB < 0 || rankR < 0 || rankA > ND_MAX_RANK || rankB > ND_MAX_RANK || rankR > ND_MAX_RANK)
+    return nd_fail(h, ND_ERR_ARG, "contract: rank out of range (max %d)", ND_MAX_RANK);
+  int64_t nA = 1, nB = 1, nR = 1;
+  for (int k = 0; k < rankA; ++k) { if (dimsA[k] < 0) return nd_fail(h, ND_ERR_ARG, "contract: negative dim"); nA *= dimsA[k]; }
+  for (int k = 0; k < rankB; ++k) { if (dimsB[k] < 0) return nd_fail(h, ND_ERR_ARG, "contract: negative dim"); nB *= dimsB[k]; }
+  for (int k = 0; k < rankR; ++k) { if (dimsR[k] < 0) return nd_fail(h, ND_ERR_ARG, "contract: negative dim"); nR *= dimsR[k]; }
+  if (nR == 0) return ND_OK;
+  if ((nA && !A) || (nB && !B) || !R) return nd_fail(h, ND_ERR_ARG, "contract: NULL data pointer");
+  // scalar branch (dense/tensoralgebra/contract.jl:100-150, 171-174)
+  if (nA == 1 || nB == 1) {
+    const double* scal = nA == 1 ? A : B;
+    const double* T = nA == 1 ? B : A;
+    int rankT = nA == 1 ? rankB : rankA;
+    const int64_t* dT = nA == 1 ? dimsB : dimsA;
+    const int32_t* lT = nA == 1 ? labelsB : labelsA;
+    if (nA == 1 && nB == 1) {
+      int64_t one = 1;
+      int p0 = 0;
+      return nd_launch_permute(h, R, B, 1, &one, &p0, alpha, beta, A);
+    }
+    // drop singletons and derive the permutation from the labels
+    std::vector<int> lr, lt;
+    std::vector<int64_t> dr, dt;
+    for (int k = 0; k < rankR; ++k) if (dimsR[k] != 1) { lr.push_back(labelsR[k]); dr.push_back(dimsR[k]); }
+    for (int k = 0; k < rankT; ++k) if (dT[k] != 1) { lt.push_back(lT[k]); dt.push_back(dT[k]); }
+    if (lr.size() != lt.size()) return nd_fail(h, ND_ERR_ARG, "contract: scalar branch rank mismatch");
+    std::vector<int> perm(lr.size());
+    for (size_t r = 0; r < lr.size(); ++r) {
+      auto it = std::find(lt.begin(), lt.end(), lr[r]);
+      if (it == lt.end()) return nd_fail(h, ND_ERR_ARG, "contract: output label %d not found", lr[r]);
+      perm[r] = (int)(it - lt.begin());
+      if (dt[perm[r]] != dr[r]) return nd_fail(h, ND_ERR_ARG, "contract: dimension mismatch in scalar branch");
+    }
+    if (lr.empty()) {
+      int64_t one = 1; int p0 = 0;
+      return nd_launch_permute(h, R, T, 1, &one, &p0, alpha, beta, scal);
+    }
+    return nd_launch_permute(h, R, T, (int)lr.size(), dt.data(), perm.data(), alpha, beta, scal);
+  }
+  Roles ro;
+  std::string why;
+  if (!nd_make_roles(rankA, labelsA, rankB, labelsB, rankR, labelsR, ro, why))
+    return nd_fail(h, ND_ERR_ARG, "contract: %s", why.c_str());
+  PairDesc pd;
+  if (!nd_make_pair(ro, dimsA, dimsB, dimsR, pd, why)) return nd_fail(h, ND_ERR_ARG, "contract: %s", why.c_str());
+  pd.group = 0; pd.first = 1; pd.job = 0; pd.a_op = 0; pd.b_op = 0;
+  if (pd.K == 0) {   // empty contraction: R = beta * R
+    int64_t n = nR; int p0 = 0;
+    return nd_launch_permute(h, R, R, 1, &n, &p0, 0.0, beta, nullptr);
+  }
+  std::vector<PairDesc> pairs{pd};
+  ExecCache c;
+  JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
+  nd_status s = nd_execute_cached(h, c, pairs, 1, ptrs, alpha, beta, precision);
+  ND_CUDA(h, cudaStreamSynchronize(h->stream));
+  c.free_all();
+  if (s != ND_OK) return s;
+  return nd_check_device_status(h, "contract");
+}
+
+// ---------------------------------------------------------------------------
+// Block-sparse plan
+// ---------------------------------------------------------------------------
+extern "C" nd_status nd_bs_plan_create(nd_handle h, const nd_bs_desc* A, const int32_t* labelsA,
+                                       const nd_bs_desc* B, const int32_t* labelsB, int32_t rankR,
+                                       const int32_t* labelsR, nd_plan* plan) {
+  if (!h || !plan) return ND_ERR_ARG;
+  *plan = nullptr;
+  auto p = new nd_bs_plan_s();
+  p->h = h;
+  nd_status s = nd_bs_import(h, A, p->A, "plan(A)");
+  if (!s) s = nd_bs_import(h, B, p->B, "plan(B)");
+  if (s) { delete p; return s; }
+  std::string why;
+  if (!nd_make_roles(p->A.rank, labelsA, p->B.rank, labelsB, rankR, labelsR, p->roles, why)) {
+    delete p;
+    return nd_fail(h, ND_ERR_ARG, "plan: %s", why.c_str());
+  }
+  p->rankR = rankR;
+  p->labelsA.assign(labelsA, labelsA + p->A.rank);
+  p->labelsB.assign(labelsB, labelsB + p->B.rank);
+  p->labelsR.assign(labelsR, labelsR + rankR);
+  const Roles& ro = p->roles;
+  // contracted indices must have identical block structure
+  for (int t = 0; t < ro.nk; ++t)
+    if (p->A.blockdims[ro.a_k[t]] != p->B.blockdims[ro.b_k[t]]) {
+      delete p;
+      return nd_fail(h, ND_ERR_ARG, "plan: contracted index %d of A and %d of B have different block dims", ro.a_k[t], ro.b_k[t]);
+    }
+  p->r_nblocks.assign(rankR, 0);
+  p->r_blockdims.assign(rankR, {});
+  for (int t = 0; t < ro.nfa; ++t) {
+    p->r_nblocks[ro.r_afree[t]] = p->A.nblocks[ro.a_free[t]];
+    p->r_blockdims[ro.r_afree[t]] = p->A.blockdims[ro.a_free[t]];
+  }
+  for (int t = 0; t < ro.nfb; ++t) {
+    p->r_nblocks[ro.r_bfree[t]] = p->B.nblocks[ro.b_free[t]];
+    p->r_blockdims[ro.r_bfree[t]] = p->B.blockdims[ro.b_free[t]];
+  }
+  s = nd_device_plan(h, ro, p->A, p->B, p->r_nblocks, p->r_blockdims, p->res);
+  if (s) { delete p; return s; }
+  *plan = p;
+  return ND_OK;
+}
+
+extern "C" nd_status nd_bs_plan_sizes(nd_plan plan, int32_t* npairs, int32_t* nR, int64_t* nnzR) {
+  if (!plan) return ND_ERR_ARG;
+  if (npairs) *npairs = plan->res.npairs;
+  if (nR) *nR = plan->res.nR;
+  if (nnzR) *nnzR = plan->res.nnzR;
+  return ND_OK;
+}
+
+extern "C" nd_status nd_bs_plan_get(nd_plan plan, int32_t* blocksR, int64_t* offsetsR, int32_t* pairs) {
+  if (!plan) return ND_ERR_ARG;
+  const PlanResult& r = plan->res;
+  if (blocksR && !r.blocksR.empty()) memcpy(blocksR, r.blocksR.data(), r.blocksR.size() * 4);
+  if (offsetsR && !r.offsetsR.empty()) memcpy(offsetsR, r.offsetsR.data(), r.offsetsR.size() * 8);
+  if (pairs && !r.pairs.empty()) memcpy(pairs, r.pairs.data(), r.pairs.size() * 4);
+  return ND_OK;
+}
+
+extern "C" nd_status nd_bs_plan_destroy(nd_plan plan) {
+  if (!plan) return ND_OK;
+  cudaStreamSynchronize(plan->h->stream);
+  for (auto& c : plan->cache) c.free_all();
+  for (auto& c : plan->adj_cache) c.free_all();
+  delete plan;
+  return ND_OK;
+}
+
+// Group the plan's pairs by output block (R block order), plan order inside a group.
+static nd_status build_forward_descs(nd_plan p) {
+  if (!p->descs.empty() || p->res.npairs == 0) return ND_OK;
+  nd_handle h = p->h;
+  const PlanResult& r = p->res;
+  const int rankR = p->rankR;
+  std::vector<std::vector<int>> by_group(r.nR);
+  for (int q = 0; q < r.npairs; ++q) by_group[r.pairs[3 * q + 2]].push_back(q);
+  std::string why;
+  for (int g = 0; g < r.nR; ++g) {
+    int64_t dR[ND_MAX_RANK];
+    for (int k = 0; k < rankR; ++k) dR[k] = p->r_blockdims[k][r.blocksR[(size_t)g * rankR + k] - 1];
+    bool first = true;
+    for (int q : by_group[g]) {
+      int iA = r.pairs[3 * q], iB = r.pairs[3 * q + 1];
+      int64_t dA[ND_MAX_RANK], dB[ND_MAX_RANK];
+      for (int k = 0; k < p->A.rank; ++k) dA[k] = p->A.bdim(iA, k);
+      for (int k = 0; k < p->B.rank; ++k) dB[k] = p->B.bdim(iB, k);
+      PairDesc pd;
+      if (!nd_make_pair(p->roles, dA, dB, dR, pd, why)) return nd_fail(h, ND_ERR_ARG, "plan: %s", why.c_str());
+      pd.a_off = p->A.offsets[iA];
+      pd.b_off = p->B.offsets[iB];
+      pd.r_off = r.offsetsR[g];
+      pd.group = g;
+      pd.first = first ? 1 : 0;
+      pd.job = 0;
+      pd.a_op = iA;
+      pd.b_op = iB;
+      first = false;
+      p->descs.push_back(pd);
+    }
+  }
+  p->ngroups = r.nR;
+  return ND_OK;
+}
+
+extern "C" nd_status nd_bs_contract_f64(nd_handle h, nd_plan p, double* R, const double* A, const double* B,
+                                        double alpha, int32_t precision) {
+  if (!h || !p) return ND_ERR_ARG;
+  if (p->res.npairs == 0) return ND_OK;
+  if (!R || !A || !B) return nd_fail(h, ND_ERR_ARG, "bs_contract: NULL data pointer");
+  if (precision < 0 || precision > 2) return nd_fail(h, ND_ERR_ARG, "bs_contract: unknown precision %d", precision);
+  nd_status s = build_forward_descs(p);
+  if (s) return s;
+  JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
+  return nd_execute_cached(h, p->cache[precision], p->descs, p->ngroups, ptrs, alpha, 0.0, precision);
+}
+
+// Pullback: job 0: Abar = Rbar * B grouped by A block; job 1: Bbar = A * Rbar grouped by B block.
+static nd_status build_adjoint_descs(nd_plan p) {
+  if (p->adj_built) return ND_OK;
+  nd_handle h = p->h;
+  const PlanResult& r = p->res;
+  Roles r1, r2;
+  std::string why;
+  if (!nd_make_roles(p->rankR, p->labelsR.data(), p->B.rank, p->labelsB.data(), p->A.rank, p->labelsA.data(), r1, why) ||
+      !nd_make_roles(p->A.rank, p->labelsA.data(), p->rankR, p->labelsR.data(), p->B.rank, p->labelsB.data(), r2, why))
+    return nd_fail(h, ND_ERR_ARG, "adjoint: %s", why.c_str());
+  const int nA = p->A.nnzblocks, nB = p->B.nnzblocks;
+  std::vector<std::vector<int>> byA(nA), byB(nB);
+  for (int q = 0; q < r.npairs; ++q) { byA[r.pairs[3 * q]].push_back(q); byB[r.pairs[3 * q + 1]].push_back(q); }
+  auto dimsR = [&](int g, int64_t* d) { for (int k = 0; k < p->rankR; ++k) d[k] = p->r_blockdims[k][r.blocksR[(size_t)g * p->rankR + k] - 1]; };
+  for (int a = 0; a < nA; ++a) {
+    bool first = true;
+    for (int q : byA[a]) {
+      int iB = r.pairs[3 * q + 1], g = r.pairs[3 * q + 2];
+      int64_t dA[ND_MAX_RANK], dB[ND_MAX_RANK], dR[ND_MAX_RANK];
+      for (int k = 0; k < p->A.rank; ++k) dA[k] = p->A.bdim(a, k);
+      for (int k = 0; k < p->B.rank; ++k) dB[k] = p->B.bdim(iB, k);
+      dimsR(g, dR);
+      PairDesc pd;
+      if (!nd_make_pair(r1, dR, dB, dA, pd, why)) return nd_fail(h, ND_ERR_ARG, "adjoint: %s", why.c_str());
+      pd.a_off = r.offsetsR[g]; pd.b_off = p->B.offsets[iB]; pd.r_off = p->A.offsets[a];
+      pd.group = a; pd.first = first; pd.job = 0; pd.a_op = g; pd.b_op = iB;
+      first = false;
+      p->adj_descs.push_back(pd);
+    }
+  }
+  for (int b = 0; b < nB; ++b) {
+    bool first = true;
+    for (int q : byB[b]) {
+      int iA = r.pairs[3 * q], g = r.pairs[3 * q + 2];
+      int64_t dA[ND_MAX_RANK], dB[ND_MAX_RANK], dR[ND_MAX_RANK];
+      for (int k = 0; k < p->A.rank; ++k) dA[k] = p->A.bdim(iA, k);
+      for (int k = 0; k < p->B.rank; ++k) dB[k] = p->B.bdim(b, k);
+      dimsR(g, dR);
+      PairDesc pd;
+      if (!nd_make_pair(r2, dA, dR, dB, pd, why)) return nd_fail(h, ND_ERR_ARG, "adjoint: %s", why.c_str());
+      pd.a_off = p->A.offsets[iA]; pd.b_off = r.offsetsR[g]; pd.r_off = p->B.offsets[b];
+      pd.group = nA + b; pd.first = first; pd.job = 1; pd.a_op = iA; pd.b_op = g;
+      first = false;
+      p->adj_descs.push_back(pd);
+    }
+  }
+  p->adj_ngroups = nA + nB;
+  p->adj_built = true;
+  return ND_OK;
+}
+
+__global__ void zero_ranges(double* base0, double* base1, const int64_t* ranges, int n) {
+  // ranges: [n][3] = (job, offset, count)
+  for (int r = blockIdx.y; r < n; r += gridDim.y) {
+    double* b = ranges[3 * r] ? base1 : base0;
+    int64_t off = ranges[3 * r + 1], cnt = ranges[3 * r + 2];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x)
+      b[off + i] = 0.0;
+  }
+}
+
+extern "C" nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan p, const double* Rbar, const double* A,
+                                                const double* B, double* Abar, double* Bbar, int32_t precision) {
+  if (!h || !p) return ND_ERR_ARG;
+  if (!Abar || !Bbar) return nd_fail(h, ND_ERR_ARG, "adjoint: NULL output");
+  if (precision < 0 || precision > 2) return nd_fail(h, ND_ERR_ARG, "adjoint: unknown precision %d", precision);
+  nd_status s = build_adjoint_descs(p);
+  if (s) return s;
+  // blocks of A / B that no pair touches have a zero cotangent
+  std::vector<int64_t> ranges;
+  {
+    std::vector<char> tA(p->A.nnzblocks, 0), tB(p->B.nnzblocks, 0);
+    for (int q = 0; q < p->res.npairs; ++q) { tA[p->res.pairs[3 * q]] = 1; tB[p->res.pairs[3 * q + 1]] = 1; }
+    for (int a = 0; a < p->A.nnzblocks; ++a) if (!tA[a]) ranges.insert(ranges.end(), {0, p->A.offsets[a], p->A.block_elems(a)});
+    for (int b = 0; b < p->B.nnzblocks; ++b) if (!tB[b]) ranges.insert(ranges.end(), {1, p->B.offsets[b], p->B.block_elems(b)});
+  }
+  if (!ranges.empty()) {
+    if (h->capturing) return nd_fail(h, ND_ERR_ARG, "adjoint with untouched blocks cannot be captured");
+    int64_t* d = nullptr;
+    ND_CUDA(h, cudaMallocAsync(&d, ranges.size() * 8, h->stream));
+    ND_CUDA(h, cudaMemcpyAsync(d, ranges.data(), ranges.size() * 8, cudaMemcpyHostToDevice, h->stream));
+    int n = (int)(ranges.size() / 3);
+    zero_ranges<<<dim3(64, std::min(n, 1024)), 256, 0, h->stream>>>(Abar, Bbar, d, n);
+    ND_LAUNCHED(h);
+    ND_CUDA(h, cudaFreeAsync(d, h->stream));
+  }
+  if (p->adj_descs.empty()) return ND_OK;
+  JobPtrs ptrs{{Rbar, A}, {B, Rbar}, {Abar, Bbar}};
+  return nd_execute_cached(h, p->adj_cache[precision], p->adj_descs, p->adj_ngroups, ptrs, 1.0, 0.0, precision);
+}
+
+extern "C" nd_status nd_bs_permutedims_f64(nd_handle h, const nd_bs_desc* T, const double* Tdata,
+                                           const int32_t* perm, const int64_t* offsetsR, double* Rdata) {
+  if (!h) return ND_ERR_ARG;
+  BsDesc d;
+  nd_status s = nd_bs_import(h, T, d, "bs_permutedims");
+  if (s) return s;
+  if (!perm || !offsetsR) return nd_fail(h, ND_ERR_ARG, "bs_permutedims: NULL perm/offsets");
+  int p0[ND_MAX_RANK];
+  bool seen[ND_MAX_RANK] = {false};
+  for (int k = 0; k < d.rank; ++k) {
+    int v = perm[k] - 1;
+    if (v < 0 || v >= d.rank || seen[v]) return nd_fail(h, ND_ERR_ARG, "bs_permutedims: bad perm");
+    seen[v] = true;
+    p0[k] = v;
+  }
+  for (int b = 0; b < d.nnzblocks; ++b) {
+    int64_t dims[ND_MAX_RANK];
+    for (int k = 0; k < d.rank; ++k) dims[k] = d.bdim(b, k);
+    s = nd_launch_permute(h, Rdata + offsetsR[b], Tdata + d.offsets[b], d.rank, dims, p0, 1.0, 0.0, nullptr);
+    if (s) return s;
+  }
+  return ND_OK;
+}

@@ -1,0 +1,153 @@
+// Plain FP64 grouped GEMM on the FP64 tensor cores (DMMA, mma.sync.m8n8k4.f64).
+//
+// This is the FP64 drop-in for BLAS.gemm! / cuBLAS mul! reached from
+// _contract! (NDTensors/src/abstractarray/tensoralgebra/contract.jl:40-85,115-188)
+// and for the per-block-pair loop of the block-sparse contraction
+// (NDTensors/src/blocksparse/contract_generic.jl:78-129).  tcgen05 has no FP64
+// kind, so DMMA is the FP64 tensor path on sm_103a; it is bound by the FP64
+// pipe, not by memory.
+//
+// One launch runs every block pair of a contraction: a work item is one 64x64
+// tile of one output block (group); the CTA walks the group's pairs in plan
+// order, accumulating in registers, so the first pair "overwrites" and the
+// rest "accumulate" exactly like beta = 0 then 1 in the reference.  Operands
+// are read through mixed-radix offset tables, so permuted inputs / outputs
+// need no separate permute pass (the permutations of ContractionProperties are
+// folded into the addressing).
+#include "nd_common.h"
+#include <algorithm>
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, LDS = BM + 4;
+
+struct GemmArgs {
+  const PairDesc* pairs;
+  const WorkItem* items;
+  int nitems;
+  JobPtrs ptrs;
+  double alpha, beta;
+};
+
+__device__ __forceinline__ void dmma(double& c0, double& c1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+               : "+d"(c0), "+d"(c1) : "d"(a), "d"(b));
+}
+
+__global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
+  __shared__ double As[BK][LDS];
+  __shared__ double Bs[BK][LDS];
+  __shared__ int64_t rowA[BM], rowR[BM], colB[BN], colR[BN];
+  __shared__ int64_t kA[BK], kB[BK];
+  __shared__ PairDesc pd;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+
+  for (int it = blockIdx.x; it < g.nitems; it += gridDim.x) {
+    const WorkItem wi = g.items[it];
+    double acc[4][4][2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+    int64_t r_base = 0;
+    double* Rp = nullptr;
+    int M = 0, N = 0;
+    for (int pi = 0; pi < wi.pair_count; ++pi) {
+      __syncthreads();
+      if (tid == 0) pd = g.pairs[wi.pair_begin + pi];
+      __syncthreads();
+      M = pd.M; N = pd.N;
+      const int m0 = wi.mt * BM, n0 = wi.nt * BN;
+      if (tid < BM) {
+        int64_t o0 = 0, o1 = 0;
+        if (m0 + tid < M) mixed_offsets(pd.rows, m0 + tid, o0, o1);
+        rowA[tid] = o0; rowR[tid] = o1;
+      } else {
+        int c = tid - BM;
+        int64_t o0 = 0, o1 = 0;
+        if (n0 + c < N) mixed_offsets(pd.cols, n0 + c, o0, o1);
+        colB[c] = o0; colR[c] = o1;
+      }
+      const double* A = g.ptrs.A[pd.job] + pd.a_off;
+      const double* B = g.ptrs.B[pd.job] + pd.b_off;
+      Rp = g.ptrs.R[pd.job];
+      r_base = pd.r_off;
+      const bool a_rows_contig = pd.rows.n > 0 && pd.rows.st0[0] == 1;
+      const bool b_cols_contig = pd.cols.n > 0 && pd.cols.st0[0] == 1;
+      for (int k0 = 0; k0 < pd.K; k0 += BK) {
+        __syncthreads();
+        if (tid < BK) {
+          int64_t o0 = 0, o1 = 0;
+          if (k0 + tid < pd.K) mixed_offsets(pd.ks, k0 + tid, o0, o1);
+          kA[tid] = o0; kB[tid] = o1;
+        }
+        __syncthreads();
+        // A tile (BM x BK) -> As[k][m]
+#pragma unroll
+        for (int e = 0; e < (BM * BK) / 128; ++e) {
+          int m, k;
+          if (a_rows_contig) { m = tid & 63; k = (tid >> 6) + 2 * e; }
+          else { k = tid & 15; m = (tid >> 4) + 8 * e; }
+          double v = 0.0;
+          if (m0 + m < M && k0 + k < pd.K) v = __ldg(A + rowA[m] + kA[k]);
+          As[k][m] = v;
+        }
+        // B tile (BK x BN) -> Bs[k][n]
+#pragma unroll
+        for (int e = 0; e < (BN * BK) / 128; ++e) {
+          int n, k;
+          if (b_cols_contig) { n = tid & 63; k = (tid >> 6) + 2 * e; }
+          else { k = tid & 15; n = (tid >> 4) + 8 * e; }
+          double v = 0.0;
+          if (n0 + n < N && k0 + k < pd.K) v = __ldg(B + kB[k] + colB[n]);
+          Bs[k][n] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; kk += 4) {
+          double af[4], bf[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) af[i] = As[kk + (lane & 3)][wm + i * 8 + (lane >> 2)];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) bf[j] = Bs[kk + (lane & 3)][wn + j * 8 + (lane >> 2)];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
+        }
+      }
+    }
+    // epilogue: R = alpha * acc + beta * R  (beta == 0 overwrites)
+    const int m0 = wi.mt * BM, n0 = wi.nt * BN;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int m = wm + i * 8 + (lane >> 2);
+      if (m0 + m >= M) continue;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int n = wn + j * 8 + 2 * (lane & 3) + h;
+          if (n0 + n >= N) continue;
+          double* dst = Rp + r_base + rowR[m] + colR[n];
+          double v = acc[i][j][h];
+          if (g.beta == 0.0) *dst = (g.alpha == 1.0) ? v : g.alpha * v;
+          else *dst = g.alpha * v + g.beta * *dst;
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+
+nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
+                             const JobPtrs& ptrs, double alpha, double beta) {
+  if (nitems == 0) return ND_OK;
+  GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta};
+  int blocks = std::min(nitems, h->num_sms * 4);
+  gemm_f64_grouped<<<blocks, 128, 0, h->stream>>>(g);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "gemm_f64_grouped");
+}

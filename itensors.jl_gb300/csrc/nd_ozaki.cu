@@ -1,0 +1,692 @@
+// Split-precision grouped GEMM on the 5th-generation tensor cores (tcgen05 + TMEM).
+//
+// Replaces the FP64 BLAS.gemm! of _contract! (NDTensors/src/abstractarray/
+// tensoralgebra/contract.jl:40-85) for the block pairs of a contraction when the
+// caller asks for ND_PREC_OZAKI or ND_PREC_BF16X3.
+//
+// Ozaki scheme (error-free splitting, Ozaki-Ogita-Oishi-Rump 2012; integer
+// slices after Ootomo et al. 2024):
+//   every row i of A (over K) gets an exponent E_i with max|A_i,:| < 2^E_i and is
+//   written as A_ik = 2^(E_i-7) * sum_p d_p 2^(-8(p-1)) with S balanced digits
+//   d_p in [-128, 128]; B likewise per column (F_j).  Digits are integers of at
+//   most 8 significant bits, so they are exact in BF16, digit products are
+//   exact in FP32 (< 2^14), and a sum of up to 2^10 of them is exact too.
+//   C = 2^(E_i+F_j-14) sum_{p+q<=S+1} 2^(-8(p+q-2)) (A_p B_q).
+// sm_103a has no tcgen05 kind::i8, so the int8-range digits run on kind::f16
+// with BF16 operands and FP32 accumulators in TMEM.
+//
+// GB300 has ~1/30 of B200's FP64 rate, so this file performs NO FP64
+// arithmetic in its hot loops: the split reads the IEEE bits with integer
+// instructions, the recombination is int64 fixed-point, and the final double
+// is assembled from integer fields.  FP64 arithmetic appears only in the
+// alpha/beta epilogue when alpha != 1 or beta != 0, and in the BF16X3 epilogue.
+//
+// Levels: level t = p+q carries weight 2^(-8(t-2)).  Levels 2 and 3 must be
+// exact; they accumulate in FP32 TMEM over chunks of 512 of K (|sum| <= 2^24),
+// double buffered, and the epilogue warps drain each chunk into int64 fixed
+// point (unit 2^-24 of a level-2 unit) while the next chunk is computed.
+// Levels >= 4 accumulate in FP32 over the whole K (their rounding is below
+// 2^-40 of the leading term) and are drained once per block pair.
+//
+// Each A-slice stage is [S][128 rows][32 k] BF16 and each B-slice stage is
+// [S][64 rows][32 k], pre-swizzled (64-byte swizzle) by the pack kernel, so one
+// cp.async.bulk per operand brings a whole stage and the slices of B sit in
+// consecutive rows: A_p x [B_q .. B_q'] is ONE tcgen05.mma with N = 64*(q'-q+1)
+// whose accumulator columns are exactly the level blocks p+q .. p+q'.
+//
+// Warp roles (320 threads): warp 0 = bulk-copy producer, warp 1 = TMEM
+// allocator + MMA issuer, warps 2..9 = epilogue (TMEM lane quarter = warp % 4,
+// column half = (warp-2)/4).  Persistent CTAs walk a cost-sorted list of
+// output tiles; each tile loops over the block pairs of its output block.
+#include "nd_plan.h"
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <map>
+
+namespace {
+
+constexpr int BM = 128, BN = 64, BK = 32;
+constexpr int A_SLICE = BM * BK * 2;   // 8192 bytes
+constexpr int B_SLICE = BN * BK * 2;   // 4096 bytes
+constexpr int CHUNK_STEPS = 16;        // 16 * 32 = 512 of K per exact chunk
+constexpr int NTHREADS = 320;
+constexpr int SMEM_BUDGET = 220 * 1024;
+
+struct SplitOp {
+  int64_t src_off;    // element offset of the block
+  int64_t pack_off;   // byte offset of its packed slices
+  int64_t exp_off;    // offset of its per-row exponents
+  int32_t rows, kdim;
+  int32_t row_tiles, k_steps;
+  int32_t is_b, job;
+  Mixed rk;           // st0: element strides of the rows
+  Mixed kk;           // st0: element strides of k
+};
+
+struct PackItem {
+  int32_t op, rt;
+};
+
+struct PackArgs {
+  const SplitOp* ops;
+  const PackItem* items;
+  int nitems;
+  JobPtrs ptrs;
+  unsigned char* pack;
+  int32_t* exps;
+  int slices;         // S (2 = BF16X3 float split)
+  DeviceStatus* st;
+};
+
+// ---- helpers ---------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, DeviceStatus* st, int site,
+                                          volatile int* abort_flag) {
+  for (uint32_t it = 0; it < ND_SPIN_LIMIT; ++it) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    if (ok) return true;
+    if ((it & 255) == 255 && abort_flag && *abort_flag) return false;
+  }
+  if (atomicCAS(&st->code, 0, ND_ERR_TIMEOUT) == 0) st->where = site;
+  if (abort_flag) *abort_flag = 1;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(b)) : "memory");
+}
+
+// Balanced base-256 digits of the fixed-point integer X (|X| <= 2^(8S-1)).
+// digit[0] is the most significant.
+__device__ __forceinline__ void balanced_digits(int64_t X, int S, int* d) {
+  for (int p = S - 1; p >= 1; --p) {
+    int lo = (int)(((X + 128) & 255)) - 128;
+    d[p] = lo;
+    X = (X - lo) >> 8;
+  }
+  d[0] = (int)X;
+}
+
+// Round |x| * 2^(8S-1-E) to an integer using only integer instructions.
+__device__ __forceinline__ int64_t fixed_point(uint64_t bits, int E, int S) {
+  int ex = (int)((bits >> 52) & 0x7ff);
+  uint64_t m = bits & 0xfffffffffffffull;
+  if (ex) m |= (1ull << 52); else ex = 1;
+  int sh = 1075 - ex - (8 * S - 1) + E;   // >= 5 because |x| < 2^E and 8S-1 <= 47
+  uint64_t mag = 0;
+  if (sh < 64 && m) mag = (sh > 0) ? ((m + (1ull << (sh - 1))) >> sh) : (m << (-sh));
+  return (bits >> 63) ? -(int64_t)mag : (int64_t)mag;
+}
+
+// FP64 -> FP32 with round-to-nearest-even using integer instructions only.
+// Values beyond the FP32 range saturate to +-Inf / flush to zero.
+__device__ __forceinline__ float f64_to_f32_int(uint64_t bits) {
+  uint32_t sign = (uint32_t)(bits >> 63) << 31;
+  int ex = (int)((bits >> 52) & 0x7ff);
+  uint64_t m = bits & 0xfffffffffffffull;
+  if (ex == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0));
+  int e = ex - 1023 + 127;
+  if (ex == 0 || e < -24) return __uint_as_float(sign);
+  m |= (1ull << 52);
+  int shift = 29;                       // 53 -> 24 bits
+  if (e <= 0) { shift += 1 - e; e = 0; }
+  uint64_t mant = m >> shift;
+  uint64_t rem = m & ((1ull << shift) - 1), half = 1ull << (shift - 1);
+  if (rem > half || (rem == half && (mant & 1))) mant++;
+  if (e == 0) return __uint_as_float(sign | (uint32_t)mant);          // denormal (carry into exponent is fine)
+  if (mant >> 24) { mant >>= 1; e++; }
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((uint32_t)e << 23) | ((uint32_t)mant & 0x7fffffu));
+}
+
+// v * 2^e rounded to the nearest double, integer instructions only.
+__device__ __forceinline__ double i64_scaled_to_f64(long long v, int e) {
+  if (v == 0) return 0.0;
+  uint64_t sign = v < 0 ? (1ull << 63) : 0ull;
+  uint64_t a = v < 0 ? (uint64_t)(-(v + 1)) + 1ull : (uint64_t)v;
+  int lz = __clzll((long long)a);
+  uint64_t n = a << lz;                  // top bit at 63
+  uint64_t mant = n >> 11, rem = n & 0x7ffull;
+  int ex2 = e + 63 - lz;                 // value = n/2^63 * 2^ex2 in [2^ex2, 2^(ex2+1))
+  if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) {
+    mant++;
+    if (mant >> 53) { mant >>= 1; ex2++; }
+  }
+  int be = ex2 + 1023;
+  if (be >= 2047) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull));
+  if (be <= 0) {
+    int s = 1 - be;
+    if (s > 53) return __longlong_as_double((long long)sign);
+    uint64_t r = mant & ((1ull << s) - 1), hf = 1ull << (s - 1);
+    uint64_t mm = mant >> s;
+    if (r > hf || (r == hf && (mm & 1ull))) mm++;
+    return __longlong_as_double((long long)(sign | mm));
+  }
+  return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (mant & 0xfffffffffffffull)));
+}
+
+__device__ __forceinline__ uint16_t bf16_bits_of_int(int d) {
+  // |d| <= 256: exact in bf16
+  return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
+}
+
+// byte offset of element (r, k) inside one [rows][32] BF16 slice, 64-byte swizzle
+__device__ __forceinline__ int swz64(int r, int k) {
+  return r * 64 + ((((k >> 3) ^ (r >> 1)) & 3) << 4) + (k & 7) * 2;
+}
+
+// ---- pack kernel -----------------------------------------------------------
+// One CTA per (operand, row tile): row maxima -> exponents -> S digit slices,
+// staged in shared memory in the tcgen05 canonical K-major SW64 layout and
+// written out as contiguous 16-byte vectors.
+__global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ unsigned long long rowmax[BM];
+  __shared__ int64_t rowoff[BM];
+  __shared__ int64_t koff[BK];
+  __shared__ int32_t Er[BM];
+  const int tid = threadIdx.x;
+  const int S = a.slices;
+  for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
+    const PackItem pi = a.items[it];
+    const SplitOp& op = a.ops[pi.op];
+    const int ROWS = op.is_b ? BN : BM;
+    const double* src = (op.is_b ? a.ptrs.B[op.job] : a.ptrs.A[op.job]) + op.src_off;
+    const int r0 = pi.rt * ROWS;
+    __syncthreads();
+    if (tid < ROWS) {
+      int64_t o = 0, dummy;
+      if (r0 + tid < op.rows) mixed_offsets(op.rk, r0 + tid, o, dummy);
+      rowoff[tid] = o;
+      rowmax[tid] = 0ull;
+    }
+    const bool rows_contig = op.rk.n > 0 && op.rk.st0[0] == 1;
+    const int per = ROWS * BK / 256;
+    // pass 1: row maxima of |x| (as IEEE bit patterns: monotonic for finite x)
+    if (S > 2) {
+      for (int ks = 0; ks < op.k_steps; ++ks) {
+        __syncthreads();
+        if (tid < BK) {
+          int64_t o = 0, dummy;
+          if (ks * BK + tid < op.kdim) mixed_offsets(op.kk, ks * BK + tid, o, dummy);
+          koff[tid] = o;
+        }
+        __syncthreads();
+        for (int e = 0; e < per; ++e) {
+          int r, k;
+          if (rows_contig) { r = tid % ROWS; k = tid / ROWS + (256 / ROWS) * e; }
+          else { k = tid & 31; r = (tid >> 5) + 8 * e; }
+          if (r0 + r < op.rows && ks * BK + k < op.kdim) {
+            uint64_t b = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k])) & 0x7fffffffffffffffull;
+            if (b >= 0x7ff0000000000000ull) {
+              if (atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
+              b = 0;
+            }
+            atomicMax(&rowmax[r], (unsigned long long)b);
+          }
+        }
+      }
+      __syncthreads();
+      if (tid < ROWS) {
+        int ex = (int)(rowmax[tid] >> 52);
+        int E = (ex ? ex : 1) - 1022;      // max|x| < 2^E
+        Er[tid] = E;
+        a.exps[op.exp_off + r0 + tid] = E;
+      }
+    }
+    // pass 2: digits
+    for (int ks = 0; ks < op.k_steps; ++ks) {
+      __syncthreads();
+      if (tid < BK) {
+        int64_t o = 0, dummy;
+        if (ks * BK + tid < op.kdim) mixed_offsets(op.kk, ks * BK + tid, o, dummy);
+        koff[tid] = o;
+      }
+      __syncthreads();
+      for (int e = 0; e < per; ++e) {
+        int r, k;
+        if (rows_contig) { r = tid % ROWS; k = tid / ROWS + (256 / ROWS) * e; }
+        else { k = tid & 31; r = (tid >> 5) + 8 * e; }
+        uint64_t bits = 0;
+        if (r0 + r < op.rows && ks * BK + k < op.kdim)
+          bits = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k]));
+        const int so = swz64(r, k);
+        if (S > 2) {
+          int d[6];
+          int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, Er[r], S);
+          balanced_digits(X, S, d);
+          for (int s = 0; s < S; ++s) *(uint16_t*)(sm + s * ROWS * 64 + so) = bf16_bits_of_int(d[s]);
+        } else {
+          float xf = f64_to_f32_int(bits);
+          __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+          __nv_bfloat16 lo = __float2bfloat16_rn(xf - __bfloat162float(hi));
+          *(uint16_t*)(sm + so) = __bfloat16_as_ushort(hi);
+          *(uint16_t*)(sm + ROWS * 64 + so) = __bfloat16_as_ushort(lo);
+        }
+      }
+      __syncthreads();
+      const int bytes = S * ROWS * 64;
+      int4* dst = (int4*)(a.pack + op.pack_off + ((int64_t)(pi.rt * op.k_steps + ks) * S) * (ROWS * 64));
+      const int4* srcs = (const int4*)sm;
+      for (int v = tid; v < bytes / 16; v += 256) dst[v] = srcs[v];
+    }
+  }
+}
+
+// ---- grouped tcgen05 GEMM ----------------------------------------------------
+struct GemmArgs {
+  const PairDesc* pairs;
+  const WorkItem* items;
+  int nitems;
+  const SplitOp* ops;
+  const unsigned char* pack;
+  const int32_t* exps;
+  JobPtrs ptrs;
+  double alpha, beta;
+  DeviceStatus* st;
+};
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+  // tcgen05 shared-memory matrix descriptor: K-major, 64-byte swizzle,
+  // 8-row core-matrix groups 512 bytes apart (SBO), LBO unused (1).
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
+}
+
+__device__ __forceinline__ uint32_t idesc(int n) {
+  // kind::f16: D=F32 (bit 4), A=BF16 (bit 7), B=BF16 (bit 10), K-major A/B, N>>3 at 17, M>>4 at 24
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t id, uint32_t acc) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+               :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+}
+
+__device__ __forceinline__ void commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(bar)) : "memory");
+}
+
+#define TMEM_LD32(taddr, r)                                                                                   \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15," \
+               "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                      \
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),          \
+                 "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),       \
+                 "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),    \
+                 "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),    \
+                 "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                            \
+               : "r"(taddr))
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+template <int S>
+struct Cfg {
+  static constexpr int STAGE = S * (A_SLICE + B_SLICE);
+  static constexpr int STAGES = (SMEM_BUDGET - 1024) / STAGE;
+  static constexpr int TAIL = S > 2 ? S - 2 : 0;           // tail level blocks (levels 4..S+1)
+  static constexpr int EXACT0 = TAIL * BN;                  // column of exact buffer 0
+  static constexpr int TMEM_COLS = (TAIL * BN + 4 * BN) <= 256 ? 256 : 512;
+  static constexpr int SMEM = STAGES * STAGE + 1024;
+};
+
+template <int S>
+__global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
+  using C = Cfg<S>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[C::STAGES], empty[C::STAGES];
+  __shared__ __align__(8) uint64_t xfull[2], xempty[2], tfull, tempty, done_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&xfull[b], 1); mbar_init(&xempty[b], 8); }
+    mbar_init(&tfull, 1);
+    mbar_init(&tempty, 8);
+    mbar_init(&done_bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(&tmem_slot)), "r"(C::TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------- producer ------------------------------
+    if (lane == 0) {
+      uint32_t n = 0;
+      bool ok = true;
+      for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
+        const WorkItem wi = g.items[it];
+        for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+          const PairDesc& pd = g.pairs[wi.pair_begin + pi];
+          const SplitOp& oa = g.ops[pd.a_op];
+          const SplitOp& ob = g.ops[pd.b_op];
+          const unsigned char* srcA = g.pack + oa.pack_off + (int64_t)wi.mt * oa.k_steps * S * A_SLICE;
+          const unsigned char* srcB = g.pack + ob.pack_off + (int64_t)wi.nt * ob.k_steps * S * B_SLICE;
+          for (int ks = 0; ks < oa.k_steps; ++ks, ++n) {
+            const uint32_t s = n % C::STAGES, u = n / C::STAGES;
+            if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (u - 1) & 1, g.st, 400, &abort_flag)) { ok = false; break; }
+            unsigned char* dA = smem + s * C::STAGE;
+            unsigned char* dB = dA + S * A_SLICE;
+            const uint32_t fb = smem_u32(&full[s]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(fb), "r"(C::STAGE) : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(smem_u32(dA)), "l"(srcA + (int64_t)ks * S * A_SLICE), "r"(S * A_SLICE), "r"(fb) : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(smem_u32(dB)), "l"(srcB + (int64_t)ks * S * B_SLICE), "r"(S * B_SLICE), "r"(fb) : "memory");
+          }
+        }
+      }
+      if (!ok) {
+        // let copies already issued land before the CTA can exit
+        for (uint32_t q = 0; q < C::STAGES && q < n; ++q) {
+          uint32_t m = n - 1 - q;
+          mbar_wait(smem_u32(&full[m % C::STAGES]), (m / C::STAGES) & 1, g.st, 401, nullptr);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------- MMA issuer ----------------------------
+    if (lane == 0) {
+      uint32_t n = 0, chunk = 0, pairs_done = 0;
+      bool ok = true;
+      const uint32_t smem_base = smem_u32(smem);
+      for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
+        const WorkItem wi = g.items[it];
+        for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+          const PairDesc& pd = g.pairs[wi.pair_begin + pi];
+          const int nks = g.ops[pd.a_op].k_steps;
+          if (S > 2 && pairs_done >= 1 && !mbar_wait(smem_u32(&tempty), (pairs_done - 1) & 1, g.st, 410, &abort_flag)) { ok = false; break; }
+          const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
+          uint32_t pbuf = 0;
+          for (int ks = 0; ks < nks; ++ks, ++n) {
+            const bool cstart = (ks % chunk_steps) == 0;
+            const bool cend = ((ks % chunk_steps) == chunk_steps - 1) || ks == nks - 1;
+            if (cstart) {
+              pbuf = chunk & 1;
+              const uint32_t v = chunk >> 1;
+              if (v >= 1 && !mbar_wait(smem_u32(&xempty[pbuf]), (v - 1) & 1, g.st, 411, &abort_flag)) { ok = false; break; }
+            }
+            const uint32_t s = n % C::STAGES, u = n / C::STAGES;
+            if (!mbar_wait(smem_u32(&full[s]), u & 1, g.st, 412, &abort_flag)) { ok = false; break; }
+            fence_after();
+            const uint32_t a0 = smem_base + s * C::STAGE;
+            const uint32_t b0 = a0 + S * A_SLICE;
+            const uint32_t xcol = tmem + C::EXACT0 + pbuf * 2 * BN;
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+              const uint32_t accx = (cstart && kk == 0) ? 0u : 1u;
+              const uint32_t acct = (ks == 0 && kk == 0) ? 0u : 1u;
+              const uint32_t ko = kk * 32;
+              // A1 x [B1 B2] -> exact (L2, L3)
+              mma(xcol, sdesc(a0 + ko), sdesc(b0 + ko), idesc(2 * BN), accx);
+              if (S == 2) {
+                // A2 x [B1] -> L3
+                mma(xcol + BN, sdesc(a0 + A_SLICE + ko), sdesc(b0 + ko), idesc(BN), 1u);
+              } else {
+                // A1 x [B3..BS] -> tail levels 4..S+1
+                mma(tmem, sdesc(a0 + ko), sdesc(b0 + 2 * B_SLICE + ko), idesc((S - 2) * BN), acct);
+                // A2 x [B1] -> L3 ; A2 x [B2..B(S-1)] -> tail
+                mma(xcol + BN, sdesc(a0 + A_SLICE + ko), sdesc(b0 + ko), idesc(BN), 1u);
+                mma(tmem, sdesc(a0 + A_SLICE + ko), sdesc(b0 + B_SLICE + ko), idesc((S - 2) * BN), 1u);
+                // Ap x [B1 .. B(S+1-p)] -> tail blocks p-3 ..
+#pragma unroll
+                for (int p = 3; p <= S; ++p)
+                  mma(tmem + (p - 3) * BN, sdesc(a0 + (p - 1) * A_SLICE + ko), sdesc(b0 + ko), idesc((S + 1 - p) * BN), 1u);
+              }
+            }
+            commit(&empty[s]);
+            if (cend) { commit(&xfull[pbuf]); ++chunk; }
+          }
+          if (!ok) break;
+          if (S > 2) commit(&tfull);
+          ++pairs_done;
+        }
+      }
+      commit(&done_bar);
+      mbar_wait(smem_u32(&done_bar), 0, g.st, 413, nullptr);
+    }
+  } else {
+    // ------------------------------- epilogue ------------------------------
+    const int q = warp & 3;                 // TMEM lane quarter
+    const int hcol = (warp - 2) >> 2;       // column half
+    const int row = q * 32 + lane;
+    const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+    uint32_t chunk = 0, pairs_done = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
+      const WorkItem wi = g.items[it];
+      const PairDesc& p0 = g.pairs[wi.pair_begin];
+      const int gm = wi.mt * BM + row;
+      const bool row_ok = gm < p0.M;
+      int64_t roff = 0, dummy;
+      if (row_ok) mixed_offsets(p0.rows, gm, dummy, roff);
+      double* Rb = g.ptrs.R[p0.job] + p0.r_off;
+      for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+        const PairDesc& pd = g.pairs[wi.pair_begin + pi];
+        const SplitOp& oa = g.ops[pd.a_op];
+        const SplitOp& ob = g.ops[pd.b_op];
+        const int nks = oa.k_steps;
+        const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
+        const int nchunks = (nks + chunk_steps - 1) / chunk_steps;
+        long long acc[32];
+        float facc[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) { acc[c] = 0; facc[c] = 0.f; }
+        for (int ch = 0; ch < nchunks; ++ch, ++chunk) {
+          const uint32_t b = chunk & 1, v = chunk >> 1;
+          if (!mbar_wait(smem_u32(&xfull[b]), v & 1, g.st, 420, &abort_flag)) { ok = false; break; }
+          fence_after();
+          uint32_t l2[32], l3[32];
+          const uint32_t xaddr = lane_addr + C::EXACT0 + b * 2 * BN + hcol * 32;
+          TMEM_LD32(xaddr, l2);
+          TMEM_LD32(xaddr + BN, l3);
+          tmem_wait_ld();
+          fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&xempty[b]);
+          if (S > 2) {
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+              long long x2 = (long long)__float2int_rn(__uint_as_float(l2[c]));
+              long long x3 = (long long)__float2int_rn(__uint_as_float(l3[c]));
+              acc[c] += (x2 << 24) + (x3 << 16);
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < 32; ++c) facc[c] = __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
+          }
+        }
+        if (!ok) break;
+        if (S > 2) {
+          if (!mbar_wait(smem_u32(&tfull), pairs_done & 1, g.st, 421, &abort_flag)) { ok = false; break; }
+          fence_after();
+#pragma unroll 1
+          for (int t = 0; t < C::TAIL; ++t) {
+            uint32_t lt[32];
+            TMEM_LD32(lane_addr + t * BN + hcol * 32, lt);
+            tmem_wait_ld();
+            const float sc = __int_as_float((127 + 8 - 8 * t) << 23);   // 2^(8 - 8t): level t+4 in units of 2^-24 L2
+#pragma unroll
+            for (int c = 0; c < 32; ++c) acc[c] += __float2ll_rn(__uint_as_float(lt[c]) * sc);
+          }
+          fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty);
+        }
+        ++pairs_done;
+        // finalize this pair into R
+        if (row_ok) {
+          const int Ei = S > 2 ? g.exps[oa.exp_off + gm] : 0;
+          const bool first = pd.first != 0;
+#pragma unroll
+          for (int c = 0; c < 32; ++c) {
+            const int gn = wi.nt * BN + hcol * 32 + c;
+            if (gn >= pd.N) continue;
+            int64_t coff, d2;
+            mixed_offsets(pd.cols, gn, d2, coff);
+            double v;
+            if (S > 2) v = i64_scaled_to_f64(acc[c], Ei + g.exps[ob.exp_off + gn] - 38);
+            else v = (double)facc[c];
+            double* dst = Rb + roff + coff;
+            if (first) {
+              if (g.beta == 0.0) *dst = (g.alpha == 1.0) ? v : g.alpha * v;
+              else *dst = g.alpha * v + g.beta * *dst;
+            } else {
+              *dst = (g.alpha == 1.0) ? *dst + v : *dst + g.alpha * v;
+            }
+          }
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(C::TMEM_COLS));
+}
+
+template <int S>
+nd_status launch_gemm(nd_handle h, const GemmArgs& g) {
+  using C = Cfg<S>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(split_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+    if (e != cudaSuccess) return nd_cuda_check(h, e, "split_gemm smem attribute");
+    attr = true;
+  }
+  int blocks = std::min(g.nitems, h->num_sms);
+  split_gemm<S><<<blocks, NTHREADS, C::SMEM, h->stream>>>(g);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "split_gemm");
+}
+
+}  // namespace
+
+// Build operand list, packed layout and work items (host; once per plan/precision).
+nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs_in, int ngroups, int precision) {
+  (void)ngroups;
+  const int S = precision == ND_PREC_OZAKI ? h->ozaki_slices : 2;
+  std::vector<PairDesc> pairs = pairs_in;
+  std::vector<SplitOp> ops;
+  std::map<std::pair<int, int64_t>, int> amap, bmap;   // (job, offset) -> op
+  int64_t pack_bytes = 0, exp_count = 0;
+  auto add_op = [&](bool is_b, const PairDesc& pd) -> int {
+    auto& mp = is_b ? bmap : amap;
+    auto key = std::make_pair(pd.job, is_b ? pd.b_off : pd.a_off);
+    auto f = mp.find(key);
+    if (f != mp.end()) return f->second;
+    SplitOp o{};
+    o.src_off = key.second;
+    o.is_b = is_b;
+    o.job = pd.job;
+    o.rows = is_b ? pd.N : pd.M;
+    o.kdim = pd.K;
+    o.rk = is_b ? pd.cols : pd.rows;          // st0 = strides in this operand
+    o.kk = pd.ks;
+    if (is_b) for (int d = 0; d < o.kk.n; ++d) o.kk.st0[d] = pd.ks.st1[d];
+    const int rows_per_tile = is_b ? BN : BM;
+    o.row_tiles = (o.rows + rows_per_tile - 1) / rows_per_tile;
+    o.k_steps = (o.kdim + BK - 1) / BK;
+    o.pack_off = pack_bytes;
+    pack_bytes += (int64_t)o.row_tiles * o.k_steps * S * (is_b ? B_SLICE : A_SLICE);
+    o.exp_off = exp_count;
+    exp_count += (int64_t)o.row_tiles * rows_per_tile;
+    ops.push_back(o);
+    mp[key] = (int)ops.size() - 1;
+    return (int)ops.size() - 1;
+  };
+  for (auto& pd : pairs) {
+    pd.a_op = add_op(false, pd);
+    pd.b_op = add_op(true, pd);
+  }
+  std::vector<PackItem> pitems;
+  for (int i = 0; i < (int)ops.size(); ++i)
+    for (int t = 0; t < ops[i].row_tiles; ++t) pitems.push_back({i, t});
+  // work items: 128 x 64 tiles, biggest first
+  struct G { int begin, count; int64_t cost; };
+  std::vector<std::pair<int64_t, WorkItem>> tmp;
+  for (size_t i = 0; i < pairs.size();) {
+    size_t j = i;
+    int64_t ksum = 0;
+    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) {
+      ksum += ((pairs[j].K + BK - 1) / BK) * BK;
+      ++j;
+    }
+    const PairDesc& p = pairs[i];
+    int mt = (p.M + BM - 1) / BM, nt = (p.N + BN - 1) / BN;
+    for (int a = 0; a < mt; ++a)
+      for (int b = 0; b < nt; ++b) tmp.push_back({ksum, WorkItem{p.group, (int)i, (int)(j - i), a, b}});
+    i = j;
+  }
+  std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+  std::vector<WorkItem> items;
+  for (auto& t : tmp) items.push_back(t.second);
+  // upload
+  auto up = [&](void** dst, const void* src, size_t bytes) -> nd_status {
+    ND_CUDA(h, cudaMalloc(dst, std::max<size_t>(bytes, 16)));
+    if (bytes) ND_CUDA(h, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    return ND_OK;
+  };
+  if (c.d_pairs) { cudaFree(c.d_pairs); c.d_pairs = nullptr; }
+  nd_status s;
+  if ((s = up((void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc)))) return s;
+  if ((s = up((void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
+  if ((s = up(&c.d_operands, ops.data(), ops.size() * sizeof(SplitOp)))) return s;
+  if ((s = up(&c.d_pack_items, pitems.data(), pitems.size() * sizeof(PackItem)))) return s;
+  ND_CUDA(h, cudaMalloc(&c.d_pack, std::max<int64_t>(pack_bytes, 16)));
+  ND_CUDA(h, cudaMalloc((void**)&c.d_exp, std::max<int64_t>(exp_count, 4) * 4));
+  c.pack_bytes = pack_bytes;
+  c.exp_count = exp_count;
+  c.nitems = (int)items.size();
+  c.npack_items = (int)pitems.size();
+  c.nops_a = (int)amap.size();
+  c.nops_b = (int)bmap.size();
+  c.slices = S;
+  return ND_OK;
+}
+
+nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double alpha, double beta) {
+  const int S = c.slices;
+  PackArgs pa{(const SplitOp*)c.d_operands, (const PackItem*)c.d_pack_items, c.npack_items, ptrs,
+              (unsigned char*)c.d_pack, c.d_exp, S, h->d_status};
+  const int psmem = S * BM * 64;
+  static bool pattr = false;
+  if (!pattr) {
+    cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * BM * 64);
+    pattr = true;
+  }
+  int pblocks = std::min(c.npack_items, h->num_sms * 6);
+  if (pblocks > 0) {
+    pack_kernel<<<pblocks, 256, psmem, h->stream>>>(pa);
+    ND_LAUNCHED(h);
+    ND_CUDA(h, cudaGetLastError());
+  }
+  GemmArgs g{c.d_pairs, c.d_items, c.nitems, (const SplitOp*)c.d_operands, (const unsigned char*)c.d_pack,
+             c.d_exp, ptrs, alpha, beta, h->d_status};
+  if (c.nitems == 0) return ND_OK;
+  switch (S) {
+    case 2: return launch_gemm<2>(h, g);
+    case 3: return launch_gemm<3>(h, g);
+    case 4: return launch_gemm<4>(h, g);
+    case 5: return launch_gemm<5>(h, g);
+    case 6: return launch_gemm<6>(h, g);
+  }
+  return nd_fail(h, ND_ERR_ARG, "unsupported slice count %d", S);
+}

@@ -1,0 +1,425 @@
+// permutedims for FP64 tensors: R = beta*R + alpha*permutedims(T, perm).
+//
+// Replaces permutedims!(::Exposed{<:Array}) (NDTensors/src/array/permutedims.jl:5-24,
+// Strided.jl) and the GPU broadcast permute of NDTensors/ext/NDTensorsCUDAExt/permutedims.jl.
+// The kernel is HBM-bound; its roofline is 16 bytes moved per element
+// (24 when beta != 0).
+//
+// Dimensions of size 1 are dropped and dimensions that stay adjacent in both
+// layouts are fused.  Then:
+//   * perm[0] == 0: both tensors share their contiguous dimension, rows are
+//     copied with 128-bit accesses (kernel permute_rows);
+//   * otherwise a tiled transpose between T's contiguous dimension (i) and the
+//     T dimension that becomes R's contiguous one (j).  Tiles of 32(i) x 64(j)
+//     FP64 are staged in shared memory by TMA (cp.async.bulk.tensor, 128-byte
+//     swizzle, 4-stage mbarrier ring in a persistent grid) and written to R
+//     with 128-bit stores along j (kernel permute_tma).  Shapes TMA cannot
+//     describe (rank > 5 after fusion, odd leading extent, unaligned base) use
+//     the same tiling with plain loads (kernel permute_tiles).
+#include "nd_common.h"
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <algorithm>
+#include <cstring>
+
+namespace {
+
+struct PermParams {
+  int64_t total;
+  int32_t n;                   // fused rank
+  int64_t d0, dq;              // extents of i (T dim 0) and j (T dim q)
+  int64_t rs_i;                // R stride of the i dimension
+  int64_t ts_j;                // T stride of the j dimension
+  int32_t nb;                  // number of batch dims
+  int64_t bdim[ND_MAX_RANK];   // batch extents
+  int64_t bts[ND_MAX_RANK];    // batch T strides
+  int64_t brs[ND_MAX_RANK];    // batch R strides
+  int32_t bcoord[ND_MAX_RANK]; // batch dim index in T (TMA coordinate slot)
+  int32_t q;                   // T dim index of j (TMA coordinate slot)
+  int64_t ntile_i, ntile_j, ntiles;
+  double alpha, beta;
+  int32_t mode;                // 0 copy, 1 scale, 2 beta==1 accumulate, 3 general, 4 zero, 5 beta-only
+  int32_t vec;                 // 128-bit stores allowed
+  const double* scalar;        // optional device scalar multiplying alpha
+};
+
+__device__ __forceinline__ double combine(const PermParams& p, double a, double t, const double* rp) {
+  switch (p.mode) {
+    case 0: return t;
+    case 1: return a * t;
+    case 2: return *rp + a * t;
+    case 3: return a * t + p.beta * *rp;
+    case 4: return 0.0;
+    default: return p.beta * *rp;
+  }
+}
+
+__device__ __forceinline__ double eff_alpha(const PermParams& p) {
+  return p.scalar ? p.alpha * __ldg(p.scalar) : p.alpha;
+}
+
+__device__ __forceinline__ void batch_offsets(const PermParams& p, int64_t b, int64_t& to, int64_t& ro, int32_t* coord) {
+  to = 0; ro = 0;
+  for (int d = 0; d < p.nb; ++d) {
+    int64_t q = b / p.bdim[d];
+    int64_t r = b - q * p.bdim[d];
+    to += r * p.bts[d];
+    ro += r * p.brs[d];
+    if (coord) coord[d] = (int32_t)r;
+    b = q;
+  }
+}
+
+// ---- mbarrier / TMA helpers (bounded waits) -------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, DeviceStatus* st, int site) {
+  for (uint32_t it = 0; it < ND_SPIN_LIMIT; ++it) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    if (ok) return true;
+    if ((it & 1023) == 1023 && *(volatile int32_t*)&st->code == ND_ERR_TIMEOUT) return false;
+  }
+  if (atomicCAS(&st->code, 0, ND_ERR_TIMEOUT) == 0) st->where = site;
+  return false;
+}
+
+constexpr int TI = 32, TJ = 64, STAGES = 4;
+constexpr int BOX_I = 16;                       // 16 doubles = 128 bytes (swizzle span)
+constexpr int TILE_BYTES = TI * TJ * 8;         // 16 KB
+constexpr int BOX_BYTES = BOX_I * TJ * 8;       // 8 KB
+
+__global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUtensorMap tmap, double* R,
+                                                   const double* Rin, PermParams p, DeviceStatus* st) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[STAGES];
+  __shared__ int s_ok;
+  const int tid = threadIdx.x;
+  const double a = eff_alpha(p);
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&full[s])), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    asm volatile("prefetch.tensormap [%0];" :: "l"(&tmap) : "memory");
+  }
+  __syncthreads();
+  const int64_t first = blockIdx.x, stride = gridDim.x;
+  auto issue = [&](int64_t t, int s) {
+    int64_t tj = t % p.ntile_j;
+    int64_t rest = t / p.ntile_j;
+    int64_t ti = rest % p.ntile_i;
+    int64_t b = rest / p.ntile_i;
+    int32_t c[5] = {0, 0, 0, 0, 0};
+    int64_t to, ro;
+    int32_t bc[ND_MAX_RANK];
+    batch_offsets(p, b, to, ro, bc);
+    for (int d = 0; d < p.nb; ++d) c[p.bcoord[d]] = bc[d];
+    c[0] = (int32_t)(ti * TI);
+    c[p.q] = (int32_t)(tj * TJ);
+    uint32_t bar = smem_u32(&full[s]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(TILE_BYTES) : "memory");
+    for (int h = 0; h < 2; ++h) {
+      uint32_t dst = smem_u32(smem + s * TILE_BYTES + h * BOX_BYTES);
+      int32_t x = c[0] + h * BOX_I;
+      asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                   :: "r"(dst), "l"(&tmap), "r"(x), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(bar) : "memory");
+    }
+  };
+  // prologue
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      int64_t t = first + s * stride;
+      if (t < p.ntiles) issue(t, s);
+    }
+  }
+  uint32_t phase[STAGES] = {0, 0, 0, 0};
+  int s = 0;
+  bool ok = true;
+  for (int64_t t = first; t < p.ntiles; t += stride) {
+    // one thread polls the barrier and broadcasts, so every thread leaves together
+    if (tid == 0) s_ok = mbar_wait(smem_u32(&full[s]), phase[s], st, 100) ? 1 : 0;
+    __syncthreads();
+    phase[s] ^= 1;
+    ok = s_ok != 0;
+    if (!ok) break;
+    int64_t tj = t % p.ntile_j;
+    int64_t rest = t / p.ntile_j;
+    int64_t ti = rest % p.ntile_i;
+    int64_t b = rest / p.ntile_i;
+    int64_t to, ro;
+    batch_offsets(p, b, to, ro, nullptr);
+    const int64_t i0 = ti * TI, j0 = tj * TJ;
+    const unsigned char* tile = smem + s * TILE_BYTES;
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int ii = warp; ii < TI; ii += 8) {
+      const int64_t i = i0 + ii;
+      if (i >= p.d0) break;
+      const int j = lane * 2;
+      const int h = ii / BOX_I, il = ii % BOX_I;
+      const unsigned char* box = tile + h * BOX_BYTES;
+      double v0 = *(const double*)(box + j * 128 + ((((il >> 1) ^ (j & 7)) << 4)) + (il & 1) * 8);
+      double v1 = *(const double*)(box + (j + 1) * 128 + ((((il >> 1) ^ ((j + 1) & 7)) << 4)) + (il & 1) * 8);
+      const int64_t jg = j0 + j;
+      const int64_t roff = ro + i * p.rs_i + jg;
+      if (p.vec && jg + 1 < p.dq) {
+        double2 o;
+        if (p.mode >= 2) {
+          double2 old = *(const double2*)(Rin + roff);
+          o.x = combine(p, a, v0, &old.x);
+          o.y = combine(p, a, v1, &old.y);
+        } else {
+          o.x = combine(p, a, v0, nullptr);
+          o.y = combine(p, a, v1, nullptr);
+        }
+        *(double2*)(R + roff) = o;
+      } else {
+        if (jg < p.dq) R[roff] = combine(p, a, v0, Rin + roff);
+        if (jg + 1 < p.dq) R[roff + 1] = combine(p, a, v1, Rin + roff + 1);
+      }
+    }
+    __syncthreads();   // every thread is done with stage s
+    if (tid == 0) {
+      int64_t tn = t + (int64_t)STAGES * stride;
+      if (tn < p.ntiles) issue(tn, s);
+    }
+    s = (s + 1) % STAGES;
+  }
+  // After a timeout, give copies still in flight a bounded chance to land
+  // before the CTA exits (on the normal path every issued tile was consumed).
+  if (!ok && tid == 0) {
+    for (int q = 0; q < STAGES; ++q) mbar_wait(smem_u32(&full[q]), phase[q], st, 101);
+  }
+}
+
+// Same tiling, plain loads: T[i, j, batch] -> smem (padded) -> R.
+__global__ void __launch_bounds__(256) permute_tiles(const double* __restrict__ T, double* R,
+                                                     const double* Rin, PermParams p) {
+  __shared__ double tile[TJ][TI + 1];
+  const double a = eff_alpha(p);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+    int64_t tj = t % p.ntile_j;
+    int64_t rest = t / p.ntile_j;
+    int64_t ti = rest % p.ntile_i;
+    int64_t b = rest / p.ntile_i;
+    int64_t to, ro;
+    batch_offsets(p, b, to, ro, nullptr);
+    const int64_t i0 = ti * TI, j0 = tj * TJ;
+    // load: lanes along i (T-contiguous)
+    for (int jj = warp; jj < TJ; jj += 8) {
+      int64_t j = j0 + jj, i = i0 + lane;
+      tile[jj][lane] = (j < p.dq && i < p.d0) ? __ldg(T + to + j * p.ts_j + i) : 0.0;
+    }
+    __syncthreads();
+    for (int ii = warp; ii < TI; ii += 8) {
+      int64_t i = i0 + ii;
+      if (i >= p.d0) break;
+      for (int jj = lane; jj < TJ; jj += 32) {
+        int64_t j = j0 + jj;
+        if (j < p.dq) {
+          int64_t roff = ro + i * p.rs_i + j;
+          R[roff] = combine(p, a, tile[jj][ii], Rin + roff);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Shared contiguous dimension: copy rows of length d0 (i) for every batch index.
+__global__ void __launch_bounds__(256) permute_rows(const double* __restrict__ T, double* R,
+                                                    const double* Rin, PermParams p) {
+  const double a = eff_alpha(p);
+  const int64_t nrows = p.ntiles;
+  const int warps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t row = (int64_t)blockIdx.x * warps + warp; row < nrows; row += (int64_t)gridDim.x * warps) {
+    int64_t to, ro;
+    batch_offsets(p, row, to, ro, nullptr);
+    if (p.vec) {
+      const int64_t n2 = p.d0 >> 1;
+      for (int64_t c = lane; c < n2; c += 32) {
+        double2 v = __ldg((const double2*)(T + to) + c);
+        double2 o;
+        if (p.mode >= 2) {
+          double2 old = *((const double2*)(Rin + ro) + c);
+          o.x = combine(p, a, v.x, &old.x);
+          o.y = combine(p, a, v.y, &old.y);
+        } else {
+          o.x = combine(p, a, v.x, nullptr);
+          o.y = combine(p, a, v.y, nullptr);
+        }
+        *((double2*)(R + ro) + c) = o;
+      }
+    } else {
+      for (int64_t c = lane; c < p.d0; c += 32) R[ro + c] = combine(p, a, __ldg(T + to + c), Rin + ro + c);
+    }
+  }
+}
+
+__global__ void permute_scalar(const double* T, double* R, PermParams p) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) R[0] = combine(p, eff_alpha(p), T[0], R);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }
+  return fn;
+}
+
+}  // namespace
+
+nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, const int64_t* dims,
+                            const int* perm0, double alpha, double beta, const double* scalar_dev) {
+  // drop singleton dims
+  int64_t d[ND_MAX_RANK];
+  int nk = 0;
+  int64_t total = 1;
+  for (int k = 0; k < rank; ++k) total *= dims[k];
+  if (total == 0) return ND_OK;
+  int newpos[ND_MAX_RANK];
+  for (int k = 0; k < rank; ++k) {
+    if (dims[k] != 1) { newpos[k] = nk; d[nk] = dims[k]; nk++; }
+    else newpos[k] = -1;
+  }
+  int pr[ND_MAX_RANK], npr = 0;   // R position -> T (reduced) dim
+  for (int r = 0; r < rank; ++r) if (newpos[perm0[r]] >= 0) pr[npr++] = newpos[perm0[r]];
+  // fuse T dims (t, t+1) that are adjacent in R
+  int posR[ND_MAX_RANK];
+  for (int r = 0; r < npr; ++r) posR[pr[r]] = r;
+  int grp[ND_MAX_RANK];  // fused group id of each reduced T dim
+  int ng = 0;
+  int64_t gd[ND_MAX_RANK];
+  for (int t = 0; t < nk; ++t) {
+    if (t > 0 && posR[t] == posR[t - 1] + 1) { grp[t] = grp[t - 1]; gd[grp[t]] *= d[t]; }
+    else { grp[t] = ng; gd[ng] = d[t]; ng++; }
+  }
+  int gperm[ND_MAX_RANK], ngp = 0;   // R order of fused groups
+  for (int r = 0; r < npr; ++r) {
+    int g = grp[pr[r]];
+    if (ngp == 0 || gperm[ngp - 1] != g) gperm[ngp++] = g;
+  }
+  // strides
+  int64_t ts[ND_MAX_RANK], rs[ND_MAX_RANK];
+  { int64_t s = 1; for (int g = 0; g < ng; ++g) { ts[g] = s; s *= gd[g]; } }
+  { int64_t s = 1; for (int r = 0; r < ngp; ++r) { rs[gperm[r]] = s; s *= gd[gperm[r]]; } }
+
+  PermParams p{};
+  p.total = total;
+  p.n = ng;
+  p.alpha = alpha;
+  p.beta = beta;
+  p.scalar = scalar_dev;
+  if (beta == 0.0) p.mode = (alpha == 0.0 && !scalar_dev) ? 4 : ((alpha == 1.0 && !scalar_dev) ? 0 : 1);
+  else if (alpha == 0.0 && !scalar_dev) p.mode = 5;
+  else p.mode = (beta == 1.0) ? 2 : 3;
+  const double* Rin = R;
+  const int threads = 256;
+
+  if (ng <= 1 || gperm[0] == 0) {
+    // shared contiguous dim (or scalar / pure copy)
+    if (total == 1) {
+      permute_scalar<<<1, 32, 0, h->stream>>>(T, R, p);
+      ND_LAUNCHED(h);
+      return nd_cuda_check(h, cudaGetLastError(), "permute_scalar");
+    }
+    p.d0 = (ng == 0) ? 1 : gd[0];
+    p.nb = 0;
+    for (int g = 1; g < ng; ++g) { p.bdim[p.nb] = gd[g]; p.bts[p.nb] = ts[g]; p.brs[p.nb] = rs[g]; p.nb++; }
+    p.ntiles = total / p.d0;   // rows
+    bool al = ((uintptr_t)T % 16 == 0) && ((uintptr_t)R % 16 == 0) && (p.d0 % 2 == 0);
+    p.vec = al ? 1 : 0;
+    int64_t blocks = std::min<int64_t>((p.ntiles + 7) / 8, (int64_t)h->num_sms * 8);
+    permute_rows<<<(unsigned)std::max<int64_t>(blocks, 1), threads, 0, h->stream>>>(T, R, Rin, p);
+    ND_LAUNCHED(h);
+    return nd_cuda_check(h, cudaGetLastError(), "permute_rows");
+  }
+  // transpose: i = T group 0, j = T group gperm[0]
+  int q = gperm[0];
+  p.d0 = gd[0];
+  p.dq = gd[q];
+  p.rs_i = rs[0];
+  p.ts_j = ts[q];
+  p.q = q;
+  p.nb = 0;
+  for (int g = 1; g < ng; ++g) {
+    if (g == q) continue;
+    p.bdim[p.nb] = gd[g]; p.bts[p.nb] = ts[g]; p.brs[p.nb] = rs[g]; p.bcoord[p.nb] = g; p.nb++;
+  }
+  p.ntile_i = (p.d0 + TI - 1) / TI;
+  p.ntile_j = (p.dq + TJ - 1) / TJ;
+  int64_t nbatch = total / (p.d0 * p.dq);
+  p.ntiles = p.ntile_i * p.ntile_j * nbatch;
+  bool rvec = ((uintptr_t)R % 16 == 0) && (p.rs_i % 2 == 0);
+  for (int b = 0; b < p.nb; ++b) if (p.brs[b] % 2) rvec = false;
+  p.vec = rvec ? 1 : 0;
+
+  auto enc = encode_fn();
+  bool tma_ok = enc && ng <= 5 && (p.d0 % 2 == 0) && ((uintptr_t)T % 16 == 0);
+  for (int g = 0; g < ng && tma_ok; ++g) if (gd[g] > (int64_t)0x7fffffff) tma_ok = false;
+  if (tma_ok) {
+    CUtensorMap tmap;
+    cuuint64_t gdim[5] = {1, 1, 1, 1, 1};
+    cuuint64_t gstride[4] = {0, 0, 0, 0};
+    cuuint32_t box[5] = {1, 1, 1, 1, 1};
+    cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    for (int g = 0; g < 5; ++g) gdim[g] = g < ng ? (cuuint64_t)gd[g] : 1;
+    for (int g = 1; g < 5; ++g) {
+      int64_t st = g < ng ? ts[g] * 8 : ts[ng - 1] * gd[ng - 1] * 8;
+      gstride[g - 1] = (cuuint64_t)st;
+    }
+    box[0] = BOX_I;
+    box[q] = TJ;
+    CUresult r = enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, (void*)T, gdim, gstride, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r == CUDA_SUCCESS) {
+      size_t smem = STAGES * TILE_BYTES + 1024;
+      static bool attr_set = false;
+      if (!attr_set) {
+        cudaFuncSetAttribute(permute_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = true;
+      }
+      int64_t blocks = std::min<int64_t>(p.ntiles, (int64_t)h->num_sms * 3);
+      permute_tma<<<(unsigned)blocks, threads, smem, h->stream>>>(tmap, R, Rin, p, h->d_status);
+      ND_LAUNCHED(h);
+      return nd_cuda_check(h, cudaGetLastError(), "permute_tma");
+    }
+  }
+  int64_t blocks = std::min<int64_t>(p.ntiles, (int64_t)h->num_sms * 8);
+  permute_tiles<<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "permute_tiles");
+}
+
+extern "C" nd_status nd_permutedims_f64(nd_handle h, double* R, const double* T, int32_t rank,
+                                        const int64_t* dimsT, const int32_t* perm, double alpha, double beta) {
+  if (!h) return ND_ERR_ARG;
+  if (rank < 0 || rank > ND_MAX_RANK) return nd_fail(h, ND_ERR_ARG, "permutedims: rank %d out of range", rank);
+  if (rank > 0 && (!dimsT || !perm)) return nd_fail(h, ND_ERR_ARG, "permutedims: NULL dims/perm");
+  int p0[ND_MAX_RANK];
+  bool seen[ND_MAX_RANK] = {false};
+  int64_t total = 1;
+  for (int k = 0; k < rank; ++k) {
+    if (dimsT[k] < 0) return nd_fail(h, ND_ERR_ARG, "permutedims: negative dim");
+    total *= dimsT[k];
+    int v = perm[k] - 1;
+    if (v < 0 || v >= rank || seen[v]) return nd_fail(h, ND_ERR_ARG, "permutedims: perm is not a permutation of 1..%d", rank);
+    seen[v] = true;
+    p0[k] = v;
+  }
+  if (total > 0 && (!R || !T)) return nd_fail(h, ND_ERR_ARG, "permutedims: NULL data pointer");
+  if (R == T && total > 1) return nd_fail(h, ND_ERR_ARG, "permutedims: R and T must not alias");
+  int64_t d1[1] = {1};
+  return nd_launch_permute(h, R, T, rank, rank ? dimsT : d1, p0, alpha, beta, nullptr);
+}

@@ -1,0 +1,17 @@
+"""ndtensors_gb300: the NDTensors contraction hot path on GB300 (sm_103a).
+
+Python host mirror of NDTensors' storage / contraction / factorization
+interface, calling libndtensors_gb300.so through its C ABI.  No CPU fallback:
+every operation runs in the library's CUDA kernels.
+"""
+from ._lib import NDError, NoConvergence, PRECISIONS, handle, load, LIB_PATH
+from .tensors import BlockSparseTensor, DenseTensor, blockoffsets
+from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
+                       get_plan, permutedims, permutedims_, permutedims_blocksparse)
+
+__all__ = [
+    "NDError", "NoConvergence", "PRECISIONS", "handle", "load", "LIB_PATH",
+    "BlockSparseTensor", "DenseTensor", "blockoffsets",
+    "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
+    "permutedims", "permutedims_", "permutedims_blocksparse",
+]

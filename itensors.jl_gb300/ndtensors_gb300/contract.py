@@ -1,0 +1,194 @@
+"""NDTensors' contraction interface on the GB300 library.
+
+Mirrors, name for name:
+  contract(T1, labelsT1, T2, labelsT2[, labelsR])      NDTensors/src/tensoroperations/generic_tensor_operations.jl:87-118
+  contract!(R, labelsR, T1, labelsT1, T2, labelsT2, a, b)  NDTensors/src/dense/tensoralgebra/contract.jl:160-216
+  contract_labels(labelsT1, labelsT2)                  NDTensors/src/tensoroperations/contraction_logic.jl:5-34
+  permutedims(T, perm), permutedims!(R, T, perm)       NDTensors/src/dense/densetensor.jl:212-275
+  contract / contraction_output for BlockSparse        NDTensors/src/blocksparse/contract.jl:3-55
+Python cannot use "!" in names: ``contract_`` is ``contract!``.
+``precision`` is "fp64" (drop-in), "ozaki" or "bf16x3".
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from ._lib import MAX_RANK, PRECISIONS, BsDesc, handle, i32arr, i64arr
+from .tensors import BlockSparseTensor, DenseTensor, blockoffsets
+
+
+def contract_labels(l1, l2):
+    """Positive labels of T1 then of T2 (contraction_logic.jl:16-34)."""
+    return tuple([l for l in l1 if l > 0] + [l for l in l2 if l > 0])
+
+
+def _prec(p):
+    if isinstance(p, int):
+        return p
+    try:
+        return PRECISIONS[p]
+    except KeyError:
+        raise ValueError(f"unknown precision {p!r}; expected one of {sorted(PRECISIONS)}")
+
+
+def _out_dims(d1, l1, d2, l2, lr):
+    out = []
+    for l in lr:
+        if l in l1:
+            out.append(d1[l1.index(l)])
+        elif l in l2:
+            out.append(d2[l2.index(l)])
+        else:
+            raise ValueError(f"output label {l} appears in neither input")
+    return tuple(out)
+
+
+# ---------------------------------------------------------------------------
+# dense
+# ---------------------------------------------------------------------------
+
+def permutedims_(R: DenseTensor, T: DenseTensor, perm, alpha=1.0, beta=0.0):
+    """permutedims!(R, T, perm) with R = beta*R + alpha*permutedims(T, perm); perm is 1-based."""
+    perm = tuple(int(p) for p in perm)
+    if tuple(T.dims[p - 1] for p in perm) != tuple(R.dims):
+        raise ValueError("permutedims!: R dims do not match permuted T dims")
+    h = handle(T.data.device.index or 0)
+    h.call("nd_permutedims_f64", C.c_void_p(R.ptr()), C.c_void_p(T.ptr()), len(T.dims), i64arr(T.dims),
+           i32arr(perm), float(alpha), float(beta))
+    return R
+
+
+def permutedims(T: DenseTensor, perm):
+    perm = tuple(int(p) for p in perm)
+    R = DenseTensor.empty(tuple(T.dims[p - 1] for p in perm), T.data.device.index or 0)
+    return permutedims_(R, T, perm)
+
+
+def contract_(R: DenseTensor, labelsR, T1: DenseTensor, labels1, T2: DenseTensor, labels2,
+              alpha=1.0, beta=0.0, precision="fp64"):
+    """contract!(R, labelsR, T1, labelsT1, T2, labelsT2, alpha, beta) for Dense storage."""
+    lr, l1, l2 = tuple(labelsR), tuple(labels1), tuple(labels2)
+    if len(lr) != len(R.dims) or len(l1) != len(T1.dims) or len(l2) != len(T2.dims):
+        raise ValueError("contract!: number of labels does not match the tensor ranks")
+    h = handle(T1.data.device.index or 0)
+    h.call("nd_contract_dense_f64",
+           C.c_void_p(R.ptr()), len(R.dims), i64arr(R.dims), i32arr(lr),
+           C.c_void_p(T1.ptr()), len(T1.dims), i64arr(T1.dims), i32arr(l1),
+           C.c_void_p(T2.ptr()), len(T2.dims), i64arr(T2.dims), i32arr(l2),
+           float(alpha), float(beta), _prec(precision))
+    return R
+
+
+# ---------------------------------------------------------------------------
+# block sparse
+# ---------------------------------------------------------------------------
+
+class ContractionPlan:
+    """Device-built block plan (contract_blockoffsets, contract_sequential.jl:1-41)."""
+
+    def __init__(self, T1: BlockSparseTensor, l1, T2: BlockSparseTensor, l2, lr):
+        self.l1, self.l2, self.lr = tuple(l1), tuple(l2), tuple(lr)
+        if len(self.l1) != T1.rank or len(self.l2) != T2.rank:
+            raise ValueError("contract: number of labels does not match the tensor ranks")
+        self.h = handle(T1.data.device.index or 0)
+        d1, d2 = T1.desc(), T2.desc()
+        self.ptr = C.c_void_p()
+        self.h.call("nd_bs_plan_create", C.byref(d1), i32arr(self.l1), C.byref(d2), i32arr(self.l2),
+                    len(self.lr), i32arr(self.lr), C.byref(self.ptr))
+        npairs, nR, nnzR = C.c_int32(), C.c_int32(), C.c_int64()
+        self.h._check(self.h.lib.nd_bs_plan_sizes(self.ptr, C.byref(npairs), C.byref(nR), C.byref(nnzR)))
+        self.npairs, self.nblocksR, self.nnzR = npairs.value, nR.value, nnzR.value
+        rank = len(self.lr)
+        br = (C.c_int32 * max(1, self.nblocksR * rank))()
+        of = (C.c_int64 * max(1, self.nblocksR))()
+        pr = (C.c_int32 * max(1, 3 * self.npairs))()
+        self.h._check(self.h.lib.nd_bs_plan_get(self.ptr, br, of, pr))
+        self.blocksR = [tuple(br[i * rank:(i + 1) * rank]) for i in range(self.nblocksR)]
+        self.offsetsR = list(of[:self.nblocksR])
+        self.pairs = [tuple(pr[3 * i:3 * i + 3]) for i in range(self.npairs)]
+        self.indsR = [tuple(T1.inds[self.l1.index(l)]) if l in self.l1 else tuple(T2.inds[self.l2.index(l)])
+                      for l in self.lr]
+        self.T1_key, self.T2_key = T1.structure_key(), T2.structure_key()
+
+    def flops(self, T1, T2):
+        tot = 0
+        for (i1, i2, _) in self.pairs:
+            d1 = T1.blockdims(T1.blocks[i1])
+            d2 = T2.blockdims(T2.blocks[i2])
+            m = 1
+            k = 1
+            for d, l in zip(d1, self.l1):
+                if l in self.l2:
+                    k *= d
+                else:
+                    m *= d
+            n = 1
+            for d, l in zip(d2, self.l2):
+                if l not in self.l1:
+                    n *= d
+            tot += 2 * m * n * k
+        return tot
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                self.h.lib.nd_bs_plan_destroy(self.ptr)
+        except Exception:
+            pass
+
+
+_plan_cache = {}
+
+
+def get_plan(T1, l1, T2, l2, lr):
+    key = (T1.structure_key(), tuple(l1), T2.structure_key(), tuple(l2), tuple(lr))
+    p = _plan_cache.get(key)
+    if p is None:
+        p = ContractionPlan(T1, l1, T2, l2, lr)
+        if len(_plan_cache) > 256:
+            _plan_cache.clear()
+        _plan_cache[key] = p
+    return p
+
+
+def contract_blocksparse(T1, l1, T2, l2, lr=None, alpha=1.0, precision="fp64", plan=None, out=None):
+    l1, l2 = tuple(l1), tuple(l2)
+    lr = contract_labels(l1, l2) if lr is None else tuple(lr)
+    plan = plan or get_plan(T1, l1, T2, l2, lr)
+    R = out
+    if R is None:
+        import torch
+        data = torch.empty(max(plan.nnzR, 1), dtype=torch.float64, device=T1.data.device)[:plan.nnzR]
+        R = BlockSparseTensor(list(plan.indsR), list(plan.blocksR), list(plan.offsetsR), data)
+    if plan.npairs:
+        plan.h.call("nd_bs_contract_f64", plan.ptr, C.c_void_p(R.data.data_ptr()), C.c_void_p(T1.data.data_ptr()),
+                    C.c_void_p(T2.data.data_ptr()), float(alpha), _prec(precision))
+    return R
+
+
+def contract(T1, labels1, T2, labels2, labelsR=None, precision="fp64"):
+    """contract(T1, labelsT1, T2, labelsT2[, labelsR]) for Dense or BlockSparse storage."""
+    l1, l2 = tuple(labels1), tuple(labels2)
+    lr = contract_labels(l1, l2) if labelsR is None else tuple(labelsR)
+    if isinstance(T1, BlockSparseTensor) and isinstance(T2, BlockSparseTensor):
+        return contract_blocksparse(T1, l1, T2, l2, lr, precision=precision)
+    if isinstance(T1, DenseTensor) and isinstance(T2, DenseTensor):
+        R = DenseTensor.empty(_out_dims(T1.dims, l1, T2.dims, l2, lr), T1.data.device.index or 0)
+        return contract_(R, lr, T1, l1, T2, l2, 1.0, 0.0, precision)
+    raise TypeError("contract: both tensors must be Dense or both BlockSparse")
+
+
+def permutedims_blocksparse(T: BlockSparseTensor, perm):
+    """Block-sparse permutedims (blocksparsetensor.jl:465-470, blockoffsets.jl:103-111)."""
+    import torch
+    p0 = [int(p) - 1 for p in perm]
+    inds = [T.inds[k] for k in p0]
+    blocks = [tuple(b[k] for k in p0) for b in T.blocks]
+    offs, nnz = blockoffsets(blocks, inds)
+    R = BlockSparseTensor(inds, blocks, offs, torch.empty(max(nnz, 1), dtype=torch.float64,
+                                                          device=T.data.device)[:nnz])
+    h = handle(T.data.device.index or 0)
+    d = T.desc()
+    h.call("nd_bs_permutedims_f64", C.byref(d), C.c_void_p(T.data.data_ptr()), i32arr([int(p) for p in perm]),
+           i64arr(offs), C.c_void_p(R.data.data_ptr()))
+    return R

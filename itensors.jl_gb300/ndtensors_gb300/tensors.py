@@ -1,0 +1,135 @@
+"""Device tensors with NDTensors' storage conventions.
+
+DenseTensor        dims + one column-major FP64 vector (NDTensors Dense, dense/dense.jl:5-18)
+BlockSparseTensor  per-dimension block dims + ordered nonzero blocks (1-based) +
+                   0-based offsets into one FP64 vector (BlockSparse,
+                   blocksparse/blocksparse.jl:5-13; BlockOffsets, blockoffsets.jl:11)
+
+Data live in torch CUDA float64 tensors; torch is only the allocator here.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _prod(xs):
+    p = 1
+    for x in xs:
+        p *= int(x)
+    return p
+
+
+@dataclass
+class DenseTensor:
+    dims: tuple
+    data: object          # torch.float64 CUDA 1-D, column-major
+
+    @property
+    def rank(self):
+        return len(self.dims)
+
+    @property
+    def nnz(self):
+        return _prod(self.dims)
+
+    @classmethod
+    def empty(cls, dims, device=0):
+        torch = _torch()
+        return cls(tuple(int(d) for d in dims),
+                   torch.empty(max(1, _prod(dims)), dtype=torch.float64, device=f"cuda:{device}")[:_prod(dims)])
+
+    @classmethod
+    def from_numpy(cls, arr, device=0):
+        torch = _torch()
+        arr = np.asarray(arr, dtype=np.float64)
+        flat = np.ascontiguousarray(arr.reshape(-1, order="F"))
+        return cls(tuple(arr.shape), torch.from_numpy(flat).to(f"cuda:{device}"))
+
+    def to_numpy(self):
+        return self.data.detach().cpu().numpy().reshape(self.dims, order="F")
+
+    def ptr(self):
+        return self.data.data_ptr()
+
+
+def blockoffsets(blocks, inds):
+    """Offsets in list order (NDTensors/src/blocksparse/blockoffsets.jl:70-79)."""
+    offs, nnz = [], 0
+    for b in blocks:
+        offs.append(nnz)
+        nnz += _prod(inds[k][b[k] - 1] for k in range(len(inds)))
+    return offs, nnz
+
+
+@dataclass
+class BlockSparseTensor:
+    inds: list            # per dimension: tuple of block dims
+    blocks: list          # list of 1-based tuples, storage order
+    offsets: list
+    data: object          # torch.float64 CUDA 1-D
+    _key: tuple = field(default=None, repr=False)
+
+    @property
+    def rank(self):
+        return len(self.inds)
+
+    @property
+    def nnz(self):
+        return int(self.data.numel())
+
+    @property
+    def nnzblocks(self):
+        return len(self.blocks)
+
+    def blockdims(self, block):
+        return tuple(self.inds[k][block[k] - 1] for k in range(self.rank))
+
+    def structure_key(self):
+        if self._key is None:
+            self._key = (tuple(tuple(i) for i in self.inds), tuple(tuple(b) for b in self.blocks),
+                         tuple(self.offsets))
+        return self._key
+
+    @classmethod
+    def empty(cls, inds, blocks, device=0):
+        torch = _torch()
+        inds = [tuple(int(x) for x in i) for i in inds]
+        blocks = [tuple(int(x) for x in b) for b in blocks]
+        offs, nnz = blockoffsets(blocks, inds)
+        return cls(inds, blocks, offs, torch.empty(max(nnz, 1), dtype=torch.float64,
+                                                   device=f"cuda:{device}")[:nnz])
+
+    @classmethod
+    def from_oracle(cls, t, device=0):
+        """From an oracle.blocksparse.BlockSparseTensor (host numpy)."""
+        torch = _torch()
+        return cls([tuple(i) for i in t.inds], [tuple(b) for b in t.blocks], list(t.offsets),
+                   torch.from_numpy(np.ascontiguousarray(t.data, dtype=np.float64)).to(f"cuda:{device}"))
+
+    def data_numpy(self):
+        return self.data.detach().cpu().numpy()
+
+    def blockview(self, i):
+        b = self.blocks[i]
+        d = self.blockdims(b)
+        n = _prod(d)
+        return self.data[self.offsets[i]:self.offsets[i] + n]
+
+    def desc(self):
+        """nd_bs_desc for the C ABI (keeps the ctypes arrays alive on the object)."""
+        from ._lib import BsDesc, i32arr, i64arr
+        nb = i32arr([len(i) for i in self.inds])
+        bd = i64arr([d for i in self.inds for d in i])
+        bl = i32arr([x for b in self.blocks for x in b])
+        of = i64arr(self.offsets)
+        d = BsDesc(self.rank, nb, bd, len(self.blocks), bl, of)
+        d._keep = (nb, bd, bl, of)
+        return d

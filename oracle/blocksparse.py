@@ -1,0 +1,269 @@
+"""Block-sparse storage and contraction (oracle restatement).
+
+Storage follows NDTensors: one flat data vector plus an insertion-ordered map
+block -> 0-based offset; each block is a dense column-major array of
+``prod(blockdims)`` elements (NDTensors/src/blocksparse/blocksparse.jl:5-13,
+blockoffsets.jl:11,70-79).  Blocks are 1-based tuples (block.jl:5-16).
+
+Follows:
+  NDTensors/src/blocksparse/contract.jl:3-55              contract / contraction_output
+  NDTensors/src/blocksparse/contract_sequential.jl:1-41   sequential block plan (bit-exact order)
+  NDTensors/src/blocksparse/contract_utilities.jl:28-91   label maps, block matching, blockR
+  NDTensors/src/blocksparse/contract_generic.jl:37-129    grouped execution, beta = 0 then 1
+  NDTensors/src/blocksparse/blockoffsets.jl:103-111       permutedims of block offsets
+  NDTensors/src/blocksparse/blocksparsetensor.jl:834-881  permutedims! per block
+  NDTensors/src/blocksparse/blocksparsetensor.jl:537-638  permutedims_combine (matricization)
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .dense import contract as dense_contract
+from .labels import check_labels, contract_labels, find_matching_positions
+
+
+def _bdims(inds, block):
+    return tuple(inds[k][block[k] - 1] for k in range(len(inds)))
+
+
+@dataclass
+class BlockSparseTensor:
+    """inds: list (per dimension) of block-dim tuples; blocks: list of 1-based tuples."""
+    inds: list
+    blocks: list
+    offsets: list
+    data: np.ndarray
+
+    @property
+    def rank(self):
+        return len(self.inds)
+
+    @property
+    def nnz(self):
+        return int(sum(np.prod(_bdims(self.inds, b)) for b in self.blocks))
+
+    def blockdims(self, block):
+        return _bdims(self.inds, block)
+
+    def block_index(self, block):
+        return self.blocks.index(tuple(block))
+
+    def blockview(self, i):
+        b = self.blocks[i]
+        d = self.blockdims(b)
+        n = int(np.prod(d)) if d else 1
+        off = self.offsets[i]
+        return self.data[off:off + n].reshape(d, order="F")
+
+    def to_dense(self):
+        full = np.zeros([sum(ix) for ix in self.inds])
+        for i, b in enumerate(self.blocks):
+            sl = []
+            for k, bk in enumerate(b):
+                start = sum(self.inds[k][:bk - 1])
+                sl.append(slice(start, start + self.inds[k][bk - 1]))
+            full[tuple(sl)] = self.blockview(i)
+        return full
+
+
+def blockoffsets(blocks, inds):
+    """Offsets in list order (blockoffsets.jl:70-79)."""
+    offs, nnz = [], 0
+    for b in blocks:
+        offs.append(nnz)
+        nnz += int(np.prod(_bdims(inds, b)))
+    return offs, nnz
+
+
+def random_blocksparse(rng, inds, blocks):
+    offs, nnz = blockoffsets(blocks, inds)
+    return BlockSparseTensor(list(map(tuple, inds)), [tuple(b) for b in blocks], offs,
+                             rng.standard_normal(nnz))
+
+
+def are_blocks_contracted(b1, b2, l1_to_l2):
+    """contract_utilities.jl:57-70."""
+    for i1, i2 in enumerate(l1_to_l2):
+        if i2 > 0 and b1[i1] != b2[i2 - 1]:
+            return False
+    return True
+
+
+def contract_blocks(b1, l1_to_lr, b2, l2_to_lr, nr):
+    """contract_utilities.jl:72-91."""
+    br = [0] * nr
+    for i1, ir in enumerate(l1_to_lr):
+        if ir > 0:
+            br[ir - 1] = b1[i1]
+    for i2, ir in enumerate(l2_to_lr):
+        if ir > 0:
+            br[ir - 1] = b2[i2]
+    return tuple(br)
+
+
+def contract_inds_dims(inds1, l1, inds2, l2, lr):
+    out = []
+    for l in lr:
+        out.append(inds1[l1.index(l)] if l in l1 else inds2[l2.index(l)])
+    return out
+
+
+def contract_blockoffsets(t1, l1, t2, l2, lr):
+    """Sequential plan: (blocksR, offsetsR, nnzR, plan) with plan entries
+    (i1, i2, iR) as 0-based indices into the block lists
+    (contract_sequential.jl:1-41)."""
+    l1_to_l2 = find_matching_positions(l1, l2)
+    l1_to_lr = find_matching_positions(l1, lr)
+    l2_to_lr = find_matching_positions(l2, lr)
+    indsr = contract_inds_dims(t1.inds, l1, t2.inds, l2, lr)
+    blocks_r, offs_r, index_r = [], [], {}
+    nnz_r = 0
+    plan = []
+    for i1, b1 in enumerate(t1.blocks):
+        for i2, b2 in enumerate(t2.blocks):
+            if are_blocks_contracted(b1, b2, l1_to_l2):
+                br = contract_blocks(b1, l1_to_lr, b2, l2_to_lr, len(lr))
+                if br not in index_r:
+                    index_r[br] = len(blocks_r)
+                    blocks_r.append(br)
+                    offs_r.append(nnz_r)
+                    nnz_r += int(np.prod(_bdims(indsr, br))) if br else 1
+                plan.append((i1, i2, index_r[br]))
+    return indsr, blocks_r, offs_r, nnz_r, plan
+
+
+def contract(t1, l1, t2, l2, lr=None, alpha=1.0):
+    """Block-sparse contract (contract.jl:3-17 + contract_generic.jl:37-129).
+
+    Pairs are grouped by output block in output-block order; within a group the
+    first pair overwrites (beta = 0) and the rest accumulate (beta = 1).
+    """
+    l1, l2 = tuple(l1), tuple(l2)
+    if lr is None:
+        lr = contract_labels(l1, l2)
+    lr = tuple(lr)
+    check_labels(l1, l2, lr)
+    indsr, blocks_r, offs_r, nnz_r, plan = contract_blockoffsets(t1, l1, t2, l2, lr)
+    r = BlockSparseTensor(indsr, blocks_r, offs_r, np.empty(nnz_r))
+    groups = [[] for _ in blocks_r]
+    for p in plan:
+        groups[p[2]].append(p)
+    for g in groups:
+        beta = 0.0
+        for (i1, i2, ir) in g:
+            rv = r.blockview(ir)
+            dense_contract(t1.blockview(i1), l1, t2.blockview(i2), l2, lr, alpha=alpha,
+                           beta=beta, r=rv)
+            beta = 1.0
+    return r, plan
+
+
+def permutedims(t, perm1):
+    """Block-sparse permutedims (blockoffsets.jl:103-111, blocksparsetensor.jl:465-470,834-881).
+
+    Blocks keep their order; block coordinates and dims are permuted and the
+    offsets are recomputed in that order.
+    """
+    p0 = [p - 1 for p in perm1]
+    inds = [t.inds[k] for k in p0]
+    blocks = [tuple(b[k] for k in p0) for b in t.blocks]
+    offs, nnz = blockoffsets(blocks, inds)
+    r = BlockSparseTensor(inds, blocks, offs, np.empty(nnz))
+    for i in range(len(blocks)):
+        r.blockview(i)[...] = np.transpose(t.blockview(i), p0)
+    return r
+
+
+def flops_of_plan(t1, l1, t2, l2, plan):
+    """Algorithmic flops: sum over pairs of 2*M*N*K."""
+    tot = 0
+    for (i1, i2, _) in plan:
+        d1 = t1.blockdims(t1.blocks[i1])
+        d2 = t2.blockdims(t2.blocks[i2])
+        m = int(np.prod([d for d, l in zip(d1, l1) if l > 0]))
+        k = int(np.prod([d for d, l in zip(d1, l1) if l < 0]))
+        n = int(np.prod([d for d, l in zip(d2, l2) if l > 0]))
+        tot += 2 * m * n * k
+    return tot
+
+
+# --------------------------------------------------------------------------
+# Combiner matricization (blocksparsetensor.jl:537-638, qnindex.jl:407-426)
+# --------------------------------------------------------------------------
+
+def _colmajor_linear(block_sub, nblocks_sub):
+    """LinearIndices(nblocks)[block...] (1-based), first dimension fastest."""
+    lin, mul = 0, 1
+    for b, n in zip(block_sub, nblocks_sub):
+        lin += (b - 1) * mul
+        mul *= n
+    return lin + 1
+
+
+def _isblockless_key(b):
+    """isblockless = CartesianIndex ordering: last dimension most significant
+    (blockoffsets.jl:35-37)."""
+    return tuple(reversed(b))
+
+
+def matricize(t, qinds, row_dims, col_dims):
+    """Fuse a QN block-sparse tensor into a 2-index block matrix.
+
+    Reproduces the structure ITensor's ``svd``/``qr`` build with two combiners
+    (src/tensor_operations/matrix_decomposition.jl:153-160): the row group and the
+    column group are each fused (first index fastest), their sectors are stably
+    sorted by charge and merged (combineblocks), and sub-blocks are placed at
+    consecutive offsets inside the merged block in sorted order.  The resulting
+    block list is ordered by isblockless (column block most significant).
+
+    ``qinds``: list of oracle.qn.QNIndex for every dimension of ``t``.
+    Returns (BlockSparseTensor matrix, row_info, col_info) where *_info holds the
+    combined sectors (charge, dim) plus, for every original block-combination of
+    the group, its (combined block, offset inside it).
+    """
+    from .qn import combineblocks, fuse
+
+    def group_info(dims):
+        idx = [qinds[d] for d in dims]
+        fused = fuse(idx)
+        csec, perm, comb = combineblocks(fused.sectors)
+        # position of each uncombined product block: combined block + offset
+        place = {}
+        for pos, orig in enumerate(perm):         # pos: sorted position (0-based), orig: 1-based
+            cb = comb[pos]
+            off = 0
+            q = pos - 1
+            while q >= 0 and comb[q] == cb:
+                off += fused.sectors[perm[q] - 1][1]
+                q -= 1
+            place[orig] = (cb, off)
+        return fused, csec, place
+
+    rfused, rsec, rplace = group_info(row_dims)
+    cfused, csec, cplace = group_info(col_dims)
+    nb_rows = [qinds[d].nblocks for d in row_dims]
+    nb_cols = [qinds[d].nblocks for d in col_dims]
+    entries = {}
+    for i, b in enumerate(t.blocks):
+        lr_ = _colmajor_linear([b[d] for d in row_dims], nb_rows)
+        lc_ = _colmajor_linear([b[d] for d in col_dims], nb_cols)
+        rb, roff = rplace[lr_]
+        cb, coff = cplace[lc_]
+        entries.setdefault((rb, cb), []).append((i, roff, coff))
+    mblocks = sorted(entries.keys(), key=_isblockless_key)
+    minds = [tuple(d for _, d in rsec), tuple(d for _, d in csec)]
+    offs, nnz = blockoffsets(mblocks, minds)
+    m = BlockSparseTensor(minds, mblocks, offs, np.zeros(nnz))
+    for j, mb in enumerate(mblocks):
+        view = m.blockview(j)
+        for (i, roff, coff) in entries[mb]:
+            blk = t.blockview(i)
+            bd = blk.shape
+            rdim = int(np.prod([bd[d] for d in row_dims]))
+            cdim = int(np.prod([bd[d] for d in col_dims]))
+            mat = np.transpose(blk, list(row_dims) + list(col_dims)).reshape(
+                (rdim, cdim), order="F")
+            view[roff:roff + rdim, coff:coff + cdim] = mat
+    return m, (rsec, rplace), (csec, cplace)

@@ -1,0 +1,135 @@
+"""Block-sparse contraction on the GPU vs the oracle (GPU).
+
+Structure (pair list, output blocks, offsets) must be bit-exact with the
+reference's sequential plan; values within the precision's tolerance
+(relative Frobenius error vs the FP64 oracle): fp64 1e-13, ozaki 1e-10,
+bf16x3 1e-4.
+"""
+import numpy as np
+import pytest
+
+from oracle import blocksparse as obs
+from oracle import dense as odense
+from oracle import networks, qn
+
+pytestmark = pytest.mark.gpu
+TOL = {"fp64": 1e-13, "ozaki": 1e-10, "bf16x3": 1e-4}
+
+
+def _q(secs, arrow=1, tag="x", prime=0):
+    return qn.QNIndex(tuple((int(a), int(b)) for a, b in secs), arrow, tag, prime)
+
+
+def _check(nd, A, la, B, lb, lr, precision="fp64"):
+    ref, plan = obs.contract(A, la, B, lb, lr)
+    GA, GB = nd.BlockSparseTensor.from_oracle(A), nd.BlockSparseTensor.from_oracle(B)
+    p = nd.get_plan(GA, la, GB, lb, lr)
+    # bit-exact structure
+    assert p.pairs == [tuple(x) for x in plan]
+    assert p.blocksR == [tuple(b) for b in ref.blocks]
+    assert p.offsetsR == list(ref.offsets)
+    assert p.nnzR == ref.nnz
+    R = nd.contract(GA, la, GB, lb, lr, precision=precision)
+    out = R.data_numpy()
+    if ref.nnz:
+        assert odense.rel_frobenius_error(out, ref.data) <= TOL[precision]
+    return p
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki", "bf16x3"])
+def test_qn_pair_workload(nd, precision):
+    A, B, _ = networks.qn_pair(2048)
+    p = _check(nd, A, (1, 2, -1), B, (-1, 3, 4), (1, 2, 3, 4), precision)
+    assert (p.npairs, p.nblocksR) == (62, 62)
+
+
+def test_multithreading_doc_structure(nd):
+    rng = np.random.default_rng(3)
+    d = 20
+    i1, i2 = _q([[0, d], [1, d]], 1, "i1"), _q([[0, d], [1, d]], 1, "i2")
+    inds = [i1.primed(), i2.primed(), i1.dag(), i2.dag()]
+    A = obs.random_blocksparse(rng, [x.dims for x in inds], qn.nzblocks(0, inds))
+    B = obs.random_blocksparse(rng, [x.dims for x in inds], qn.nzblocks(0, inds))
+    for prec in ("fp64", "ozaki"):
+        p = _check(nd, A, (1, 2, -1, -2), B, (-1, -2, 3, 4), (1, 2, 3, 4), prec)
+        assert p.npairs == 10                       # several pairs per output block
+
+
+def test_empty_result(nd):
+    inds = [[1, 1], [1, 1]]
+    A = obs.random_blocksparse(np.random.default_rng(4), inds, [(1, 1)])
+    B = obs.random_blocksparse(np.random.default_rng(5), inds, [(2, 2)])
+    p = _check(nd, A, (1, -1), B, (-1, 2), (1, 2))
+    assert p.npairs == 0 and p.nblocksR == 0 and p.nnzR == 0
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_structures(nd, seed):
+    """Random QN tensors, random label placement and output order (permuted blocks)."""
+    rng = np.random.default_rng(100 + seed)
+    nq = int(rng.integers(2, 5))
+    def idx(tag):
+        return _q([[q, int(rng.integers(1, 9))] for q in range(-nq, nq + 1)], 1, tag)
+    i, j, k, m = idx("i"), idx("j"), idx("k"), idx("m")
+    A_inds = [i, k.dag(), j]
+    B_inds = [m, k, j.dag()]
+    A = obs.random_blocksparse(rng, [x.dims for x in A_inds], qn.nzblocks(int(rng.integers(-1, 2)), A_inds))
+    B = obs.random_blocksparse(rng, [x.dims for x in B_inds], qn.nzblocks(0, B_inds))
+    la, lb = (1, -1, -2), (2, -1, -2)
+    lr = (2, 1) if seed % 2 else (1, 2)
+    for prec in ("fp64", "ozaki"):
+        _check(nd, A, la, B, lb, lr, prec)
+
+
+def test_heff_steps_blocksparse(nd):
+    net = networks.qn_heff(chi=256, seed=12)
+    st = networks.heff_steps()
+    t = net["psi"]
+    tensors = [(net["L"], st[0], True), (net["W1"], st[1], False), (net["W2"], st[2], False), (net["R"], st[3], False)]
+    cur = None
+    for (T, (l1, l2, lr), first) in tensors:
+        if first:
+            ref, _ = obs.contract(T, l1, t, l2, lr)
+            _check(nd, T, l1, t, l2, lr, "fp64")
+            _check(nd, T, l1, t, l2, lr, "ozaki")
+        else:
+            ref, _ = obs.contract(cur, l1, T, l2, lr)
+            _check(nd, cur, l1, T, l2, lr, "fp64")
+            _check(nd, cur, l1, T, l2, lr, "ozaki")
+        cur = ref
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_adjoint(nd, precision):
+    from oracle.adjoint import contract_pullback
+    A, B, _ = networks.qn_pair(256, seed=21)
+    la, lb, lr = (1, 2, -1), (-1, 3, 4), (1, 2, 3, 4)
+    R, plan = obs.contract(A, la, B, lb, lr)
+    rng = np.random.default_rng(22)
+    Rbar = obs.BlockSparseTensor(R.inds, R.blocks, R.offsets, rng.standard_normal(R.nnz))
+    # oracle pullback in dense form, projected on the block structures of A and B
+    Ad, Bd, Rbd = A.to_dense(), B.to_dense(), Rbar.to_dense()
+    gA, gB = contract_pullback(Ad, (1, 2, 5), Bd, (5, 3, 4), (1, 2, 3, 4), Rbd)
+    GA, GB = nd.BlockSparseTensor.from_oracle(A), nd.BlockSparseTensor.from_oracle(B)
+    p = nd.get_plan(GA, la, GB, lb, lr)
+    import torch
+    GR = torch.from_numpy(Rbar.data).cuda()
+    Abar = torch.full((A.nnz,), float("nan"), dtype=torch.float64, device="cuda")
+    Bbar = torch.full((B.nnz,), float("nan"), dtype=torch.float64, device="cuda")
+    import ctypes as C
+    from ndtensors_gb300._lib import PRECISIONS
+    p.h.call("nd_bs_contract_adjoint_f64", p.ptr, C.c_void_p(GR.data_ptr()), C.c_void_p(GA.data.data_ptr()),
+             C.c_void_p(GB.data.data_ptr()), C.c_void_p(Abar.data_ptr()), C.c_void_p(Bbar.data_ptr()),
+             PRECISIONS[precision])
+    Ab = obs.BlockSparseTensor(A.inds, A.blocks, A.offsets, Abar.cpu().numpy()).to_dense()
+    Bb = obs.BlockSparseTensor(B.inds, B.blocks, B.offsets, Bbar.cpu().numpy()).to_dense()
+    assert odense.rel_frobenius_error(Ab, gA) <= TOL[precision]
+    assert odense.rel_frobenius_error(Bb, gB) <= TOL[precision]
+
+
+def test_plan_rejects_mismatched_blocks(nd):
+    A = obs.random_blocksparse(np.random.default_rng(0), [[2, 3], [4, 5]], [(1, 1)])
+    B = obs.random_blocksparse(np.random.default_rng(0), [[4, 6], [2]], [(1, 1)])
+    with pytest.raises(nd.NDError):
+        nd.get_plan(nd.BlockSparseTensor.from_oracle(A), (1, -1), nd.BlockSparseTensor.from_oracle(B), (-1, 2),
+                    (1, 2))

@@ -1,0 +1,113 @@
+"""Dense contract! on the GPU vs the oracle (GPU).
+
+Tolerances (relative Frobenius error vs the FP64 oracle):
+  fp64   <= 1e-13   (the dense pair workload's bar)
+  ozaki  <= 1e-10
+  bf16x3 <= 1e-4
+"""
+import numpy as np
+import pytest
+
+from oracle import dense as odense
+from oracle import networks
+
+pytestmark = pytest.mark.gpu
+TOL = {"fp64": 1e-13, "ozaki": 1e-10, "bf16x3": 1e-4}
+
+
+def _run(nd, a, la, b, lb, lr, precision, alpha=1.0, beta=0.0, r0=None):
+    A = nd.DenseTensor.from_numpy(a)
+    B = nd.DenseTensor.from_numpy(b)
+    ref = odense.contract(a, la, b, lb, lr, alpha=alpha, beta=beta, r=None if r0 is None else r0.copy())
+    R = nd.DenseTensor.from_numpy(r0 if r0 is not None else np.full(ref.shape, np.nan))
+    nd.contract_(R, lr, A, la, B, lb, alpha, beta, precision)
+    return R.to_numpy(), ref
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki", "bf16x3"])
+def test_dense_pair_workload(nd, precision):
+    a, b = networks.dense_pair(seed=0)
+    out, ref = _run(nd, a, (1, 2, -1), b, (-1, 3, 4), (1, 2, 3, 4), precision)
+    assert odense.rel_frobenius_error(out, ref) <= TOL[precision]
+    # followed by permutedims to (s, a, c, t)
+    C = nd.DenseTensor.from_numpy(out)
+    P = nd.permutedims(C, (2, 1, 4, 3))
+    np.testing.assert_array_equal(P.to_numpy(), np.transpose(out, (1, 0, 3, 2)))
+
+
+# a shape matrix in the spirit of test/base/test_contract.jl:7-264
+SHAPES = [
+    ((3, 4), (1, -1), (4, 5), (-1, 2), (1, 2)),
+    ((3, 4), (-1, 1), (4, 5), (-1, 2), (2, 1)),
+    ((4, 3), (-1, 1), (5, 4), (2, -1), (1, 2)),
+    ((2, 3, 4), (1, -1, -2), (3, 4, 5), (-1, -2, 2), (1, 2)),
+    ((2, 3, 4), (-2, 1, -1), (4, 5, 2), (-1, 2, -2), (2, 1)),
+    ((6, 5, 4, 3), (1, -1, 2, -2), (3, 7, 5), (-2, 3, -1), (3, 2, 1)),
+    ((5, 4), (1, 2), (3,), (3,), (2, 3, 1)),                      # outer product
+    ((4, 5, 6), (-1, -2, -3), (6, 5, 4), (-3, -2, -1), ()),       # full contraction to a scalar
+    ((130, 70), (1, -1), (70, 200), (-1, 2), (1, 2)),
+    ((33, 65, 17), (1, -1, 2), (65, 19), (-1, 3), (3, 1, 2)),
+    ((129, 600), (1, -1), (600, 65), (-1, 2), (1, 2)),           # K spans two exact chunks
+]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki", "bf16x3"])
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: str(s[0]) + str(s[2]))
+def test_shape_matrix(nd, shape, precision):
+    da, la, db, lb, lr = shape
+    rng = np.random.default_rng(abs(hash(shape)) % 2**32)
+    a, b = rng.standard_normal(da), rng.standard_normal(db)
+    out, ref = _run(nd, a, la, b, lb, lr, precision)
+    assert odense.rel_frobenius_error(out, ref) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("alpha,beta", [(2.0, 0.0), (1.0, 1.0), (-0.5, 2.0), (0.0, 1.5)])
+def test_alpha_beta(nd, precision, alpha, beta):
+    rng = np.random.default_rng(5)
+    a, b, r0 = rng.standard_normal((20, 30)), rng.standard_normal((30, 40)), rng.standard_normal((20, 40))
+    out, ref = _run(nd, a, (1, -1), b, (-1, 2), (1, 2), precision, alpha, beta, r0)
+    assert odense.rel_frobenius_error(out, ref) <= TOL[precision]
+
+
+@pytest.mark.parametrize("lr", [(1, 2, 3), (2, 1, 3)])
+def test_scalar_branch_overwrites_nan(nd, lr):
+    # NDTensors/test/test_dense.jl:237-259
+    rng = np.random.default_rng(6)
+    t1 = rng.standard_normal((2, 2, 1))
+    t2 = rng.standard_normal((1, 1))
+    R = nd.DenseTensor.from_numpy(np.full((2, 2, 1), np.nan))
+    nd.contract_(R, lr, nd.DenseTensor.from_numpy(t1), (1, 2, -1), nd.DenseTensor.from_numpy(t2), (-1, 1))
+    ref = np.full((2, 2, 1), np.nan)
+    odense.contract_into(ref, lr, t1, (1, 2, -1), t2, (-1, 1))
+    assert not np.isnan(R.to_numpy()).any()
+    np.testing.assert_allclose(R.to_numpy(), ref, rtol=1e-15)
+
+
+def test_ozaki_adversarial_digits(nd):
+    # all digits at their extreme (+-128 patterns) stress exactness of FP32 accumulation in TMEM
+    rng = np.random.default_rng(7)
+    K = 1024
+    a = np.where(rng.random((128, K)) < 0.5, -1.0, 1.0) * (1 - 2.0 ** -40)
+    b = np.where(rng.random((K, 64)) < 0.5, -1.0, 1.0) * (1 - 2.0 ** -40)
+    out, ref = _run(nd, a, (1, -1), b, (-1, 2), (1, 2), "ozaki")
+    assert odense.rel_frobenius_error(out, ref) <= 1e-12
+
+
+def test_ozaki_wide_dynamic_range(nd):
+    rng = np.random.default_rng(8)
+    a = rng.standard_normal((200, 300)) * np.exp(rng.uniform(-20, 20, (200, 1)))
+    b = rng.standard_normal((300, 100)) * np.exp(rng.uniform(-20, 20, (1, 100)))
+    out, ref = _run(nd, a, (1, -1), b, (-1, 2), (1, 2), "ozaki")
+    assert odense.rel_frobenius_error(out, ref) <= 1e-10
+
+
+def test_bad_labels_rejected(nd):
+    a = nd.DenseTensor.from_numpy(np.ones((2, 3)))
+    b = nd.DenseTensor.from_numpy(np.ones((3, 4)))
+    r = nd.DenseTensor.from_numpy(np.ones((2, 4)))
+    with pytest.raises(nd.NDError):
+        nd.contract_(r, (1, 5), a, (1, -1), b, (-1, 2))
+    with pytest.raises(nd.NDError):
+        nd.contract_(nd.DenseTensor.from_numpy(np.ones((2, 4))), (1, 2), a, (1, -1),
+                     nd.DenseTensor.from_numpy(np.ones((4, 4))), (-1, 2))
