@@ -57,7 +57,7 @@ typedef struct nd_bs_plan_s *nd_plan;
 nd_status nd_create(int32_t device, nd_handle *out);
 nd_status nd_destroy(nd_handle h);
 const char *nd_last_error(nd_handle h);
-nd_status nd_set_stream(nd_handle h, void *cuda_stream);      /* NULL = library-owned stream */
+nd_status nd_set_stream(nd_handle h, void *cuda_stream);      /* NULL = legacy default stream */
 nd_status nd_get_stream(nd_handle h, void **cuda_stream);
 nd_status nd_sync(nd_handle h);
 nd_status nd_alloc(nd_handle h, size_t bytes, void **dptr);
@@ -69,6 +69,14 @@ nd_status nd_memset0(nd_handle h, void *dst, size_t bytes);
 nd_status nd_set_ozaki_slices(nd_handle h, int32_t slices);
 /* Count of kernel launches this handle enqueued so far (diagnostics). */
 nd_status nd_launch_count(nd_handle h, int64_t *count);
+/* Kernel timing: when enabled, every library kernel launch is bracketed by CUDA
+ * events on the handle's stream.  nd_profile_read synchronises, then reports per
+ * kernel name (up to `cap` entries, names copied into `names` as 64-byte
+ * NUL-terminated slots) the launch count and the summed device time in ms, and
+ * clears the records. */
+nd_status nd_profile_enable(nd_handle h, int32_t enable);
+nd_status nd_profile_read(nd_handle h, int32_t cap, char *names, int64_t *counts, double *total_ms,
+                          int32_t *n_out);
 
 /* ---- dense permutation --------------------------------------------------
  * R = beta*R + alpha*permutedims(T, perm), with the reference's rules: beta == 0
@@ -86,8 +94,8 @@ nd_status nd_permutedims_f64(nd_handle h, double *R, const double *T, int32_t ra
  * (NDTensors/src/dense/tensoralgebra/contract.jl:160-216), i.e. the cuTENSOR hook
  * NDTensors/ext/NDTensorscuTENSORExt/contract.jl:15-58 and the cuBLAS mul! of
  * NDTensors/ext/NDTensorsCUDAExt/mul.jl:7-47.  A one-element operand takes the
- * reference's scalar branch (contract.jl:100-150).  rel_err_estimate (nullable,
- * host) receives the a-priori error bound of the chosen precision. */
+ * reference's scalar branch (contract.jl:100-150).  The call synchronises the
+ * handle's stream before it returns. */
 nd_status nd_contract_dense_f64(nd_handle h,
                                 double *R, int32_t rankR, const int64_t *dimsR, const int32_t *labelsR,
                                 const double *A, int32_t rankA, const int64_t *dimsA, const int32_t *labelsA,

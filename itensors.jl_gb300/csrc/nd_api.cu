@@ -101,6 +101,8 @@ nd_status nd_destroy(nd_handle h) {
   cudaStreamSynchronize(h->stream);
   if (h->ws) cudaFree(h->ws);
   if (h->d_status) cudaFree(h->d_status);
+  for (auto& r : h->prof) { cudaEventDestroy(r.e0); cudaEventDestroy(r.e1); }
+  for (auto e : h->event_pool) cudaEventDestroy(e);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
   return ND_OK;
@@ -110,12 +112,14 @@ const char* nd_last_error(nd_handle h) { return h ? h->last_error.c_str() : g_no
 
 nd_status nd_set_stream(nd_handle h, void* s) {
   if (!h) return ND_ERR_ARG;
-  if (h->own_stream && s) { cudaStreamSynchronize(h->stream); cudaStreamDestroy(h->stream); h->own_stream = false; }
-  if (s) h->stream = (cudaStream_t)s;
-  else if (!h->own_stream) {
-    ND_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-    h->own_stream = true;
+  if (h->capturing) return nd_fail(h, ND_ERR_ARG, "nd_set_stream: cannot change streams during graph capture");
+  if ((cudaStream_t)s == h->stream) return ND_OK;
+  if (h->own_stream) {
+    ND_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaStreamDestroy(h->stream);
+    h->own_stream = false;
   }
+  h->stream = (cudaStream_t)s;   // NULL selects the legacy default stream, as everywhere in CUDA
   return ND_OK;
 }
 
@@ -179,6 +183,40 @@ nd_status nd_launch_count(nd_handle h, int64_t* c) {
   return ND_OK;
 }
 
+nd_status nd_profile_enable(nd_handle h, int32_t enable) {
+  if (!h) return ND_ERR_ARG;
+  h->profiling = enable != 0;
+  return ND_OK;
+}
+
+nd_status nd_profile_read(nd_handle h, int32_t cap, char* names, int64_t* counts, double* total_ms, int32_t* n_out) {
+  if (!h || !n_out) return ND_ERR_ARG;
+  ND_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<std::string> keys;
+  std::vector<int64_t> cnt;
+  std::vector<double> tot;
+  for (auto& r : h->prof) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.e0, r.e1);
+    size_t k = 0;
+    for (; k < keys.size(); ++k) if (keys[k] == r.name) break;
+    if (k == keys.size()) { keys.push_back(r.name); cnt.push_back(0); tot.push_back(0.0); }
+    cnt[k]++;
+    tot[k] += ms;
+    h->event_pool.push_back(r.e0);
+    h->event_pool.push_back(r.e1);
+  }
+  h->prof.clear();
+  int n = (int)keys.size();
+  for (int k = 0; k < n && k < cap; ++k) {
+    if (names) { strncpy(names + 64 * k, keys[k].c_str(), 63); names[64 * k + 63] = 0; }
+    if (counts) counts[k] = cnt[k];
+    if (total_ms) total_ms[k] = tot[k];
+  }
+  *n_out = n;
+  return ND_OK;
+}
+
 nd_status nd_graph_begin(nd_handle h) {
   if (!h) return ND_ERR_ARG;
   if (h->capturing) return nd_fail(h, ND_ERR_ARG, "nd_graph_begin: already capturing");
@@ -213,6 +251,23 @@ nd_status nd_graph_destroy(void* exec) {
 }
 
 }  // extern "C"
+
+void nd_prof_begin(nd_handle h, const char* name) {
+  if (!h->profiling || h->capturing) return;
+  auto get = [&]() {
+    if (!h->event_pool.empty()) { cudaEvent_t e = h->event_pool.back(); h->event_pool.pop_back(); return e; }
+    cudaEvent_t e; cudaEventCreate(&e); return e;
+  };
+  nd_context::ProfRec r{name, get(), get()};
+  cudaEventRecord(r.e0, h->stream);
+  h->prof.push_back(r);
+}
+
+void nd_prof_end(nd_handle h) {
+  if (!h->profiling || h->capturing || h->prof.empty()) return;
+  cudaEventRecord(h->prof.back().e1, h->stream);
+}
+
 
 // ---------------------------------------------------------------------------
 // Label roles: which dimensions of A and B are free / contracted and where the

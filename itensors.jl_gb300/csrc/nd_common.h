@@ -35,6 +35,11 @@ struct nd_context {
   // graph capture
   cudaGraph_t graph = nullptr;
   bool capturing = false;
+  // kernel timing
+  bool profiling = false;
+  struct ProfRec { const char* name; cudaEvent_t e0, e1; };
+  std::vector<ProfRec> prof;
+  std::vector<cudaEvent_t> event_pool;
 };
 
 // Host helpers -------------------------------------------------------------
@@ -50,6 +55,10 @@ nd_status nd_check_device_status(nd_handle h, const char* what);  // syncs
   } while (0)
 
 #define ND_LAUNCHED(h) do { (h)->launches++; } while (0)
+
+// Bracket a launch with timing events when profiling is on (not inside capture).
+void nd_prof_begin(nd_handle h, const char* name);
+void nd_prof_end(nd_handle h);
 
 // Mixed-radix index decomposition ------------------------------------------
 // A GEMM row / column / reduction index enumerates several tensor dimensions,

@@ -425,7 +425,9 @@ extern "C" nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan p, const do
     ND_CUDA(h, cudaMallocAsync(&d, ranges.size() * 8, h->stream));
     ND_CUDA(h, cudaMemcpyAsync(d, ranges.data(), ranges.size() * 8, cudaMemcpyHostToDevice, h->stream));
     int n = (int)(ranges.size() / 3);
+    nd_prof_begin(h, "zero_ranges");
     zero_ranges<<<dim3(64, std::min(n, 1024)), 256, 0, h->stream>>>(Abar, Bbar, d, n);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
     ND_CUDA(h, cudaFreeAsync(d, h->stream));
   }

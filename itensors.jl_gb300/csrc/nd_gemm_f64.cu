@@ -147,7 +147,9 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
   if (nitems == 0) return ND_OK;
   GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta};
   int blocks = std::min(nitems, h->num_sms * 4);
+  nd_prof_begin(h, "gemm_f64_grouped");
   gemm_f64_grouped<<<blocks, 128, 0, h->stream>>>(g);
+  nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "gemm_f64_grouped");
 }

@@ -572,7 +572,9 @@ nd_status launch_gemm(nd_handle h, const GemmArgs& g) {
     attr = true;
   }
   int blocks = std::min(g.nitems, h->num_sms);
+  nd_prof_begin(h, "split_gemm");
   split_gemm<S><<<blocks, NTHREADS, C::SMEM, h->stream>>>(g);
+  nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "split_gemm");
 }
@@ -674,7 +676,9 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
   }
   int pblocks = std::min(c.npack_items, h->num_sms * 6);
   if (pblocks > 0) {
+    nd_prof_begin(h, "pack_kernel");
     pack_kernel<<<pblocks, 256, psmem, h->stream>>>(pa);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
     ND_CUDA(h, cudaGetLastError());
   }

@@ -329,7 +329,9 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
   if (ng <= 1 || gperm[0] == 0) {
     // shared contiguous dim (or scalar / pure copy)
     if (total == 1) {
+      nd_prof_begin(h, "permute_scalar");
       permute_scalar<<<1, 32, 0, h->stream>>>(T, R, p);
+      nd_prof_end(h);
       ND_LAUNCHED(h);
       return nd_cuda_check(h, cudaGetLastError(), "permute_scalar");
     }
@@ -340,7 +342,9 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
     bool al = ((uintptr_t)T % 16 == 0) && ((uintptr_t)R % 16 == 0) && (p.d0 % 2 == 0);
     p.vec = al ? 1 : 0;
     int64_t blocks = std::min<int64_t>((p.ntiles + 7) / 8, (int64_t)h->num_sms * 8);
+    nd_prof_begin(h, "permute_rows");
     permute_rows<<<(unsigned)std::max<int64_t>(blocks, 1), threads, 0, h->stream>>>(T, R, Rin, p);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
     return nd_cuda_check(h, cudaGetLastError(), "permute_rows");
   }
@@ -391,13 +395,17 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
         attr_set = true;
       }
       int64_t blocks = std::min<int64_t>(p.ntiles, (int64_t)h->num_sms * 3);
+      nd_prof_begin(h, "permute_tma");
       permute_tma<<<(unsigned)blocks, threads, smem, h->stream>>>(tmap, R, Rin, p, h->d_status);
+      nd_prof_end(h);
       ND_LAUNCHED(h);
       return nd_cuda_check(h, cudaGetLastError(), "permute_tma");
     }
   }
   int64_t blocks = std::min<int64_t>(p.ntiles, (int64_t)h->num_sms * 8);
+  nd_prof_begin(h, "permute_tiles");
   permute_tiles<<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
+  nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "permute_tiles");
 }

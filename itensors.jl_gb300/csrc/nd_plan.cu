@@ -174,20 +174,30 @@ nd_status nd_device_exclusive_scan(nd_handle h, int64_t* data, int64_t n, int64_
   int64_t* last = nullptr;
   ND_CUDA(h, cudaMallocAsync(&sums, (nb + 2) * sizeof(int64_t), h->stream));
   last = sums + nb;
+  nd_prof_begin(h, "copy_last");
   copy_last<<<1, 32, 0, h->stream>>>(data, n, last);
+  nd_prof_end(h);
   ND_LAUNCHED(h);
   if (nb == 1) {
+    nd_prof_begin(h, "scan_apply");
     scan_apply<<<1, SCAN_BLOCK, 0, h->stream>>>(data, nullptr, n);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
   } else {
+    nd_prof_begin(h, "scan_block_sums");
     scan_block_sums<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(data, sums, n);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
     nd_status s = nd_device_exclusive_scan(h, sums, nb, sums + nb + 1);
     if (s != ND_OK) return s;
+    nd_prof_begin(h, "scan_apply");
     scan_apply<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(data, sums, n);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
   }
+  nd_prof_begin(h, "write_total");
   write_total<<<1, 32, 0, h->stream>>>(data, last, n, total_dev);
+  nd_prof_end(h);
   ND_LAUNCHED(h);
   ND_CUDA(h, cudaFreeAsync(sums, h->stream));
   return nd_cuda_check(h, cudaGetLastError(), "scan");
@@ -236,7 +246,9 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
   ND_CUDA(h, cudaMemcpyAsync(rbd_d, rbd.data(), rbd.size() * 8, cudaMemcpyHostToDevice, s));
   const int threads = 256;
   int grid = (int)std::min<int64_t>((ncand + threads - 1) / threads, (int64_t)h->num_sms * 16);
+  nd_prof_begin(h, "match_kernel");
   match_kernel<<<grid, threads, 0, s>>>(p, dA, dB, flags);
+  nd_prof_end(h);
   ND_LAUNCHED(h);
   // positions = exclusive scan of flags (kept in a copy: flags still needed)
   int64_t* pos = nullptr;
@@ -260,10 +272,14 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
     ND_CUDA(h, cudaMallocAsync(&firstof, npairs * 4, s));
     ND_CUDA(h, cudaMemsetAsync(tk, 0xff, (size_t)tsize * 8, s));
     ND_CUDA(h, cudaMemsetAsync(tv, 0x7f, (size_t)tsize * 4, s));
+    nd_prof_begin(h, "compact_kernel");
     compact_kernel<<<grid, threads, 0, s>>>(p, dA, dB, flags, pos, pairs, keys, tk, tv, mask, h->d_status);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
     int pg = (int)std::min<int64_t>((npairs + threads - 1) / threads, (int64_t)h->num_sms * 16);
+    nd_prof_begin(h, "first_flags_kernel");
     first_flags_kernel<<<pg, threads, 0, s>>>(npairs, keys, tk, tv, mask, isfirst, firstof);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
     // block ids = exclusive scan of first-appearance flags
     int64_t* blockid = nullptr;
@@ -277,7 +293,9 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
     out.nR = (int32_t)nR;
     ND_CUDA(h, cudaMallocAsync(&blocksR, std::max<int64_t>(1, nR * rankR) * 4, s));
     ND_CUDA(h, cudaMallocAsync(&sizeR, std::max<int64_t>(1, nR) * 8, s));
+    nd_prof_begin(h, "assign_kernel");
     assign_kernel<<<pg, threads, 0, s>>>(p, npairs, dA, dB, pairs, isfirst, blockid, firstof, rbd_d, blocksR, sizeR);
+    nd_prof_end(h);
     ND_LAUNCHED(h);
     stt = nd_device_exclusive_scan(h, sizeR, nR, tot + 2);
     if (stt != ND_OK) return stt;

@@ -6,11 +6,12 @@ every operation runs in the library's CUDA kernels.
 """
 from ._lib import NDError, NoConvergence, PRECISIONS, handle, load, LIB_PATH
 from .tensors import BlockSparseTensor, DenseTensor, blockoffsets
+from . import workloads
 from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
 
 __all__ = [
-    "NDError", "NoConvergence", "PRECISIONS", "handle", "load", "LIB_PATH",
+    "workloads", "NDError", "NoConvergence", "PRECISIONS", "handle", "load", "LIB_PATH",
     "BlockSparseTensor", "DenseTensor", "blockoffsets",
     "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
     "permutedims", "permutedims_", "permutedims_blocksparse",

@@ -8,6 +8,8 @@ from __future__ import annotations
 import ctypes as C
 import os
 import threading
+import atexit
+import weakref
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libndtensors_gb300.so"
@@ -57,6 +59,8 @@ SIGNATURES = {
     "nd_memset0": [_P, _P, C.c_size_t],
     "nd_set_ozaki_slices": [_P, _I32],
     "nd_launch_count": [_P, _PI64],
+    "nd_profile_enable": [_P, _I32],
+    "nd_profile_read": [_P, _I32, C.c_char_p, _PI64, _PD, _PI32],
     "nd_permutedims_f64": [_P, _P, _P, _I32, _PI64, _PI32, _D, _D],
     "nd_contract_dense_f64": [_P, _P, _I32, _PI64, _PI32, _P, _I32, _PI64, _PI32, _P, _I32, _PI64, _PI32,
                               _D, _D, _I32],
@@ -80,6 +84,26 @@ _RESTYPE = {"nd_last_error": C.c_char_p}
 
 _lib = None
 _lock = threading.Lock()
+_shutting_down = False
+_live_plans = weakref.WeakSet()
+
+
+@atexit.register
+def _teardown():
+    """Destroy plans before handles, before the CUDA runtime unloads."""
+    global _shutting_down
+    for p in list(_live_plans):
+        try:
+            p.destroy()
+        except Exception:
+            pass
+    for h in list(_handles.values()):
+        try:
+            h.close()
+        except Exception:
+            pass
+    _handles.clear()
+    _shutting_down = True
 
 
 def load():
@@ -129,6 +153,23 @@ class Handle:
     def sync(self):
         self._check(self.lib.nd_sync(self.ptr))
 
+    def profile(self, enable=True):
+        self._check(self.lib.nd_profile_enable(self.ptr, 1 if enable else 0))
+
+    def profile_read(self):
+        """{kernel name: (launches, total ms)} since the last read; synchronises."""
+        cap = 64
+        names = C.create_string_buffer(64 * cap)
+        counts = (C.c_int64 * cap)()
+        tot = (C.c_double * cap)()
+        n = C.c_int32()
+        self._check(self.lib.nd_profile_read(self.ptr, cap, names, counts, tot, C.byref(n)))
+        out = {}
+        for k in range(min(n.value, cap)):
+            nm = names.raw[64 * k:64 * k + 64].split(b"\0", 1)[0].decode()
+            out[nm] = (counts[k], tot[k])
+        return out
+
     def launches(self):
         c = C.c_int64()
         self._check(self.lib.nd_launch_count(self.ptr, C.byref(c)))
@@ -140,6 +181,8 @@ class Handle:
             self.ptr = _P()
 
     def __del__(self):
+        if _shutting_down:
+            return
         try:
             self.close()
         except Exception:

@@ -109,6 +109,8 @@ class ContractionPlan:
         self.indsR = [tuple(T1.inds[self.l1.index(l)]) if l in self.l1 else tuple(T2.inds[self.l2.index(l)])
                       for l in self.lr]
         self.T1_key, self.T2_key = T1.structure_key(), T2.structure_key()
+        from ._lib import _live_plans
+        _live_plans.add(self)
 
     def flops(self, T1, T2):
         tot = 0
@@ -129,10 +131,17 @@ class ContractionPlan:
             tot += 2 * m * n * k
         return tot
 
+    def destroy(self):
+        if self.ptr and self.h.ptr:
+            self.h.lib.nd_bs_plan_destroy(self.ptr)
+        self.ptr = C.c_void_p()
+
     def __del__(self):
+        from . import _lib
+        if _lib._shutting_down:
+            return
         try:
-            if self.ptr:
-                self.h.lib.nd_bs_plan_destroy(self.ptr)
+            self.destroy()
         except Exception:
             pass
 

@@ -114,6 +114,13 @@ class BlockSparseTensor:
         return cls([tuple(i) for i in t.inds], [tuple(b) for b in t.blocks], list(t.offsets),
                    torch.from_numpy(np.ascontiguousarray(t.data, dtype=np.float64)).to(f"cuda:{device}"))
 
+    @classmethod
+    def from_host(cls, t, device=0):
+        """From a workloads.HostBlockSparse (host numpy)."""
+        torch = _torch()
+        return cls([tuple(i) for i in t.inds], [tuple(b) for b in t.blocks], list(t.offsets),
+                   torch.from_numpy(np.ascontiguousarray(t.data, dtype=np.float64)).to(f"cuda:{device}"))
+
     def data_numpy(self):
         return self.data.detach().cpu().numpy()
 

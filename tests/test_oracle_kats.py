@@ -216,3 +216,20 @@ def test_adjoint_oracle_matches_finite_differences():
         d2 = rng.standard_normal(x2.shape)
         fd = (f(x1, x2 + h * d2) - f(x1, x2 - h * d2)) / (2 * h)
         assert abs(fd - np.sum(g2 * d2)) <= 1e-6 * max(1.0, abs(fd))
+
+
+def test_package_workloads_match_oracle_generators():
+    """Product-side generators (bench inputs) equal the oracle's restatement bit for bit."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "itensors.jl_gb300"))
+    from ndtensors_gb300 import workloads as wl
+    A, B, _ = networks.qn_pair(512)
+    pA, pB = wl.qn_pair(512)
+    for o, p in ((A, pA), (B, pB)):
+        assert [tuple(b) for b in o.blocks] == p.blocks and list(o.offsets) == p.offsets
+        np.testing.assert_array_equal(o.data, p.data)
+    net, pnet = networks.qn_heff(chi=256, seed=4), wl.qn_heff(chi=256, seed=4)
+    for k in ("L", "psi", "W1", "R"):
+        assert [tuple(b) for b in net[k].blocks] == pnet[k].blocks
+        np.testing.assert_array_equal(net[k].data, pnet[k].data)
