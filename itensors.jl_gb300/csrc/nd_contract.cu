@@ -24,6 +24,9 @@ void ExecCache::free_all() {
   if (d_pack) cudaFree(d_pack);
   if (d_exp) cudaFree(d_exp);
   if (d_pack_items) cudaFree(d_pack_items);
+  if (d_sk_items) cudaFree(d_sk_items);
+  if (d_split_pairs) cudaFree(d_split_pairs);
+  if (d_split_items) cudaFree(d_split_items);
   *this = ExecCache{};
 }
 
@@ -100,30 +103,41 @@ static nd_status upload(nd_handle h, void** dst, const void* src, size_t bytes) 
   return ND_OK;
 }
 
-// Work items for the FP64 kernel: 64x64 tiles, biggest groups first.
-static void make_items(const std::vector<PairDesc>& pairs, int bm, int bn, std::vector<WorkItem>& items) {
+// Work items: tiles of bm x bn over each group, biggest groups first.  Only the
+// groups selected by `pick` (all pairs of a group share M and N) are listed.
+template <class Pick>
+static void make_items(const std::vector<PairDesc>& pairs, int bm, int bn, Pick pick, std::vector<WorkItem>& items) {
   items.clear();
-  struct G { int begin, count; int64_t cost; };
-  std::vector<G> groups;
+  std::vector<std::pair<int64_t, WorkItem>> tmp;
   for (size_t i = 0; i < pairs.size();) {
     size_t j = i;
     int64_t ksum = 0;
-    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) { ksum += pairs[j].K; ++j; }
-    groups.push_back({(int)i, (int)(j - i), ksum});
+    bool all = true;
+    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) {
+      ksum += pairs[j].K;
+      all = all && pick(pairs[j]);
+      ++j;
+    }
+    if (all) {
+      const PairDesc& p = pairs[i];
+      int mt = (p.M + bm - 1) / bm, nt = (p.N + bn - 1) / bn;
+      for (int a = 0; a < mt; ++a)
+        for (int b = 0; b < nt; ++b) {
+          int64_t mm = std::min(bm, p.M - a * bm), nn = std::min(bn, p.N - b * bn);
+          tmp.push_back({mm * nn * std::max<int64_t>(ksum, 1), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
+        }
+    }
     i = j;
-  }
-  std::vector<std::pair<int64_t, WorkItem>> tmp;
-  for (auto& g : groups) {
-    const PairDesc& p = pairs[g.begin];
-    int mt = (p.M + bm - 1) / bm, nt = (p.N + bn - 1) / bn;
-    for (int a = 0; a < mt; ++a)
-      for (int b = 0; b < nt; ++b) {
-        int64_t mm = std::min(bm, p.M - a * bm), nn = std::min(bn, p.N - b * bn);
-        tmp.push_back({mm * nn * std::max<int64_t>(g.cost, 1), WorkItem{p.group, g.begin, g.count, a, b}});
-      }
   }
   std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
   for (auto& t : tmp) items.push_back(t.second);
+}
+
+// A group runs on the skinny kernel when every one of its pairs is skinny.
+static bool group_skinny(const std::vector<PairDesc>& pairs, size_t i) {
+  for (size_t j = i; j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job; ++j)
+    if (!nd_pair_is_skinny(pairs[j])) return false;
+  return true;
 }
 
 nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups,
@@ -139,18 +153,31 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
     c.slices = want_slices;
     nd_status s = upload(h, (void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc));
     if (s) return s;
+    // which pairs sit in skinny groups
+    std::vector<char> sk(pairs.size(), 0);
+    for (size_t i = 0; i < pairs.size();) {
+      size_t j = i;
+      bool g = group_skinny(pairs, i);
+      while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) sk[j++] = g;
+      i = j;
+    }
+    std::vector<WorkItem> items;
+    make_items(pairs, nd_skinny_rows(), 1 << 30, [&](const PairDesc& p) { return sk[&p - pairs.data()] != 0; }, items);
+    c.nsk_items = (int)items.size();
+    if ((s = upload(h, (void**)&c.d_sk_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
     if (precision == ND_PREC_FP64) {
-      std::vector<WorkItem> items;
-      make_items(pairs, 64, 64, items);
+      make_items(pairs, 64, 64, [&](const PairDesc& p) { return sk[&p - pairs.data()] == 0; }, items);
       c.nitems = (int)items.size();
-      s = upload(h, (void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem));
-      if (s) return s;
+      if ((s = upload(h, (void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
     } else {
-      s = nd_split_build(h, c, pairs, ngroups, precision);
-      if (s) return s;
+      std::vector<PairDesc> regular;
+      for (size_t i = 0; i < pairs.size(); ++i) if (!sk[i]) regular.push_back(pairs[i]);
+      if (!regular.empty() && (s = nd_split_build(h, c, regular, ngroups, precision))) return s;
     }
     c.built = true;
   }
+  nd_status s = nd_launch_skinny_f64(h, c.d_pairs, c.d_sk_items, c.nsk_items, ptrs, alpha, beta);
+  if (s) return s;
   if (precision == ND_PREC_FP64) return nd_launch_gemm_f64(h, c.d_pairs, c.d_items, c.nitems, ptrs, alpha, beta);
   return nd_split_run(h, c, ptrs, alpha, beta);
 }

@@ -153,3 +153,92 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "gemm_f64_grouped");
 }
+
+// ---------------------------------------------------------------------------
+// Skinny block pairs (N <= 32 and K <= 32): FP64 on the CUDA cores.
+//
+// Contractions with an MPO tensor (T1 * W1, T2 * W2 in the two-site H_eff)
+// are tall and skinny: M is a product of bond dimensions while N and K are
+// MPO-link x physical sector sizes (1..3 each).  Their arithmetic intensity
+// is a few flops per 8-byte element, far below any tensor-core tile's ridge
+// point, so they are HBM-bound and run here in plain FP64 (exact, no split),
+// in every precision mode: one thread per output row, the B block of each
+// pair staged in shared memory, the group's pairs accumulated in registers.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int SK_ROWS = 128, SK_MAXN = 32, SK_MAXK = 32;
+
+__global__ void __launch_bounds__(SK_ROWS) gemm_skinny_f64(GemmArgs g) {
+  __shared__ double Bs[SK_MAXK][SK_MAXN + 1];
+  __shared__ int64_t kA[SK_MAXK], colR[SK_MAXN];
+  __shared__ PairDesc pd;
+  const int tid = threadIdx.x;
+  for (int it = blockIdx.x; it < g.nitems; it += gridDim.x) {
+    const WorkItem wi = g.items[it];
+    double acc[SK_MAXN];
+#pragma unroll
+    for (int j = 0; j < SK_MAXN; ++j) acc[j] = 0.0;
+    int64_t rrow = 0;
+    double* Rp = nullptr;
+    int M = 0, N = 0;
+    const int i = wi.mt * SK_ROWS + tid;
+    for (int pi = 0; pi < wi.pair_count; ++pi) {
+      __syncthreads();
+      if (tid == 0) pd = g.pairs[wi.pair_begin + pi];
+      __syncthreads();
+      M = pd.M; N = pd.N;
+      const double* B = g.ptrs.B[pd.job] + pd.b_off;
+      // B block (K x N) into shared memory, k offsets of A
+      for (int e = tid; e < pd.K * N; e += SK_ROWS) {
+        int k = e % pd.K, j = e / pd.K;
+        int64_t ka, kb, cb, cr;
+        mixed_offsets(pd.ks, k, ka, kb);
+        mixed_offsets(pd.cols, j, cb, cr);
+        Bs[k][j] = __ldg(B + kb + cb);
+      }
+      if (tid < pd.K) { int64_t ka, kb; mixed_offsets(pd.ks, tid, ka, kb); kA[tid] = ka; }
+      if (tid < N) { int64_t cb, cr; mixed_offsets(pd.cols, tid, cb, cr); colR[tid] = cr; }
+      __syncthreads();
+      Rp = g.ptrs.R[pd.job] + pd.r_off;
+      if (i < M) {
+        int64_t ra, rr;
+        mixed_offsets(pd.rows, i, ra, rr);
+        rrow = rr;
+        const double* A = g.ptrs.A[pd.job] + pd.a_off + ra;
+        for (int k = 0; k < pd.K; ++k) {
+          const double a = __ldg(A + kA[k]);
+#pragma unroll
+          for (int j = 0; j < SK_MAXN; ++j)
+            if (j < N) acc[j] = fma(a, Bs[k][j], acc[j]);
+        }
+      }
+    }
+    if (i < M) {
+#pragma unroll
+      for (int j = 0; j < SK_MAXN; ++j) {
+        if (j < N) {
+          double* dst = Rp + rrow + colR[j];
+          double v = acc[j];
+          if (g.beta == 0.0) *dst = (g.alpha == 1.0) ? v : g.alpha * v;
+          else *dst = g.alpha * v + g.beta * *dst;
+        }
+      }
+    }
+  }
+}
+}  // namespace
+
+bool nd_pair_is_skinny(const PairDesc& p) { return p.N <= SK_MAXN && p.K <= SK_MAXK; }
+int nd_skinny_rows() { return SK_ROWS; }
+
+nd_status nd_launch_skinny_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
+                               const JobPtrs& ptrs, double alpha, double beta) {
+  if (nitems == 0) return ND_OK;
+  GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta};
+  int blocks = std::min(nitems, h->num_sms * 8);
+  nd_prof_begin(h, "gemm_skinny_f64");
+  gemm_skinny_f64<<<blocks, SK_ROWS, 0, h->stream>>>(g);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "gemm_skinny_f64");
+}

@@ -21,18 +21,22 @@
 // is assembled from integer fields.  FP64 arithmetic appears only in the
 // alpha/beta epilogue when alpha != 1 or beta != 0, and in the BF16X3 epilogue.
 //
-// Levels: level t = p+q carries weight 2^(-8(t-2)).  Levels 2 and 3 must be
-// exact; they accumulate in FP32 TMEM over chunks of 512 of K (|sum| <= 2^24),
-// double buffered, and the epilogue warps drain each chunk into int64 fixed
-// point (unit 2^-24 of a level-2 unit) while the next chunk is computed.
-// Levels >= 4 accumulate in FP32 over the whole K (their rounding is below
-// 2^-40 of the leading term) and are drained once per block pair.
+// Levels: level t = p+q carries weight 2^(-8(t-2)).  Slices are stored
+// pre-scaled (slice p holds d_p * 2^(-8(p-1)), still exact in BF16), so every
+// product already carries its level weight.  Levels 2 and 3 must be exact:
+// they accumulate in an "X" accumulator pair (L2 | L3) in FP32 TMEM over
+// chunks of 512 of K (|sum| <= 2^24 units), and the epilogue warps drain each
+// chunk into int64 fixed point (unit 2^-24 of a level-2 unit).  Levels >= 4
+// go to a "T" pair (T4 | T5+) in FP32 over the whole K of a block pair: their
+// rounding is below 2^-40 of the leading term.  X slots alternate per chunk
+// and T slots per block pair, both double buffered in the 512 TMEM columns,
+// so the epilogue of one pair overlaps the MMAs of the next.
 //
 // Each A-slice stage is [S][128 rows][32 k] BF16 and each B-slice stage is
 // [S][64 rows][32 k], pre-swizzled (64-byte swizzle) by the pack kernel, so one
 // cp.async.bulk per operand brings a whole stage and the slices of B sit in
-// consecutive rows: A_p x [B_q .. B_q'] is ONE tcgen05.mma with N = 64*(q'-q+1)
-// whose accumulator columns are exactly the level blocks p+q .. p+q'.
+// consecutive rows: A_p x [B_q, B_q+1] is ONE tcgen05.mma with N = 128 whose
+// two 64-column halves land in adjacent accumulator blocks (L2|L3 or T4|T5+).
 //
 // Warp roles (320 threads): warp 0 = bulk-copy producer, warp 1 = TMEM
 // allocator + MMA issuer, warps 2..9 = epilogue (TMEM lane quarter = warp % 4,
@@ -184,14 +188,16 @@ __device__ __forceinline__ int swz64(int r, int k) {
 // ---- pack kernel -----------------------------------------------------------
 // One CTA per (operand, row tile): row maxima -> exponents -> S digit slices,
 // staged in shared memory in the tcgen05 canonical K-major SW64 layout and
-// written out as contiguous 16-byte vectors.
+// written out as contiguous 16-byte vectors.  Thread mapping follows the
+// operand's contiguous dimension (rows or k) so global reads coalesce; row
+// maxima are kept in registers (no shared-memory atomics per element).
 __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ unsigned long long rowmax[BM];
   __shared__ int64_t rowoff[BM];
   __shared__ int64_t koff[BK];
   __shared__ int32_t Er[BM];
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int S = a.slices;
   for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
     const PackItem pi = a.items[it];
@@ -207,9 +213,14 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
       rowmax[tid] = 0ull;
     }
     const bool rows_contig = op.rk.n > 0 && op.rk.st0[0] == 1;
-    const int per = ROWS * BK / 256;
-    // pass 1: row maxima of |x| (as IEEE bit patterns: monotonic for finite x)
+    const int per = ROWS * BK / 256;            // elements per thread per k-step (16 or 8)
+    const int tpr = 256 / ROWS;                 // threads per row in the row-contiguous mapping
+    // pass 1: row maxima of |x| as IEEE bit patterns (monotonic for finite x)
     if (S > 2) {
+      unsigned long long mx[16];
+#pragma unroll
+      for (int e = 0; e < 16; ++e) mx[e] = 0ull;
+      bool bad = false;
       for (int ks = 0; ks < op.k_steps; ++ks) {
         __syncthreads();
         if (tid < BK) {
@@ -218,18 +229,35 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
           koff[tid] = o;
         }
         __syncthreads();
-        for (int e = 0; e < per; ++e) {
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          if (e >= per) break;
           int r, k;
-          if (rows_contig) { r = tid % ROWS; k = tid / ROWS + (256 / ROWS) * e; }
-          else { k = tid & 31; r = (tid >> 5) + 8 * e; }
+          if (rows_contig) { r = tid % ROWS; k = tid / ROWS + tpr * e; }
+          else { k = lane; r = warp + 8 * e; }
           if (r0 + r < op.rows && ks * BK + k < op.kdim) {
             uint64_t b = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k])) & 0x7fffffffffffffffull;
-            if (b >= 0x7ff0000000000000ull) {
-              if (atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
-              b = 0;
-            }
-            atomicMax(&rowmax[r], (unsigned long long)b);
+            if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
+            if (rows_contig) mx[0] = b > mx[0] ? b : mx[0];
+            else mx[e] = b > mx[e] ? b : mx[e];
           }
+        }
+      }
+      if (bad && atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
+      __syncthreads();
+      if (rows_contig) {
+        atomicMax(&rowmax[tid % ROWS], mx[0]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          if (e >= per) break;
+          unsigned long long v = mx[e];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+            v = w > v ? w : v;
+          }
+          if (lane == 0) rowmax[warp + 8 * e] = v;
         }
       }
       __syncthreads();
@@ -240,7 +268,7 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
         a.exps[op.exp_off + r0 + tid] = E;
       }
     }
-    // pass 2: digits
+    // pass 2: digits (pre-scaled: slice p holds d_p * 2^(-8(p-1)))
     for (int ks = 0; ks < op.k_steps; ++ks) {
       __syncthreads();
       if (tid < BK) {
@@ -251,8 +279,8 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
       __syncthreads();
       for (int e = 0; e < per; ++e) {
         int r, k;
-        if (rows_contig) { r = tid % ROWS; k = tid / ROWS + (256 / ROWS) * e; }
-        else { k = tid & 31; r = (tid >> 5) + 8 * e; }
+        if (rows_contig) { r = tid % ROWS; k = tid / ROWS + tpr * e; }
+        else { k = lane; r = warp + 8 * e; }
         uint64_t bits = 0;
         if (r0 + r < op.rows && ks * BK + k < op.kdim)
           bits = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k]));
@@ -261,7 +289,10 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
           int d[6];
           int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, Er[r], S);
           balanced_digits(X, S, d);
-          for (int s = 0; s < S; ++s) *(uint16_t*)(sm + s * ROWS * 64 + so) = bf16_bits_of_int(d[s]);
+          for (int q = 0; q < S; ++q) {
+            const float sc = __int_as_float((127 - 8 * q) << 23);      // 2^(-8q)
+            *(uint16_t*)(sm + q * ROWS * 64 + so) = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * sc));
+          }
         } else {
           float xf = f64_to_f32_int(bits);
           __nv_bfloat16 hi = __float2bfloat16_rn(xf);
@@ -289,6 +320,8 @@ struct GemmArgs {
   const int32_t* exps;
   JobPtrs ptrs;
   double alpha, beta;
+  int32_t amode;      // 0: alpha == 1, 1: general alpha
+  int32_t bmode;      // 0: beta == 0 (overwrite), 1: general beta
   DeviceStatus* st;
 };
 
@@ -326,16 +359,20 @@ __device__ __forceinline__ void commit(uint64_t* bar) {
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
 template <int S>
 struct Cfg {
   static constexpr int STAGE = S * (A_SLICE + B_SLICE);
   static constexpr int STAGES = (SMEM_BUDGET - 1024) / STAGE;
-  static constexpr int TAIL = S > 2 ? S - 2 : 0;           // tail level blocks (levels 4..S+1)
-  static constexpr int EXACT0 = TAIL * BN;                  // column of exact buffer 0
-  static constexpr int TMEM_COLS = (TAIL * BN + 4 * BN) <= 256 ? 256 : 512;
+  static constexpr int TBLK = S >= 4 ? 2 : (S == 3 ? 1 : 0);   // tail blocks (T4, T5+)
+  static constexpr int TMEM_COLS = 512;                        // X0 T0 X1 T1, 128 columns each
   static constexpr int SMEM = STAGES * STAGE + 1024;
 };
+
+// TMEM column of X slot x / T slot t
+__device__ __forceinline__ uint32_t xcol(uint32_t x) { return x * 256u; }
+__device__ __forceinline__ uint32_t tcol(uint32_t t) { return t * 256u + 128u; }
 
 template <int S>
 __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
@@ -343,16 +380,18 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full[C::STAGES], empty[C::STAGES];
-  __shared__ __align__(8) uint64_t xfull[2], xempty[2], tfull, tempty, done_bar;
+  __shared__ __align__(8) uint64_t xfull[2], xempty[2], tfull[2], tempty[2], done_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
+  __shared__ int64_t colR_s[BN];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
     for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    for (int b = 0; b < 2; ++b) { mbar_init(&xfull[b], 1); mbar_init(&xempty[b], 8); }
-    mbar_init(&tfull, 1);
-    mbar_init(&tempty, 8);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&xfull[b], 1); mbar_init(&xempty[b], 8);
+      mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 8);
+    }
     mbar_init(&done_bar, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -404,59 +443,67 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   } else if (warp == 1) {
     // ------------------------------- MMA issuer ----------------------------
     if (lane == 0) {
-      uint32_t n = 0, chunk = 0, pairs_done = 0;
+      uint32_t n = 0, chunk = 0, npair = 0;
       bool ok = true;
       const uint32_t smem_base = smem_u32(smem);
+      const uint32_t i64 = idesc(BN), i128 = idesc(2 * BN);
       for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
         const WorkItem wi = g.items[it];
-        for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+        for (int pi = 0; pi < wi.pair_count && ok; ++pi, ++npair) {
           const PairDesc& pd = g.pairs[wi.pair_begin + pi];
           const int nks = g.ops[pd.a_op].k_steps;
-          if (S > 2 && pairs_done >= 1 && !mbar_wait(smem_u32(&tempty), (pairs_done - 1) & 1, g.st, 410, &abort_flag)) { ok = false; break; }
+          const uint32_t ts = npair & 1, tu = npair >> 1;
+          if (C::TBLK && tu >= 1 && !mbar_wait(smem_u32(&tempty[ts]), (tu - 1) & 1, g.st, 410, &abort_flag)) { ok = false; break; }
+          const uint32_t T = tmem + tcol(ts);
           const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
-          uint32_t pbuf = 0;
+          uint32_t X = tmem;
           for (int ks = 0; ks < nks; ++ks, ++n) {
             const bool cstart = (ks % chunk_steps) == 0;
             const bool cend = ((ks % chunk_steps) == chunk_steps - 1) || ks == nks - 1;
             if (cstart) {
-              pbuf = chunk & 1;
-              const uint32_t v = chunk >> 1;
-              if (v >= 1 && !mbar_wait(smem_u32(&xempty[pbuf]), (v - 1) & 1, g.st, 411, &abort_flag)) { ok = false; break; }
+              const uint32_t xs = chunk & 1, xu = chunk >> 1;
+              if (xu >= 1 && !mbar_wait(smem_u32(&xempty[xs]), (xu - 1) & 1, g.st, 411, &abort_flag)) { ok = false; break; }
+              X = tmem + xcol(xs);
             }
             const uint32_t s = n % C::STAGES, u = n / C::STAGES;
             if (!mbar_wait(smem_u32(&full[s]), u & 1, g.st, 412, &abort_flag)) { ok = false; break; }
             fence_after();
             const uint32_t a0 = smem_base + s * C::STAGE;
             const uint32_t b0 = a0 + S * A_SLICE;
-            const uint32_t xcol = tmem + C::EXACT0 + pbuf * 2 * BN;
 #pragma unroll
             for (int kk = 0; kk < 2; ++kk) {
               const uint32_t accx = (cstart && kk == 0) ? 0u : 1u;
               const uint32_t acct = (ks == 0 && kk == 0) ? 0u : 1u;
               const uint32_t ko = kk * 32;
-              // A1 x [B1 B2] -> exact (L2, L3)
-              mma(xcol, sdesc(a0 + ko), sdesc(b0 + ko), idesc(2 * BN), accx);
-              if (S == 2) {
-                // A2 x [B1] -> L3
-                mma(xcol + BN, sdesc(a0 + A_SLICE + ko), sdesc(b0 + ko), idesc(BN), 1u);
-              } else {
-                // A1 x [B3..BS] -> tail levels 4..S+1
-                mma(tmem, sdesc(a0 + ko), sdesc(b0 + 2 * B_SLICE + ko), idesc((S - 2) * BN), acct);
-                // A2 x [B1] -> L3 ; A2 x [B2..B(S-1)] -> tail
-                mma(xcol + BN, sdesc(a0 + A_SLICE + ko), sdesc(b0 + ko), idesc(BN), 1u);
-                mma(tmem, sdesc(a0 + A_SLICE + ko), sdesc(b0 + B_SLICE + ko), idesc((S - 2) * BN), 1u);
-                // Ap x [B1 .. B(S+1-p)] -> tail blocks p-3 ..
+              auto A = [&](int p) { return sdesc(a0 + (p - 1) * A_SLICE + ko); };
+              auto B = [&](int q) { return sdesc(b0 + (q - 1) * B_SLICE + ko); };
+              // exact levels: A1 x [B1 B2] -> (L2 | L3), A2 x B1 -> L3
+              mma(X, A(1), B(1), i128, accx);
+              mma(X + BN, A(2), B(1), i64, 1u);
+              if (S == 3) {
+                mma(T, A(1), B(3), i64, acct);
+                mma(T, A(2), B(2), i64, 1u);
+                mma(T, A(3), B(1), i64, 1u);
+              } else if (S >= 4) {
+                // level 4 -> T4, levels >= 5 -> T5+ : A_p x [B_(4-p), B_(5-p)] is one N = 128 MMA for p <= 3
+                mma(T, A(1), B(3), i128, acct);
+                mma(T, A(2), B(2), i128, 1u);
+                mma(T, A(3), B(1), i128, 1u);
 #pragma unroll
-                for (int p = 3; p <= S; ++p)
-                  mma(tmem + (p - 3) * BN, sdesc(a0 + (p - 1) * A_SLICE + ko), sdesc(b0 + ko), idesc((S + 1 - p) * BN), 1u);
+                for (int p = 1; p <= S; ++p)
+#pragma unroll
+                  for (int q = 1; q <= S + 1 - p; ++q) {
+                    const int lv = p + q;
+                    const bool covered = (p <= 3) && (q == 4 - p || q == 5 - p);
+                    if (lv >= 5 && !covered) mma(T + BN, A(p), B(q), i64, 1u);
+                  }
               }
             }
             commit(&empty[s]);
-            if (cend) { commit(&xfull[pbuf]); ++chunk; }
+            if (cend) { commit(&xfull[chunk & 1]); ++chunk; }
           }
           if (!ok) break;
-          if (S > 2) commit(&tfull);
-          ++pairs_done;
+          if (C::TBLK) commit(&tfull[ts]);
         }
       }
       commit(&done_bar);
@@ -467,8 +514,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
     const int q = warp & 3;                 // TMEM lane quarter
     const int hcol = (warp - 2) >> 2;       // column half
     const int row = q * 32 + lane;
-    const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
-    uint32_t chunk = 0, pairs_done = 0;
+    const int etid = tid - 64;
+    const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + hcol * 32;
+    uint32_t chunk = 0, npair = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
       const WorkItem wi = g.items[it];
@@ -477,8 +525,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
       const bool row_ok = gm < p0.M;
       int64_t roff = 0, dummy;
       if (row_ok) mixed_offsets(p0.rows, gm, dummy, roff);
-      double* Rb = g.ptrs.R[p0.job] + p0.r_off;
-      for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+      epi_sync();                                   // previous item done with colR_s
+      if (etid < BN) {
+        int64_t co = 0, d2;
+        const int gn = wi.nt * BN + etid;
+        if (gn < p0.N) mixed_offsets(p0.cols, gn, d2, co);
+        colR_s[etid] = co;
+      }
+      epi_sync();
+      double* Rb = g.ptrs.R[p0.job] + p0.r_off + roff;
+      const int ncols = min(32, p0.N - (wi.nt * BN + hcol * 32));
+      for (int pi = 0; pi < wi.pair_count && ok; ++pi, ++npair) {
         const PairDesc& pd = g.pairs[wi.pair_begin + pi];
         const SplitOp& oa = g.ops[pd.a_op];
         const SplitOp& ob = g.ops[pd.b_op];
@@ -490,66 +547,62 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
 #pragma unroll
         for (int c = 0; c < 32; ++c) { acc[c] = 0; facc[c] = 0.f; }
         for (int ch = 0; ch < nchunks; ++ch, ++chunk) {
-          const uint32_t b = chunk & 1, v = chunk >> 1;
-          if (!mbar_wait(smem_u32(&xfull[b]), v & 1, g.st, 420, &abort_flag)) { ok = false; break; }
+          const uint32_t xs = chunk & 1, xu = chunk >> 1;
+          if (!mbar_wait(smem_u32(&xfull[xs]), xu & 1, g.st, 420, &abort_flag)) { ok = false; break; }
           fence_after();
           uint32_t l2[32], l3[32];
-          const uint32_t xaddr = lane_addr + C::EXACT0 + b * 2 * BN + hcol * 32;
-          TMEM_LD32(xaddr, l2);
-          TMEM_LD32(xaddr + BN, l3);
+          TMEM_LD32(lane_addr + xcol(xs), l2);
+          TMEM_LD32(lane_addr + xcol(xs) + BN, l3);
           tmem_wait_ld();
           fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&xempty[b]);
+          if (lane == 0) mbar_arrive(&xempty[xs]);
           if (S > 2) {
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
+              // L2: integer units; L3 was computed with pre-scaled slices: an integer multiple of 2^-8
               long long x2 = (long long)__float2int_rn(__uint_as_float(l2[c]));
-              long long x3 = (long long)__float2int_rn(__uint_as_float(l3[c]));
+              long long x3 = (long long)__float2int_rn(__uint_as_float(l3[c]) * 256.0f);
               acc[c] += (x2 << 24) + (x3 << 16);
             }
           } else {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) facc[c] = __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
+            for (int c = 0; c < 32; ++c) facc[c] += __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
           }
         }
         if (!ok) break;
-        if (S > 2) {
-          if (!mbar_wait(smem_u32(&tfull), pairs_done & 1, g.st, 421, &abort_flag)) { ok = false; break; }
+        if (C::TBLK) {
+          const uint32_t ts = npair & 1, tu = npair >> 1;
+          if (!mbar_wait(smem_u32(&tfull[ts]), tu & 1, g.st, 421, &abort_flag)) { ok = false; break; }
           fence_after();
 #pragma unroll 1
-          for (int t = 0; t < C::TAIL; ++t) {
+          for (int t = 0; t < C::TBLK; ++t) {
             uint32_t lt[32];
-            TMEM_LD32(lane_addr + t * BN + hcol * 32, lt);
+            TMEM_LD32(lane_addr + tcol(ts) + t * BN, lt);
             tmem_wait_ld();
-            const float sc = __int_as_float((127 + 8 - 8 * t) << 23);   // 2^(8 - 8t): level t+4 in units of 2^-24 L2
 #pragma unroll
-            for (int c = 0; c < 32; ++c) acc[c] += __float2ll_rn(__uint_as_float(lt[c]) * sc);
+            for (int c = 0; c < 32; ++c) acc[c] += __float2ll_rn(__uint_as_float(lt[c]) * 16777216.0f);  // x 2^24
           }
           fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&tempty);
+          if (lane == 0) mbar_arrive(&tempty[ts]);
         }
-        ++pairs_done;
         // finalize this pair into R
-        if (row_ok) {
+        if (row_ok && ncols > 0) {
           const int Ei = S > 2 ? g.exps[oa.exp_off + gm] : 0;
+          const int32_t* Fj = g.exps + ob.exp_off + wi.nt * BN + hcol * 32;
           const bool first = pd.first != 0;
 #pragma unroll
           for (int c = 0; c < 32; ++c) {
-            const int gn = wi.nt * BN + hcol * 32 + c;
-            if (gn >= pd.N) continue;
-            int64_t coff, d2;
-            mixed_offsets(pd.cols, gn, d2, coff);
-            double v;
-            if (S > 2) v = i64_scaled_to_f64(acc[c], Ei + g.exps[ob.exp_off + gn] - 38);
-            else v = (double)facc[c];
-            double* dst = Rb + roff + coff;
-            if (first) {
-              if (g.beta == 0.0) *dst = (g.alpha == 1.0) ? v : g.alpha * v;
-              else *dst = g.alpha * v + g.beta * *dst;
-            } else {
-              *dst = (g.alpha == 1.0) ? *dst + v : *dst + g.alpha * v;
+            if (c < ncols) {
+              double v = (S > 2) ? i64_scaled_to_f64(acc[c], Ei + __ldg(Fj + c) - 38) : (double)facc[c];
+              double* dst = Rb + colR_s[hcol * 32 + c];
+              if (first) {
+                if (g.bmode == 0) *dst = g.amode ? g.alpha * v : v;
+                else *dst = g.alpha * v + g.beta * *dst;
+              } else {
+                *dst = g.amode ? *dst + g.alpha * v : *dst + v;
+              }
             }
           }
         }
@@ -646,17 +699,16 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
     if (bytes) ND_CUDA(h, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
     return ND_OK;
   };
-  if (c.d_pairs) { cudaFree(c.d_pairs); c.d_pairs = nullptr; }
   nd_status s;
-  if ((s = up((void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc)))) return s;
-  if ((s = up((void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
+  if ((s = up((void**)&c.d_split_pairs, pairs.data(), pairs.size() * sizeof(PairDesc)))) return s;
+  if ((s = up((void**)&c.d_split_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
   if ((s = up(&c.d_operands, ops.data(), ops.size() * sizeof(SplitOp)))) return s;
   if ((s = up(&c.d_pack_items, pitems.data(), pitems.size() * sizeof(PackItem)))) return s;
   ND_CUDA(h, cudaMalloc(&c.d_pack, std::max<int64_t>(pack_bytes, 16)));
   ND_CUDA(h, cudaMalloc((void**)&c.d_exp, std::max<int64_t>(exp_count, 4) * 4));
   c.pack_bytes = pack_bytes;
   c.exp_count = exp_count;
-  c.nitems = (int)items.size();
+  c.nsplit_items = (int)items.size();
   c.npack_items = (int)pitems.size();
   c.nops_a = (int)amap.size();
   c.nops_b = (int)bmap.size();
@@ -682,9 +734,10 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
     ND_LAUNCHED(h);
     ND_CUDA(h, cudaGetLastError());
   }
-  GemmArgs g{c.d_pairs, c.d_items, c.nitems, (const SplitOp*)c.d_operands, (const unsigned char*)c.d_pack,
-             c.d_exp, ptrs, alpha, beta, h->d_status};
-  if (c.nitems == 0) return ND_OK;
+  GemmArgs g{c.d_split_pairs, c.d_split_items, c.nsplit_items, (const SplitOp*)c.d_operands,
+             (const unsigned char*)c.d_pack, c.d_exp, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1,
+             h->d_status};
+  if (c.nsplit_items == 0) return ND_OK;
   switch (S) {
     case 2: return launch_gemm<2>(h, g);
     case 3: return launch_gemm<3>(h, g);

@@ -42,9 +42,14 @@ struct ExecCache {
   int precision = -1;
   int slices = 0;
   PairDesc* d_pairs = nullptr;
-  WorkItem* d_items = nullptr;
+  WorkItem* d_items = nullptr;     // FP64 tensor-core tiles of the regular groups
   int nitems = 0;
-  // split-precision operands
+  WorkItem* d_sk_items = nullptr;  // skinny groups (FP64 CUDA-core kernel, every precision)
+  int nsk_items = 0;
+  // split-precision operands (regular groups only)
+  PairDesc* d_split_pairs = nullptr;
+  WorkItem* d_split_items = nullptr;
+  int nsplit_items = 0;
   void* d_operands = nullptr;      // OperandDesc[nops]
   int nops_a = 0, nops_b = 0;
   void* d_pack = nullptr;          // packed slices (bytes)
@@ -79,6 +84,11 @@ struct nd_bs_plan_s {
 // Build the PairDesc of one block pair.
 bool nd_make_pair(const Roles& ro, const int64_t* dA, const int64_t* dB, const int64_t* dR, PairDesc& pd,
                   std::string& why);
+
+bool nd_pair_is_skinny(const PairDesc& p);
+int nd_skinny_rows();
+nd_status nd_launch_skinny_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
+                               const JobPtrs& ptrs, double alpha, double beta);
 
 // Execute grouped pairs with a cache (built on first call, outside capture).
 nd_status nd_execute_cached(nd_handle h, ExecCache& cache, const std::vector<PairDesc>& pairs, int ngroups,
