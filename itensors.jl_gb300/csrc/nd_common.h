@@ -84,6 +84,21 @@ ND_HOSTDEV void mixed_offsets(const Mixed& m, int64_t lin, int64_t& o0, int64_t&
   o1 = b;
 }
 
+// Same for indices below 2^31 with 32-bit division (GEMM extents are < 2^31).
+ND_HOSTDEV void mixed_offsets32(const Mixed& m, uint32_t lin, int64_t& o0, int64_t& o1) {
+  int64_t a = 0, b = 0;
+  for (int d = 0; d < m.n; ++d) {
+    uint32_t dd = (uint32_t)m.dim[d];
+    uint32_t q = lin / dd;
+    uint32_t r = lin - q * dd;
+    a += (int64_t)r * m.st0[d];
+    b += (int64_t)r * m.st1[d];
+    lin = q;
+  }
+  o0 = a;
+  o1 = b;
+}
+
 // Merge adjacent dimensions that are contiguous in both strided views.
 inline void mixed_simplify(Mixed& m) {
   Mixed o{};

@@ -155,7 +155,7 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
 }
 
 // ---------------------------------------------------------------------------
-// Skinny block pairs (N <= 32 and K <= 32): FP64 on the CUDA cores.
+// Skinny block pairs (N <= 8 and K <= 32): FP64 on the CUDA cores.
 //
 // Contractions with an MPO tensor (T1 * W1, T2 * W2 in the two-site H_eff)
 // are tall and skinny: M is a product of bond dimensions while N and K are
@@ -166,59 +166,71 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
 // pair staged in shared memory, the group's pairs accumulated in registers.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int SK_ROWS = 128, SK_MAXN = 32, SK_MAXK = 32;
+constexpr int SK_THREADS = 256, SK_RPT = 4, SK_ROWS = SK_THREADS * SK_RPT, SK_MAXN = 8, SK_MAXK = 32;
 
-__global__ void __launch_bounds__(SK_ROWS) gemm_skinny_f64(GemmArgs g) {
-  __shared__ double Bs[SK_MAXK][SK_MAXN + 1];
+__global__ void __launch_bounds__(SK_THREADS) gemm_skinny_f64(GemmArgs g) {
+  __shared__ double Bs[SK_MAXK][SK_MAXN];
   __shared__ int64_t kA[SK_MAXK], colR[SK_MAXN];
-  __shared__ PairDesc pd;
+  __shared__ __align__(16) PairDesc pd;
   const int tid = threadIdx.x;
+  constexpr int PD_VECS = (int)(sizeof(PairDesc) / 16);
+  static_assert(sizeof(PairDesc) % 16 == 0, "PairDesc must be a multiple of 16 bytes");
   for (int it = blockIdx.x; it < g.nitems; it += gridDim.x) {
     const WorkItem wi = g.items[it];
-    double acc[SK_MAXN];
+    double acc[SK_RPT][SK_MAXN];
 #pragma unroll
-    for (int j = 0; j < SK_MAXN; ++j) acc[j] = 0.0;
-    int64_t rrow = 0;
+    for (int r = 0; r < SK_RPT; ++r)
+#pragma unroll
+      for (int j = 0; j < SK_MAXN; ++j) acc[r][j] = 0.0;
+    int64_t rrow[SK_RPT] = {0, 0, 0, 0};
     double* Rp = nullptr;
     int M = 0, N = 0;
-    const int i = wi.mt * SK_ROWS + tid;
+    const int i0 = wi.mt * SK_ROWS + tid;
     for (int pi = 0; pi < wi.pair_count; ++pi) {
       __syncthreads();
-      if (tid == 0) pd = g.pairs[wi.pair_begin + pi];
+      if (tid < PD_VECS) ((int4*)&pd)[tid] = __ldg((const int4*)(g.pairs + wi.pair_begin + pi) + tid);
       __syncthreads();
       M = pd.M; N = pd.N;
+      const int K = pd.K;
       const double* B = g.ptrs.B[pd.job] + pd.b_off;
-      // B block (K x N) into shared memory, k offsets of A
-      for (int e = tid; e < pd.K * N; e += SK_ROWS) {
-        int k = e % pd.K, j = e / pd.K;
+      if (tid < K * N) {
+        int k = tid % K, j = tid / K;
         int64_t ka, kb, cb, cr;
-        mixed_offsets(pd.ks, k, ka, kb);
-        mixed_offsets(pd.cols, j, cb, cr);
+        mixed_offsets32(pd.ks, k, ka, kb);
+        mixed_offsets32(pd.cols, j, cb, cr);
         Bs[k][j] = __ldg(B + kb + cb);
       }
-      if (tid < pd.K) { int64_t ka, kb; mixed_offsets(pd.ks, tid, ka, kb); kA[tid] = ka; }
-      if (tid < N) { int64_t cb, cr; mixed_offsets(pd.cols, tid, cb, cr); colR[tid] = cr; }
+      if (tid < K) { int64_t ka, kb; mixed_offsets32(pd.ks, tid, ka, kb); kA[tid] = ka; }
+      if (tid >= 64 && tid < 64 + N) { int64_t cb, cr; mixed_offsets32(pd.cols, tid - 64, cb, cr); colR[tid - 64] = cr; }
       __syncthreads();
       Rp = g.ptrs.R[pd.job] + pd.r_off;
-      if (i < M) {
-        int64_t ra, rr;
-        mixed_offsets(pd.rows, i, ra, rr);
-        rrow = rr;
-        const double* A = g.ptrs.A[pd.job] + pd.a_off + ra;
-        for (int k = 0; k < pd.K; ++k) {
-          const double a = __ldg(A + kA[k]);
+      const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
 #pragma unroll
-          for (int j = 0; j < SK_MAXN; ++j)
-            if (j < N) acc[j] = fma(a, Bs[k][j], acc[j]);
+      for (int r = 0; r < SK_RPT; ++r) {
+        const int i = i0 + r * SK_THREADS;
+        if (i < M) {
+          int64_t ra, rr;
+          mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
+          rrow[r] = rr;
+          const double* A = Ab + ra;
+          for (int k = 0; k < K; ++k) {
+            const double a = __ldg(A + kA[k]);
+#pragma unroll
+            for (int j = 0; j < SK_MAXN; ++j)
+              if (j < N) acc[r][j] = fma(a, Bs[k][j], acc[r][j]);
+          }
         }
       }
     }
-    if (i < M) {
+#pragma unroll
+    for (int r = 0; r < SK_RPT; ++r) {
+      const int i = i0 + r * SK_THREADS;
+      if (i >= M) continue;
 #pragma unroll
       for (int j = 0; j < SK_MAXN; ++j) {
         if (j < N) {
-          double* dst = Rp + rrow + colR[j];
-          double v = acc[j];
+          double* dst = Rp + rrow[r] + colR[j];
+          double v = acc[r][j];
           if (g.beta == 0.0) *dst = (g.alpha == 1.0) ? v : g.alpha * v;
           else *dst = g.alpha * v + g.beta * *dst;
         }
@@ -237,7 +249,7 @@ nd_status nd_launch_skinny_f64(nd_handle h, const PairDesc* d_pairs, const WorkI
   GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta};
   int blocks = std::min(nitems, h->num_sms * 8);
   nd_prof_begin(h, "gemm_skinny_f64");
-  gemm_skinny_f64<<<blocks, SK_ROWS, 0, h->stream>>>(g);
+  gemm_skinny_f64<<<blocks, SK_THREADS, 0, h->stream>>>(g);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "gemm_skinny_f64");

@@ -208,13 +208,17 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
     __syncthreads();
     if (tid < ROWS) {
       int64_t o = 0, dummy;
-      if (r0 + tid < op.rows) mixed_offsets(op.rk, r0 + tid, o, dummy);
+      if (r0 + tid < op.rows) mixed_offsets32(op.rk, r0 + tid, o, dummy);
       rowoff[tid] = o;
       rowmax[tid] = 0ull;
     }
     const bool rows_contig = op.rk.n > 0 && op.rk.st0[0] == 1;
-    const int per = ROWS * BK / 256;            // elements per thread per k-step (16 or 8)
-    const int tpr = 256 / ROWS;                 // threads per row in the row-contiguous mapping
+    // Mappings.  Row-contiguous operands: a thread owns (row, 8-wide k chunk)
+    // units u = tid + 256*j, r = u % ROWS, chunk = u / ROWS, and writes each
+    // slice chunk as one 16-byte vector.  k-contiguous operands: lane = k,
+    // warp = row (+8 per step), 2-byte stores that fill 64 consecutive bytes.
+    const int units = ROWS * (BK / 8) / 256;    // 2 (A) or 1 (B)
+    const int per = ROWS * BK / 256;            // k-contiguous elements per thread (16 or 8)
     // pass 1: row maxima of |x| as IEEE bit patterns (monotonic for finite x)
     if (S > 2) {
       unsigned long long mx[16];
@@ -225,28 +229,41 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
         __syncthreads();
         if (tid < BK) {
           int64_t o = 0, dummy;
-          if (ks * BK + tid < op.kdim) mixed_offsets(op.kk, ks * BK + tid, o, dummy);
+          if (ks * BK + tid < op.kdim) mixed_offsets32(op.kk, ks * BK + tid, o, dummy);
           koff[tid] = o;
         }
         __syncthreads();
+        if (rows_contig) {
+          for (int j = 0; j < units; ++j) {
+            const int u = tid + 256 * j, r = u % ROWS, c = u / ROWS;
+            if (r0 + r >= op.rows) continue;
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          if (e >= per) break;
-          int r, k;
-          if (rows_contig) { r = tid % ROWS; k = tid / ROWS + tpr * e; }
-          else { k = lane; r = warp + 8 * e; }
-          if (r0 + r < op.rows && ks * BK + k < op.kdim) {
-            uint64_t b = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k])) & 0x7fffffffffffffffull;
-            if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
-            if (rows_contig) mx[0] = b > mx[0] ? b : mx[0];
-            else mx[e] = b > mx[e] ? b : mx[e];
+            for (int e = 0; e < 8; ++e) {
+              const int k = c * 8 + e;
+              if (ks * BK + k < op.kdim) {
+                uint64_t b = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k])) & 0x7fffffffffffffffull;
+                if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
+                mx[j] = b > mx[j] ? b : mx[j];
+              }
+            }
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            if (e >= per) break;
+            const int k = lane, r = warp + 8 * e;
+            if (r0 + r < op.rows && ks * BK + k < op.kdim) {
+              uint64_t b = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k])) & 0x7fffffffffffffffull;
+              if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
+              mx[e] = b > mx[e] ? b : mx[e];
+            }
           }
         }
       }
       if (bad && atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
       __syncthreads();
       if (rows_contig) {
-        atomicMax(&rowmax[tid % ROWS], mx[0]);
+        for (int j = 0; j < units; ++j) atomicMax(&rowmax[(tid + 256 * j) % ROWS], mx[j]);
       } else {
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
@@ -273,32 +290,68 @@ __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
       __syncthreads();
       if (tid < BK) {
         int64_t o = 0, dummy;
-        if (ks * BK + tid < op.kdim) mixed_offsets(op.kk, ks * BK + tid, o, dummy);
+        if (ks * BK + tid < op.kdim) mixed_offsets32(op.kk, ks * BK + tid, o, dummy);
         koff[tid] = o;
       }
       __syncthreads();
-      for (int e = 0; e < per; ++e) {
-        int r, k;
-        if (rows_contig) { r = tid % ROWS; k = tid / ROWS + tpr * e; }
-        else { k = lane; r = warp + 8 * e; }
-        uint64_t bits = 0;
-        if (r0 + r < op.rows && ks * BK + k < op.kdim)
-          bits = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k]));
-        const int so = swz64(r, k);
-        if (S > 2) {
-          int d[6];
-          int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, Er[r], S);
-          balanced_digits(X, S, d);
-          for (int q = 0; q < S; ++q) {
-            const float sc = __int_as_float((127 - 8 * q) << 23);      // 2^(-8q)
-            *(uint16_t*)(sm + q * ROWS * 64 + so) = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * sc));
+      if (rows_contig) {
+        for (int j = 0; j < units; ++j) {
+          const int u = tid + 256 * j, r = u % ROWS, c = u / ROWS;
+          uint32_t w[6][4];
+#pragma unroll
+          for (int e = 0; e < 8; e += 2) {
+            uint16_t h0[6], h1[6];
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+              const int k = c * 8 + e + t;
+              uint64_t bits = 0;
+              if (r0 + r < op.rows && ks * BK + k < op.kdim)
+                bits = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k]));
+              uint16_t* hh = t ? h1 : h0;
+              if (S > 2) {
+                int d[6];
+                int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, Er[r], S);
+                balanced_digits(X, S, d);
+#pragma unroll
+                for (int q = 0; q < 6; ++q)
+                  if (q < S) hh[q] = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * __int_as_float((127 - 8 * q) << 23)));
+              } else {
+                float xf = f64_to_f32_int(bits);
+                __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+                hh[0] = __bfloat16_as_ushort(hi);
+                hh[1] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(hi)));
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < 6; ++q) w[q][e / 2] = (uint32_t)h0[q] | ((uint32_t)h1[q] << 16);
           }
-        } else {
-          float xf = f64_to_f32_int(bits);
-          __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-          __nv_bfloat16 lo = __float2bfloat16_rn(xf - __bfloat162float(hi));
-          *(uint16_t*)(sm + so) = __bfloat16_as_ushort(hi);
-          *(uint16_t*)(sm + ROWS * 64 + so) = __bfloat16_as_ushort(lo);
+          const int so = r * 64 + (((c ^ (r >> 1)) & 3) << 4);
+#pragma unroll
+          for (int q = 0; q < 6; ++q)
+            if (q < S) *(uint4*)(sm + q * ROWS * 64 + so) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+        }
+      } else {
+        for (int e = 0; e < per; ++e) {
+          const int k = lane, r = warp + 8 * e;
+          uint64_t bits = 0;
+          if (r0 + r < op.rows && ks * BK + k < op.kdim)
+            bits = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k]));
+          const int so = swz64(r, k);
+          if (S > 2) {
+            int d[6];
+            int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, Er[r], S);
+            balanced_digits(X, S, d);
+            for (int q = 0; q < S; ++q) {
+              const float sc = __int_as_float((127 - 8 * q) << 23);      // 2^(-8q)
+              *(uint16_t*)(sm + q * ROWS * 64 + so) = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * sc));
+            }
+          } else {
+            float xf = f64_to_f32_int(bits);
+            __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+            __nv_bfloat16 lo = __float2bfloat16_rn(xf - __bfloat162float(hi));
+            *(uint16_t*)(sm + so) = __bfloat16_as_ushort(hi);
+            *(uint16_t*)(sm + ROWS * 64 + so) = __bfloat16_as_ushort(lo);
+          }
         }
       }
       __syncthreads();
