@@ -205,20 +205,33 @@ __global__ void __launch_bounds__(SK_THREADS) gemm_skinny_f64(GemmArgs g) {
       __syncthreads();
       Rp = g.ptrs.R[pd.job] + pd.r_off;
       const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
+      const double* Ar[SK_RPT];
+      bool rok[SK_RPT];
 #pragma unroll
       for (int r = 0; r < SK_RPT; ++r) {
         const int i = i0 + r * SK_THREADS;
-        if (i < M) {
-          int64_t ra, rr;
-          mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
-          rrow[r] = rr;
-          const double* A = Ab + ra;
-          for (int k = 0; k < K; ++k) {
-            const double a = __ldg(A + kA[k]);
+        rok[r] = i < M;
+        int64_t ra = 0, rr = 0;
+        if (rok[r]) mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
+        rrow[r] = rr;
+        Ar[r] = Ab + ra;
+      }
+      // 4 k x 4 rows of independent loads in flight before the FMAs
+      for (int k0 = 0; k0 < K; k0 += 4) {
+        double av[4][SK_RPT];
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int r = 0; r < SK_RPT; ++r)
+            av[kk][r] = (k0 + kk < K && rok[r]) ? __ldg(Ar[r] + kA[k0 + kk]) : 0.0;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          if (k0 + kk >= K) break;
+#pragma unroll
+          for (int r = 0; r < SK_RPT; ++r)
 #pragma unroll
             for (int j = 0; j < SK_MAXN; ++j)
-              if (j < N) acc[r][j] = fma(a, Bs[k][j], acc[r][j]);
-          }
+              if (j < N) acc[r][j] = fma(av[kk][r], Bs[k0 + kk][j], acc[r][j]);
         }
       }
     }

@@ -186,179 +186,119 @@ __device__ __forceinline__ int swz64(int r, int k) {
 }
 
 // ---- pack kernel -----------------------------------------------------------
-// One CTA per (operand, row tile): row maxima -> exponents -> S digit slices,
-// staged in shared memory in the tcgen05 canonical K-major SW64 layout and
-// written out as contiguous 16-byte vectors.  Thread mapping follows the
-// operand's contiguous dimension (rows or k) so global reads coalesce; row
-// maxima are kept in registers (no shared-memory atomics per element).
+// One CTA per (operand, row tile): row maxima -> exponents -> S digit slices
+// written straight to global memory in the tcgen05 canonical K-major SW64
+// layout.  A thread owns (row, 8-wide k chunk) units: the four lanes of a row
+// read its 32 k values (coalesced whether rows or k are contiguous in the
+// tensor) and each writes one 16-byte chunk per slice, so four lanes fill a
+// 64-byte row and a warp a 512-byte run.  Offsets of every k of the operand
+// live in shared memory, so the k loop runs without block-wide barriers.
+constexpr int PACK_MAXK = 24576;   // 192 KB of k offsets in shared memory
+
+__device__ __forceinline__ void pack_unit_digits(uint64_t bits, int E, int S, uint16_t* hh) {
+  if (S > 2) {
+    int d[6];
+    int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, E, S);
+    balanced_digits(X, S, d);
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+      if (q < S) hh[q] = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * __int_as_float((127 - 8 * q) << 23)));
+  } else {
+    float xf = f64_to_f32_int(bits);
+    __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+    hh[0] = __bfloat16_as_ushort(hi);
+    hh[1] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(hi)));
+  }
+}
+
 __global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
-  extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ unsigned long long rowmax[BM];
+  extern __shared__ __align__(16) int64_t koff[];     // [k_steps * 32]
   __shared__ int64_t rowoff[BM];
-  __shared__ int64_t koff[BK];
   __shared__ int32_t Er[BM];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int S = a.slices;
+  const int c = lane & 3;                               // k chunk of this lane
   for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
     const PackItem pi = a.items[it];
     const SplitOp& op = a.ops[pi.op];
     const int ROWS = op.is_b ? BN : BM;
+    const int units = ROWS / 64;                        // rows per thread: 2 (A) or 1 (B)
     const double* src = (op.is_b ? a.ptrs.B[op.job] : a.ptrs.A[op.job]) + op.src_off;
     const int r0 = pi.rt * ROWS;
+    const int kpad = op.k_steps * BK;
     __syncthreads();
     if (tid < ROWS) {
       int64_t o = 0, dummy;
       if (r0 + tid < op.rows) mixed_offsets32(op.rk, r0 + tid, o, dummy);
       rowoff[tid] = o;
-      rowmax[tid] = 0ull;
     }
-    const bool rows_contig = op.rk.n > 0 && op.rk.st0[0] == 1;
-    // Mappings.  Row-contiguous operands: a thread owns (row, 8-wide k chunk)
-    // units u = tid + 256*j, r = u % ROWS, chunk = u / ROWS, and writes each
-    // slice chunk as one 16-byte vector.  k-contiguous operands: lane = k,
-    // warp = row (+8 per step), 2-byte stores that fill 64 consecutive bytes.
-    const int units = ROWS * (BK / 8) / 256;    // 2 (A) or 1 (B)
-    const int per = ROWS * BK / 256;            // k-contiguous elements per thread (16 or 8)
-    // pass 1: row maxima of |x| as IEEE bit patterns (monotonic for finite x)
-    if (S > 2) {
-      unsigned long long mx[16];
+    for (int k = tid; k < kpad; k += 256) {
+      int64_t o = -1, dummy;
+      if (k < op.kdim) mixed_offsets32(op.kk, k, o, dummy);
+      koff[k] = o;                                      // -1 marks padding
+    }
+    __syncthreads();
+    int rr[2];
+    bool rv[2];
 #pragma unroll
-      for (int e = 0; e < 16; ++e) mx[e] = 0ull;
+    for (int j = 0; j < 2; ++j) { rr[j] = (lane >> 2) + 8 * warp + 64 * j; rv[j] = j < units && r0 + rr[j] < op.rows; }
+    // pass 1: row maxima of |x| (IEEE bit patterns are monotonic for finite x)
+    int E[2] = {0, 0};
+    if (S > 2) {
+      unsigned long long mx[2] = {0ull, 0ull};
       bool bad = false;
       for (int ks = 0; ks < op.k_steps; ++ks) {
-        __syncthreads();
-        if (tid < BK) {
-          int64_t o = 0, dummy;
-          if (ks * BK + tid < op.kdim) mixed_offsets32(op.kk, ks * BK + tid, o, dummy);
-          koff[tid] = o;
-        }
-        __syncthreads();
-        if (rows_contig) {
-          for (int j = 0; j < units; ++j) {
-            const int u = tid + 256 * j, r = u % ROWS, c = u / ROWS;
-            if (r0 + r >= op.rows) continue;
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-              const int k = c * 8 + e;
-              if (ks * BK + k < op.kdim) {
-                uint64_t b = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k])) & 0x7fffffffffffffffull;
-                if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
-                mx[j] = b > mx[j] ? b : mx[j];
-              }
-            }
-          }
-        } else {
+        for (int j = 0; j < 2; ++j) {
+          if (!rv[j]) continue;
+          const double* rowp = src + rowoff[rr[j]];
 #pragma unroll
-          for (int e = 0; e < 16; ++e) {
-            if (e >= per) break;
-            const int k = lane, r = warp + 8 * e;
-            if (r0 + r < op.rows && ks * BK + k < op.kdim) {
-              uint64_t b = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k])) & 0x7fffffffffffffffull;
+          for (int e = 0; e < 8; ++e) {
+            const int64_t ko = koff[ks * BK + c * 8 + e];
+            if (ko >= 0) {
+              uint64_t b = (uint64_t)__double_as_longlong(__ldg(rowp + ko)) & 0x7fffffffffffffffull;
               if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
-              mx[e] = b > mx[e] ? b : mx[e];
+              mx[j] = b > mx[j] ? b : mx[j];
             }
           }
         }
       }
       if (bad && atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
-      __syncthreads();
-      if (rows_contig) {
-        for (int j = 0; j < units; ++j) atomicMax(&rowmax[(tid + 256 * j) % ROWS], mx[j]);
-      } else {
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          if (e >= per) break;
-          unsigned long long v = mx[e];
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-            v = w > v ? w : v;
-          }
-          if (lane == 0) rowmax[warp + 8 * e] = v;
-        }
-      }
-      __syncthreads();
-      if (tid < ROWS) {
-        int ex = (int)(rowmax[tid] >> 52);
-        int E = (ex ? ex : 1) - 1022;      // max|x| < 2^E
-        Er[tid] = E;
-        a.exps[op.exp_off + r0 + tid] = E;
+      for (int j = 0; j < 2; ++j) {
+        unsigned long long v = mx[j];
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, 1); v = w > v ? w : v;
+        w = __shfl_xor_sync(0xffffffffu, v, 2); v = w > v ? w : v;
+        const int ex = (int)(v >> 52);
+        E[j] = (ex ? ex : 1) - 1022;                    // max|x| < 2^E
+        if (j < units && c == 0) a.exps[op.exp_off + r0 + rr[j]] = E[j];
       }
     }
-    // pass 2: digits (pre-scaled: slice p holds d_p * 2^(-8(p-1)))
+    // pass 2: digits (pre-scaled: slice p holds d_p * 2^(-8(p-1))), 16-byte stores
     for (int ks = 0; ks < op.k_steps; ++ks) {
-      __syncthreads();
-      if (tid < BK) {
-        int64_t o = 0, dummy;
-        if (ks * BK + tid < op.kdim) mixed_offsets32(op.kk, ks * BK + tid, o, dummy);
-        koff[tid] = o;
-      }
-      __syncthreads();
-      if (rows_contig) {
-        for (int j = 0; j < units; ++j) {
-          const int u = tid + 256 * j, r = u % ROWS, c = u / ROWS;
-          uint32_t w[6][4];
+      unsigned char* tile = a.pack + op.pack_off + ((int64_t)(pi.rt * op.k_steps + ks) * S) * (ROWS * 64);
 #pragma unroll
-          for (int e = 0; e < 8; e += 2) {
-            uint16_t h0[6], h1[6];
+      for (int j = 0; j < 2; ++j) {
+        if (j >= units) continue;
+        const int r = rr[j];
+        const double* rowp = src + rowoff[r];
+        uint32_t w[6][4];
 #pragma unroll
-            for (int t = 0; t < 2; ++t) {
-              const int k = c * 8 + e + t;
-              uint64_t bits = 0;
-              if (r0 + r < op.rows && ks * BK + k < op.kdim)
-                bits = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k]));
-              uint16_t* hh = t ? h1 : h0;
-              if (S > 2) {
-                int d[6];
-                int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, Er[r], S);
-                balanced_digits(X, S, d);
+        for (int e = 0; e < 8; e += 2) {
+          uint16_t h0[6], h1[6];
+          const int64_t k0 = koff[ks * BK + c * 8 + e], k1 = koff[ks * BK + c * 8 + e + 1];
+          const uint64_t b0 = (rv[j] && k0 >= 0) ? (uint64_t)__double_as_longlong(__ldg(rowp + k0)) : 0ull;
+          const uint64_t b1 = (rv[j] && k1 >= 0) ? (uint64_t)__double_as_longlong(__ldg(rowp + k1)) : 0ull;
+          pack_unit_digits(b0, E[j], S, h0);
+          pack_unit_digits(b1, E[j], S, h1);
 #pragma unroll
-                for (int q = 0; q < 6; ++q)
-                  if (q < S) hh[q] = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * __int_as_float((127 - 8 * q) << 23)));
-              } else {
-                float xf = f64_to_f32_int(bits);
-                __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-                hh[0] = __bfloat16_as_ushort(hi);
-                hh[1] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(hi)));
-              }
-            }
-#pragma unroll
-            for (int q = 0; q < 6; ++q) w[q][e / 2] = (uint32_t)h0[q] | ((uint32_t)h1[q] << 16);
-          }
-          const int so = r * 64 + (((c ^ (r >> 1)) & 3) << 4);
-#pragma unroll
-          for (int q = 0; q < 6; ++q)
-            if (q < S) *(uint4*)(sm + q * ROWS * 64 + so) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+          for (int q = 0; q < 6; ++q) w[q][e / 2] = (uint32_t)h0[q] | ((uint32_t)h1[q] << 16);
         }
-      } else {
-        for (int e = 0; e < per; ++e) {
-          const int k = lane, r = warp + 8 * e;
-          uint64_t bits = 0;
-          if (r0 + r < op.rows && ks * BK + k < op.kdim)
-            bits = (uint64_t)__double_as_longlong(__ldg(src + rowoff[r] + koff[k]));
-          const int so = swz64(r, k);
-          if (S > 2) {
-            int d[6];
-            int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, Er[r], S);
-            balanced_digits(X, S, d);
-            for (int q = 0; q < S; ++q) {
-              const float sc = __int_as_float((127 - 8 * q) << 23);      // 2^(-8q)
-              *(uint16_t*)(sm + q * ROWS * 64 + so) = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * sc));
-            }
-          } else {
-            float xf = f64_to_f32_int(bits);
-            __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-            __nv_bfloat16 lo = __float2bfloat16_rn(xf - __bfloat162float(hi));
-            *(uint16_t*)(sm + so) = __bfloat16_as_ushort(hi);
-            *(uint16_t*)(sm + ROWS * 64 + so) = __bfloat16_as_ushort(lo);
-          }
-        }
+        const int so = r * 64 + (((c ^ (r >> 1)) & 3) << 4);
+#pragma unroll
+        for (int q = 0; q < 6; ++q)
+          if (q < S) *(uint4*)(tile + q * ROWS * 64 + so) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
       }
-      __syncthreads();
-      const int bytes = S * ROWS * 64;
-      int4* dst = (int4*)(a.pack + op.pack_off + ((int64_t)(pi.rt * op.k_steps + ks) * S) * (ROWS * 64));
-      const int4* srcs = (const int4*)sm;
-      for (int v = tid; v < bytes / 16; v += 256) dst[v] = srcs[v];
     }
   }
 }
@@ -724,6 +664,11 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
     pd.a_op = add_op(false, pd);
     pd.b_op = add_op(true, pd);
   }
+  int maxk = BK;
+  for (auto& o : ops) maxk = std::max(maxk, o.k_steps * BK);
+  if (maxk > PACK_MAXK)
+    return nd_fail(h, ND_ERR_UNSUPPORTED, "split GEMM: contracted extent %d exceeds %d (use ND_PREC_FP64)", maxk, PACK_MAXK);
+  c.pack_maxk = maxk;
   std::vector<PackItem> pitems;
   for (int i = 0; i < (int)ops.size(); ++i)
     for (int t = 0; t < ops[i].row_tiles; ++t) pitems.push_back({i, t});
@@ -773,10 +718,10 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
   const int S = c.slices;
   PackArgs pa{(const SplitOp*)c.d_operands, (const PackItem*)c.d_pack_items, c.npack_items, ptrs,
               (unsigned char*)c.d_pack, c.d_exp, S, h->d_status};
-  const int psmem = S * BM * 64;
+  const int psmem = (int)(c.pack_maxk * sizeof(int64_t));
   static bool pattr = false;
   if (!pattr) {
-    cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * BM * 64);
+    cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, PACK_MAXK * 8);
     pattr = true;
   }
   int pblocks = std::min(c.npack_items, h->num_sms * 6);
