@@ -24,6 +24,7 @@ void ExecCache::free_all() {
   if (d_pack) cudaFree(d_pack);
   if (d_exp) cudaFree(d_exp);
   if (d_pack_items) cudaFree(d_pack_items);
+  if (d_rowmax) cudaFree(d_rowmax);
   if (d_sk_items) cudaFree(d_sk_items);
   if (d_split_pairs) cudaFree(d_split_pairs);
   if (d_split_items) cudaFree(d_split_items);

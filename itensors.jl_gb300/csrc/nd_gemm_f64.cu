@@ -27,6 +27,8 @@ struct GemmArgs {
   int nitems;
   JobPtrs ptrs;
   double alpha, beta;
+  int32_t amode;   // 0: alpha == 1
+  int32_t bmode;   // 0: beta == 0 (overwrite)
 };
 
 __device__ __forceinline__ void dmma(double& c0, double& c1, double a, double b) {
@@ -132,7 +134,7 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
           if (n0 + n >= N) continue;
           double* dst = Rp + r_base + rowR[m] + colR[n];
           double v = acc[i][j][h];
-          if (g.beta == 0.0) *dst = (g.alpha == 1.0) ? v : g.alpha * v;
+          if (g.bmode == 0) *dst = g.amode ? g.alpha * v : v;
           else *dst = g.alpha * v + g.beta * *dst;
         }
       }
@@ -145,7 +147,7 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
 nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
                              const JobPtrs& ptrs, double alpha, double beta) {
   if (nitems == 0) return ND_OK;
-  GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta};
+  GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1};
   int blocks = std::min(nitems, h->num_sms * 4);
   nd_prof_begin(h, "gemm_f64_grouped");
   gemm_f64_grouped<<<blocks, 128, 0, h->stream>>>(g);
@@ -168,86 +170,97 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
 namespace {
 constexpr int SK_THREADS = 256, SK_RPT = 4, SK_ROWS = SK_THREADS * SK_RPT, SK_MAXN = 8, SK_MAXK = 32;
 
-__global__ void __launch_bounds__(SK_THREADS) gemm_skinny_f64(GemmArgs g) {
-  __shared__ double Bs[SK_MAXK][SK_MAXN];
-  __shared__ int64_t kA[SK_MAXK], colR[SK_MAXN];
-  __shared__ __align__(16) PairDesc pd;
+// One row chunk of one group with exactly NN output columns (no predicated FMAs:
+// the FP64 pipe is the bound for these pairs on GB300).
+template <int NN>
+__device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& wi, PairDesc& pd,
+                                            double (*Bs)[SK_MAXN], int64_t* kA, int64_t* colR) {
   const int tid = threadIdx.x;
   constexpr int PD_VECS = (int)(sizeof(PairDesc) / 16);
-  static_assert(sizeof(PairDesc) % 16 == 0, "PairDesc must be a multiple of 16 bytes");
-  for (int it = blockIdx.x; it < g.nitems; it += gridDim.x) {
-    const WorkItem wi = g.items[it];
-    double acc[SK_RPT][SK_MAXN];
+  double acc[SK_RPT][NN];
 #pragma unroll
-    for (int r = 0; r < SK_RPT; ++r)
+  for (int r = 0; r < SK_RPT; ++r)
 #pragma unroll
-      for (int j = 0; j < SK_MAXN; ++j) acc[r][j] = 0.0;
-    int64_t rrow[SK_RPT] = {0, 0, 0, 0};
-    double* Rp = nullptr;
-    int M = 0, N = 0;
-    const int i0 = wi.mt * SK_ROWS + tid;
-    for (int pi = 0; pi < wi.pair_count; ++pi) {
-      __syncthreads();
-      if (tid < PD_VECS) ((int4*)&pd)[tid] = __ldg((const int4*)(g.pairs + wi.pair_begin + pi) + tid);
-      __syncthreads();
-      M = pd.M; N = pd.N;
-      const int K = pd.K;
-      const double* B = g.ptrs.B[pd.job] + pd.b_off;
-      if (tid < K * N) {
-        int k = tid % K, j = tid / K;
-        int64_t ka, kb, cb, cr;
-        mixed_offsets32(pd.ks, k, ka, kb);
-        mixed_offsets32(pd.cols, j, cb, cr);
-        Bs[k][j] = __ldg(B + kb + cb);
-      }
-      if (tid < K) { int64_t ka, kb; mixed_offsets32(pd.ks, tid, ka, kb); kA[tid] = ka; }
-      if (tid >= 64 && tid < 64 + N) { int64_t cb, cr; mixed_offsets32(pd.cols, tid - 64, cb, cr); colR[tid - 64] = cr; }
-      __syncthreads();
-      Rp = g.ptrs.R[pd.job] + pd.r_off;
-      const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
-      const double* Ar[SK_RPT];
-      bool rok[SK_RPT];
-#pragma unroll
-      for (int r = 0; r < SK_RPT; ++r) {
-        const int i = i0 + r * SK_THREADS;
-        rok[r] = i < M;
-        int64_t ra = 0, rr = 0;
-        if (rok[r]) mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
-        rrow[r] = rr;
-        Ar[r] = Ab + ra;
-      }
-      // 4 k x 4 rows of independent loads in flight before the FMAs
-      for (int k0 = 0; k0 < K; k0 += 4) {
-        double av[4][SK_RPT];
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
-#pragma unroll
-          for (int r = 0; r < SK_RPT; ++r)
-            av[kk][r] = (k0 + kk < K && rok[r]) ? __ldg(Ar[r] + kA[k0 + kk]) : 0.0;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          if (k0 + kk >= K) break;
-#pragma unroll
-          for (int r = 0; r < SK_RPT; ++r)
-#pragma unroll
-            for (int j = 0; j < SK_MAXN; ++j)
-              if (j < N) acc[r][j] = fma(av[kk][r], Bs[k0 + kk][j], acc[r][j]);
-        }
-      }
+    for (int j = 0; j < NN; ++j) acc[r][j] = 0.0;
+  int64_t rrow[SK_RPT] = {0, 0, 0, 0};
+  bool rok[SK_RPT];
+  double* Rp = nullptr;
+  const int i0 = wi.mt * SK_ROWS + tid;
+  for (int pi = 0; pi < wi.pair_count; ++pi) {
+    __syncthreads();
+    if (tid < PD_VECS) ((int4*)&pd)[tid] = __ldg((const int4*)(g.pairs + wi.pair_begin + pi) + tid);
+    __syncthreads();
+    const int K = pd.K, M = pd.M;
+    const double* B = g.ptrs.B[pd.job] + pd.b_off;
+    if (tid < K * NN) {
+      int k = tid % K, j = tid / K;
+      int64_t ka, kb, cb, cr;
+      mixed_offsets32(pd.ks, k, ka, kb);
+      mixed_offsets32(pd.cols, j, cb, cr);
+      Bs[k][j] = __ldg(B + kb + cb);
     }
+    if (tid < K) { int64_t ka, kb; mixed_offsets32(pd.ks, tid, ka, kb); kA[tid] = ka; }
+    if (tid >= 64 && tid < 64 + NN) { int64_t cb, cr; mixed_offsets32(pd.cols, tid - 64, cb, cr); colR[tid - 64] = cr; }
+    __syncthreads();
+    Rp = g.ptrs.R[pd.job] + pd.r_off;
+    const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
+    const double* Ar[SK_RPT];
 #pragma unroll
     for (int r = 0; r < SK_RPT; ++r) {
       const int i = i0 + r * SK_THREADS;
-      if (i >= M) continue;
+      rok[r] = i < M;
+      int64_t ra = 0, rr = 0;
+      if (rok[r]) mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
+      rrow[r] = rr;
+      Ar[r] = Ab + ra;
+    }
+    for (int k0 = 0; k0 < K; k0 += 4) {
+      double av[4][SK_RPT];
 #pragma unroll
-      for (int j = 0; j < SK_MAXN; ++j) {
-        if (j < N) {
-          double* dst = Rp + rrow[r] + colR[j];
-          double v = acc[r][j];
-          if (g.beta == 0.0) *dst = (g.alpha == 1.0) ? v : g.alpha * v;
-          else *dst = g.alpha * v + g.beta * *dst;
-        }
+      for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int r = 0; r < SK_RPT; ++r)
+          av[kk][r] = (k0 + kk < K && rok[r]) ? __ldg(Ar[r] + kA[k0 + kk]) : 0.0;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        if (k0 + kk >= K) break;
+#pragma unroll
+        for (int r = 0; r < SK_RPT; ++r)
+#pragma unroll
+          for (int j = 0; j < NN; ++j) acc[r][j] = fma(av[kk][r], Bs[k0 + kk][j], acc[r][j]);
       }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < SK_RPT; ++r) {
+    if (!rok[r]) continue;
+#pragma unroll
+    for (int j = 0; j < NN; ++j) {
+      double* dst = Rp + rrow[r] + colR[j];
+      const double v = acc[r][j];
+      if (g.bmode == 0) *dst = g.amode ? g.alpha * v : v;
+      else *dst = g.alpha * v + g.beta * *dst;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(SK_THREADS, 1) gemm_skinny_f64(GemmArgs g) {
+  __shared__ double Bs[SK_MAXK][SK_MAXN];
+  __shared__ int64_t kA[SK_MAXK], colR[SK_MAXN];
+  __shared__ __align__(16) PairDesc pd;
+  static_assert(sizeof(PairDesc) % 16 == 0, "PairDesc must be a multiple of 16 bytes");
+  for (int it = blockIdx.x; it < g.nitems; it += gridDim.x) {
+    const WorkItem wi = g.items[it];
+    const int N = __ldg(&g.pairs[wi.pair_begin].N);
+    switch (N) {
+      case 1: skinny_item<1>(g, wi, pd, Bs, kA, colR); break;
+      case 2: skinny_item<2>(g, wi, pd, Bs, kA, colR); break;
+      case 3: skinny_item<3>(g, wi, pd, Bs, kA, colR); break;
+      case 4: skinny_item<4>(g, wi, pd, Bs, kA, colR); break;
+      case 5: skinny_item<5>(g, wi, pd, Bs, kA, colR); break;
+      case 6: skinny_item<6>(g, wi, pd, Bs, kA, colR); break;
+      case 7: skinny_item<7>(g, wi, pd, Bs, kA, colR); break;
+      default: skinny_item<8>(g, wi, pd, Bs, kA, colR); break;
     }
   }
 }
@@ -259,7 +272,7 @@ int nd_skinny_rows() { return SK_ROWS; }
 nd_status nd_launch_skinny_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
                                const JobPtrs& ptrs, double alpha, double beta) {
   if (nitems == 0) return ND_OK;
-  GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta};
+  GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1};
   int blocks = std::min(nitems, h->num_sms * 8);
   nd_prof_begin(h, "gemm_skinny_f64");
   gemm_skinny_f64<<<blocks, SK_THREADS, 0, h->stream>>>(g);

@@ -67,21 +67,6 @@ struct SplitOp {
   Mixed kk;           // st0: element strides of k
 };
 
-struct PackItem {
-  int32_t op, rt;
-};
-
-struct PackArgs {
-  const SplitOp* ops;
-  const PackItem* items;
-  int nitems;
-  JobPtrs ptrs;
-  unsigned char* pack;
-  int32_t* exps;
-  int slices;         // S (2 = BF16X3 float split)
-  DeviceStatus* st;
-};
-
 // ---- helpers ---------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -185,15 +170,33 @@ __device__ __forceinline__ int swz64(int r, int k) {
   return r * 64 + ((((k >> 3) ^ (r >> 1)) & 3) << 4) + (k & 7) * 2;
 }
 
-// ---- pack kernel -----------------------------------------------------------
-// One CTA per (operand, row tile): row maxima -> exponents -> S digit slices
-// written straight to global memory in the tcgen05 canonical K-major SW64
-// layout.  A thread owns (row, 8-wide k chunk) units: the four lanes of a row
-// read its 32 k values (coalesced whether rows or k are contiguous in the
-// tensor) and each writes one 16-byte chunk per slice, so four lanes fill a
-// 64-byte row and a warp a 512-byte run.  Offsets of every k of the operand
-// live in shared memory, so the k loop runs without block-wide barriers.
-constexpr int PACK_MAXK = 24576;   // 192 KB of k offsets in shared memory
+// ---- pack kernels ----------------------------------------------------------
+// Two launches over fine-grained items (operand, row tile, chunk of PACK_KC
+// k-steps), so every SM has work: pack_rowmax folds |x| maxima of its chunk
+// into a per-row global maximum (IEEE bit patterns are monotonic for finite
+// x, so an integer atomicMax suffices); pack_digits turns each element into S
+// digit slices written straight to global memory in the tcgen05 canonical
+// K-major SW64 layout.  A thread owns (row, 8-wide k chunk) units: the four
+// lanes of a row read its 32 k values (coalesced whether rows or k are
+// contiguous in the tensor) and each writes one 16-byte chunk per slice, so
+// four lanes fill a 64-byte row and a warp a 512-byte run.
+constexpr int PACK_KC = 8;                 // k-steps (of 32) per pack item
+
+struct PackItem2 {
+  int32_t op, rt, kc;
+};
+
+struct PackArgs2 {
+  const SplitOp* ops;
+  const PackItem2* items;
+  int nitems;
+  JobPtrs ptrs;
+  unsigned char* pack;
+  int32_t* exps;
+  unsigned long long* rowmax;
+  int slices;
+  DeviceStatus* st;
+};
 
 __device__ __forceinline__ void pack_unit_digits(uint64_t bits, int E, int S, uint16_t* hh) {
   if (S > 2) {
@@ -211,86 +214,107 @@ __device__ __forceinline__ void pack_unit_digits(uint64_t bits, int E, int S, ui
   }
 }
 
-__global__ void __launch_bounds__(256) pack_kernel(PackArgs a) {
-  extern __shared__ __align__(16) int64_t koff[];     // [k_steps * 32]
+// shared set-up of one pack item: row offsets and k offsets of the chunk
+__device__ __forceinline__ void pack_setup(const SplitOp& op, const PackItem2& pi, int ROWS, int64_t* rowoff,
+                                           int64_t* koff, int& ks0, int& ks1) {
+  const int tid = threadIdx.x;
+  const int r0 = pi.rt * ROWS;
+  ks0 = pi.kc * PACK_KC;
+  ks1 = min(op.k_steps, ks0 + PACK_KC);
+  if (tid < ROWS) {
+    int64_t o = 0, dummy;
+    if (r0 + tid < op.rows) mixed_offsets32(op.rk, r0 + tid, o, dummy);
+    rowoff[tid] = o;
+  }
+  {
+    const int k = ks0 * BK + tid;          // 256 threads = PACK_KC * 32 k values
+    int64_t o = -1, dummy;
+    if (k < op.kdim && tid < (ks1 - ks0) * BK) mixed_offsets32(op.kk, k, o, dummy);
+    koff[tid] = o;                         // -1 marks padding
+  }
+}
+
+__global__ void __launch_bounds__(256) pack_rowmax(PackArgs2 a) {
   __shared__ int64_t rowoff[BM];
-  __shared__ int32_t Er[BM];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int S = a.slices;
-  const int c = lane & 3;                               // k chunk of this lane
+  __shared__ int64_t koff[PACK_KC * BK];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, c = lane & 3;
   for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
-    const PackItem pi = a.items[it];
+    const PackItem2 pi = a.items[it];
     const SplitOp& op = a.ops[pi.op];
     const int ROWS = op.is_b ? BN : BM;
-    const int units = ROWS / 64;                        // rows per thread: 2 (A) or 1 (B)
+    const int units = ROWS / 64;
     const double* src = (op.is_b ? a.ptrs.B[op.job] : a.ptrs.A[op.job]) + op.src_off;
-    const int r0 = pi.rt * ROWS;
-    const int kpad = op.k_steps * BK;
+    int ks0, ks1;
     __syncthreads();
-    if (tid < ROWS) {
-      int64_t o = 0, dummy;
-      if (r0 + tid < op.rows) mixed_offsets32(op.rk, r0 + tid, o, dummy);
-      rowoff[tid] = o;
-    }
-    for (int k = tid; k < kpad; k += 256) {
-      int64_t o = -1, dummy;
-      if (k < op.kdim) mixed_offsets32(op.kk, k, o, dummy);
-      koff[k] = o;                                      // -1 marks padding
-    }
+    pack_setup(op, pi, ROWS, rowoff, koff, ks0, ks1);
     __syncthreads();
-    int rr[2];
-    bool rv[2];
+    bool bad = false;
 #pragma unroll
-    for (int j = 0; j < 2; ++j) { rr[j] = (lane >> 2) + 8 * warp + 64 * j; rv[j] = j < units && r0 + rr[j] < op.rows; }
-    // pass 1: row maxima of |x| (IEEE bit patterns are monotonic for finite x)
-    int E[2] = {0, 0};
-    if (S > 2) {
-      unsigned long long mx[2] = {0ull, 0ull};
-      bool bad = false;
-      for (int ks = 0; ks < op.k_steps; ++ks) {
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          if (!rv[j]) continue;
-          const double* rowp = src + rowoff[rr[j]];
+    for (int j = 0; j < 2; ++j) {
+      if (j >= units) continue;
+      const int r = (lane >> 2) + 8 * warp + 64 * j;
+      const bool rv = pi.rt * ROWS + r < op.rows;
+      unsigned long long mx = 0ull;
+      if (rv) {
+        const double* rowp = src + rowoff[r];
+        for (int ks = 0; ks < ks1 - ks0; ++ks) {
 #pragma unroll
           for (int e = 0; e < 8; ++e) {
             const int64_t ko = koff[ks * BK + c * 8 + e];
             if (ko >= 0) {
               uint64_t b = (uint64_t)__double_as_longlong(__ldg(rowp + ko)) & 0x7fffffffffffffffull;
               if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
-              mx[j] = b > mx[j] ? b : mx[j];
+              mx = b > mx ? b : mx;
             }
           }
         }
       }
-      if (bad && atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        unsigned long long v = mx[j];
-        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, 1); v = w > v ? w : v;
-        w = __shfl_xor_sync(0xffffffffu, v, 2); v = w > v ? w : v;
-        const int ex = (int)(v >> 52);
-        E[j] = (ex ? ex : 1) - 1022;                    // max|x| < 2^E
-        if (j < units && c == 0) a.exps[op.exp_off + r0 + rr[j]] = E[j];
-      }
+      unsigned long long w = __shfl_xor_sync(0xffffffffu, mx, 1); mx = w > mx ? w : mx;
+      w = __shfl_xor_sync(0xffffffffu, mx, 2); mx = w > mx ? w : mx;
+      if (c == 0 && rv && mx) atomicMax(&a.rowmax[op.exp_off + pi.rt * ROWS + r], mx);
     }
-    // pass 2: digits (pre-scaled: slice p holds d_p * 2^(-8(p-1))), 16-byte stores
-    for (int ks = 0; ks < op.k_steps; ++ks) {
-      unsigned char* tile = a.pack + op.pack_off + ((int64_t)(pi.rt * op.k_steps + ks) * S) * (ROWS * 64);
+    if (bad && atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
+  }
+}
+
+__global__ void __launch_bounds__(256) pack_digits(PackArgs2 a) {
+  __shared__ int64_t rowoff[BM];
+  __shared__ int64_t koff[PACK_KC * BK];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, c = lane & 3;
+  const int S = a.slices;
+  for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
+    const PackItem2 pi = a.items[it];
+    const SplitOp& op = a.ops[pi.op];
+    const int ROWS = op.is_b ? BN : BM;
+    const int units = ROWS / 64;
+    const double* src = (op.is_b ? a.ptrs.B[op.job] : a.ptrs.A[op.job]) + op.src_off;
+    int ks0, ks1;
+    __syncthreads();
+    pack_setup(op, pi, ROWS, rowoff, koff, ks0, ks1);
+    __syncthreads();
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        if (j >= units) continue;
-        const int r = rr[j];
-        const double* rowp = src + rowoff[r];
+    for (int j = 0; j < 2; ++j) {
+      if (j >= units) continue;
+      const int r = (lane >> 2) + 8 * warp + 64 * j;
+      const bool rv = pi.rt * ROWS + r < op.rows;
+      int E = 0;
+      if (S > 2) {
+        const int ex = (int)(a.rowmax[op.exp_off + pi.rt * ROWS + r] >> 52);
+        E = (ex ? ex : 1) - 1022;                      // max|x| < 2^E
+        if (pi.kc == 0 && c == 0) a.exps[op.exp_off + pi.rt * ROWS + r] = E;
+      }
+      const double* rowp = src + rowoff[r];
+      for (int ks = ks0; ks < ks1; ++ks) {
+        unsigned char* tile = a.pack + op.pack_off + ((int64_t)(pi.rt * op.k_steps + ks) * S) * (ROWS * 64);
         uint32_t w[6][4];
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
           uint16_t h0[6], h1[6];
-          const int64_t k0 = koff[ks * BK + c * 8 + e], k1 = koff[ks * BK + c * 8 + e + 1];
-          const uint64_t b0 = (rv[j] && k0 >= 0) ? (uint64_t)__double_as_longlong(__ldg(rowp + k0)) : 0ull;
-          const uint64_t b1 = (rv[j] && k1 >= 0) ? (uint64_t)__double_as_longlong(__ldg(rowp + k1)) : 0ull;
-          pack_unit_digits(b0, E[j], S, h0);
-          pack_unit_digits(b1, E[j], S, h1);
+          const int64_t k0 = koff[(ks - ks0) * BK + c * 8 + e], k1 = koff[(ks - ks0) * BK + c * 8 + e + 1];
+          const uint64_t b0 = (rv && k0 >= 0) ? (uint64_t)__double_as_longlong(__ldg(rowp + k0)) : 0ull;
+          const uint64_t b1 = (rv && k1 >= 0) ? (uint64_t)__double_as_longlong(__ldg(rowp + k1)) : 0ull;
+          pack_unit_digits(b0, E, S, h0);
+          pack_unit_digits(b1, E, S, h1);
 #pragma unroll
           for (int q = 0; q < 6; ++q) w[q][e / 2] = (uint32_t)h0[q] | ((uint32_t)h1[q] << 16);
         }
@@ -664,14 +688,10 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
     pd.a_op = add_op(false, pd);
     pd.b_op = add_op(true, pd);
   }
-  int maxk = BK;
-  for (auto& o : ops) maxk = std::max(maxk, o.k_steps * BK);
-  if (maxk > PACK_MAXK)
-    return nd_fail(h, ND_ERR_UNSUPPORTED, "split GEMM: contracted extent %d exceeds %d (use ND_PREC_FP64)", maxk, PACK_MAXK);
-  c.pack_maxk = maxk;
-  std::vector<PackItem> pitems;
+  std::vector<PackItem2> pitems;
   for (int i = 0; i < (int)ops.size(); ++i)
-    for (int t = 0; t < ops[i].row_tiles; ++t) pitems.push_back({i, t});
+    for (int t = 0; t < ops[i].row_tiles; ++t)
+      for (int kc = 0; kc * PACK_KC < ops[i].k_steps; ++kc) pitems.push_back({i, t, kc});
   // work items: 128 x 64 tiles, biggest first
   struct G { int begin, count; int64_t cost; };
   std::vector<std::pair<int64_t, WorkItem>> tmp;
@@ -701,7 +721,8 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
   if ((s = up((void**)&c.d_split_pairs, pairs.data(), pairs.size() * sizeof(PairDesc)))) return s;
   if ((s = up((void**)&c.d_split_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
   if ((s = up(&c.d_operands, ops.data(), ops.size() * sizeof(SplitOp)))) return s;
-  if ((s = up(&c.d_pack_items, pitems.data(), pitems.size() * sizeof(PackItem)))) return s;
+  if ((s = up(&c.d_pack_items, pitems.data(), pitems.size() * sizeof(PackItem2)))) return s;
+  ND_CUDA(h, cudaMalloc((void**)&c.d_rowmax, std::max<int64_t>(exp_count, 1) * 8));
   ND_CUDA(h, cudaMalloc(&c.d_pack, std::max<int64_t>(pack_bytes, 16)));
   ND_CUDA(h, cudaMalloc((void**)&c.d_exp, std::max<int64_t>(exp_count, 4) * 4));
   c.pack_bytes = pack_bytes;
@@ -716,18 +737,19 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
 
 nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double alpha, double beta) {
   const int S = c.slices;
-  PackArgs pa{(const SplitOp*)c.d_operands, (const PackItem*)c.d_pack_items, c.npack_items, ptrs,
-              (unsigned char*)c.d_pack, c.d_exp, S, h->d_status};
-  const int psmem = (int)(c.pack_maxk * sizeof(int64_t));
-  static bool pattr = false;
-  if (!pattr) {
-    cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, PACK_MAXK * 8);
-    pattr = true;
-  }
-  int pblocks = std::min(c.npack_items, h->num_sms * 6);
+  PackArgs2 pa{(const SplitOp*)c.d_operands, (const PackItem2*)c.d_pack_items, c.npack_items, ptrs,
+               (unsigned char*)c.d_pack, c.d_exp, (unsigned long long*)c.d_rowmax, S, h->d_status};
+  int pblocks = std::min(c.npack_items, h->num_sms * 8);
   if (pblocks > 0) {
-    nd_prof_begin(h, "pack_kernel");
-    pack_kernel<<<pblocks, 256, psmem, h->stream>>>(pa);
+    if (S > 2) {
+      ND_CUDA(h, cudaMemsetAsync(c.d_rowmax, 0, c.exp_count * 8, h->stream));
+      nd_prof_begin(h, "pack_rowmax");
+      pack_rowmax<<<pblocks, 256, 0, h->stream>>>(pa);
+      nd_prof_end(h);
+      ND_LAUNCHED(h);
+    }
+    nd_prof_begin(h, "pack_digits");
+    pack_digits<<<pblocks, 256, 0, h->stream>>>(pa);
     nd_prof_end(h);
     ND_LAUNCHED(h);
     ND_CUDA(h, cudaGetLastError());

@@ -58,7 +58,7 @@ struct ExecCache {
   size_t exp_count = 0;
   void* d_pack_items = nullptr;    // pack work list
   int npack_items = 0;
-  int pack_maxk = 0;               // largest padded K of a split operand
+  void* d_rowmax = nullptr;        // per-row |x| maxima (IEEE bits) of the split operands
   void free_all();
 };
 
