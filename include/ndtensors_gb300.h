@@ -186,6 +186,21 @@ nd_status nd_truncate_f64(nd_handle h, const double *P, int32_t n, int32_t mindi
                           double cutoff, int32_t use_absolute_cutoff, int32_t use_relative_cutoff,
                           int32_t *newlen, double *truncerr, double *docut);
 
+/* Strided block copies: for each entry, dst[dst_off + sum_k i_k*dst_strides[k]] =
+ * src[src_off + sum_k i_k*src_strides[k]] over the box dims[0..rank).  This is the
+ * data motion of the block-sparse combiner (permutedims_combine / uncombine,
+ * NDTensors/src/blocksparse/blocksparsetensor.jl:537-638,693-791): the host
+ * computes the combined block structure, the device gathers / scatters. */
+typedef struct {
+  int64_t src_off, dst_off;
+  int32_t rank;
+  int64_t dims[ND_MAX_RANK];
+  int64_t src_strides[ND_MAX_RANK];
+  int64_t dst_strides[ND_MAX_RANK];
+} nd_block_copy;
+nd_status nd_block_copy_f64(nd_handle h, int32_t n, const nd_block_copy *list /* host */, const double *src,
+                            double *dst);
+
 /* ---- CUDA graphs ---------------------------------------------------------
  * Capture the handle's stream into a graph (a sweep step) and replay it. */
 nd_status nd_graph_begin(nd_handle h);

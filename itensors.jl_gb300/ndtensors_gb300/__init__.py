@@ -7,6 +7,8 @@ every operation runs in the library's CUDA kernels.
 from ._lib import NDError, NoConvergence, PRECISIONS, handle, load, LIB_PATH
 from .tensors import BlockSparseTensor, DenseTensor, blockoffsets
 from . import workloads
+from . import linalg
+from .linalg import Spectrum, matricize, qr, svd, truncate
 from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
 
@@ -15,4 +17,5 @@ __all__ = [
     "BlockSparseTensor", "DenseTensor", "blockoffsets",
     "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
     "permutedims", "permutedims_", "permutedims_blocksparse",
+    "linalg", "Spectrum", "matricize", "qr", "svd", "truncate",
 ]

@@ -31,6 +31,12 @@ class NoConvergence(NDError):
     pass
 
 
+class BlockCopy(C.Structure):
+    _fields_ = [("src_off", C.c_int64), ("dst_off", C.c_int64), ("rank", C.c_int32),
+                ("dims", C.c_int64 * MAX_RANK), ("src_strides", C.c_int64 * MAX_RANK),
+                ("dst_strides", C.c_int64 * MAX_RANK)]
+
+
 class BsDesc(C.Structure):
     _fields_ = [("rank", C.c_int32), ("nblocks", C.POINTER(C.c_int32)), ("blockdims", C.POINTER(C.c_int64)),
                 ("nnzblocks", C.c_int32), ("blocks", C.POINTER(C.c_int32)), ("offsets", C.POINTER(C.c_int64))]
@@ -75,6 +81,7 @@ SIGNATURES = {
                       _PI32, _PD, _PI32, _PD, _PD],
     "nd_bs_qr_f64": [_P, _I32, _PI64, _PI64, _PI64, _P, _P, _P, _I32],
     "nd_truncate_f64": [_P, _P, _I32, _I32, _I32, _D, _I32, _I32, _PI32, _PD, _PD],
+    "nd_block_copy_f64": [_P, _I32, C.POINTER(BlockCopy), _P, _P],
     "nd_graph_begin": [_P],
     "nd_graph_end": [_P, C.POINTER(_P)],
     "nd_graph_launch": [_P, _P],

@@ -1,0 +1,223 @@
+"""Blockwise factorizations and the block-sparse combiner on the GB300 library.
+
+Mirrors:
+  svd(T::BlockSparseMatrix; mindim, maxdim, cutoff, use_absolute_cutoff,
+      use_relative_cutoff, min_blockdim)        NDTensors/src/blocksparse/linearalgebra.jl:45-215
+  qr(T::BlockSparseMatrix; positive)            NDTensors/src/blocksparse/linearalgebra.jl:351-415
+  truncate!(P; ...)                             NDTensors/src/truncate.jl:23-107
+  combiner matricization (permutedims_combine)  NDTensors/src/blocksparse/blocksparsetensor.jl:537-638,
+                                                src/qn/qnindex.jl:359-426
+The factorizations, the spectrum sort and truncate! run on the device; only
+the block structure (which blocks survive, their new dims) is host logic.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+
+import numpy as np
+
+from ._lib import BlockCopy, MAX_RANK, NoConvergence, handle, i32arr, i64arr
+from .tensors import BlockSparseTensor, blockoffsets
+
+
+def _opt(x, none=-1):
+    return none if x is None else x
+
+
+class Spectrum:
+    """Spectrum(eigs, truncerr) (NDTensors/src/lib/RankFactorization/src/spectrum.jl:6-9)."""
+
+    def __init__(self, eigs, truncerr):
+        self.eigs = np.asarray(eigs)
+        self.truncerr = float(truncerr)
+
+
+def _matrix_blocks(T: BlockSparseTensor):
+    if T.rank != 2:
+        raise ValueError("factorizations need an order-2 block-sparse tensor")
+    rows = [T.inds[0][b[0] - 1] for b in T.blocks]
+    cols = [T.inds[1][b[1] - 1] for b in T.blocks]
+    return rows, cols
+
+
+def svd(T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absolute_cutoff=None,
+        use_relative_cutoff=None, min_blockdim=None):
+    """Returns (U, S, V, Spectrum, kept) or raises NoConvergence (the reference returns nothing).
+
+    U has inds (T.inds[0], u), S is a list of per-block singular values (Diag),
+    V has inds (T.inds[1], v); u and v carry one block per surviving nz block.
+    """
+    import torch
+    rows, cols = _matrix_blocks(T)
+    nb = len(T.blocks)
+    h = handle(T.data.device.index or 0)
+    ks = [min(r, c) for r, c in zip(rows, cols)]
+    dev = T.data.device
+    U = torch.empty(max(1, sum(r * k for r, k in zip(rows, ks))), dtype=torch.float64, device=dev)
+    S = torch.empty(max(1, sum(ks)), dtype=torch.float64, device=dev)
+    V = torch.empty(max(1, sum(c * k for c, k in zip(cols, ks))), dtype=torch.float64, device=dev)
+    kept = (C.c_int32 * max(1, nb))()
+    spec = (C.c_double * max(1, sum(ks)))()
+    slen, terr, dcut = C.c_int32(), C.c_double(), C.c_double()
+    h.call("nd_bs_svd_f64", nb, i64arr(rows), i64arr(cols), i64arr(T.offsets), C.c_void_p(T.data.data_ptr()),
+           C.c_void_p(U.data_ptr()), C.c_void_p(S.data_ptr()), C.c_void_p(V.data_ptr()),
+           int(_opt(mindim, 1)), int(_opt(maxdim, -1)), float(_opt(cutoff, -1.0)),
+           int(bool(use_absolute_cutoff)) if use_absolute_cutoff is not None else 0,
+           int(bool(use_relative_cutoff)) if use_relative_cutoff is not None else 1,
+           int(_opt(min_blockdim, 0)), kept, spec, C.byref(slen), C.byref(terr), C.byref(dcut))
+    kept = list(kept[:nb])
+    surv = [n for n in range(nb) if kept[n] > 0]
+    kdims = [kept[n] for n in surv]
+    # new indices u, v: one block per surviving block (linearalgebra.jl:124-156)
+    u_ind = tuple(kdims)
+    Ublocks = [(T.blocks[n][0], i + 1) for i, n in enumerate(surv)]
+    Vblocks = [(T.blocks[n][1], i + 1) for i, n in enumerate(surv)]
+    Uo, nu = blockoffsets(Ublocks, [T.inds[0], u_ind])
+    Vo, nv = blockoffsets(Vblocks, [T.inds[1], u_ind])
+    Ut = BlockSparseTensor([tuple(T.inds[0]), u_ind], Ublocks, Uo, U[:nu])
+    Vt = BlockSparseTensor([tuple(T.inds[1]), u_ind], Vblocks, Vo, V[:nv])
+    Sv, o = [], 0
+    for k in kdims:
+        Sv.append(S[o:o + k])
+        o += k
+    sp = np.array(spec[:slen.value])          # sorted s^2, computed on the device
+    return Ut, Sv, Vt, Spectrum(sp, terr.value), kept
+
+
+def qr(T: BlockSparseTensor, positive=False):
+    """Q with inds (T.inds[0], q), R with inds (q, T.inds[1]); q has one block per nz block."""
+    import torch
+    rows, cols = _matrix_blocks(T)
+    nb = len(T.blocks)
+    ks = [min(r, c) for r, c in zip(rows, cols)]
+    dev = T.data.device
+    Q = torch.empty(max(1, sum(r * k for r, k in zip(rows, ks))), dtype=torch.float64, device=dev)
+    R = torch.empty(max(1, sum(c * k for c, k in zip(cols, ks))), dtype=torch.float64, device=dev)
+    h = handle(T.data.device.index or 0)
+    h.call("nd_bs_qr_f64", nb, i64arr(rows), i64arr(cols), i64arr(T.offsets), C.c_void_p(T.data.data_ptr()),
+           C.c_void_p(Q.data_ptr()), C.c_void_p(R.data_ptr()), 1 if positive else 0)
+    q_ind = tuple(ks)
+    Qb = [(T.blocks[n][0], n + 1) for n in range(nb)]
+    Rb = [(n + 1, T.blocks[n][1]) for n in range(nb)]
+    Qo, nq = blockoffsets(Qb, [T.inds[0], q_ind])
+    Ro, nr = blockoffsets(Rb, [q_ind, T.inds[1]])
+    return (BlockSparseTensor([tuple(T.inds[0]), q_ind], Qb, Qo, Q[:nq]),
+            BlockSparseTensor([q_ind, tuple(T.inds[1])], Rb, Ro, R[:nr]))
+
+
+def truncate(P, mindim=None, maxdim=None, cutoff=None, use_absolute_cutoff=None, use_relative_cutoff=None):
+    """truncate! of a device vector of descending weights -> (new length, truncerr, docut)."""
+    h = handle(P.device.index or 0)
+    n, te, dc = C.c_int32(), C.c_double(), C.c_double()
+    h.call("nd_truncate_f64", C.c_void_p(P.data_ptr()), int(P.numel()), int(_opt(mindim, 1)), int(_opt(maxdim, -1)),
+           float(_opt(cutoff, -1.0)), int(bool(use_absolute_cutoff)) if use_absolute_cutoff is not None else 0,
+           int(bool(use_relative_cutoff)) if use_relative_cutoff is not None else 1, C.byref(n), C.byref(te),
+           C.byref(dc))
+    return n.value, te.value, dc.value
+
+
+# ---------------------------------------------------------------------------
+# QN combiner: fuse a group of indices (host structure, device data motion)
+# ---------------------------------------------------------------------------
+
+def fused_sectors(group):
+    """Sectors of the fused index of [(sectors, arrow), ...], first index fastest
+    (src/qn/qnindex.jl:359-379; outer over several indices folds pairwise).  The
+    fused arrow is Out unless all arrows agree; charges are arrow*sum(a_k q_k)."""
+    arrows = [a for _, a in group]
+    arrow = arrows[0] if all(a == arrows[0] for a in arrows) else 1
+    out = []
+    for combo in itertools.product(*[range(len(s)) for s, _ in reversed(group)]):
+        combo = tuple(reversed(combo))
+        q = sum(a * s[i][0] for (s, a), i in zip(group, combo))
+        d = 1
+        for (s, _), i in zip(group, combo):
+            d *= s[i][1]
+        out.append((arrow * q, d))
+    return out, arrow
+
+
+def combine_blocks(sectors):
+    """(combined sectors, perm, comb): stable sort by charge then merge (qnindex.jl:407-426)."""
+    perm = sorted(range(len(sectors)), key=lambda i: sectors[i][0])
+    comb, merged = [], []
+    for pos, i in enumerate(perm):
+        if pos > 0 and sectors[i][0] == sectors[perm[pos - 1]][0]:
+            merged[-1][1] += sectors[i][1]
+        else:
+            merged.append([sectors[i][0], sectors[i][1]])
+        comb.append(len(merged))
+    return [tuple(m) for m in merged], perm, comb
+
+
+def _group_place(group):
+    fused, _ = fused_sectors(group)
+    merged, perm, comb = combine_blocks(fused)
+    place = {}
+    for pos, orig in enumerate(perm):
+        off = sum(fused[perm[q]][1] for q in range(pos) if comb[q] == comb[pos])
+        place[orig] = (comb[pos], off)          # orig is 0-based fused position
+    return merged, place
+
+
+def matricize(T: BlockSparseTensor, qinds, row_dims, col_dims):
+    """Fuse T's dimensions into (row group, column group) as ITensor's svd / qr do
+    with two combiners (src/tensor_operations/matrix_decomposition.jl:153-160).
+    qinds: per dimension (sectors, arrow).  Returns (matrix, row_info, col_info)."""
+    import torch
+    rows_g = [qinds[d] for d in row_dims]
+    cols_g = [qinds[d] for d in col_dims]
+    rsec, rplace = _group_place(rows_g)
+    csec, cplace = _group_place(cols_g)
+    nbr = [len(qinds[d][0]) for d in row_dims]
+    nbc = [len(qinds[d][0]) for d in col_dims]
+
+    def lin(b, dims, nbs):
+        v, mul = 0, 1
+        for d, n in zip(dims, nbs):
+            v += (b[d] - 1) * mul
+            mul *= n
+        return v
+
+    entries = {}
+    for i, b in enumerate(T.blocks):
+        rb, roff = rplace[lin(b, row_dims, nbr)]
+        cb, coff = cplace[lin(b, col_dims, nbc)]
+        entries.setdefault((rb, cb), []).append((i, roff, coff))
+    mblocks = sorted(entries, key=lambda x: (x[1], x[0]))       # isblockless: column block most significant
+    minds = [tuple(d for _, d in rsec), tuple(d for _, d in csec)]
+    offs, nnz = blockoffsets(mblocks, minds)
+    data = torch.zeros(max(nnz, 1), dtype=torch.float64, device=T.data.device)[:nnz]
+    M = BlockSparseTensor(minds, mblocks, offs, data)
+    copies = []
+    for j, mb in enumerate(mblocks):
+        ld = minds[0][mb[0] - 1]
+        for (i, roff, coff) in entries[mb]:
+            bd = T.blockdims(T.blocks[i])
+            st = [1]
+            for d in bd[:-1]:
+                st.append(st[-1] * d)
+            c = BlockCopy()
+            c.src_off = T.offsets[i]
+            c.dst_off = offs[j] + roff + coff * ld
+            c.rank = len(bd)
+            # destination strides: row dims fastest inside the fused row index, then columns (times ld)
+            rs, cs = 1, ld
+            dst = [0] * len(bd)
+            for d in row_dims:
+                dst[d] = rs
+                rs *= bd[d]
+            for d in col_dims:
+                dst[d] = cs
+                cs *= bd[d]
+            for k in range(len(bd)):
+                c.dims[k] = bd[k]
+                c.src_strides[k] = st[k]
+                c.dst_strides[k] = dst[k]
+            copies.append(c)
+    if copies:
+        arr = (BlockCopy * len(copies))(*copies)
+        handle(T.data.device.index or 0).call("nd_block_copy_f64", len(copies), arr, C.c_void_p(T.data.data_ptr()),
+                                              C.c_void_p(data.data_ptr()))
+    return M, (rsec, rplace), (csec, cplace)

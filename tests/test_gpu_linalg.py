@@ -1,0 +1,181 @@
+"""Blockwise SVD / QR / truncate! / combiner on the GPU vs the oracle (GPU).
+
+Singular values: within 1e-12 of LAPACK gesdd relative to the block's largest;
+reconstruction U S V^T within 1e-12 relative Frobenius; truncation decisions
+(kept dims per block, truncerr, spectrum length) identical to the oracle.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import blocksparse as obs
+from oracle import dense as odense
+from oracle import linalg as olin
+from oracle import networks, qn
+from oracle import truncate as otr
+
+pytestmark = pytest.mark.gpu
+KATS = json.loads((Path(__file__).parent / "golden" / "reference_kats.json").read_text())
+
+
+def _gpu(nd, t):
+    return nd.BlockSparseTensor.from_oracle(t)
+
+
+def _blocks(nd, T):
+    """Per-block dense numpy matrices of a GPU block-sparse matrix."""
+    out = []
+    data = T.data_numpy()
+    for i, b in enumerate(T.blocks):
+        d = T.blockdims(b)
+        out.append(data[T.offsets[i]:T.offsets[i] + d[0] * d[1]].reshape(d, order="F"))
+    return out
+
+
+# the five structures of NDTensors/test/test_blocksparse.jl:276-321
+SVD_EXAMPLES = [
+    ([(2, 1), (1, 2)], [2, 2], [2, 2]),
+    ([(1, 2), (2, 3)], [2, 2], [3, 2, 3]),
+    ([(2, 1), (3, 2)], [3, 2, 3], [2, 2]),
+    ([(2, 1), (3, 2)], [2, 3, 4], [5, 6]),
+    ([(1, 2), (2, 3)], [5, 6], [2, 3, 4]),
+]
+
+
+@pytest.mark.parametrize("ex", SVD_EXAMPLES)
+def test_svd_reference_examples(nd, ex):
+    blocks, i1, i2 = ex
+    A = obs.random_blocksparse(np.random.default_rng(1), [i1, i2], blocks)
+    U, S, V, spec, kept = nd.svd(_gpu(nd, A))
+    Ub, Vb = _blocks(nd, U), _blocks(nd, V)
+    for n, m in enumerate(_blocks(nd, _gpu(nd, A))):
+        s = S[n].cpu().numpy()
+        np.testing.assert_allclose(Ub[n] @ np.diag(s) @ Vb[n].T, m, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(s, np.linalg.svd(m, compute_uv=False), rtol=1e-12, atol=1e-12 * s[0])
+
+
+@pytest.mark.parametrize("shape", [(40, 40), (130, 33), (33, 130), (257, 255), (1, 7), (600, 64)])
+def test_svd_dense_block(nd, shape):
+    rng = np.random.default_rng(sum(shape))
+    m = rng.standard_normal(shape)
+    A = obs.BlockSparseTensor([[shape[0]], [shape[1]]], [(1, 1)], [0], m.reshape(-1, order="F"))
+    U, S, V, spec, kept = nd.svd(_gpu(nd, A))
+    u, s, v = _blocks(nd, U)[0], S[0].cpu().numpy(), _blocks(nd, V)[0]
+    ref = np.linalg.svd(m, compute_uv=False)
+    np.testing.assert_allclose(s, ref, rtol=0, atol=1e-12 * ref[0])
+    assert odense.rel_frobenius_error(u @ np.diag(s) @ v.T, m) <= 1e-12
+    k = len(s)
+    np.testing.assert_allclose(u.T @ u, np.eye(k), atol=1e-12)
+    np.testing.assert_allclose(v.T @ v, np.eye(k), atol=1e-12)
+    np.testing.assert_allclose(spec.eigs, np.sort(ref ** 2)[::-1], rtol=1e-12, atol=1e-12 * ref[0] ** 2)
+
+
+def test_svd_graded_spectrum_truncation(nd):
+    """Blocks with geometric singular values: truncation by cutoff must match the oracle exactly."""
+    rng = np.random.default_rng(5)
+    mats = []
+    for n, (r, c) in enumerate([(60, 50), (40, 70), (30, 30), (8, 12)]):
+        q1, _ = np.linalg.qr(rng.standard_normal((r, r)))
+        q2, _ = np.linalg.qr(rng.standard_normal((c, c)))
+        k = min(r, c)
+        sv = np.exp(-np.arange(k) * (0.35 + 0.1 * n)) * (1.0 + n)
+        d = np.zeros((r, c))
+        d[:k, :k] = np.diag(sv)
+        mats.append(q1 @ d @ q2.T)
+    inds = [[m.shape[0] for m in mats], [m.shape[1] for m in mats]]
+    blocks = [(i + 1, i + 1) for i in range(len(mats))]
+    offs, nnz = obs.blockoffsets(blocks, inds)
+    A = obs.BlockSparseTensor(inds, blocks, offs, np.concatenate([m.reshape(-1, order="F") for m in mats]))
+    for kw in ({"cutoff": 1e-10}, {"cutoff": 1e-6, "maxdim": 40}, {"maxdim": 25},
+               {"cutoff": 1e-8, "use_absolute_cutoff": True}, {"cutoff": 1e-1, "min_blockdim": 2}):
+        ref = olin.svd_blocks(mats, **kw)
+        U, S, V, spec, kept = nd.svd(_gpu(nd, A), **kw)
+        assert kept == ref["kept"], kw
+        assert len(spec.eigs) == len(ref["spectrum"])
+        np.testing.assert_allclose(spec.eigs, ref["spectrum"], rtol=1e-10, atol=1e-14)
+        assert abs(spec.truncerr - ref["truncerr"]) <= 1e-10 * max(1.0, abs(ref["truncerr"])) + 1e-15
+
+
+@pytest.mark.parametrize("case", KATS["truncate"], ids=lambda c: c["src"])
+def test_truncate_kats_on_device(nd, case):
+    import torch
+    P = torch.tensor(case["P"], dtype=torch.float64, device="cuda")
+    n, te, dc = nd.truncate(P, **case["kwargs"])
+    assert (te, dc) == (case["truncerr"], case["docut"])
+    assert n == case["len"]
+
+
+def test_svd_min_blockdim_kat(nd):
+    k = KATS["svd_min_blockdim"]
+    i = qn.QNIndex(tuple(tuple(x) for x in k["i"]), 1, "i")
+    j = qn.QNIndex(tuple(tuple(x) for x in k["i"]), 1, "j")
+    X = obs.random_blocksparse(np.random.default_rng(7), [i.dims, j.dims], qn.nzblocks(0, [i, j]))
+    mats = [X.blockview(n) for n in range(len(X.blocks))]
+    ref = olin.svd_blocks(mats, cutoff=k["cutoff"], min_blockdim=k["min_blockdim"])
+    U, S, V, spec, kept = nd.svd(_gpu(nd, X), cutoff=k["cutoff"], min_blockdim=k["min_blockdim"])
+    assert kept == ref["kept"]
+    for n, m in enumerate(mats):
+        assert kept[n] == min(m.shape) or kept[n] >= k["min_blockdim"]
+
+
+@pytest.mark.parametrize("positive", [False, True])
+@pytest.mark.parametrize("shape", [(30, 30), (50, 20), (20, 50), (1, 5), (200, 100)])
+def test_qr_blocks(nd, shape, positive):
+    rng = np.random.default_rng(shape[0] * 7 + shape[1])
+    mats = [rng.standard_normal(shape), rng.standard_normal((shape[1], shape[0]))]
+    inds = [[shape[0], shape[1]], [shape[1], shape[0]]]
+    blocks = [(1, 1), (2, 2)]
+    offs, nnz = obs.blockoffsets(blocks, inds)
+    A = obs.BlockSparseTensor(inds, blocks, offs, np.concatenate([m.reshape(-1, order="F") for m in mats]))
+    Q, R = nd.qr(_gpu(nd, A), positive=positive)
+    oq, orr = olin.qr_blocks(mats, positive=positive)
+    for n, m in enumerate(mats):
+        q, r = _blocks(nd, Q)[n], _blocks(nd, R)[n]
+        np.testing.assert_allclose(q @ r, m, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(q.T @ q, np.eye(q.shape[1]), atol=1e-12)
+        assert np.allclose(np.tril(r, -1), 0)
+        if positive:
+            assert (np.diag(r) >= 0).all()
+        # same sign convention as LAPACK geqrf (and unique when positive)
+        np.testing.assert_allclose(q, oq[n], rtol=1e-10, atol=1e-10)
+        np.testing.assert_allclose(r, orr[n], rtol=1e-10, atol=1e-10)
+
+
+def test_matricize_matches_oracle(nd):
+    net = networks.qn_heff(chi=256, seed=11)
+    psi = net["psi"]
+    qinds = net["qinds"]["psi"]
+    ref, rinfo, cinfo = obs.matricize(psi, qinds, (0, 1), (2, 3))
+    M, _, _ = nd.matricize(_gpu(nd, psi), [(q.sectors, q.arrow) for q in qinds], (0, 1), (2, 3))
+    assert M.blocks == [tuple(b) for b in ref.blocks]
+    assert M.offsets == list(ref.offsets)
+    np.testing.assert_array_equal(M.data_numpy(), ref.data)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_two_site_step(nd, precision):
+    """H_eff matvec -> matricize (l,s1)x(s2,r) -> truncated blockwise SVD, vs the oracle."""
+    net = networks.qn_heff(chi=512, seed=13)
+    steps = networks.heff_steps()
+    # oracle
+    t, _ = obs.contract(net["L"], steps[0][0], net["psi"], steps[0][1], steps[0][2])
+    for (a, b, c), key in zip(steps[1:], ("W1", "W2", "R")):
+        t, _ = obs.contract(t, a, net[key], b, c)
+    qi = [net["qinds"]["psi"][k] for k in range(4)]          # result has psi's structure (lo, s1o, s2o, ro)
+    Mref, _, _ = obs.matricize(t, qi, (0, 1), (2, 3))
+    mats = [Mref.blockview(n) for n in range(len(Mref.blocks))]
+    ref = olin.svd_blocks(mats, maxdim=512, cutoff=1e-10)
+    # GPU
+    G = {k: _gpu(nd, net[k]) for k in ("L", "psi", "W1", "W2", "R")}
+    x = nd.contract(G["L"], steps[0][0], G["psi"], steps[0][1], steps[0][2], precision=precision)
+    for (a, b, c), key in zip(steps[1:], ("W1", "W2", "R")):
+        x = nd.contract(x, a, G[key], b, c, precision=precision)
+    assert x.blocks == [tuple(b) for b in t.blocks]
+    assert odense.rel_frobenius_error(x.data_numpy(), t.data) <= (1e-13 if precision == "fp64" else 1e-10)
+    M, _, _ = nd.matricize(x, [(q.sectors, q.arrow) for q in qi], (0, 1), (2, 3))
+    U, S, V, spec, kept = nd.svd(M, maxdim=512, cutoff=1e-10)
+    assert kept == ref["kept"]
+    np.testing.assert_allclose(spec.eigs, ref["spectrum"], rtol=1e-8, atol=1e-13 * ref["spectrum"][0])
+    assert abs(spec.truncerr - ref["truncerr"]) <= 1e-8 * ref["truncerr"] + 1e-16
