@@ -274,8 +274,9 @@ __device__ void truncate_serial(double* P, int n, const TruncParams& tp, int* ne
   *truncerr = te;
 }
 
-__global__ void __launch_bounds__(1024) sort_truncate(const double* sig, int n, int npow2, int squared, TruncParams tp,
-                                                      double* P_out, int* newlen, double* truncerr, double* docut) {
+__global__ void __launch_bounds__(1024) sort_truncate(const double* sig, int n, int npow2, int squared, int do_sort,
+                                                      TruncParams tp, double* P_out, int* newlen, double* truncerr,
+                                                      double* docut) {
   extern __shared__ double P[];
   for (int i = threadIdx.x; i < npow2; i += blockDim.x) {
     double v = -INFINITY;
@@ -284,7 +285,7 @@ __global__ void __launch_bounds__(1024) sort_truncate(const double* sig, int n, 
   }
   __syncthreads();
   // bitonic sort, descending
-  for (int k = 2; k <= npow2; k <<= 1) {
+  for (int k = 2; do_sort && k <= npow2; k <<= 1) {
     for (int j = k >> 1; j > 0; j >>= 1) {
       for (int i = threadIdx.x; i < npow2; i += blockDim.x) {
         const int l = i ^ j;
@@ -586,7 +587,7 @@ extern "C" nd_status nd_bs_svd_f64(nd_handle h, int32_t nb, const int64_t* rows,
   static bool attr = false;
   if (!attr) { cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
   nd_prof_begin(h, "sort_truncate");
-  sort_truncate<<<1, 1024, npow2 * 8, s>>>(sig, total, npow2, 1, tp, P, dlen, res, res + 1);
+  sort_truncate<<<1, 1024, npow2 * 8, s>>>(sig, total, npow2, 1, 1, tp, P, dlen, res, res + 1);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   nd_prof_begin(h, "kept_dims");
@@ -637,9 +638,10 @@ extern "C" nd_status nd_truncate_f64(nd_handle h, const double* Pin, int32_t n, 
   TruncParams tp{mindim < 1 ? 1 : mindim, maxdim, cutoff, cutoff >= 0.0 ? 1 : 0, use_absolute_cutoff, use_relative_cutoff};
   static bool attr = false;
   if (!attr) { cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
-  // the input is documented as already descending; sorting keeps that order
+  // the caller's order is kept (truncate! takes a descending spectrum; a negative
+  // spectrum is descending in magnitude, which a value sort would reverse)
   nd_prof_begin(h, "sort_truncate");
-  sort_truncate<<<1, 1024, npow2 * 8, s>>>(Pin, n, npow2, 0, tp, P, len, res, res + 1);
+  sort_truncate<<<1, 1024, npow2 * 8, s>>>(Pin, n, npow2, 0, 0, tp, P, len, res, res + 1);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   double hr[2];
