@@ -102,6 +102,22 @@ nd_status nd_contract_dense_f64(nd_handle h,
                                 const double *B, int32_t rankB, const int64_t *dimsB, const int32_t *labelsB,
                                 double alpha, double beta, int32_t precision);
 
+/* Same contraction as nd_contract_dense_f64 with ND_PREC_OZAKI, for callers that
+ * cannot allocate device memory during the call (their memory belongs to another
+ * allocator with a hard budget, or they cannot afford cudaMalloc's
+ * synchronisation).  It allocates nothing: its scratch is a fixed 32 MiB device
+ * array inside the library, held by every GPU that loads the library until exit.
+ * Its address is looked up on the first call per device; make that first call
+ * before any stream capture.  Contractions needing more scratch are rejected with
+ * ND_ERR_ARG.  All calls share the array, so calls whose GPU work overlaps race.
+ * No counterpart in the reference: NDTensors always allocates its outputs and
+ * BLAS manages its own workspace. */
+nd_status nd_contract_dense_ozaki_noalloc_f64(nd_handle h,
+                                              double *R, int32_t rankR, const int64_t *dimsR, const int32_t *labelsR,
+                                              const double *A, int32_t rankA, const int64_t *dimsA, const int32_t *labelsA,
+                                              const double *B, int32_t rankB, const int64_t *dimsB, const int32_t *labelsB,
+                                              double alpha, double beta);
+
 /* ---- block-sparse structure ---------------------------------------------
  * A block-sparse operand: per-dimension block dims plus the ordered list of
  * nonzero blocks and their offsets (NDTensors BlockSparse + BlockOffsets,

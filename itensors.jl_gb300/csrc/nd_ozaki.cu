@@ -767,3 +767,86 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
   }
   return nd_fail(h, ND_ERR_ARG, "unsupported slice count %d", S);
 }
+
+// Lay out one split-precision launch inside caller-provided device memory
+// instead of allocating: computes the same operand / pack / tile lists as
+// nd_split_build, reports the bytes needed, and when `base` holds enough,
+// uploads the descriptors there and points the cache's fields into it.
+nd_status nd_split_layout_into(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs_in, int S,
+                               unsigned char* base, size_t capacity, size_t* needed) {
+  std::vector<PairDesc> pairs = pairs_in;
+  std::vector<SplitOp> ops;
+  std::map<std::pair<int, int64_t>, int> amap, bmap;
+  int64_t pack_bytes = 0, exp_count = 0;
+  auto add_op = [&](bool is_b, const PairDesc& pd) -> int {
+    auto& mp = is_b ? bmap : amap;
+    auto key = std::make_pair(pd.job, is_b ? pd.b_off : pd.a_off);
+    auto f = mp.find(key);
+    if (f != mp.end()) return f->second;
+    SplitOp o{};
+    o.src_off = key.second;
+    o.is_b = is_b;
+    o.job = pd.job;
+    o.rows = is_b ? pd.N : pd.M;
+    o.kdim = pd.K;
+    o.rk = is_b ? pd.cols : pd.rows;
+    o.kk = pd.ks;
+    if (is_b) for (int d = 0; d < o.kk.n; ++d) o.kk.st0[d] = pd.ks.st1[d];
+    const int rpt = is_b ? BN : BM;
+    o.row_tiles = (o.rows + rpt - 1) / rpt;
+    o.k_steps = (o.kdim + BK - 1) / BK;
+    o.pack_off = pack_bytes;
+    pack_bytes += (int64_t)o.row_tiles * o.k_steps * S * (is_b ? B_SLICE : A_SLICE);
+    o.exp_off = exp_count;
+    exp_count += (int64_t)o.row_tiles * rpt;
+    ops.push_back(o);
+    mp[key] = (int)ops.size() - 1;
+    return (int)ops.size() - 1;
+  };
+  for (auto& pd : pairs) { pd.a_op = add_op(false, pd); pd.b_op = add_op(true, pd); }
+  std::vector<PackItem2> pitems;
+  for (int i = 0; i < (int)ops.size(); ++i)
+    for (int t = 0; t < ops[i].row_tiles; ++t)
+      for (int kc = 0; kc * PACK_KC < ops[i].k_steps; ++kc) pitems.push_back({i, t, kc});
+  std::vector<WorkItem> items;
+  for (size_t i = 0; i < pairs.size();) {
+    size_t j = i;
+    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) ++j;
+    const PairDesc& p = pairs[i];
+    for (int a = 0; a < (p.M + BM - 1) / BM; ++a)
+      for (int b = 0; b < (p.N + BN - 1) / BN; ++b) items.push_back(WorkItem{p.group, (int)i, (int)(j - i), a, b});
+    i = j;
+  }
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_pairs = 0;
+  const size_t o_items = al(o_pairs + pairs.size() * sizeof(PairDesc));
+  const size_t o_ops = al(o_items + items.size() * sizeof(WorkItem));
+  const size_t o_pit = al(o_ops + ops.size() * sizeof(SplitOp));
+  const size_t o_exp = al(o_pit + pitems.size() * sizeof(PackItem2));
+  const size_t o_rmx = al(o_exp + (size_t)exp_count * 4);
+  const size_t o_pack = al(o_rmx + (size_t)exp_count * 8);
+  const size_t total = o_pack + (size_t)pack_bytes;
+  if (needed) *needed = total;
+  if (!base) return ND_OK;
+  if (total > capacity) return ND_ERR_ARG;
+  cudaStream_t s = h->stream;
+  ND_CUDA(h, cudaMemcpyAsync(base + o_pairs, pairs.data(), pairs.size() * sizeof(PairDesc), cudaMemcpyHostToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(base + o_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(base + o_ops, ops.data(), ops.size() * sizeof(SplitOp), cudaMemcpyHostToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(base + o_pit, pitems.data(), pitems.size() * sizeof(PackItem2), cudaMemcpyHostToDevice, s));
+  c.d_split_pairs = (PairDesc*)(base + o_pairs);
+  c.d_split_items = (WorkItem*)(base + o_items);
+  c.nsplit_items = (int)items.size();
+  c.d_operands = base + o_ops;
+  c.nops_a = (int)amap.size();
+  c.nops_b = (int)bmap.size();
+  c.d_pack_items = base + o_pit;
+  c.npack_items = (int)pitems.size();
+  c.d_exp = (int32_t*)(base + o_exp);
+  c.exp_count = exp_count;
+  c.d_rowmax = base + o_rmx;
+  c.d_pack = base + o_pack;
+  c.pack_bytes = pack_bytes;
+  c.slices = S;
+  return ND_OK;
+}

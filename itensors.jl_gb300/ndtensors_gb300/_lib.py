@@ -70,6 +70,8 @@ SIGNATURES = {
     "nd_permutedims_f64": [_P, _P, _P, _I32, _PI64, _PI32, _D, _D],
     "nd_contract_dense_f64": [_P, _P, _I32, _PI64, _PI32, _P, _I32, _PI64, _PI32, _P, _I32, _PI64, _PI32,
                               _D, _D, _I32],
+    "nd_contract_dense_ozaki_noalloc_f64": [_P, _P, _I32, _PI64, _PI32, _P, _I32, _PI64, _PI32, _P, _I32, _PI64,
+                                            _PI32, _D, _D],
     "nd_bs_plan_create": [_P, C.POINTER(BsDesc), _PI32, C.POINTER(BsDesc), _PI32, _I32, _PI32, C.POINTER(_P)],
     "nd_bs_plan_sizes": [_P, _PI32, _PI32, _PI64],
     "nd_bs_plan_get": [_P, _PI32, _PI64, _PI32],
