@@ -112,8 +112,8 @@ const char* nd_last_error(nd_handle h) { return h ? h->last_error.c_str() : g_no
 
 nd_status nd_set_stream(nd_handle h, void* s) {
   if (!h) return ND_ERR_ARG;
-  if (h->capturing) return nd_fail(h, ND_ERR_ARG, "nd_set_stream: cannot change streams during graph capture");
   if ((cudaStream_t)s == h->stream) return ND_OK;
+  if (h->capturing) return nd_fail(h, ND_ERR_ARG, "nd_set_stream: cannot change streams during graph capture");
   if (h->own_stream) {
     ND_CUDA(h, cudaStreamSynchronize(h->stream));
     cudaStreamDestroy(h->stream);

@@ -8,6 +8,8 @@ from ._lib import NDError, NoConvergence, PRECISIONS, handle, load, LIB_PATH
 from .tensors import BlockSparseTensor, DenseTensor, blockoffsets
 from . import workloads
 from . import linalg
+from . import autodiff
+from .autodiff import contract_autograd, contract_rrule, dense_structure
 from .linalg import Spectrum, matricize, qr, svd, truncate
 from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
@@ -18,4 +20,5 @@ __all__ = [
     "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
     "permutedims", "permutedims_", "permutedims_blocksparse",
     "linalg", "Spectrum", "matricize", "qr", "svd", "truncate",
+    "autodiff", "contract_autograd", "contract_rrule", "dense_structure",
 ]
