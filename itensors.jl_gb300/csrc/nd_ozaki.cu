@@ -160,31 +160,6 @@ __device__ __forceinline__ double i64_scaled_to_f64(long long v, int e) {
   return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (mant & 0xfffffffffffffull)));
 }
 
-// Exact integer value of an FP32 that holds an integer of magnitude < 2^31,
-// from its bit fields (integer pipe only; FP32->int conversion instructions
-// share GB300's narrow FP64 pipe).
-__device__ __forceinline__ int64_t f32_exact_int(float x) {
-  const uint32_t b = __float_as_uint(x);
-  const int e = (int)((b >> 23) & 0xff) - 150;          // value = m * 2^e
-  const int64_t m = (int64_t)((b & 0x7fffffu) | 0x800000u);
-  int64_t v = (b & 0x7fffffffu) == 0 ? 0 : (e >= 0 ? (m << e) : (m >> (-e)));
-  return (b >> 31) ? -v : v;
-}
-
-// round(x * 2^s) for an FP32 x, as int64, integer pipe only (|result| < 2^62).
-// Rounds half away from zero; values below one unit round to 0 or +-1.
-__device__ __forceinline__ int64_t f32_scaled_round(float x, int s) {
-  const uint32_t b = __float_as_uint(x);
-  if ((b & 0x7fffffffu) == 0) return 0;
-  const int e = (int)((b >> 23) & 0xff) - 150 + s;      // value = m * 2^e
-  const int64_t m = (int64_t)((b & 0x7fffffu) | 0x800000u);
-  int64_t v;
-  if (e >= 0) v = m << e;
-  else if (e < -25) v = 0;
-  else v = (m + (1ll << (-e - 1))) >> (-e);
-  return (b >> 31) ? -v : v;
-}
-
 __device__ __forceinline__ uint16_t bf16_bits_of_int(int d) {
   // |d| <= 256: exact in bf16
   return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
@@ -223,18 +198,6 @@ struct PackArgs2 {
   DeviceStatus* st;
 };
 
-// BF16 bits of d * 2^(-8q) for an integer digit |d| <= 128, integer pipe only
-// (exact: the digit has at most 8 significant bits).
-__device__ __forceinline__ uint16_t digit_bf16(int d, int q) {
-  if (d == 0) return 0;
-  const uint32_t sgn = d < 0 ? 0x8000u : 0u;
-  const uint32_t a = (uint32_t)(d < 0 ? -d : d);
-  const int p = 31 - __clz(a);                          // leading bit, 0..7
-  const uint32_t ex = (uint32_t)(127 + p - 8 * q);
-  const uint32_t mant = (a << (7 - p)) & 0x7fu;
-  return (uint16_t)(sgn | (ex << 7) | mant);
-}
-
 __device__ __forceinline__ void pack_unit_digits(uint64_t bits, int E, int S, uint16_t* hh) {
   if (S > 2) {
     int d[6];
@@ -242,7 +205,7 @@ __device__ __forceinline__ void pack_unit_digits(uint64_t bits, int E, int S, ui
     balanced_digits(X, S, d);
 #pragma unroll
     for (int q = 0; q < 6; ++q)
-      if (q < S) hh[q] = digit_bf16(d[q], q);
+      if (q < S) hh[q] = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * __int_as_float((127 - 8 * q) << 23)));
   } else {
     float xf = f64_to_f32_int(bits);
     __nv_bfloat16 hi = __float2bfloat16_rn(xf);
@@ -615,8 +578,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
               // L2: integer units; L3 was computed with pre-scaled slices: an integer multiple of 2^-8
-              const long long x2 = f32_exact_int(__uint_as_float(l2[c]));
-              const long long x3 = f32_exact_int(__uint_as_float(l3[c]) * 256.0f);
+              long long x2 = (long long)__float2int_rn(__uint_as_float(l2[c]));
+              long long x3 = (long long)__float2int_rn(__uint_as_float(l3[c]) * 256.0f);
               acc[c] += (x2 << 24) + (x3 << 16);
             }
           } else {
@@ -635,7 +598,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
             TMEM_LD32(lane_addr + tcol(ts) + t * BN, lt);
             tmem_wait_ld();
 #pragma unroll
-            for (int c = 0; c < 32; ++c) acc[c] += f32_scaled_round(__uint_as_float(lt[c]), 24);  // x 2^24
+            for (int c = 0; c < 32; ++c) acc[c] += __float2ll_rn(__uint_as_float(lt[c]) * 16777216.0f);  // x 2^24
           }
           fence_before();
           __syncwarp();
