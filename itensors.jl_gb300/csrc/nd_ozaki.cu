@@ -38,9 +38,9 @@
 // consecutive rows: A_p x [B_q, B_q+1] is ONE tcgen05.mma with N = 128 whose
 // two 64-column halves land in adjacent accumulator blocks (L2|L3 or T4|T5+).
 //
-// Warp roles (320 threads): warp 0 = bulk-copy producer, warp 1 = TMEM
-// allocator + MMA issuer, warps 2..9 = epilogue (TMEM lane quarter = warp % 4,
-// column half = (warp-2)/4).  Persistent CTAs walk a cost-sorted list of
+// Warp roles (576 threads): warp 0 = bulk-copy producer, warp 1 = TMEM
+// allocator + MMA issuer, warps 2..17 = epilogue (TMEM lane quarter = warp % 4,
+// 16-column group = (warp-2)/4).  Persistent CTAs walk a cost-sorted list of
 // output tiles; each tile loops over the block pairs of its output block.
 #include "nd_plan.h"
 #include <cuda_bf16.h>
@@ -53,7 +53,9 @@ constexpr int BM = 128, BN = 64, BK = 32;
 constexpr int A_SLICE = BM * BK * 2;   // 8192 bytes
 constexpr int B_SLICE = BN * BK * 2;   // 4096 bytes
 constexpr int CHUNK_STEPS = 16;        // 16 * 32 = 512 of K per exact chunk
-constexpr int NTHREADS = 320;
+constexpr int NTHREADS = 576;          // producer warp, MMA warp, 16 epilogue warps
+constexpr int EPI_WARPS = 16;
+constexpr int EPI_COLS = BN * 4 / EPI_WARPS;   // columns per epilogue thread (16)
 constexpr int SMEM_BUDGET = 220 * 1024;
 
 struct SplitOp {
@@ -363,6 +365,13 @@ __device__ __forceinline__ void commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(bar)) : "memory");
 }
 
+#define TMEM_LD16(taddr, r)                                                                                   \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),          \
+                 "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),       \
+                 "=r"(r[14]), "=r"(r[15])                                                                      \
+               : "r"(taddr))
+
 #define TMEM_LD32(taddr, r)                                                                                   \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15," \
                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                      \
@@ -376,7 +385,7 @@ __device__ __forceinline__ void commit(uint64_t* bar) {
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, %0;" :: "r"(EPI_WARPS * 32) : "memory"); }
 
 template <int S>
 struct Cfg {
@@ -406,8 +415,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   if (tid == 0) {
     for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&xfull[b], 1); mbar_init(&xempty[b], 8);
-      mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 8);
+      mbar_init(&xfull[b], 1); mbar_init(&xempty[b], EPI_WARPS);
+      mbar_init(&tfull[b], 1); mbar_init(&tempty[b], EPI_WARPS);
     }
     mbar_init(&done_bar, 1);
     abort_flag = 0;
@@ -529,10 +538,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   } else {
     // ------------------------------- epilogue ------------------------------
     const int q = warp & 3;                 // TMEM lane quarter
-    const int hcol = (warp - 2) >> 2;       // column half
+    const int cg = (warp - 2) >> 2;         // 16-column group
     const int row = q * 32 + lane;
     const int etid = tid - 64;
-    const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + hcol * 32;
+    const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + cg * EPI_COLS;
     uint32_t chunk = 0, npair = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
@@ -551,7 +560,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
       }
       epi_sync();
       double* Rb = g.ptrs.R[p0.job] + p0.r_off + roff;
-      const int ncols = min(32, p0.N - (wi.nt * BN + hcol * 32));
+      const int ncols = min(EPI_COLS, p0.N - (wi.nt * BN + cg * EPI_COLS));
       for (int pi = 0; pi < wi.pair_count && ok; ++pi, ++npair) {
         const PairDesc& pd = g.pairs[wi.pair_begin + pi];
         const SplitOp& oa = g.ops[pd.a_op];
@@ -559,24 +568,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
         const int nks = oa.k_steps;
         const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
         const int nchunks = (nks + chunk_steps - 1) / chunk_steps;
-        long long acc[32];
-        float facc[32];
+        long long acc[EPI_COLS];
+        float facc[EPI_COLS];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) { acc[c] = 0; facc[c] = 0.f; }
+        for (int c = 0; c < EPI_COLS; ++c) { acc[c] = 0; facc[c] = 0.f; }
         for (int ch = 0; ch < nchunks; ++ch, ++chunk) {
           const uint32_t xs = chunk & 1, xu = chunk >> 1;
           if (!mbar_wait(smem_u32(&xfull[xs]), xu & 1, g.st, 420, &abort_flag)) { ok = false; break; }
           fence_after();
-          uint32_t l2[32], l3[32];
-          TMEM_LD32(lane_addr + xcol(xs), l2);
-          TMEM_LD32(lane_addr + xcol(xs) + BN, l3);
+          uint32_t l2[EPI_COLS], l3[EPI_COLS];
+          TMEM_LD16(lane_addr + xcol(xs), l2);
+          TMEM_LD16(lane_addr + xcol(xs) + BN, l3);
           tmem_wait_ld();
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&xempty[xs]);
           if (S > 2) {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) {
+            for (int c = 0; c < EPI_COLS; ++c) {
               // L2: integer units; L3 was computed with pre-scaled slices: an integer multiple of 2^-8
               long long x2 = (long long)__float2int_rn(__uint_as_float(l2[c]));
               long long x3 = (long long)__float2int_rn(__uint_as_float(l3[c]) * 256.0f);
@@ -584,7 +593,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
             }
           } else {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) facc[c] += __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
+            for (int c = 0; c < EPI_COLS; ++c) facc[c] += __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
           }
         }
         if (!ok) break;
@@ -592,28 +601,29 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
           const uint32_t ts = npair & 1, tu = npair >> 1;
           if (!mbar_wait(smem_u32(&tfull[ts]), tu & 1, g.st, 421, &abort_flag)) { ok = false; break; }
           fence_after();
-#pragma unroll 1
-          for (int t = 0; t < C::TBLK; ++t) {
-            uint32_t lt[32];
-            TMEM_LD32(lane_addr + tcol(ts) + t * BN, lt);
-            tmem_wait_ld();
-#pragma unroll
-            for (int c = 0; c < 32; ++c) acc[c] += __float2ll_rn(__uint_as_float(lt[c]) * 16777216.0f);  // x 2^24
-          }
+          uint32_t t4[EPI_COLS], t5[EPI_COLS];
+          TMEM_LD16(lane_addr + tcol(ts), t4);
+          if (C::TBLK > 1) TMEM_LD16(lane_addr + tcol(ts) + BN, t5);
+          tmem_wait_ld();
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&tempty[ts]);
+#pragma unroll
+          for (int c = 0; c < EPI_COLS; ++c) {
+            acc[c] += __float2ll_rn(__uint_as_float(t4[c]) * 16777216.0f);                    // x 2^24
+            if (C::TBLK > 1) acc[c] += __float2ll_rn(__uint_as_float(t5[c]) * 16777216.0f);
+          }
         }
         // finalize this pair into R
         if (row_ok && ncols > 0) {
           const int Ei = S > 2 ? g.exps[oa.exp_off + gm] : 0;
-          const int32_t* Fj = g.exps + ob.exp_off + wi.nt * BN + hcol * 32;
+          const int32_t* Fj = g.exps + ob.exp_off + wi.nt * BN + cg * EPI_COLS;
           const bool first = pd.first != 0;
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
+          for (int c = 0; c < EPI_COLS; ++c) {
             if (c < ncols) {
               double v = (S > 2) ? i64_scaled_to_f64(acc[c], Ei + __ldg(Fj + c) - 38) : (double)facc[c];
-              double* dst = Rb + colR_s[hcol * 32 + c];
+              double* dst = Rb + colR_s[cg * EPI_COLS + c];
               if (first) {
                 if (g.bmode == 0) *dst = g.amode ? g.alpha * v : v;
                 else *dst = g.alpha * v + g.beta * *dst;

@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 
+from . import _lib as _libmod
 from ._lib import MAX_RANK, PRECISIONS, BsDesc, handle, i32arr, i64arr
 from .tensors import BlockSparseTensor, DenseTensor, blockoffsets
 
@@ -137,10 +138,9 @@ class ContractionPlan:
         self.ptr = C.c_void_p()
 
     def __del__(self):
-        from . import _lib
-        if _lib._shutting_down:
-            return
         try:
+            if _libmod._shutting_down:
+                return
             self.destroy()
         except Exception:
             pass
