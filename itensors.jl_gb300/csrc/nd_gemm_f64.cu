@@ -168,7 +168,7 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
 // pair staged in shared memory, the group's pairs accumulated in registers.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int SK_THREADS = 256, SK_RPT = 4, SK_ROWS = SK_THREADS * SK_RPT, SK_MAXN = 8, SK_MAXK = 32;
+constexpr int SK_THREADS = 256, SK_RPT = 2, SK_ROWS = SK_THREADS * SK_RPT, SK_MAXN = 8, SK_MAXK = 32;
 
 // One row chunk of one group with exactly NN output columns (no predicated FMAs:
 // the FP64 pipe is the bound for these pairs on GB300).
@@ -182,7 +182,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
   for (int r = 0; r < SK_RPT; ++r)
 #pragma unroll
     for (int j = 0; j < NN; ++j) acc[r][j] = 0.0;
-  int64_t rrow[SK_RPT] = {0, 0, 0, 0};
+  int64_t rrow[SK_RPT] = {};
   bool rok[SK_RPT];
   double* Rp = nullptr;
   const int i0 = wi.mt * SK_ROWS + tid;
@@ -244,7 +244,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
   }
 }
 
-__global__ void __launch_bounds__(SK_THREADS, 1) gemm_skinny_f64(GemmArgs g) {
+__global__ void __launch_bounds__(SK_THREADS, 3) gemm_skinny_f64(GemmArgs g) {
   __shared__ double Bs[SK_MAXK][SK_MAXN];
   __shared__ int64_t kA[SK_MAXK], colR[SK_MAXN];
   __shared__ __align__(16) PairDesc pd;

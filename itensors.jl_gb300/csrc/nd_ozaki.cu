@@ -200,14 +200,45 @@ struct PackArgs2 {
   DeviceStatus* st;
 };
 
+// Digits of one element.  |x| * 2^(8S-1-E) is rounded to an integer with at
+// most 8S-1 <= 47 bits, split into two 32-bit halves, and read byte by byte
+// from the least significant end; a carry pass turns bytes in [0, 255] into
+// balanced digits in [-128, 128] (digit >= 128 becomes digit - 256, carry 1).
+// The sign of x is applied to every digit.  All arithmetic is 32-bit.
 __device__ __forceinline__ void pack_unit_digits(uint64_t bits, int E, int S, uint16_t* hh) {
   if (S > 2) {
+    const uint32_t hi_w = (uint32_t)(bits >> 32);
+    const int ex = (int)((hi_w >> 20) & 0x7ff);
+    uint32_t mag_lo = 0, mag_hi = 0;
+    if (ex != 0x7ff && (bits << 1) != 0) {
+      const uint64_t m = (bits & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
+      const int sh = 1075 - (ex ? ex : 1) - (8 * S - 1) + E;   // >= 5
+      if (sh < 64) {
+        const uint64_t mag = (m + (1ull << (sh - 1))) >> sh;
+        mag_lo = (uint32_t)mag;
+        mag_hi = (uint32_t)(mag >> 32);
+      }
+    }
+    const bool neg = (hi_w >> 31) != 0;
+    int carry = 0;
     int d[6];
-    int64_t X = ((bits & 0x7fffffffffffffffull) >= 0x7ff0000000000000ull) ? 0 : fixed_point(bits, E, S);
-    balanced_digits(X, S, d);
+#pragma unroll
+    for (int p = 5; p >= 0; --p) {
+      const int byte_idx = 5 - p;                           // 0 = least significant
+      if (p >= S) continue;
+      const int lsb = (S - 1 - p);                          // byte position of digit p
+      const uint32_t byte = lsb < 4 ? ((mag_lo >> (8 * lsb)) & 0xffu) : ((mag_hi >> (8 * (lsb - 4))) & 0xffu);
+      (void)byte_idx;
+      int v = (int)byte + carry;
+      carry = (p > 0 && v >= 128) ? 1 : 0;
+      d[p] = v - 256 * carry;
+    }
 #pragma unroll
     for (int q = 0; q < 6; ++q)
-      if (q < S) hh[q] = __bfloat16_as_ushort(__float2bfloat16_rn((float)d[q] * __int_as_float((127 - 8 * q) << 23)));
+      if (q < S) {
+        const int dq = neg ? -d[q] : d[q];
+        hh[q] = __bfloat16_as_ushort(__float2bfloat16_rn((float)dq * __int_as_float((127 - 8 * q) << 23)));
+      }
   } else {
     float xf = f64_to_f32_int(bits);
     __nv_bfloat16 hi = __float2bfloat16_rn(xf);
