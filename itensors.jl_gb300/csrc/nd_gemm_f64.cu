@@ -244,7 +244,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
   }
 }
 
-__global__ void __launch_bounds__(SK_THREADS, 3) gemm_skinny_f64(GemmArgs g) {
+__global__ void __launch_bounds__(SK_THREADS, 4) gemm_skinny_f64(GemmArgs g) {
   __shared__ double Bs[SK_MAXK][SK_MAXN];
   __shared__ int64_t kA[SK_MAXK], colR[SK_MAXN];
   __shared__ __align__(16) PairDesc pd;
