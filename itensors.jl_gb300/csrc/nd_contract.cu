@@ -26,7 +26,6 @@ void ExecCache::free_all() {
   if (d_pack_items) cudaFree(d_pack_items);
   if (d_rowmax) cudaFree(d_rowmax);
   if (d_sk_items) cudaFree(d_sk_items);
-  if (d_ss_items) cudaFree(d_ss_items);
   if (d_split_pairs) cudaFree(d_split_pairs);
   if (d_split_items) cudaFree(d_split_items);
   *this = ExecCache{};
@@ -155,43 +154,30 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
     c.slices = want_slices;
     nd_status s = upload(h, (void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc));
     if (s) return s;
-    // Route every group (all its pairs share M and N): 1 = FP64 CUDA-core skinny kernel,
-    // 2 = fused split skinny kernel (Ozaki), 0 = the precision's tile kernel.
-    std::vector<char> route(pairs.size(), 0);
+    // which pairs sit in skinny groups
+    std::vector<char> sk(pairs.size(), 0);
     for (size_t i = 0; i < pairs.size();) {
       size_t j = i;
-      bool fsk = true, ssk = true;
-      while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) {
-        fsk = fsk && nd_pair_is_skinny(pairs[j]);
-        ssk = ssk && nd_pair_fits_split_skinny(pairs[j]);
-        ++j;
-      }
-      ssk = ssk && (int)(j - i) <= nd_split_skinny_max_pairs();
-      const char r = (precision == ND_PREC_OZAKI && ssk) ? 2 : (fsk ? 1 : 0);
-      for (size_t k = i; k < j; ++k) route[k] = r;
+      bool g = group_skinny(pairs, i);
+      while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) sk[j++] = g;
       i = j;
     }
     std::vector<WorkItem> items;
-    make_items(pairs, nd_skinny_rows(), 1 << 30, [&](const PairDesc& p) { return route[&p - pairs.data()] == 1; }, items);
+    make_items(pairs, nd_skinny_rows(), 1 << 30, [&](const PairDesc& p) { return sk[&p - pairs.data()] != 0; }, items);
     c.nsk_items = (int)items.size();
     if ((s = upload(h, (void**)&c.d_sk_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
-    make_items(pairs, 128, 1 << 30, [&](const PairDesc& p) { return route[&p - pairs.data()] == 2; }, items);
-    c.nss_items = (int)items.size();
-    if ((s = upload(h, (void**)&c.d_ss_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
     if (precision == ND_PREC_FP64) {
-      make_items(pairs, 64, 64, [&](const PairDesc& p) { return route[&p - pairs.data()] == 0; }, items);
+      make_items(pairs, 64, 64, [&](const PairDesc& p) { return sk[&p - pairs.data()] == 0; }, items);
       c.nitems = (int)items.size();
       if ((s = upload(h, (void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
     } else {
       std::vector<PairDesc> regular;
-      for (size_t i = 0; i < pairs.size(); ++i) if (route[i] == 0) regular.push_back(pairs[i]);
+      for (size_t i = 0; i < pairs.size(); ++i) if (!sk[i]) regular.push_back(pairs[i]);
       if (!regular.empty() && (s = nd_split_build(h, c, regular, ngroups, precision))) return s;
     }
     c.built = true;
   }
   nd_status s = nd_launch_skinny_f64(h, c.d_pairs, c.d_sk_items, c.nsk_items, ptrs, alpha, beta);
-  if (s) return s;
-  s = nd_launch_split_skinny(h, c.slices, c.d_pairs, c.d_ss_items, c.nss_items, ptrs, alpha, beta);
   if (s) return s;
   if (precision == ND_PREC_FP64) return nd_launch_gemm_f64(h, c.d_pairs, c.d_items, c.nitems, ptrs, alpha, beta);
   return nd_split_run(h, c, ptrs, alpha, beta);

@@ -891,305 +891,3 @@ nd_status nd_split_layout_into(nd_handle h, ExecCache& c, const std::vector<Pair
   c.slices = S;
   return ND_OK;
 }
-
-// ===========================================================================
-// Fused split GEMM for skinny groups (every pair K <= 32, N <= 16, <= 16 pairs).
-//
-// The MPO contractions of a two-site H_eff (T1 * W1, T2 * W2) have tiny K and N
-// per block pair but millions of rows.  One CTA takes 128 rows of one output
-// block and ALL pairs of that block: the pairs' K ranges (each padded to one
-// 32-wide k-step) are treated as one concatenated K, so a single row exponent
-// E_i (max over every pair) and column exponent F_j serve the whole group and
-// every pair accumulates into the same TMEM levels.  No pack kernels, no
-// global scratch: A values are read from the tensor, digits are written to
-// shared memory in the SW64 K-major layout, B (the small MPO blocks) padded to
-// 16 rows.  Exactness: levels 2 and 3 hold at most 16 pairs * 32 * 2 * 2^14
-// <= 2^24 units.  256 threads; thread 0 issues the MMAs, warps 0-3 drain TMEM.
-// ===========================================================================
-namespace {
-
-constexpr int SS_BN = 16;                          // padded N
-constexpr int SS_ASL = BM * BK * 2;               // 8 KB per A slice
-constexpr int SS_BSL = SS_BN * BK * 2;            // 1 KB per B slice
-constexpr int SS_MAXPAIRS = 16;
-
-struct SkinnyArgs {
-  const PairDesc* pairs;
-  const WorkItem* items;
-  int nitems;
-  JobPtrs ptrs;
-  double alpha, beta;
-  int32_t amode, bmode;
-  DeviceStatus* st;
-};
-
-template <int S>
-__global__ void __launch_bounds__(256, 2) split_skinny(SkinnyArgs g) {
-  constexpr int BUF = S * (SS_ASL + SS_BSL);
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t bufbar[2], accbar;
-  __shared__ uint32_t tmem_slot;
-  __shared__ unsigned long long rmax[BM];
-  __shared__ unsigned long long cmax[SS_BN];
-  __shared__ int32_t Es[BM], Fs[SS_BN];
-  __shared__ int64_t colR[SS_BN];
-  __shared__ __align__(16) PairDesc pd;
-  __shared__ int s_ok;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  constexpr int PD_VECS = (int)(sizeof(PairDesc) / 16);
-
-  if (tid == 0) {
-    mbar_init(&bufbar[0], 1); mbar_init(&bufbar[1], 1); mbar_init(&accbar, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(&tmem_slot)), "r"(64));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  fence_before();
-  __syncthreads();
-  fence_after();
-  const uint32_t tmem = tmem_slot;
-  uint32_t bufuse[2] = {0, 0}, accuse = 0;
-  bool ok = true;
-  const uint32_t i16 = idesc(SS_BN), i32 = idesc(2 * SS_BN);
-
-  for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
-    const WorkItem wi = g.items[it];
-    const int r = tid & (BM - 1), kh = tid >> 7;          // row, 16-wide k half
-    const int grow = wi.mt * BM + r;
-    // ---- pass 1: common row / column maxima over every pair of the group
-    if (tid < BM) rmax[tid] = 0ull;
-    if (tid < SS_BN) cmax[tid] = 0ull;
-    unsigned long long mxr = 0ull;
-    bool bad = false;
-    int M = 0, N = 0;
-    for (int pi = 0; pi < wi.pair_count; ++pi) {
-      __syncthreads();
-      if (tid < PD_VECS) ((int4*)&pd)[tid] = __ldg((const int4*)(g.pairs + wi.pair_begin + pi) + tid);
-      __syncthreads();
-      M = pd.M; N = pd.N;
-      if (grow < M) {
-        int64_t ra, rr;
-        mixed_offsets32(pd.rows, (uint32_t)grow, ra, rr);
-        const double* Arow = g.ptrs.A[pd.job] + pd.a_off + ra;
-#pragma unroll 4
-        for (int e = 0; e < 16; ++e) {
-          const int k = kh * 16 + e;
-          if (k < pd.K) {
-            int64_t ka, kb;
-            mixed_offsets32(pd.ks, k, ka, kb);
-            uint64_t b = (uint64_t)__double_as_longlong(__ldg(Arow + ka)) & 0x7fffffffffffffffull;
-            if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
-            mxr = b > mxr ? b : mxr;
-          }
-        }
-      }
-      if (tid < SS_BN && tid < N) {
-        const double* B = g.ptrs.B[pd.job] + pd.b_off;
-        int64_t cb, cr;
-        mixed_offsets32(pd.cols, tid, cb, cr);
-        unsigned long long m = 0ull;
-        for (int k = 0; k < pd.K; ++k) {
-          int64_t ka, kb;
-          mixed_offsets32(pd.ks, k, ka, kb);
-          uint64_t b = (uint64_t)__double_as_longlong(__ldg(B + kb + cb)) & 0x7fffffffffffffffull;
-          if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
-          m = b > m ? b : m;
-        }
-        cmax[tid] = m > cmax[tid] ? m : cmax[tid];
-        colR[tid] = cr;
-      }
-    }
-    if (bad && atomicCAS(&g.st->code, 0, ND_ERR_NONFINITE) == 0) g.st->where = 310;
-    atomicMax(&rmax[r], mxr);
-    __syncthreads();
-    if (tid < BM) { const int ex = (int)(rmax[tid] >> 52); Es[tid] = (ex ? ex : 1) - 1022; }
-    if (tid < SS_BN) { const int ex = (int)(cmax[tid] >> 52); Fs[tid] = (ex ? ex : 1) - 1022; }
-    __syncthreads();
-    // ---- pass 2: per pair, digits into a smem buffer, then the MMAs
-    for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
-      const int b = pi & 1;
-      unsigned char* A_s = smem + b * BUF;
-      unsigned char* B_s = A_s + S * SS_ASL;
-      // the MMAs that last read this buffer must be complete
-      if (bufuse[b] >= 1) {
-        if (tid == 0) s_ok = mbar_wait(smem_u32(&bufbar[b]), (bufuse[b] - 1) & 1, g.st, 430, nullptr) ? 1 : 0;
-        __syncthreads();
-        if (!s_ok) { ok = false; break; }
-      }
-      __syncthreads();
-      if (tid < PD_VECS) ((int4*)&pd)[tid] = __ldg((const int4*)(g.pairs + wi.pair_begin + pi) + tid);
-      __syncthreads();
-      {
-        // A: thread owns row r and k in [16*kh, 16*kh+16): two 16-byte chunks per slice
-        uint64_t bits[16];
-        const int E = Es[r];
-        int64_t ra = 0, rr;
-        if (grow < pd.M) mixed_offsets32(pd.rows, (uint32_t)grow, ra, rr);
-        const double* Arow = g.ptrs.A[pd.job] + pd.a_off + ra;
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          const int k = kh * 16 + e;
-          bits[e] = 0ull;
-          if (grow < pd.M && k < pd.K) {
-            int64_t ka, kb;
-            mixed_offsets32(pd.ks, k, ka, kb);
-            bits[e] = (uint64_t)__double_as_longlong(__ldg(Arow + ka));
-          }
-        }
-#pragma unroll
-        for (int cc = 0; cc < 2; ++cc) {
-          uint32_t w[6][4];
-#pragma unroll
-          for (int e = 0; e < 8; e += 2) {
-            uint16_t h0[6], h1[6];
-            pack_unit_digits(bits[cc * 8 + e], E, S, h0);
-            pack_unit_digits(bits[cc * 8 + e + 1], E, S, h1);
-#pragma unroll
-            for (int q = 0; q < 6; ++q) w[q][e / 2] = (uint32_t)h0[q] | ((uint32_t)h1[q] << 16);
-          }
-          const int c = kh * 2 + cc;                       // 16-byte chunk of the 64-byte row
-          const int so = r * 64 + (((c ^ (r >> 1)) & 3) << 4);
-#pragma unroll
-          for (int q = 0; q < 6; ++q)
-            if (q < S) *(uint4*)(A_s + q * SS_ASL + so) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
-        }
-      }
-      // B: SS_BN rows (output columns) x 32 k, zero padded
-      for (int u = tid; u < SS_BN * BK; u += 256) {
-        const int j = u / BK, k = u % BK;
-        uint64_t bb = 0ull;
-        if (j < pd.N && k < pd.K) {
-          int64_t ka, kb, cb, cr;
-          mixed_offsets32(pd.ks, k, ka, kb);
-          mixed_offsets32(pd.cols, j, cb, cr);
-          bb = (uint64_t)__double_as_longlong(__ldg(g.ptrs.B[pd.job] + pd.b_off + kb + cb));
-        }
-        uint16_t hh[6];
-        pack_unit_digits(bb, Fs[j], S, hh);
-        const int so = swz64(j, k);
-#pragma unroll
-        for (int q = 0; q < 6; ++q)
-          if (q < S) *(uint16_t*)(B_s + q * SS_BSL + so) = hh[q];
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) {
-        fence_after();
-        const uint32_t a0 = smem_u32(A_s), b0 = smem_u32(B_s);
-        const uint32_t X = tmem, T = tmem + 2 * SS_BN;
-#pragma unroll
-        for (int kk = 0; kk < 2; ++kk) {
-          const uint32_t acc0 = (pi == 0 && kk == 0) ? 0u : 1u;
-          const uint32_t ko = kk * 32;
-          auto A = [&](int p) { return sdesc(a0 + (p - 1) * SS_ASL + ko); };
-          auto Bq = [&](int q) { return sdesc(b0 + (q - 1) * SS_BSL + ko); };
-          mma(X, A(1), Bq(1), i32, acc0);
-          mma(X + SS_BN, A(2), Bq(1), i16, 1u);
-          if (S == 3) {
-            mma(T, A(1), Bq(3), i16, acc0);
-            mma(T, A(2), Bq(2), i16, 1u);
-            mma(T, A(3), Bq(1), i16, 1u);
-          } else if (S >= 4) {
-            mma(T, A(1), Bq(3), i32, acc0);
-            mma(T, A(2), Bq(2), i32, 1u);
-            mma(T, A(3), Bq(1), i32, 1u);
-#pragma unroll
-            for (int p = 1; p <= S; ++p)
-#pragma unroll
-              for (int q = 1; q <= S + 1 - p; ++q) {
-                const bool covered = (p <= 3) && (q == 4 - p || q == 5 - p);
-                if (p + q >= 5 && !covered) mma(T + SS_BN, A(p), Bq(q), i16, 1u);
-              }
-          }
-        }
-        commit(&bufbar[b]);
-      }
-      bufuse[b]++;
-    }
-    if (!ok) break;
-    // ---- drain: every MMA of the item complete, then TMEM -> FP64 -> R
-    if (tid == 0) commit(&accbar);
-    if (warp < 4) {
-      if (!mbar_wait(smem_u32(&accbar), accuse & 1, g.st, 431, nullptr)) ok = false;
-      fence_after();
-      const uint32_t la = tmem + ((uint32_t)(warp * 32) << 16);
-      uint32_t l2[16], l3[16], t4[16], t5[16];
-      TMEM_LD16(la, l2);
-      TMEM_LD16(la + SS_BN, l3);
-      TMEM_LD16(la + 2 * SS_BN, t4);
-      TMEM_LD16(la + 3 * SS_BN, t5);
-      tmem_wait_ld();
-      fence_before();
-      const int rowi = warp * 32 + lane;
-      const int gm = wi.mt * BM + rowi;
-      if (ok && gm < pd.M) {
-        int64_t ra, roff;
-        mixed_offsets32(pd.rows, (uint32_t)gm, ra, roff);
-        double* Rrow = g.ptrs.R[pd.job] + pd.r_off + roff;
-        const int Ei = Es[rowi];
-#pragma unroll
-        for (int c = 0; c < SS_BN; ++c) {
-          if (c < pd.N) {
-            long long acc = ((long long)__float2int_rn(__uint_as_float(l2[c])) << 24) +
-                            ((long long)__float2int_rn(__uint_as_float(l3[c]) * 256.0f) << 16);
-            if (S >= 3) acc += __float2ll_rn(__uint_as_float(t4[c]) * 16777216.0f);
-            if (S >= 4) acc += __float2ll_rn(__uint_as_float(t5[c]) * 16777216.0f);
-            const double v = i64_scaled_to_f64(acc, Ei + Fs[c] - 38);
-            double* dst = Rrow + colR[c];
-            if (g.bmode == 0) *dst = g.amode ? g.alpha * v : v;
-            else *dst = g.alpha * v + g.beta * *dst;
-          }
-        }
-      }
-    }
-    accuse++;
-    __syncthreads();
-  }
-  // every MMA this CTA issued must be complete before TMEM is released
-  if (tid == 0) {
-    commit(&accbar);
-    mbar_wait(smem_u32(&accbar), accuse & 1, g.st, 432, nullptr);
-  }
-  fence_before();
-  __syncthreads();
-  fence_after();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(64));
-}
-
-template <int S>
-nd_status launch_skinny(nd_handle h, const SkinnyArgs& a) {
-  constexpr int SMEM = 2 * S * (SS_ASL + SS_BSL) + 1024;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(split_skinny<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
-    if (e != cudaSuccess) return nd_cuda_check(h, e, "split_skinny smem attribute");
-    attr = true;
-  }
-  int blocks = std::min(a.nitems, h->num_sms * 2);
-  nd_prof_begin(h, "split_skinny");
-  split_skinny<S><<<blocks, 256, SMEM, h->stream>>>(a);
-  nd_prof_end(h);
-  ND_LAUNCHED(h);
-  return nd_cuda_check(h, cudaGetLastError(), "split_skinny");
-}
-
-}  // namespace
-
-bool nd_pair_fits_split_skinny(const PairDesc& p) { return p.K <= BK && p.N <= SS_BN; }
-int nd_split_skinny_max_pairs() { return SS_MAXPAIRS; }
-
-nd_status nd_launch_split_skinny(nd_handle h, int slices, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
-                                 const JobPtrs& ptrs, double alpha, double beta) {
-  if (nitems == 0) return ND_OK;
-  SkinnyArgs a{d_pairs, d_items, nitems, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1, h->d_status};
-  switch (slices) {
-    case 3: return launch_skinny<3>(h, a);
-    case 4: return launch_skinny<4>(h, a);
-    case 5: return launch_skinny<5>(h, a);
-    case 6: return launch_skinny<6>(h, a);
-  }
-  return nd_fail(h, ND_ERR_ARG, "split_skinny: unsupported slice count %d", slices);
-}

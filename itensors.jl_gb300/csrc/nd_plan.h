@@ -44,10 +44,8 @@ struct ExecCache {
   PairDesc* d_pairs = nullptr;
   WorkItem* d_items = nullptr;     // FP64 tensor-core tiles of the regular groups
   int nitems = 0;
-  WorkItem* d_sk_items = nullptr;  // skinny groups (FP64 CUDA-core kernel)
+  WorkItem* d_sk_items = nullptr;  // skinny groups (FP64 CUDA-core kernel, every precision)
   int nsk_items = 0;
-  WorkItem* d_ss_items = nullptr;  // skinny groups on the fused split kernel (Ozaki precision)
-  int nss_items = 0;
   // split-precision operands (regular groups only)
   PairDesc* d_split_pairs = nullptr;
   WorkItem* d_split_items = nullptr;
@@ -89,10 +87,6 @@ bool nd_make_pair(const Roles& ro, const int64_t* dA, const int64_t* dB, const i
                   std::string& why);
 
 bool nd_pair_is_skinny(const PairDesc& p);
-bool nd_pair_fits_split_skinny(const PairDesc& p);
-int nd_split_skinny_max_pairs();
-nd_status nd_launch_split_skinny(nd_handle h, int slices, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
-                                 const JobPtrs& ptrs, double alpha, double beta);
 int nd_skinny_rows();
 nd_status nd_launch_skinny_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
                                const JobPtrs& ptrs, double alpha, double beta);
