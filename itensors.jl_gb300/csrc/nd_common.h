@@ -165,6 +165,18 @@ struct WorkItem {
   int32_t pair_begin;   // first pair (pairs sorted by group)
   int32_t pair_count;
   int32_t mt, nt;       // tile coordinates
+  // split-K (FP64 tile kernel only): the item covers [kbeg, kend) of the group's
+  // k axis (the pairs' K ranges concatenated in plan order) and writes its
+  // partial tile to workspace slot `slot`; slot < 0 means the whole k axis,
+  // written to R.
+  int32_t kbeg = 0, kend = 0, slot = -1;
+};
+
+// One output tile whose split-K partials are summed into R (in slot order).
+struct ReduceItem {
+  int32_t pair;         // first pair of the group (rows / cols / job / r_off)
+  int32_t mt, nt;
+  int32_t slot0, nslots;
 };
 
 // Split-precision parameters
@@ -183,13 +195,7 @@ struct JobPtrs {
   double* R[2];
 };
 
-// Grouped execution shared by dense / block-sparse / adjoint paths.
-// pairs: sorted by (job, group); items derived inside.  Groups are numbered
-// globally across jobs.
-nd_status nd_execute_grouped(nd_handle h, const std::vector<PairDesc>& pairs, int ngroups,
-                             const JobPtrs& ptrs, double alpha, double beta, int precision);
 nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items,
-                             int nitems, const JobPtrs& ptrs, double alpha, double beta);
-nd_status nd_run_split_gemm(nd_handle h, int precision, const std::vector<PairDesc>& pairs,
-                            const std::vector<WorkItem>& items, const JobPtrs& ptrs,
-                            double alpha, double beta);
+                             int nitems, const JobPtrs& ptrs, double alpha, double beta, double* ws,
+                             const ReduceItem* d_red, int nred);
+int nd_gemm_f64_tile_elems();

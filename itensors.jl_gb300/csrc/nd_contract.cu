@@ -28,6 +28,8 @@ void ExecCache::free_all() {
   if (d_sk_items) cudaFree(d_sk_items);
   if (d_split_pairs) cudaFree(d_split_pairs);
   if (d_split_items) cudaFree(d_split_items);
+  if (d_ws) cudaFree(d_ws);
+  if (d_red) cudaFree(d_red);
   *this = ExecCache{};
 }
 
@@ -134,6 +136,54 @@ static void make_items(const std::vector<PairDesc>& pairs, int bm, int bn, Pick 
   for (auto& t : tmp) items.push_back(t.second);
 }
 
+// Split-K for the FP64 tile kernel.  The launch's work is measured in k-steps
+// of 16 summed over its tiles (each tile's k axis is its group's pairs' K
+// concatenated in plan order); `ctas` resident CTAs share it.  Any tile longer
+// than twice the fair share per CTA (and at least 4 k-steps) is cut into chunks
+// of about that share, so one long-K tile cannot serialise the launch; the
+// partial tiles go to a workspace and splitk_reduce sums them in chunk order
+// (deterministic) before applying alpha / beta.
+static nd_status plan_split_k(nd_handle h, const std::vector<PairDesc>& pairs, std::vector<WorkItem>& items,
+                              ExecCache& c, int ctas) {
+  if (ctas <= 0 || items.empty()) return ND_OK;
+  std::vector<int64_t> ksum(items.size());
+  int64_t total = 0;
+  for (size_t i = 0; i < items.size(); ++i) {
+    int64_t k = 0;
+    for (int p = 0; p < items[i].pair_count; ++p) k += pairs[items[i].pair_begin + p].K;
+    ksum[i] = k;
+    total += (k + 15) / 16;
+  }
+  const int64_t share = std::max<int64_t>(4, 2 * ((total + ctas - 1) / ctas));   // k-steps per chunk
+  std::vector<WorkItem> out;
+  std::vector<ReduceItem> red;
+  int slot = 0;
+  for (size_t i = 0; i < items.size(); ++i) {
+    const WorkItem& wi = items[i];
+    const int64_t steps = (ksum[i] + 15) / 16;
+    if (steps <= share || ksum[i] >= INT32_MAX) { out.push_back(wi); continue; }
+    const int64_t s = (steps + share - 1) / share;
+    const int64_t kc = ((steps + s - 1) / s) * 16;
+    const int64_t nch = (ksum[i] + kc - 1) / kc;
+    red.push_back(ReduceItem{wi.pair_begin, wi.mt, wi.nt, slot, (int32_t)nch});
+    for (int64_t q = 0; q < nch; ++q) {
+      WorkItem x = wi;
+      x.kbeg = (int32_t)(q * kc);
+      x.kend = (int32_t)std::min(ksum[i], (q + 1) * kc);
+      x.slot = slot++;
+      out.push_back(x);
+    }
+  }
+  if (red.empty()) return ND_OK;
+  items.swap(out);
+  if (c.d_ws) { cudaFree(c.d_ws); c.d_ws = nullptr; }
+  ND_CUDA(h, cudaMalloc((void**)&c.d_ws, (size_t)slot * nd_gemm_f64_tile_elems() * sizeof(double)));
+  nd_status st = upload(h, (void**)&c.d_red, red.data(), red.size() * sizeof(ReduceItem));
+  if (st) return st;
+  c.nred = (int)red.size();
+  return ND_OK;
+}
+
 // A group runs on the skinny kernel when every one of its pairs is skinny.
 static bool group_skinny(const std::vector<PairDesc>& pairs, size_t i) {
   for (size_t j = i; j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job; ++j)
@@ -168,6 +218,7 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
     if ((s = upload(h, (void**)&c.d_sk_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
     if (precision == ND_PREC_FP64) {
       make_items(pairs, 64, 64, [&](const PairDesc& p) { return sk[&p - pairs.data()] == 0; }, items);
+      if ((s = plan_split_k(h, pairs, items, c, 4 * h->num_sms))) return s;
       c.nitems = (int)items.size();
       if ((s = upload(h, (void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
     } else {
@@ -179,7 +230,8 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
   }
   nd_status s = nd_launch_skinny_f64(h, c.d_pairs, c.d_sk_items, c.nsk_items, ptrs, alpha, beta);
   if (s) return s;
-  if (precision == ND_PREC_FP64) return nd_launch_gemm_f64(h, c.d_pairs, c.d_items, c.nitems, ptrs, alpha, beta);
+  if (precision == ND_PREC_FP64)
+    return nd_launch_gemm_f64(h, c.d_pairs, c.d_items, c.nitems, ptrs, alpha, beta, c.d_ws, c.d_red, c.nred);
   return nd_split_run(h, c, ptrs, alpha, beta);
 }
 

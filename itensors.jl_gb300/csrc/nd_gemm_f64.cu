@@ -29,6 +29,7 @@ struct GemmArgs {
   double alpha, beta;
   int32_t amode;   // 0: alpha == 1
   int32_t bmode;   // 0: beta == 0 (overwrite)
+  double* ws;      // split-K partial tiles, BM * BN doubles per slot (column-major in the tile)
 };
 
 __device__ __forceinline__ void dmma(double& c0, double& c1, double a, double b) {
@@ -55,11 +56,18 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
     int64_t r_base = 0;
     double* Rp = nullptr;
     int M = 0, N = 0;
+    int kcur = 0;                      // start of this pair on the group's concatenated k axis
     for (int pi = 0; pi < wi.pair_count; ++pi) {
       __syncthreads();
       if (tid == 0) pd = g.pairs[wi.pair_begin + pi];
       __syncthreads();
       M = pd.M; N = pd.N;
+      int klo = 0, khi = pd.K;
+      if (wi.slot >= 0) {
+        klo = max(0, wi.kbeg - kcur);
+        khi = min(pd.K, wi.kend - kcur);
+      }
+      kcur += pd.K;
       const int m0 = wi.mt * BM, n0 = wi.nt * BN;
       if (tid < BM) {
         int64_t o0 = 0, o1 = 0;
@@ -77,11 +85,11 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
       r_base = pd.r_off;
       const bool a_rows_contig = pd.rows.n > 0 && pd.rows.st0[0] == 1;
       const bool b_cols_contig = pd.cols.n > 0 && pd.cols.st0[0] == 1;
-      for (int k0 = 0; k0 < pd.K; k0 += BK) {
+      for (int k0 = klo; k0 < khi; k0 += BK) {
         __syncthreads();
         if (tid < BK) {
           int64_t o0 = 0, o1 = 0;
-          if (k0 + tid < pd.K) mixed_offsets(pd.ks, k0 + tid, o0, o1);
+          if (k0 + tid < khi) mixed_offsets(pd.ks, k0 + tid, o0, o1);
           kA[tid] = o0; kB[tid] = o1;
         }
         __syncthreads();
@@ -92,7 +100,7 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
           if (a_rows_contig) { m = tid & 63; k = (tid >> 6) + 2 * e; }
           else { k = tid & 15; m = (tid >> 4) + 8 * e; }
           double v = 0.0;
-          if (m0 + m < M && k0 + k < pd.K) v = __ldg(A + rowA[m] + kA[k]);
+          if (m0 + m < M && k0 + k < khi) v = __ldg(A + rowA[m] + kA[k]);
           As[k][m] = v;
         }
         // B tile (BK x BN) -> Bs[k][n]
@@ -102,7 +110,7 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
           if (b_cols_contig) { n = tid & 63; k = (tid >> 6) + 2 * e; }
           else { k = tid & 15; n = (tid >> 4) + 8 * e; }
           double v = 0.0;
-          if (n0 + n < N && k0 + k < pd.K) v = __ldg(B + kB[k] + colB[n]);
+          if (n0 + n < N && k0 + k < khi) v = __ldg(B + kB[k] + colB[n]);
           Bs[k][n] = v;
         }
         __syncthreads();
@@ -119,6 +127,18 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
             for (int j = 0; j < 4; ++j) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
         }
       }
+    }
+    if (wi.slot >= 0) {
+      // split-K: the partial tile goes to its workspace slot; splitk_reduce applies alpha / beta
+      double* wsl = g.ws + (int64_t)wi.slot * (BM * BN);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+          for (int h = 0; h < 2; ++h)
+            wsl[(wn + j * 8 + 2 * (lane & 3) + h) * BM + wm + i * 8 + (lane >> 2)] = acc[i][j][h];
+      continue;
     }
     // epilogue: R = alpha * acc + beta * R  (beta == 0 overwrites)
     const int m0 = wi.mt * BM, n0 = wi.nt * BN;
@@ -142,18 +162,58 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
   }
 }
 
+// Sum the split-K partial tiles of one output tile in slot order (deterministic)
+// and apply R = alpha * sum + beta * R.
+__global__ void __launch_bounds__(256) splitk_reduce(const PairDesc* pairs, const ReduceItem* items, const double* ws,
+                                                     JobPtrs ptrs, double alpha, double beta, int amode, int bmode) {
+  __shared__ int64_t rowR[BM], colR[BN];
+  const ReduceItem ri = items[blockIdx.x];
+  const PairDesc& pd = pairs[ri.pair];
+  const int m0 = ri.mt * BM, n0 = ri.nt * BN;
+  if (threadIdx.x < BM) {
+    int64_t a = 0, r = 0;
+    if (m0 + threadIdx.x < pd.M) mixed_offsets(pd.rows, m0 + threadIdx.x, a, r);
+    rowR[threadIdx.x] = r;
+  } else if (threadIdx.x < BM + BN) {
+    int64_t b = 0, r = 0;
+    const int j = threadIdx.x - BM;
+    if (n0 + j < pd.N) mixed_offsets(pd.cols, n0 + j, b, r);
+    colR[j] = r;
+  }
+  __syncthreads();
+  double* R = ptrs.R[pd.job] + pd.r_off;
+  for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
+    const int m = e % BM, n = e / BM;
+    if (m0 + m >= pd.M || n0 + n >= pd.N) continue;
+    double sum = 0.0;
+    for (int sl = 0; sl < ri.nslots; ++sl) sum += ws[(int64_t)(ri.slot0 + sl) * (BM * BN) + e];
+    double* dst = R + rowR[m] + colR[n];
+    if (bmode == 0) *dst = amode ? alpha * sum : sum;
+    else *dst = alpha * sum + beta * *dst;
+  }
+}
+
 }  // namespace
 
+int nd_gemm_f64_tile_elems() { return BM * BN; }
+
 nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items, int nitems,
-                             const JobPtrs& ptrs, double alpha, double beta) {
+                             const JobPtrs& ptrs, double alpha, double beta, double* ws,
+                             const ReduceItem* d_red, int nred) {
   if (nitems == 0) return ND_OK;
-  GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1};
+  GemmArgs g{d_pairs, d_items, nitems, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1, ws};
   int blocks = std::min(nitems, h->num_sms * 4);
   nd_prof_begin(h, "gemm_f64_grouped");
   gemm_f64_grouped<<<blocks, 128, 0, h->stream>>>(g);
   nd_prof_end(h);
   ND_LAUNCHED(h);
-  return nd_cuda_check(h, cudaGetLastError(), "gemm_f64_grouped");
+  nd_status s = nd_cuda_check(h, cudaGetLastError(), "gemm_f64_grouped");
+  if (s || nred == 0) return s;
+  nd_prof_begin(h, "splitk_reduce");
+  splitk_reduce<<<nred, 256, 0, h->stream>>>(d_pairs, d_red, ws, ptrs, alpha, beta, g.amode, g.bmode);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "splitk_reduce");
 }
 
 // ---------------------------------------------------------------------------

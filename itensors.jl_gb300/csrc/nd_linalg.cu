@@ -113,6 +113,8 @@ struct SweepArgs {
   int nrounds;       // max npad - 1
   double* W;
   double* V;
+  double* nrm;       // |w_j|^2 per column (pooled like the singular values), updated by every rotation
+  const int32_t* active;        // per block: 0 once a sweep left it without rotations (converged)
   unsigned long long* offmax;   // per block, bits of the largest relative off-diagonal seen this sweep
   unsigned int* bar_count;
   unsigned int* bar_gen;
@@ -120,63 +122,81 @@ struct SweepArgs {
   double tol;
 };
 
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// |w_j|^2 of every column of the active blocks (one warp per column), at the start of a sweep.
+__global__ void __launch_bounds__(256) svd_norms(const SvdBlock* blocks, int nb, const int32_t* active,
+                                                 const double* W, double* nrm, int total_cols) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int c = gw; c < total_cols; c += nw) {
+    int bi = 0;
+    while (bi + 1 < nb && blocks[bi + 1].s_off <= c) ++bi;
+    if (!active[bi]) continue;
+    const SvdBlock& b = blocks[bi];
+    const double* w = W + b.w_off + (int64_t)(c - b.s_off) * b.mm;
+    double acc = 0.0;
+    for (int i = lane; i < b.mm; i += 32) acc = fma(w[i], w[i], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) nrm[c] = acc;
+  }
+}
+
+// One sweep: every round, one warp per column pair (p, q) of every active block:
+// gamma = w_p . w_q, the Jacobi rotation from (|w_p|^2, |w_q|^2, gamma), applied
+// to the two columns of W and of V.  The squared norms follow the exact
+// identities |w_p'|^2 = |w_p|^2 - t gamma, |w_q'|^2 = |w_q|^2 + t gamma, so a
+// pair costs one dot product instead of three; they are recomputed every sweep.
 __global__ void __launch_bounds__(256) svd_sweep(SweepArgs a) {
-  __shared__ double red[8];
-  __shared__ double rot[3];
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int r = 0; r < a.nrounds; ++r) {
-    for (int t = blockIdx.x; t < a.ntasks; t += gridDim.x) {
-      // locate block (linear scan over a small block list)
+    for (int t = gw; t < a.ntasks; t += nw) {
       int bi = 0;
       while (bi + 1 < a.nb && a.blocks[bi + 1].task0 <= t) ++bi;
       const SvdBlock& b = a.blocks[bi];
-      if (r >= b.npad - 1) continue;                 // this block has fewer rounds
+      if (r >= b.npad - 1 || !a.active[bi]) continue;   // block has fewer rounds / has converged
       int p, q;
       rr_pair(b.npad, r, t - b.task0, p, q);
-      if (p >= b.nn || q >= b.nn) continue;          // dummy column
+      if (p >= b.nn || q >= b.nn) continue;            // dummy column
       if (p > q) { int x = p; p = q; q = x; }
       double* wp = a.W + b.w_off + (int64_t)p * b.mm;
       double* wq = a.W + b.w_off + (int64_t)q * b.mm;
-      double al = 0.0, be = 0.0, ga = 0.0;
-      for (int i = threadIdx.x; i < b.mm; i += blockDim.x) {
-        const double x = wp[i], y = wq[i];
-        al = fma(x, x, al); be = fma(y, y, be); ga = fma(x, y, ga);
-      }
-      al = block_reduce_sum(al, red);
-      be = block_reduce_sum(be, red);
-      ga = block_reduce_sum(ga, red);
-      if (threadIdx.x == 0) {
-        double c = 1.0, s = 0.0;
-        const double nrm = sqrt(al) * sqrt(be);
-        double rel = nrm > 0.0 ? fabs(ga) / nrm : 0.0;
-        const double tolb = a.tol * (double)b.mm;     // m * eps, as one-sided Jacobi codes use
-        if (rel > tolb && ga != 0.0) {
-          const double zeta = (be - al) / (2.0 * ga);
-          const double tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-          c = 1.0 / sqrt(1.0 + tt * tt);
-          s = c * tt;
-        } else {
-          rel = 0.0;
-        }
-        rot[0] = c; rot[1] = s; rot[2] = (c != 1.0 || s != 0.0) ? 1.0 : 0.0;
-        atomicMax(&a.offmax[bi], (unsigned long long)__double_as_longlong(rel));
-      }
-      __syncthreads();
-      if (rot[2] != 0.0) {
-        const double c = rot[0], s = rot[1];
-        for (int i = threadIdx.x; i < b.mm; i += blockDim.x) {
+      double ga = 0.0;
+      for (int i = lane; i < b.mm; i += 32) ga = fma(wp[i], wq[i], ga);
+      ga = warp_sum(ga);
+      const double al = a.nrm[b.s_off + p], be = a.nrm[b.s_off + q];
+      const double nrm = sqrt(al) * sqrt(be);
+      double rel = nrm > 0.0 ? fabs(ga) / nrm : 0.0;
+      const double tolb = a.tol * (double)b.mm;        // m * eps, as one-sided Jacobi codes use
+      if (rel > tolb && ga != 0.0) {
+        const double zeta = (be - al) / (2.0 * ga);
+        const double tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + tt * tt);
+        const double s = c * tt;
+        for (int i = lane; i < b.mm; i += 32) {
           const double x = wp[i], y = wq[i];
           wp[i] = c * x - s * y;
           wq[i] = s * x + c * y;
         }
         double* vp = a.V + b.v_off + (int64_t)p * b.nn;
         double* vq = a.V + b.v_off + (int64_t)q * b.nn;
-        for (int i = threadIdx.x; i < b.nn; i += blockDim.x) {
+        for (int i = lane; i < b.nn; i += 32) {
           const double x = vp[i], y = vq[i];
           vp[i] = c * x - s * y;
           vq[i] = s * x + c * y;
         }
+        if (lane == 0) {
+          a.nrm[b.s_off + p] = al - tt * ga;
+          a.nrm[b.s_off + q] = be + tt * ga;
+        }
+      } else {
+        rel = 0.0;
       }
-      __syncthreads();
+      if (lane == 0 && rel > 0.0) atomicMax(&a.offmax[bi], (unsigned long long)__double_as_longlong(rel));
     }
     if (!grid_barrier(a.bar_count, a.bar_gen, gridDim.x, a.st)) return;
   }
@@ -490,29 +510,46 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
   // sweeps
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, svd_sweep, 256, 0);
-  int grid = std::max(1, std::min(task0, per_sm * h->num_sms));
+  per_sm = std::max(per_sm, 1);
+  const int warps_needed = std::max(task0, 1);
+  int grid = std::max(1, std::min((warps_needed + 7) / 8, per_sm * h->num_sms));
   const double tol = 2.220446049250313e-16;
   const int max_sweeps = 60;
   std::vector<unsigned long long> om(nb);
+  std::vector<int32_t> act(nb, 1);
+  double* nrm = nullptr;
+  int32_t* dact = nullptr;
+  ND_CUDA(h, cudaMallocAsync(&nrm, std::max(soff, 1) * 8, s));
+  ND_CUDA(h, cudaMallocAsync(&dact, nb * 4, s));
   bool converged = false;
   for (int sw = 0; sw < max_sweeps && maxr > 0; ++sw) {
+    ND_CUDA(h, cudaMemcpyAsync(dact, act.data(), nb * 4, cudaMemcpyHostToDevice, s));
     ND_CUDA(h, cudaMemsetAsync(offmax, 0, nb * 8, s));
-    SweepArgs sa{dblk, nb, task0, maxr, W, V, offmax, bar, bar + 1, h->d_status, tol};
+    nd_prof_begin(h, "svd_norms");
+    svd_norms<<<std::max(1, std::min((soff + 7) / 8, 8 * h->num_sms)), 256, 0, s>>>(dblk, nb, dact, W, nrm, soff);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    SweepArgs sa{dblk, nb, task0, maxr, W, V, nrm, dact, offmax, bar, bar + 1, h->d_status, tol};
     void* args[] = {&sa};
     nd_prof_begin(h, "svd_sweep");
     cudaError_t e = cudaLaunchCooperativeKernel((void*)svd_sweep, grid, 256, args, 0, s);
     nd_prof_end(h);
     ND_LAUNCHED(h);
-    if (e != cudaSuccess) return nd_cuda_check(h, e, "svd_sweep (cooperative launch)");
+    if (e != cudaSuccess) { cudaFreeAsync(nrm, s); cudaFreeAsync(dact, s); return nd_cuda_check(h, e, "svd_sweep (cooperative launch)"); }
     ND_CUDA(h, cudaMemcpyAsync(om.data(), offmax, nb * 8, cudaMemcpyDeviceToHost, s));
     ND_CUDA(h, cudaStreamSynchronize(s));
     nd_status st = nd_check_device_status(h, "svd");
-    if (st) return st;
-    // a sweep without any rotation above m*eps means every block has converged
+    if (st) { cudaFreeAsync(nrm, s); cudaFreeAsync(dact, s); return st; }
+    // a sweep without any rotation above m*eps leaves its block converged; stop when all are
     bool any = false;
-    for (auto v : om) any = any || (v != 0ull);
+    for (int i = 0; i < nb; ++i) {
+      if (act[i] && om[i] == 0ull) act[i] = 0;
+      any = any || act[i];
+    }
     if (!any) { converged = true; break; }
   }
+  cudaFreeAsync(nrm, s);
+  cudaFreeAsync(dact, s);
   if (maxr == 0) converged = true;
   if (!converged) {
     cudaFreeAsync(W, s); cudaFreeAsync(V, s); cudaFreeAsync(sig, s); cudaFreeAsync(order, s);

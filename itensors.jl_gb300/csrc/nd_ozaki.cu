@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full[C::STAGES], empty[C::STAGES];
-  __shared__ __align__(8) uint64_t xfull[2], xempty[2], tfull[2], tempty[2], done_bar;
+  __shared__ __align__(8) uint64_t xfull[2], xempty[2], done_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
   __shared__ int64_t colR_s[BN];
@@ -445,10 +445,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
 
   if (tid == 0) {
     for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&xfull[b], 1); mbar_init(&xempty[b], EPI_WARPS);
-      mbar_init(&tfull[b], 1); mbar_init(&tempty[b], EPI_WARPS);
-    }
+    for (int b = 0; b < 2; ++b) { mbar_init(&xfull[b], 1); mbar_init(&xempty[b], EPI_WARPS); }
     mbar_init(&done_bar, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -500,27 +497,26 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   } else if (warp == 1) {
     // ------------------------------- MMA issuer ----------------------------
     if (lane == 0) {
-      uint32_t n = 0, chunk = 0, npair = 0;
+      uint32_t n = 0, chunk = 0;
       bool ok = true;
       const uint32_t smem_base = smem_u32(smem);
       const uint32_t i64 = idesc(BN), i128 = idesc(2 * BN);
       for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
         const WorkItem wi = g.items[it];
-        for (int pi = 0; pi < wi.pair_count && ok; ++pi, ++npair) {
+        for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
           const PairDesc& pd = g.pairs[wi.pair_begin + pi];
           const int nks = g.ops[pd.a_op].k_steps;
-          const uint32_t ts = npair & 1, tu = npair >> 1;
-          if (C::TBLK && tu >= 1 && !mbar_wait(smem_u32(&tempty[ts]), (tu - 1) & 1, g.st, 410, &abort_flag)) { ok = false; break; }
-          const uint32_t T = tmem + tcol(ts);
           const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
-          uint32_t X = tmem;
+          uint32_t X = tmem, T = tmem + tcol(0);
           for (int ks = 0; ks < nks; ++ks, ++n) {
             const bool cstart = (ks % chunk_steps) == 0;
             const bool cend = ((ks % chunk_steps) == chunk_steps - 1) || ks == nks - 1;
             if (cstart) {
+              // every level is drained per chunk: slot xs holds both X and T of this chunk
               const uint32_t xs = chunk & 1, xu = chunk >> 1;
               if (xu >= 1 && !mbar_wait(smem_u32(&xempty[xs]), (xu - 1) & 1, g.st, 411, &abort_flag)) { ok = false; break; }
               X = tmem + xcol(xs);
+              T = tmem + tcol(xs);
             }
             const uint32_t s = n % C::STAGES, u = n / C::STAGES;
             if (!mbar_wait(smem_u32(&full[s]), u & 1, g.st, 412, &abort_flag)) { ok = false; break; }
@@ -530,7 +526,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
 #pragma unroll
             for (int kk = 0; kk < 2; ++kk) {
               const uint32_t accx = (cstart && kk == 0) ? 0u : 1u;
-              const uint32_t acct = (ks == 0 && kk == 0) ? 0u : 1u;
+              const uint32_t acct = accx;
               const uint32_t ko = kk * 32;
               auto A = [&](int p) { return sdesc(a0 + (p - 1) * A_SLICE + ko); };
               auto B = [&](int q) { return sdesc(b0 + (q - 1) * B_SLICE + ko); };
@@ -560,7 +556,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
             if (cend) { commit(&xfull[chunk & 1]); ++chunk; }
           }
           if (!ok) break;
-          if (C::TBLK) commit(&tfull[ts]);
         }
       }
       commit(&done_bar);
@@ -573,7 +568,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
     const int row = q * 32 + lane;
     const int etid = tid - 64;
     const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + cg * EPI_COLS;
-    uint32_t chunk = 0, npair = 0;
+    uint32_t chunk = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
       const WorkItem wi = g.items[it];
@@ -592,7 +587,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
       epi_sync();
       double* Rb = g.ptrs.R[p0.job] + p0.r_off + roff;
       const int ncols = min(EPI_COLS, p0.N - (wi.nt * BN + cg * EPI_COLS));
-      for (int pi = 0; pi < wi.pair_count && ok; ++pi, ++npair) {
+      for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
         const PairDesc& pd = g.pairs[wi.pair_begin + pi];
         const SplitOp& oa = g.ops[pd.a_op];
         const SplitOp& ob = g.ops[pd.b_op];
@@ -607,44 +602,41 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
           const uint32_t xs = chunk & 1, xu = chunk >> 1;
           if (!mbar_wait(smem_u32(&xfull[xs]), xu & 1, g.st, 420, &abort_flag)) { ok = false; break; }
           fence_after();
-          uint32_t l2[EPI_COLS], l3[EPI_COLS];
-          TMEM_LD16(lane_addr + xcol(xs), l2);
-          TMEM_LD16(lane_addr + xcol(xs) + BN, l3);
-          tmem_wait_ld();
+          {
+            uint32_t l2[EPI_COLS], l3[EPI_COLS];
+            TMEM_LD16(lane_addr + xcol(xs), l2);
+            TMEM_LD16(lane_addr + xcol(xs) + BN, l3);
+            tmem_wait_ld();
+            if (S > 2) {
+#pragma unroll
+              for (int c = 0; c < EPI_COLS; ++c) {
+                // L2: integer units; L3 was computed with pre-scaled slices: an integer multiple of 2^-8
+                long long x2 = (long long)__float2int_rn(__uint_as_float(l2[c]));
+                long long x3 = (long long)__float2int_rn(__uint_as_float(l3[c]) * 256.0f);
+                acc[c] += (x2 << 24) + (x3 << 16);
+              }
+            } else {
+#pragma unroll
+              for (int c = 0; c < EPI_COLS; ++c) facc[c] += __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
+            }
+          }
+          if (C::TBLK) {
+            // levels >= 4 of this chunk (FP32, rounded once per chunk into the fixed point)
+            uint32_t t4[EPI_COLS], t5[EPI_COLS];
+            TMEM_LD16(lane_addr + tcol(xs), t4);
+            if (C::TBLK > 1) TMEM_LD16(lane_addr + tcol(xs) + BN, t5);
+            tmem_wait_ld();
+#pragma unroll
+            for (int c = 0; c < EPI_COLS; ++c) {
+              acc[c] += __float2ll_rn(__uint_as_float(t4[c]) * 16777216.0f);                    // x 2^24
+              if (C::TBLK > 1) acc[c] += __float2ll_rn(__uint_as_float(t5[c]) * 16777216.0f);
+            }
+          }
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&xempty[xs]);
-          if (S > 2) {
-#pragma unroll
-            for (int c = 0; c < EPI_COLS; ++c) {
-              // L2: integer units; L3 was computed with pre-scaled slices: an integer multiple of 2^-8
-              long long x2 = (long long)__float2int_rn(__uint_as_float(l2[c]));
-              long long x3 = (long long)__float2int_rn(__uint_as_float(l3[c]) * 256.0f);
-              acc[c] += (x2 << 24) + (x3 << 16);
-            }
-          } else {
-#pragma unroll
-            for (int c = 0; c < EPI_COLS; ++c) facc[c] += __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
-          }
         }
         if (!ok) break;
-        if (C::TBLK) {
-          const uint32_t ts = npair & 1, tu = npair >> 1;
-          if (!mbar_wait(smem_u32(&tfull[ts]), tu & 1, g.st, 421, &abort_flag)) { ok = false; break; }
-          fence_after();
-          uint32_t t4[EPI_COLS], t5[EPI_COLS];
-          TMEM_LD16(lane_addr + tcol(ts), t4);
-          if (C::TBLK > 1) TMEM_LD16(lane_addr + tcol(ts) + BN, t5);
-          tmem_wait_ld();
-          fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&tempty[ts]);
-#pragma unroll
-          for (int c = 0; c < EPI_COLS; ++c) {
-            acc[c] += __float2ll_rn(__uint_as_float(t4[c]) * 16777216.0f);                    // x 2^24
-            if (C::TBLK > 1) acc[c] += __float2ll_rn(__uint_as_float(t5[c]) * 16777216.0f);
-          }
-        }
         // finalize this pair into R
         if (row_ok && ncols > 0) {
           const int Ei = S > 2 ? g.exps[oa.exp_off + gm] : 0;

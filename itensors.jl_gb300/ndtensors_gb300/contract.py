@@ -113,9 +113,10 @@ class ContractionPlan:
         from ._lib import _live_plans
         _live_plans.add(self)
 
-    def flops(self, T1, T2):
-        tot = 0
-        for (i1, i2, _) in self.pairs:
+    def pair_shapes(self, T1, T2):
+        """(M, N, K, output block) of every block pair, in plan order."""
+        out = []
+        for (i1, i2, ir) in self.pairs:
             d1 = T1.blockdims(T1.blocks[i1])
             d2 = T2.blockdims(T2.blocks[i2])
             m = 1
@@ -129,8 +130,11 @@ class ContractionPlan:
             for d, l in zip(d2, self.l2):
                 if l not in self.l1:
                     n *= d
-            tot += 2 * m * n * k
-        return tot
+            out.append((m, n, k, ir))
+        return out
+
+    def flops(self, T1, T2):
+        return sum(2 * m * n * k for (m, n, k, _) in self.pair_shapes(T1, T2))
 
     def destroy(self):
         if self.ptr and self.h.ptr:

@@ -70,6 +70,21 @@ def test_alpha_beta(nd, precision, alpha, beta):
     assert odense.rel_frobenius_error(out, ref) <= TOL[precision]
 
 
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("alpha,beta", [(1.0, 0.0), (-0.5, 2.0)])
+def test_long_k_small_output(nd, precision, alpha, beta):
+    """Tiny M x N with K = 3e5 (the W-cotangent shape of the H_eff gradient): the FP64
+    path splits K across CTAs and sums the partial tiles in a fixed order."""
+    rng = np.random.default_rng(21)
+    a = rng.standard_normal((10, 600, 500))
+    b = rng.standard_normal((500, 600, 12))
+    r0 = rng.standard_normal((10, 12))
+    out, ref = _run(nd, a, (1, -1, -2), b, (-2, -1, 2), (1, 2), precision, alpha, beta, r0)
+    assert odense.rel_frobenius_error(out, ref) <= TOL[precision]
+    out2, _ = _run(nd, a, (1, -1, -2), b, (-2, -1, 2), (1, 2), precision, alpha, beta, r0)
+    np.testing.assert_array_equal(out, out2)          # deterministic reduction order
+
+
 @pytest.mark.parametrize("lr", [(1, 2, 3), (2, 1, 3)])
 def test_scalar_branch_overwrites_nan(nd, lr):
     # NDTensors/test/test_dense.jl:237-259
