@@ -106,30 +106,33 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, volatile unsig
   return ok != 0;
 }
 
+template <typename T>
 struct SweepArgs {
   const SvdBlock* blocks;
   int nb;
   int ntasks;        // tasks per round (sum of npad/2)
   int nrounds;       // max npad - 1
-  double* W;
-  double* V;
-  double* nrm;       // |w_j|^2 per column (pooled like the singular values), updated by every rotation
+  T* W;
+  T* V;
+  T* nrm;            // |w_j|^2 per column (pooled like the singular values), updated by every rotation
   const int32_t* active;        // per block: 0 once a sweep left it without rotations (converged)
-  unsigned long long* offmax;   // per block, bits of the largest relative off-diagonal seen this sweep
+  unsigned long long* offmax;   // per block, bits of the largest relative off-diagonal (as a double) this sweep
   unsigned int* bar_count;
   unsigned int* bar_gen;
   DeviceStatus* st;
-  double tol;
+  double tol;        // unit roundoff of T; rotations below mm * tol are skipped
 };
 
-__device__ __forceinline__ double warp_sum(double v) {
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
 // |w_j|^2 of every column of the active blocks (one warp per column), at the start of a sweep.
+template <typename T>
 __global__ void __launch_bounds__(256) svd_norms(const SvdBlock* blocks, int nb, const int32_t* active,
-                                                 const double* W, double* nrm, int total_cols) {
+                                                 const T* W, T* nrm, int total_cols) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int c = gw; c < total_cols; c += nw) {
@@ -137,11 +140,40 @@ __global__ void __launch_bounds__(256) svd_norms(const SvdBlock* blocks, int nb,
     while (bi + 1 < nb && blocks[bi + 1].s_off <= c) ++bi;
     if (!active[bi]) continue;
     const SvdBlock& b = blocks[bi];
-    const double* w = W + b.w_off + (int64_t)(c - b.s_off) * b.mm;
-    double acc = 0.0;
-    for (int i = lane; i < b.mm; i += 32) acc = fma(w[i], w[i], acc);
+    const T* w = W + b.w_off + (int64_t)(c - b.s_off) * b.mm;
+    constexpr int CH = sizeof(T) == 4 ? 16 : 8;
+    T acc = 0;
+    for (int base = lane; base < b.mm; base += 32 * CH) {
+      T x[CH];
+#pragma unroll
+      for (int u = 0; u < CH; ++u) { const int i = base + 32 * u; x[u] = i < b.mm ? w[i] : T(0); }
+#pragma unroll
+      for (int u = 0; u < CH; ++u) acc = fma(x[u], x[u], acc);
+    }
     acc = warp_sum(acc);
     if (lane == 0) nrm[c] = acc;
+  }
+}
+
+// (x, y) <- (c x - s y, s x + c y) over n elements, one warp, CH loads per lane in flight.
+template <typename T, int CH>
+__device__ __forceinline__ void rotate_batched(T* xp, T* yp, int n, int lane, T c, T s) {
+  for (int base = lane; base < n; base += 32 * CH) {
+    T x[CH], y[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int i = base + 32 * u;
+      x[u] = i < n ? xp[i] : T(0);
+      y[u] = i < n ? yp[i] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int i = base + 32 * u;
+      if (i < n) {
+        xp[i] = c * x[u] - s * y[u];
+        yp[i] = s * x[u] + c * y[u];
+      }
+    }
   }
 }
 
@@ -150,7 +182,8 @@ __global__ void __launch_bounds__(256) svd_norms(const SvdBlock* blocks, int nb,
 // to the two columns of W and of V.  The squared norms follow the exact
 // identities |w_p'|^2 = |w_p|^2 - t gamma, |w_q'|^2 = |w_q|^2 + t gamma, so a
 // pair costs one dot product instead of three; they are recomputed every sweep.
-__global__ void __launch_bounds__(256) svd_sweep(SweepArgs a) {
+template <typename T>
+__global__ void __launch_bounds__(512, 2) svd_sweep(SweepArgs<T> a) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int r = 0; r < a.nrounds; ++r) {
@@ -163,32 +196,34 @@ __global__ void __launch_bounds__(256) svd_sweep(SweepArgs a) {
       rr_pair(b.npad, r, t - b.task0, p, q);
       if (p >= b.nn || q >= b.nn) continue;            // dummy column
       if (p > q) { int x = p; p = q; q = x; }
-      double* wp = a.W + b.w_off + (int64_t)p * b.mm;
-      double* wq = a.W + b.w_off + (int64_t)q * b.mm;
-      double ga = 0.0;
-      for (int i = lane; i < b.mm; i += 32) ga = fma(wp[i], wq[i], ga);
+      T* wp = a.W + b.w_off + (int64_t)p * b.mm;
+      T* wq = a.W + b.w_off + (int64_t)q * b.mm;
+      // loads are batched CH per lane so a column costs a few memory round trips, not one per element
+      constexpr int CH = sizeof(T) == 4 ? 16 : 8;
+      T ga = 0;
+      for (int base = lane; base < b.mm; base += 32 * CH) {
+        T x[CH], y[CH];
+#pragma unroll
+        for (int u = 0; u < CH; ++u) {
+          const int i = base + 32 * u;
+          x[u] = i < b.mm ? wp[i] : T(0);
+          y[u] = i < b.mm ? wq[i] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < CH; ++u) ga = fma(x[u], y[u], ga);
+      }
       ga = warp_sum(ga);
-      const double al = a.nrm[b.s_off + p], be = a.nrm[b.s_off + q];
-      const double nrm = sqrt(al) * sqrt(be);
-      double rel = nrm > 0.0 ? fabs(ga) / nrm : 0.0;
-      const double tolb = a.tol * (double)b.mm;        // m * eps, as one-sided Jacobi codes use
-      if (rel > tolb && ga != 0.0) {
-        const double zeta = (be - al) / (2.0 * ga);
-        const double tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + tt * tt);
-        const double s = c * tt;
-        for (int i = lane; i < b.mm; i += 32) {
-          const double x = wp[i], y = wq[i];
-          wp[i] = c * x - s * y;
-          wq[i] = s * x + c * y;
-        }
-        double* vp = a.V + b.v_off + (int64_t)p * b.nn;
-        double* vq = a.V + b.v_off + (int64_t)q * b.nn;
-        for (int i = lane; i < b.nn; i += 32) {
-          const double x = vp[i], y = vq[i];
-          vp[i] = c * x - s * y;
-          vq[i] = s * x + c * y;
-        }
+      const T al = a.nrm[b.s_off + p], be = a.nrm[b.s_off + q];
+      const T nrm = sqrt(al) * sqrt(be);
+      double rel = nrm > T(0) ? (double)(fabs(ga) / nrm) : 0.0;
+      const double tolb = a.tol * (double)b.mm;        // m * unit roundoff, as one-sided Jacobi codes use
+      if (rel > tolb && ga != T(0)) {
+        const T zeta = (be - al) / (T(2) * ga);
+        const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+        const T c = T(1) / sqrt(T(1) + tt * tt);
+        const T s = c * tt;
+        rotate_batched<T, CH>(wp, wq, b.mm, lane, c, s);
+        rotate_batched<T, CH>(a.V + b.v_off + (int64_t)p * b.nn, a.V + b.v_off + (int64_t)q * b.nn, b.nn, lane, c, s);
         if (lane == 0) {
           a.nrm[b.s_off + p] = al - tt * ga;
           a.nrm[b.s_off + q] = be + tt * ga;
@@ -199,6 +234,43 @@ __global__ void __launch_bounds__(256) svd_sweep(SweepArgs a) {
       if (lane == 0 && rel > 0.0) atomicMax(&a.offmax[bi], (unsigned long long)__double_as_longlong(rel));
     }
     if (!grid_barrier(a.bar_count, a.bar_gen, gridDim.x, a.st)) return;
+  }
+}
+
+// Largest |W| of every block (IEEE bits), for the power-of-two scaling of the FP32 copy.
+__global__ void block_absmax(const SvdBlock* blocks, const double* W, unsigned long long* mx) {
+  const SvdBlock b = blocks[blockIdx.y];
+  const int64_t tot = (int64_t)b.mm * b.nn;
+  unsigned long long m = 0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long v = (unsigned long long)__double_as_longlong(W[b.w_off + e]) & 0x7fffffffffffffffull;
+    m = v > m ? v : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) { const unsigned long long u = __shfl_xor_sync(0xffffffffu, m, o); m = u > m ? u : m; }
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(&mx[blockIdx.y], m);
+}
+
+// W32 = W * 2^-E_b (E_b: exponent of the block's largest |W|), V32 = I.
+__global__ void to_f32_scaled(const SvdBlock* blocks, const double* W, const unsigned long long* mx, float* W32,
+                              float* V32) {
+  const SvdBlock b = blocks[blockIdx.y];
+  const int ex = (int)(mx[blockIdx.y] >> 52);
+  const double sc = ex ? ldexp(1.0, 1023 - ex) : 1.0;
+  const int64_t tot = (int64_t)b.mm * b.nn;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x)
+    W32[b.w_off + e] = (float)(W[b.w_off + e] * sc);
+  const int64_t tv = (int64_t)b.nn * b.nn;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tv; e += (int64_t)gridDim.x * blockDim.x)
+    V32[b.v_off + e] = (e % b.nn == e / b.nn) ? 1.0f : 0.0f;
+}
+
+// V = double(V32), and Y = I (the accumulator of I - V^T V), per block.
+__global__ void to_f64_and_identity(const SvdBlock* blocks, const float* V32, double* V, double* Y) {
+  const SvdBlock b = blocks[blockIdx.y];
+  const int64_t tv = (int64_t)b.nn * b.nn;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tv; e += (int64_t)gridDim.x * blockDim.x) {
+    V[b.v_off + e] = (double)V32[b.v_off + e];
+    Y[b.v_off + e] = (e % b.nn == e / b.nn) ? 1.0 : 0.0;
   }
 }
 
@@ -455,11 +527,110 @@ __global__ void __launch_bounds__(256) qr_blocks(const QrBlock* blocks, const do
   }
 }
 
+__global__ void set_identity(const SvdBlock* blocks, double* Y) {
+  const SvdBlock b = blocks[blockIdx.y];
+  const int64_t tv = (int64_t)b.nn * b.nn;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tv; e += (int64_t)gridDim.x * blockDim.x)
+    Y[b.v_off + e] = (e % b.nn == e / b.nn) ? 1.0 : 0.0;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// Jacobi sweeps of element type T on (Wt, Vt) until every block has had a sweep
+// without rotations or max_sweeps have run.
+template <typename T>
+static nd_status run_sweeps(nd_handle h, const SvdBlock* dblk, int nb, int task0, int maxr, int soff, T* Wt, T* Vt,
+                            unsigned long long* offmax, unsigned int* bar, double tol, int max_sweeps,
+                            bool& converged, int& sweeps) {
+  cudaStream_t s = h->stream;
+  converged = maxr == 0;
+  sweeps = 0;
+  if (converged) return ND_OK;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, svd_sweep<T>, 512, 0);
+  per_sm = std::max(per_sm, 1);
+  const int grid = std::max(1, std::min((task0 + 15) / 16, per_sm * h->num_sms));
+  const char* name = sizeof(T) == 4 ? "svd_sweep_f32" : "svd_sweep";
+  std::vector<unsigned long long> om(nb);
+  std::vector<int32_t> act(nb, 1);
+  T* nrm = nullptr;
+  int32_t* dact = nullptr;
+  ND_CUDA(h, cudaMallocAsync(&nrm, std::max(soff, 1) * sizeof(T), s));
+  ND_CUDA(h, cudaMallocAsync(&dact, nb * 4, s));
+  nd_status st = ND_OK;
+  for (int sw = 0; sw < max_sweeps; ++sw) {
+    cudaError_t e = cudaMemcpyAsync(dact, act.data(), nb * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(offmax, 0, nb * 8, s);
+    if (e != cudaSuccess) { st = nd_cuda_check(h, e, "svd sweep set-up"); break; }
+    nd_prof_begin(h, "svd_norms");
+    svd_norms<T><<<std::max(1, std::min((soff + 7) / 8, 8 * h->num_sms)), 256, 0, s>>>(dblk, nb, dact, Wt, nrm, soff);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    SweepArgs<T> sa{dblk, nb, task0, maxr, Wt, Vt, nrm, dact, offmax, bar, bar + 1, h->d_status, tol};
+    void* args[] = {&sa};
+    nd_prof_begin(h, name);
+    e = cudaLaunchCooperativeKernel((void*)svd_sweep<T>, grid, 512, args, 0, s);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    if (e != cudaSuccess) { st = nd_cuda_check(h, e, "svd_sweep (cooperative launch)"); break; }
+    e = cudaMemcpyAsync(om.data(), offmax, nb * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { st = nd_cuda_check(h, e, "svd sweep"); break; }
+    ++sweeps;
+    if ((st = nd_check_device_status(h, "svd"))) break;
+    // a sweep without any rotation above m * unit roundoff leaves its block converged
+    bool any = false;
+    for (int i = 0; i < nb; ++i) {
+      if (act[i] && om[i] == 0ull) act[i] = 0;
+      any = any || act[i];
+    }
+    if (!any) { converged = true; break; }
+  }
+  cudaFreeAsync(nrm, s);
+  cudaFreeAsync(dact, s);
+  return st;
+}
+
+static Mixed mixed1(int64_t dim, int64_t st0, int64_t st1) {
+  Mixed m{};
+  m.n = 1;
+  m.dim[0] = (int32_t)dim;
+  m.st0[0] = st0;
+  m.st1[0] = st1;
+  return m;
+}
+
+// R = alpha * op(A) * B + beta * R for every block in one grouped FP64 launch.
+//   kind 0: Y  (nn x nn) = alpha * V^T V + beta * Y
+//   kind 1: Vn (nn x nn) = alpha * V Y   + beta * Vn
+//   kind 2: W0 (mm x nn) = alpha * W Q   + beta * W0
+static nd_status block_gemm(nd_handle h, const std::vector<SvdBlock>& blocks, int kind, const double* A,
+                            const double* B, double* R, double alpha, double beta) {
+  std::vector<PairDesc> pairs(blocks.size());
+  for (size_t i = 0; i < blocks.size(); ++i) {
+    const SvdBlock& b = blocks[i];
+    PairDesc pd{};
+    const int64_t M = kind == 2 ? b.mm : b.nn, N = b.nn, K = b.nn;
+    pd.M = (int32_t)M; pd.N = (int32_t)N; pd.K = (int32_t)K;
+    pd.group = (int32_t)i; pd.first = 1; pd.job = 0;
+    pd.a_off = kind == 2 ? b.w_off : b.v_off;
+    pd.b_off = b.v_off;
+    pd.r_off = kind == 2 ? b.w_off : b.v_off;
+    pd.rows = mixed1(M, kind == 0 ? b.nn : 1, 1);    // A row stride, R row stride
+    pd.cols = mixed1(N, b.nn, M);                    // B column stride, R column stride
+    pd.ks = mixed1(K, kind == 0 ? 1 : M, 1);         // A k stride, B k stride
+    pairs[i] = pd;
+  }
+  ExecCache c;
+  JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
+  nd_status st = nd_execute_cached(h, c, pairs, (int)blocks.size(), ptrs, alpha, beta, ND_PREC_FP64);
+  c.free_all();
+  return st;
+}
+
 static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_t* cols, const int64_t* offsets,
                           const double* A, std::vector<SvdBlock>& blocks, double** d_sig_out, int32_t** d_order_out,
                           double** d_W_out, double** d_V_out, SvdBlock** d_blocks_out, int& total_k) {
@@ -507,49 +678,65 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
     nd_prof_end(h);
     ND_LAUNCHED(h);
   }
-  // sweeps
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, svd_sweep, 256, 0);
-  per_sm = std::max(per_sm, 1);
-  const int warps_needed = std::max(task0, 1);
-  int grid = std::max(1, std::min((warps_needed + 7) / 8, per_sm * h->num_sms));
-  const double tol = 2.220446049250313e-16;
-  const int max_sweeps = 60;
-  std::vector<unsigned long long> om(nb);
-  std::vector<int32_t> act(nb, 1);
-  double* nrm = nullptr;
-  int32_t* dact = nullptr;
-  ND_CUDA(h, cudaMallocAsync(&nrm, std::max(soff, 1) * 8, s));
-  ND_CUDA(h, cudaMallocAsync(&dact, nb * 4, s));
+  // Preconditioner for the larger problems: the same Jacobi sweeps in FP32 on a
+  // power-of-two scaled copy (the FP32 pipe is ~64x the FP64 one), its V
+  // re-orthogonalised in FP64 by two Newton-Schulz steps V <- V + V (I - V^T V) / 2
+  // (quadratic: 1e-6 -> 1e-12 -> roundoff), then W0 = W Q.  The FP64 sweeps that
+  // follow start nearly orthogonal and converge in a few sweeps; the result is
+  // the FP64 one-sided Jacobi SVD of W0, so accuracy is unchanged.
+  double work = 0.0;
+  for (auto& b : blocks) work += (double)b.mm * b.nn * b.nn;
   bool converged = false;
-  for (int sw = 0; sw < max_sweeps && maxr > 0; ++sw) {
-    ND_CUDA(h, cudaMemcpyAsync(dact, act.data(), nb * 4, cudaMemcpyHostToDevice, s));
-    ND_CUDA(h, cudaMemsetAsync(offmax, 0, nb * 8, s));
-    nd_prof_begin(h, "svd_norms");
-    svd_norms<<<std::max(1, std::min((soff + 7) / 8, 8 * h->num_sms)), 256, 0, s>>>(dblk, nb, dact, W, nrm, soff);
+  int sweeps32 = 0, sweeps64 = 0;
+  nd_status st = ND_OK;
+  if (work >= 2e8 && maxr > 0) {
+    float *W32 = nullptr, *V32 = nullptr;
+    double *Y = nullptr, *Vn = nullptr, *W0 = nullptr;
+    unsigned long long* bmax = nullptr;
+    ND_CUDA(h, cudaMallocAsync(&W32, std::max<int64_t>(woff, 1) * 4, s));
+    ND_CUDA(h, cudaMallocAsync(&V32, std::max<int64_t>(voff, 1) * 4, s));
+    ND_CUDA(h, cudaMallocAsync(&Y, std::max<int64_t>(voff, 1) * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&Vn, std::max<int64_t>(voff, 1) * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&W0, std::max<int64_t>(woff, 1) * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&bmax, nb * 8, s));
+    ND_CUDA(h, cudaMemsetAsync(bmax, 0, nb * 8, s));
+    int64_t maxe = 0, maxv = 0;
+    for (auto& b : blocks) { maxe = std::max(maxe, (int64_t)b.mm * b.nn); maxv = std::max(maxv, (int64_t)b.nn * b.nn); }
+    const dim3 ge((unsigned)std::min<int64_t>((maxe + 255) / 256, 1024), nb);
+    const dim3 gv((unsigned)std::min<int64_t>((maxv + 255) / 256, 1024), nb);
+    nd_prof_begin(h, "svd_precondition");
+    block_absmax<<<ge, 256, 0, s>>>(dblk, W, bmax);
+    to_f32_scaled<<<ge, 256, 0, s>>>(dblk, W, bmax, W32, V32);
     nd_prof_end(h);
     ND_LAUNCHED(h);
-    SweepArgs sa{dblk, nb, task0, maxr, W, V, nrm, dact, offmax, bar, bar + 1, h->d_status, tol};
-    void* args[] = {&sa};
-    nd_prof_begin(h, "svd_sweep");
-    cudaError_t e = cudaLaunchCooperativeKernel((void*)svd_sweep, grid, 256, args, 0, s);
-    nd_prof_end(h);
     ND_LAUNCHED(h);
-    if (e != cudaSuccess) { cudaFreeAsync(nrm, s); cudaFreeAsync(dact, s); return nd_cuda_check(h, e, "svd_sweep (cooperative launch)"); }
-    ND_CUDA(h, cudaMemcpyAsync(om.data(), offmax, nb * 8, cudaMemcpyDeviceToHost, s));
-    ND_CUDA(h, cudaStreamSynchronize(s));
-    nd_status st = nd_check_device_status(h, "svd");
-    if (st) { cudaFreeAsync(nrm, s); cudaFreeAsync(dact, s); return st; }
-    // a sweep without any rotation above m*eps leaves its block converged; stop when all are
-    bool any = false;
-    for (int i = 0; i < nb; ++i) {
-      if (act[i] && om[i] == 0ull) act[i] = 0;
-      any = any || act[i];
+    bool c32 = false;
+    st = run_sweeps<float>(h, dblk, nb, task0, maxr, soff, W32, V32, offmax, bar, 5.9604644775390625e-08, 40, c32,
+                           sweeps32);
+    if (!st) {
+      to_f64_and_identity<<<gv, 256, 0, s>>>(dblk, V32, V, Y);
+      ND_LAUNCHED(h);
+      for (int it = 0; it < 2 && !st; ++it) {
+        if (it) { set_identity<<<gv, 256, 0, s>>>(dblk, Y); ND_LAUNCHED(h); }
+        st = block_gemm(h, blocks, 0, V, V, Y, -1.0, 1.0);                  // Y = I - V^T V
+        if (!st) st = nd_cuda_check(h, cudaMemcpyAsync(Vn, V, voff * 8, cudaMemcpyDeviceToDevice, s), "svd copy");
+        if (!st) st = block_gemm(h, blocks, 1, V, Y, Vn, 0.5, 1.0);         // Vn = V + V Y / 2
+        std::swap(V, Vn);
+      }
+      if (!st) st = block_gemm(h, blocks, 2, W, V, W0, 1.0, 0.0);           // W0 = W Q
+      if (!st) std::swap(W, W0);
     }
-    if (!any) { converged = true; break; }
+    cudaFreeAsync(W32, s); cudaFreeAsync(V32, s); cudaFreeAsync(Y, s); cudaFreeAsync(Vn, s);
+    cudaFreeAsync(W0, s); cudaFreeAsync(bmax, s);
   }
-  cudaFreeAsync(nrm, s);
-  cudaFreeAsync(dact, s);
+  if (!st) st = run_sweeps<double>(h, dblk, nb, task0, maxr, soff, W, V, offmax, bar, 2.220446049250313e-16, 60,
+                                   converged, sweeps64);
+  const int max_sweeps = 60;
+  if (st) {
+    cudaFreeAsync(W, s); cudaFreeAsync(V, s); cudaFreeAsync(sig, s); cudaFreeAsync(order, s);
+    cudaFreeAsync(dblk, s); cudaFreeAsync(offmax, s); cudaFreeAsync(bar, s);
+    return st;
+  }
   if (maxr == 0) converged = true;
   if (!converged) {
     cudaFreeAsync(W, s); cudaFreeAsync(V, s); cudaFreeAsync(sig, s); cudaFreeAsync(order, s);

@@ -56,6 +56,45 @@ def test_svd_reference_examples(nd, ex):
         np.testing.assert_allclose(s, np.linalg.svd(m, compute_uv=False), rtol=1e-12, atol=1e-12 * s[0])
 
 
+@pytest.mark.parametrize("spectrum", ["gaussian", "graded", "clustered"])
+def test_svd_preconditioned_blocks(nd, spectrum):
+    """Blocks large enough for the FP32-preconditioned path (work >= 2e8): same bars as
+    the plain FP64 path, including singular values down to 1e-13 of the largest and
+    near-degenerate clusters (which the FP32 phase cannot separate)."""
+    rng = np.random.default_rng({"gaussian": 31, "graded": 32, "clustered": 33}[spectrum])
+    dims = [(700, 600), (520, 560), (64, 90)]
+    mats = []
+    for (r, c) in dims:
+        k = min(r, c)
+        if spectrum == "gaussian":
+            m = rng.standard_normal((r, c))
+        else:
+            if spectrum == "graded":
+                sv = np.logspace(0, -13, k)
+            else:
+                sv = np.repeat(np.linspace(1.0, 0.1, 8), -(-k // 8))[:k] * (1 + 1e-9 * rng.standard_normal(k))
+            qu, _ = np.linalg.qr(rng.standard_normal((r, k)))
+            qv, _ = np.linalg.qr(rng.standard_normal((c, k)))
+            m = (qu * sv) @ qv.T
+        mats.append(m)
+    inds = [[d[0] for d in dims], [d[1] for d in dims]]
+    blocks = [(i + 1, i + 1) for i in range(len(dims))]
+    offs, o = [], 0
+    for m in mats:
+        offs.append(o)
+        o += m.size
+    A = obs.BlockSparseTensor(inds, blocks, offs, np.concatenate([m.reshape(-1, order="F") for m in mats]))
+    U, S, V, spec, kept = nd.svd(_gpu(nd, A))
+    Ub, Vb = _blocks(nd, U), _blocks(nd, V)
+    for n, m in enumerate(mats):
+        s = S[n].cpu().numpy()
+        ref = np.linalg.svd(m, compute_uv=False)
+        np.testing.assert_allclose(s, ref, rtol=0, atol=1e-12 * ref[0])
+        assert odense.rel_frobenius_error(Ub[n] @ np.diag(s) @ Vb[n].T, m) <= 1e-12
+        k = len(s)
+        np.testing.assert_allclose(Vb[n].T @ Vb[n], np.eye(k), atol=1e-12)
+
+
 @pytest.mark.parametrize("shape", [(40, 40), (130, 33), (33, 130), (257, 255), (1, 7), (600, 64)])
 def test_svd_dense_block(nd, shape):
     rng = np.random.default_rng(sum(shape))
