@@ -184,6 +184,25 @@ def split_routed_flops(shapes):
     return tot
 
 
+def tune_summary(h):
+    """Entries of the handle's autotune cache: key -> (choice, best ms, default ms)."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        path = Path(d) / "tune.txt"
+        h.tune_save(path)
+        out = []
+        for line in path.read_text().splitlines():
+            if line.startswith("#") or not line.strip():
+                continue
+            key, mult, skinny, best, dflt = line.split("\t")
+            prec = key.split("/")[1]
+            npairs = sum(int(b.split("x")[1]) for b in key.split("/")[3].split(","))
+            out.append({"precision": {"p0": "fp64", "p1": "ozaki", "p2": "bf16x3"}.get(prec, prec),
+                        "block_pairs": npairs, "splitk_mult": int(mult), "skinny_fp64": int(skinny),
+                        "best_ms": round(float(best), 4), "default_ms": round(float(dflt), 4)})
+    return {"entries": len(out), "choices": out}
+
+
 def run_ours(args):
     import torch
     rank, ws, local, dist = dist_init()
@@ -197,6 +216,7 @@ def run_ours(args):
     h = nd.handle(local)
     if args.slices:
         h.call("nd_set_ozaki_slices", int(args.slices))
+    h.tune(True)          # execution parameters timed on first use, cached per block-size histogram
 
     # plans (built once, as in a sweep) and flops
     plans = []
@@ -338,6 +358,7 @@ def run_ours(args):
                     "plans_rebuilt_each_step": {"value": round(ws * flops / (e2e_cold_ms * 1e-3) / 1e9, 2),
                                                 "ms_per_step": round(e2e_cold_ms, 3)}},
             "gpu_launches": launches,
+            "autotune": tune_summary(h),
             "clocks": cs.summary()}
 
     # CPU baseline: the oracle on the same workload, one matvec (rank 0, N=1 only)

@@ -217,6 +217,23 @@ typedef struct {
 nd_status nd_block_copy_f64(nd_handle h, int32_t n, const nd_block_copy *list /* host */, const double *src,
                             double *dst);
 
+/* ---- autotuner -------------------------------------------------------------
+ * Execution parameters of a contraction (today: the split-K target of the FP64
+ * tile kernel and whether skinny block pairs, N <= 8 and K <= 32, run on the FP64
+ * CUDA-core kernel or with the precision's tile kernel) are chosen per
+ * block-size histogram: the key is the device's SM count, the precision, the
+ * Ozaki slice count and the counts of block pairs per (log2 M, log2 N, log2 K)
+ * bucket.  With tuning on, the first execution of a contraction whose key is
+ * not cached times every candidate on the real operands (only when beta == 0,
+ * never inside a capture) and caches the fastest; otherwise a cached choice is
+ * used, else the defaults.  The cache persists as a text file.  No counterpart
+ * in the reference (its tuning knobs are the BLAS/backend choice,
+ * NDTensors/src/lib/BackendSelection/src/backend_types.jl:45-52). */
+nd_status nd_tune_enable(nd_handle h, int32_t enable);
+nd_status nd_tune_count(nd_handle h, int32_t *entries);
+nd_status nd_tune_save(nd_handle h, const char *path);
+nd_status nd_tune_load(nd_handle h, const char *path);   /* merges; ND_ERR_ARG on a malformed file */
+
 /* ---- CUDA graphs ---------------------------------------------------------
  * Capture the handle's stream into a graph (a sweep step) and replay it. */
 nd_status nd_graph_begin(nd_handle h);

@@ -177,6 +177,66 @@ nd_status nd_set_ozaki_slices(nd_handle h, int32_t s) {
   return ND_OK;
 }
 
+// ---- autotuner cache ---------------------------------------------------------
+// File format: '#' comment lines, then one line per entry:
+//   <key> TAB <splitk_mult> TAB <skinny> TAB <best_ms> TAB <default_ms>
+nd_status nd_tune_enable(nd_handle h, int32_t enable) {
+  if (!h) return ND_ERR_ARG;
+  h->tuning = enable != 0;
+  return ND_OK;
+}
+
+nd_status nd_tune_count(nd_handle h, int32_t* entries) {
+  if (!h || !entries) return ND_ERR_ARG;
+  *entries = (int32_t)h->tune.size();
+  return ND_OK;
+}
+
+nd_status nd_tune_save(nd_handle h, const char* path) {
+  if (!h) return ND_ERR_ARG;
+  if (!path) return nd_fail(h, ND_ERR_ARG, "tune_save: NULL path");
+  FILE* f = std::fopen(path, "w");
+  if (!f) return nd_fail(h, ND_ERR_ARG, "tune_save: cannot open %s", path);
+  std::fprintf(f, "# ndtensors_gb300 autotune cache v1: key splitk_mult skinny best_ms default_ms\n");
+  for (const auto& e : h->tune)
+    std::fprintf(f, "%s\t%d\t%d\t%.6f\t%.6f\n", e.first.c_str(), e.second.choice.splitk_mult,
+                 e.second.choice.skinny, e.second.best_ms, e.second.default_ms);
+  const bool ok = std::fclose(f) == 0;
+  return ok ? ND_OK : nd_fail(h, ND_ERR_ARG, "tune_save: write to %s failed", path);
+}
+
+nd_status nd_tune_load(nd_handle h, const char* path) {
+  if (!h) return ND_ERR_ARG;
+  if (!path) return nd_fail(h, ND_ERR_ARG, "tune_load: NULL path");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return nd_fail(h, ND_ERR_ARG, "tune_load: cannot open %s", path);
+  std::map<std::string, TuneEntry> got;
+  char line[8192];
+  int lineno = 0;
+  nd_status st = ND_OK;
+  while (std::fgets(line, sizeof line, f)) {
+    ++lineno;
+    size_t n = std::strlen(line);
+    if (n + 1 == sizeof line && line[n - 1] != '\n') { st = nd_fail(h, ND_ERR_ARG, "tune_load: line %d too long", lineno); break; }
+    while (n && (line[n - 1] == '\n' || line[n - 1] == '\r')) line[--n] = 0;
+    if (!n || line[0] == '#') continue;
+    char* tab = std::strchr(line, '\t');
+    TuneEntry e;
+    int used = 0;
+    if (!tab || std::sscanf(tab + 1, "%d\t%d\t%lf\t%lf%n", &e.choice.splitk_mult, &e.choice.skinny, &e.best_ms,
+                            &e.default_ms, &used) != 4 || tab[1 + used] != 0 || e.choice.splitk_mult < 0 ||
+        e.choice.splitk_mult > 64 || (e.choice.skinny != 0 && e.choice.skinny != 1)) {
+      st = nd_fail(h, ND_ERR_ARG, "tune_load: malformed entry at %s:%d", path, lineno);
+      break;
+    }
+    got[std::string(line, tab - line)] = e;
+  }
+  std::fclose(f);
+  if (st) return st;
+  for (auto& e : got) h->tune[e.first] = e.second;
+  return ND_OK;
+}
+
 nd_status nd_launch_count(nd_handle h, int64_t* c) {
   if (!h || !c) return ND_ERR_ARG;
   *c = h->launches;

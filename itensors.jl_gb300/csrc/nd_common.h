@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <string>
 #include <vector>
+#include <map>
 #include <mutex>
 #include "../../include/ndtensors_gb300.h"
 
@@ -18,6 +19,16 @@
 struct DeviceStatus {
   int32_t code;
   int32_t where;
+};
+
+// Execution parameters chosen by the autotuner (per block-size histogram).
+struct TuneChoice {
+  int32_t splitk_mult = 4;   // FP64 tile kernel: split-K balances work over splitk_mult x SMs CTAs (0 = off)
+  int32_t skinny = 1;        // 1: skinny groups (N <= 8, K <= 32) on the FP64 CUDA-core kernel
+};
+struct TuneEntry {
+  TuneChoice choice;
+  double best_ms = 0.0, default_ms = 0.0;
 };
 
 struct nd_context {
@@ -40,6 +51,9 @@ struct nd_context {
   struct ProfRec { const char* name; cudaEvent_t e0, e1; };
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> event_pool;
+  // autotuner
+  bool tuning = false;
+  std::map<std::string, TuneEntry> tune;
 };
 
 // Host helpers -------------------------------------------------------------

@@ -13,6 +13,8 @@
 #include <algorithm>
 #include <numeric>
 #include <cstring>
+#include <map>
+#include <string>
 
 nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups, int precision);
 nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double alpha, double beta);
@@ -191,6 +193,106 @@ static bool group_skinny(const std::vector<PairDesc>& pairs, size_t i) {
   return true;
 }
 
+// Device state of one contraction for one set of execution parameters.
+static nd_status build_exec(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups,
+                            int precision, int slices, const TuneChoice& tc) {
+  c.free_all();
+  c.precision = precision;
+  c.slices = slices;
+  nd_status s = upload(h, (void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc));
+  if (s) return s;
+  // which pairs sit in skinny groups (routed to the FP64 CUDA-core kernel)
+  std::vector<char> sk(pairs.size(), 0);
+  for (size_t i = 0; i < pairs.size();) {
+    size_t j = i;
+    const bool g = tc.skinny && group_skinny(pairs, i);
+    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) sk[j++] = g;
+    i = j;
+  }
+  std::vector<WorkItem> items;
+  make_items(pairs, nd_skinny_rows(), 1 << 30, [&](const PairDesc& p) { return sk[&p - pairs.data()] != 0; }, items);
+  c.nsk_items = (int)items.size();
+  if ((s = upload(h, (void**)&c.d_sk_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
+  if (precision == ND_PREC_FP64) {
+    make_items(pairs, 64, 64, [&](const PairDesc& p) { return sk[&p - pairs.data()] == 0; }, items);
+    if ((s = plan_split_k(h, pairs, items, c, tc.splitk_mult * h->num_sms))) return s;
+    c.nitems = (int)items.size();
+    if ((s = upload(h, (void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
+  } else {
+    std::vector<PairDesc> regular;
+    for (size_t i = 0; i < pairs.size(); ++i) if (!sk[i]) regular.push_back(pairs[i]);
+    if (!regular.empty() && (s = nd_split_build(h, c, regular, ngroups, precision))) return s;
+  }
+  c.built = true;
+  return ND_OK;
+}
+
+static nd_status launch_exec(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double alpha, double beta) {
+  nd_status s = nd_launch_skinny_f64(h, c.d_pairs, c.d_sk_items, c.nsk_items, ptrs, alpha, beta);
+  if (s) return s;
+  if (c.precision == ND_PREC_FP64)
+    return nd_launch_gemm_f64(h, c.d_pairs, c.d_items, c.nitems, ptrs, alpha, beta, c.d_ws, c.d_red, c.nred);
+  return nd_split_run(h, c, ptrs, alpha, beta);
+}
+
+// Autotuner key: SM count, precision, slices and the block-size histogram
+// (block pairs counted per (bit length of M, N, K) bucket).
+static std::string tune_key(nd_handle h, const std::vector<PairDesc>& pairs, int precision, int slices) {
+  auto bl = [](int64_t v) { int b = 0; while (v > 0) { ++b; v >>= 1; } return b; };
+  std::map<int, int> hist;
+  for (const PairDesc& p : pairs) hist[(bl(p.M) << 16) | (bl(p.N) << 8) | bl(p.K)]++;
+  std::string k = "sm" + std::to_string(h->num_sms) + "/p" + std::to_string(precision) + "/s" + std::to_string(slices) + "/";
+  bool first = true;
+  for (auto& e : hist) {
+    if (!first) k += ",";
+    first = false;
+    k += std::to_string(e.first >> 16) + "." + std::to_string((e.first >> 8) & 255) + "." +
+         std::to_string(e.first & 255) + "x" + std::to_string(e.second);
+  }
+  return k;
+}
+
+// Time every candidate on the real operands (R is overwritten: beta == 0), keep the fastest.
+static nd_status tune_exec(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups,
+                           const JobPtrs& ptrs, double alpha, int precision, int slices, TuneEntry& out) {
+  std::vector<TuneChoice> cands;
+  if (precision == ND_PREC_FP64) {
+    for (int sk = 1; sk >= 0; --sk)
+      for (int m : {4, 0, 2, 8}) cands.push_back(TuneChoice{m, sk});
+  } else {
+    cands.push_back(TuneChoice{4, 1});
+    cands.push_back(TuneChoice{4, 0});
+  }
+  cudaEvent_t e0, e1;
+  ND_CUDA(h, cudaEventCreate(&e0));
+  ND_CUDA(h, cudaEventCreate(&e1));
+  nd_status st = ND_OK;
+  double best = 1e300;
+  TuneChoice bestc = cands[0];
+  for (size_t i = 0; i < cands.size() && !st; ++i) {
+    if ((st = build_exec(h, c, pairs, ngroups, precision, slices, cands[i]))) break;
+    if ((st = launch_exec(h, c, ptrs, alpha, 0.0))) break;           // warm-up
+    float ms = 0.f, tot = 0.f;
+    for (int r = 0; r < 2 && !st; ++r) {
+      cudaEventRecord(e0, h->stream);
+      st = launch_exec(h, c, ptrs, alpha, 0.0);
+      cudaEventRecord(e1, h->stream);
+      if (!st) st = nd_cuda_check(h, cudaEventSynchronize(e1), "tune timing");
+      if (!st) { cudaEventElapsedTime(&ms, e0, e1); tot += ms; }
+    }
+    if (st) break;
+    if (i == 0) out.default_ms = tot / 2;
+    if (tot / 2 < best) { best = tot / 2; bestc = cands[i]; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if ((st = nd_check_device_status(h, "autotune"))) return st;
+  out.choice = bestc;
+  out.best_ms = best;
+  return build_exec(h, c, pairs, ngroups, precision, slices, bestc);
+}
+
 nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups,
                             const JobPtrs& ptrs, double alpha, double beta, int precision) {
   if (pairs.empty()) return ND_OK;
@@ -199,40 +301,21 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
   const int want_slices = precision == ND_PREC_OZAKI ? h->ozaki_slices : (precision == ND_PREC_BF16X3 ? 2 : 0);
   if (!c.built || c.precision != precision || c.slices != want_slices) {
     if (h->capturing) return nd_fail(h, ND_ERR_ARG, "contraction state must be built before graph capture (run once first)");
-    c.free_all();
-    c.precision = precision;
-    c.slices = want_slices;
-    nd_status s = upload(h, (void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc));
-    if (s) return s;
-    // which pairs sit in skinny groups
-    std::vector<char> sk(pairs.size(), 0);
-    for (size_t i = 0; i < pairs.size();) {
-      size_t j = i;
-      bool g = group_skinny(pairs, i);
-      while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) sk[j++] = g;
-      i = j;
-    }
-    std::vector<WorkItem> items;
-    make_items(pairs, nd_skinny_rows(), 1 << 30, [&](const PairDesc& p) { return sk[&p - pairs.data()] != 0; }, items);
-    c.nsk_items = (int)items.size();
-    if ((s = upload(h, (void**)&c.d_sk_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
-    if (precision == ND_PREC_FP64) {
-      make_items(pairs, 64, 64, [&](const PairDesc& p) { return sk[&p - pairs.data()] == 0; }, items);
-      if ((s = plan_split_k(h, pairs, items, c, 4 * h->num_sms))) return s;
-      c.nitems = (int)items.size();
-      if ((s = upload(h, (void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
+    const std::string key = tune_key(h, pairs, precision, want_slices);
+    auto it = h->tune.find(key);
+    nd_status s;
+    if (it != h->tune.end()) {
+      s = build_exec(h, c, pairs, ngroups, precision, want_slices, it->second.choice);
+    } else if (h->tuning && beta == 0.0) {
+      TuneEntry e;
+      s = tune_exec(h, c, pairs, ngroups, ptrs, alpha, precision, want_slices, e);
+      if (!s) h->tune[key] = e;
     } else {
-      std::vector<PairDesc> regular;
-      for (size_t i = 0; i < pairs.size(); ++i) if (!sk[i]) regular.push_back(pairs[i]);
-      if (!regular.empty() && (s = nd_split_build(h, c, regular, ngroups, precision))) return s;
+      s = build_exec(h, c, pairs, ngroups, precision, want_slices, TuneChoice{});
     }
-    c.built = true;
+    if (s) return s;
   }
-  nd_status s = nd_launch_skinny_f64(h, c.d_pairs, c.d_sk_items, c.nsk_items, ptrs, alpha, beta);
-  if (s) return s;
-  if (precision == ND_PREC_FP64)
-    return nd_launch_gemm_f64(h, c.d_pairs, c.d_items, c.nitems, ptrs, alpha, beta, c.d_ws, c.d_red, c.nred);
-  return nd_split_run(h, c, ptrs, alpha, beta);
+  return launch_exec(h, c, ptrs, alpha, beta);
 }
 
 // ---------------------------------------------------------------------------

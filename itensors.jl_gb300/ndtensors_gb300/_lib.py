@@ -67,6 +67,10 @@ SIGNATURES = {
     "nd_launch_count": [_P, _PI64],
     "nd_profile_enable": [_P, _I32],
     "nd_profile_read": [_P, _I32, C.c_char_p, _PI64, _PD, _PI32],
+    "nd_tune_enable": [_P, _I32],
+    "nd_tune_count": [_P, _PI32],
+    "nd_tune_save": [_P, C.c_char_p],
+    "nd_tune_load": [_P, C.c_char_p],
     "nd_permutedims_f64": [_P, _P, _P, _I32, _PI64, _PI32, _D, _D],
     "nd_contract_dense_f64": [_P, _P, _I32, _PI64, _PI32, _P, _I32, _PI64, _PI32, _P, _I32, _PI64, _PI32,
                               _D, _D, _I32],
@@ -178,6 +182,22 @@ class Handle:
             nm = names.raw[64 * k:64 * k + 64].split(b"\0", 1)[0].decode()
             out[nm] = (counts[k], tot[k])
         return out
+
+    def tune(self, enable=True):
+        """Autotune the execution parameters of contractions built from now on (cached per
+        block-size histogram)."""
+        self._check(self.lib.nd_tune_enable(self.ptr, 1 if enable else 0))
+
+    def tune_count(self):
+        n = C.c_int32()
+        self._check(self.lib.nd_tune_count(self.ptr, C.byref(n)))
+        return n.value
+
+    def tune_save(self, path):
+        self._check(self.lib.nd_tune_save(self.ptr, os.fsencode(str(path))))
+
+    def tune_load(self, path):
+        self._check(self.lib.nd_tune_load(self.ptr, os.fsencode(str(path))))
 
     def launches(self):
         c = C.c_int64()
