@@ -81,9 +81,36 @@ void nd_prof_end(nd_handle h);
 struct Mixed {
   int32_t n;
   int32_t dim[ND_MAX_RANK];
+  // division by dim[d] as a multiply-high (Granlund & Montgomery, "Division by
+  // invariant integers using multiplication", PLDI 1994, round-up multiplier):
+  // for 0 <= x < 2^31, x / d == (umulhi(x, mul) + x) >> shr with shr = ceil(log2 d),
+  // mul = floor(2^32 (2^shr - d) / d) + 1.  mul == 0 means "not computed".
+  uint32_t mul[ND_MAX_RANK];
+  uint32_t shr[ND_MAX_RANK];
   int64_t st0[ND_MAX_RANK];
   int64_t st1[ND_MAX_RANK];
 };
+
+// Fill mul / shr of every dimension (host).
+inline void mixed_finalize(Mixed& m) {
+  for (int d = 0; d < ND_MAX_RANK; ++d) { m.mul[d] = 0; m.shr[d] = 0; }
+  for (int d = 0; d < m.n; ++d) {
+    const uint64_t dd = (uint64_t)(uint32_t)m.dim[d];
+    if (dd == 0) continue;
+    uint32_t shr = 0;
+    while ((1ull << shr) < dd) ++shr;
+    m.shr[d] = shr;
+    m.mul[d] = (uint32_t)((((1ull << 32) * ((1ull << shr) - dd)) / dd) + 1ull);
+  }
+}
+
+ND_HOSTDEV uint32_t nd_umulhi(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __umulhi(a, b);
+#else
+  return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
 
 ND_HOSTDEV void mixed_offsets(const Mixed& m, int64_t lin, int64_t& o0, int64_t& o1) {
   int64_t a = 0, b = 0;
@@ -98,13 +125,15 @@ ND_HOSTDEV void mixed_offsets(const Mixed& m, int64_t lin, int64_t& o0, int64_t&
   o1 = b;
 }
 
-// Same for indices below 2^31 with 32-bit division (GEMM extents are < 2^31).
+// Same for indices below 2^31 (GEMM extents are < 2^31), dividing by multiply-high
+// when the divisors were computed: integer instructions only, no conversion or
+// FP64 pipe work (which GB300 runs at a fraction of the integer rate).
 ND_HOSTDEV void mixed_offsets32(const Mixed& m, uint32_t lin, int64_t& o0, int64_t& o1) {
   int64_t a = 0, b = 0;
   for (int d = 0; d < m.n; ++d) {
-    uint32_t dd = (uint32_t)m.dim[d];
-    uint32_t q = lin / dd;
-    uint32_t r = lin - q * dd;
+    const uint32_t dd = (uint32_t)m.dim[d];
+    const uint32_t q = m.mul[d] ? (nd_umulhi(lin, m.mul[d]) + lin) >> m.shr[d] : lin / dd;
+    const uint32_t r = lin - q * dd;
     a += (int64_t)r * m.st0[d];
     b += (int64_t)r * m.st1[d];
     lin = q;
@@ -131,6 +160,7 @@ inline void mixed_simplify(Mixed& m) {
     o.st1[o.n] = m.st1[d];
     o.n++;
   }
+  mixed_finalize(o);
   m = o;
 }
 

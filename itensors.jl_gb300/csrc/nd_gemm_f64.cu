@@ -71,12 +71,12 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
       const int m0 = wi.mt * BM, n0 = wi.nt * BN;
       if (tid < BM) {
         int64_t o0 = 0, o1 = 0;
-        if (m0 + tid < M) mixed_offsets(pd.rows, m0 + tid, o0, o1);
+        if (m0 + tid < M) mixed_offsets32(pd.rows, (uint32_t)(m0 + tid), o0, o1);
         rowA[tid] = o0; rowR[tid] = o1;
       } else {
         int c = tid - BM;
         int64_t o0 = 0, o1 = 0;
-        if (n0 + c < N) mixed_offsets(pd.cols, n0 + c, o0, o1);
+        if (n0 + c < N) mixed_offsets32(pd.cols, (uint32_t)(n0 + c), o0, o1);
         colB[c] = o0; colR[c] = o1;
       }
       const double* A = g.ptrs.A[pd.job] + pd.a_off;
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
         __syncthreads();
         if (tid < BK) {
           int64_t o0 = 0, o1 = 0;
-          if (k0 + tid < khi) mixed_offsets(pd.ks, k0 + tid, o0, o1);
+          if (k0 + tid < khi) mixed_offsets32(pd.ks, (uint32_t)(k0 + tid), o0, o1);
           kA[tid] = o0; kB[tid] = o1;
         }
         __syncthreads();
@@ -172,12 +172,12 @@ __global__ void __launch_bounds__(256) splitk_reduce(const PairDesc* pairs, cons
   const int m0 = ri.mt * BM, n0 = ri.nt * BN;
   if (threadIdx.x < BM) {
     int64_t a = 0, r = 0;
-    if (m0 + threadIdx.x < pd.M) mixed_offsets(pd.rows, m0 + threadIdx.x, a, r);
+    if (m0 + threadIdx.x < pd.M) mixed_offsets32(pd.rows, (uint32_t)(m0 + threadIdx.x), a, r);
     rowR[threadIdx.x] = r;
   } else if (threadIdx.x < BM + BN) {
     int64_t b = 0, r = 0;
     const int j = threadIdx.x - BM;
-    if (n0 + j < pd.N) mixed_offsets(pd.cols, n0 + j, b, r);
+    if (n0 + j < pd.N) mixed_offsets32(pd.cols, (uint32_t)(n0 + j), b, r);
     colR[j] = r;
   }
   __syncthreads();

@@ -600,6 +600,7 @@ static Mixed mixed1(int64_t dim, int64_t st0, int64_t st1) {
   m.dim[0] = (int32_t)dim;
   m.st0[0] = st0;
   m.st1[0] = st1;
+  mixed_finalize(m);
   return m;
 }
 

@@ -576,12 +576,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
       const int gm = wi.mt * BM + row;
       const bool row_ok = gm < p0.M;
       int64_t roff = 0, dummy;
-      if (row_ok) mixed_offsets(p0.rows, gm, dummy, roff);
+      if (row_ok) mixed_offsets32(p0.rows, (uint32_t)gm, dummy, roff);
       epi_sync();                                   // previous item done with colR_s
       if (etid < BN) {
         int64_t co = 0, d2;
         const int gn = wi.nt * BN + etid;
-        if (gn < p0.N) mixed_offsets(p0.cols, gn, d2, co);
+        if (gn < p0.N) mixed_offsets32(p0.cols, (uint32_t)gn, d2, co);
         colR_s[etid] = co;
       }
       epi_sync();

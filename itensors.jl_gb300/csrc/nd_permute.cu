@@ -41,7 +41,27 @@ struct PermParams {
   int32_t mode;                // 0 copy, 1 scale, 2 beta==1 accumulate, 3 general, 4 zero, 5 beta-only
   int32_t vec;                 // 128-bit stores allowed
   const double* scalar;        // optional device scalar multiplying alpha
+  // tile / batch index decomposition by multiply-high (all indices < 2^31 when fast != 0)
+  int32_t fast;
+  uint32_t mul_j, shr_j, mul_i, shr_i;
+  uint32_t bmul[ND_MAX_RANK], bshr[ND_MAX_RANK];
 };
+
+// q = x / d for 0 <= x < 2^31 with the divisor's precomputed (mul, shr), else plain division
+__device__ __forceinline__ int64_t pdiv(const PermParams& p, int64_t x, int64_t d, uint32_t mul, uint32_t shr) {
+  if (p.fast) {
+    const uint32_t u = (uint32_t)x;
+    return (int64_t)((__umulhi(u, mul) + u) >> shr);
+  }
+  return x / d;
+}
+
+// divisor magic for the multiply-high division (Granlund & Montgomery, round-up multiplier)
+void fast_divisor(int64_t d, uint32_t& mul, uint32_t& shr) {
+  shr = 0;
+  while ((1ll << shr) < d) ++shr;
+  mul = (uint32_t)((((1ull << 32) * ((1ull << shr) - (uint64_t)d)) / (uint64_t)d) + 1ull);
+}
 
 __device__ __forceinline__ double combine(const PermParams& p, double a, double t, const double* rp) {
   switch (p.mode) {
@@ -61,7 +81,7 @@ __device__ __forceinline__ double eff_alpha(const PermParams& p) {
 __device__ __forceinline__ void batch_offsets(const PermParams& p, int64_t b, int64_t& to, int64_t& ro, int32_t* coord) {
   to = 0; ro = 0;
   for (int d = 0; d < p.nb; ++d) {
-    int64_t q = b / p.bdim[d];
+    int64_t q = pdiv(p, b, p.bdim[d], p.bmul[d], p.bshr[d]);
     int64_t r = b - q * p.bdim[d];
     to += r * p.bts[d];
     ro += r * p.brs[d];
@@ -107,10 +127,10 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
   __syncthreads();
   const int64_t first = blockIdx.x, stride = gridDim.x;
   auto issue = [&](int64_t t, int s) {
-    int64_t tj = t % p.ntile_j;
-    int64_t rest = t / p.ntile_j;
-    int64_t ti = rest % p.ntile_i;
-    int64_t b = rest / p.ntile_i;
+    int64_t rest = pdiv(p, t, p.ntile_j, p.mul_j, p.shr_j);
+    int64_t tj = t - rest * p.ntile_j;
+    int64_t b = pdiv(p, rest, p.ntile_i, p.mul_i, p.shr_i);
+    int64_t ti = rest - b * p.ntile_i;
     int32_t c[5] = {0, 0, 0, 0, 0};
     int64_t to, ro;
     int32_t bc[ND_MAX_RANK];
@@ -144,10 +164,10 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
     phase[s] ^= 1;
     ok = s_ok != 0;
     if (!ok) break;
-    int64_t tj = t % p.ntile_j;
-    int64_t rest = t / p.ntile_j;
-    int64_t ti = rest % p.ntile_i;
-    int64_t b = rest / p.ntile_i;
+    int64_t rest = pdiv(p, t, p.ntile_j, p.mul_j, p.shr_j);
+    int64_t tj = t - rest * p.ntile_j;
+    int64_t b = pdiv(p, rest, p.ntile_i, p.mul_i, p.shr_i);
+    int64_t ti = rest - b * p.ntile_i;
     int64_t to, ro;
     batch_offsets(p, b, to, ro, nullptr);
     const int64_t i0 = ti * TI, j0 = tj * TJ;
@@ -200,10 +220,10 @@ __global__ void __launch_bounds__(256) permute_tiles(const double* __restrict__ 
   const double a = eff_alpha(p);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-    int64_t tj = t % p.ntile_j;
-    int64_t rest = t / p.ntile_j;
-    int64_t ti = rest % p.ntile_i;
-    int64_t b = rest / p.ntile_i;
+    int64_t rest = pdiv(p, t, p.ntile_j, p.mul_j, p.shr_j);
+    int64_t tj = t - rest * p.ntile_j;
+    int64_t b = pdiv(p, rest, p.ntile_i, p.mul_i, p.shr_i);
+    int64_t ti = rest - b * p.ntile_i;
     int64_t to, ro;
     batch_offsets(p, b, to, ro, nullptr);
     const int64_t i0 = ti * TI, j0 = tj * TJ;
@@ -339,6 +359,8 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
     p.nb = 0;
     for (int g = 1; g < ng; ++g) { p.bdim[p.nb] = gd[g]; p.bts[p.nb] = ts[g]; p.brs[p.nb] = rs[g]; p.nb++; }
     p.ntiles = total / p.d0;   // rows
+    p.fast = p.ntiles < (int64_t)0x7fffffff;
+    for (int b = 0; b < p.nb; ++b) fast_divisor(p.bdim[b], p.bmul[b], p.bshr[b]);
     bool al = ((uintptr_t)T % 16 == 0) && ((uintptr_t)R % 16 == 0) && (p.d0 % 2 == 0);
     p.vec = al ? 1 : 0;
     int64_t blocks = std::min<int64_t>((p.ntiles + 7) / 8, (int64_t)h->num_sms * 8);
@@ -364,6 +386,10 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
   p.ntile_j = (p.dq + TJ - 1) / TJ;
   int64_t nbatch = total / (p.d0 * p.dq);
   p.ntiles = p.ntile_i * p.ntile_j * nbatch;
+  p.fast = p.ntiles < (int64_t)0x7fffffff;
+  fast_divisor(p.ntile_j, p.mul_j, p.shr_j);
+  fast_divisor(p.ntile_i, p.mul_i, p.shr_i);
+  for (int b = 0; b < p.nb; ++b) fast_divisor(p.bdim[b], p.bmul[b], p.bshr[b]);
   bool rvec = ((uintptr_t)R % 16 == 0) && (p.rs_i % 2 == 0);
   for (int b = 0; b < p.nb; ++b) if (p.brs[b] % 2) rvec = false;
   p.vec = rvec ? 1 : 0;
