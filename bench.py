@@ -216,7 +216,7 @@ def run_ours(args):
     h = nd.handle(local)
     if args.slices:
         h.call("nd_set_ozaki_slices", int(args.slices))
-    h.tune(True)          # execution parameters timed on first use, cached per block-size histogram
+    h.tune(not args.no_tune)   # execution parameters timed on first use, cached per block-size histogram
 
     # plans (built once, as in a sweep) and flops
     plans = []
@@ -739,6 +739,7 @@ def main():
     ap.add_argument("--precision", default="ozaki", choices=["ozaki", "bf16x3", "fp64"])
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="default execution parameters (no autotuning runs)")
     ap.add_argument("--config", default="heff", choices=["heff", "all"] + list(CONFIGS),
                     help="heff (default): the headline line; others: one line per workload")
     args = ap.parse_args()

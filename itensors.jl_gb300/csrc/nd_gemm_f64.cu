@@ -140,23 +140,37 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
             wsl[(wn + j * 8 + 2 * (lane & 3) + h) * BM + wm + i * 8 + (lane >> 2)] = acc[i][j][h];
       continue;
     }
-    // epilogue: R = alpha * acc + beta * R  (beta == 0 overwrites)
+    // epilogue: R = alpha * acc + beta * R  (beta == 0 overwrites); the uniform choice is
+    // made outside the element loops so the plain store path has no FP64 arithmetic
     const int m0 = wi.mt * BM, n0 = wi.nt * BN;
+    if (g.bmode == 0 && g.amode == 0) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int m = wm + i * 8 + (lane >> 2);
-      if (m0 + m >= M) continue;
+      for (int i = 0; i < 4; ++i) {
+        const int m = wm + i * 8 + (lane >> 2);
+        if (m0 + m >= M) continue;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < 4; ++j)
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int n = wn + j * 8 + 2 * (lane & 3) + h;
-          if (n0 + n >= N) continue;
-          double* dst = Rp + r_base + rowR[m] + colR[n];
-          double v = acc[i][j][h];
-          if (g.bmode == 0) *dst = g.amode ? g.alpha * v : v;
-          else *dst = g.alpha * v + g.beta * *dst;
-        }
+          for (int h = 0; h < 2; ++h) {
+            const int n = wn + j * 8 + 2 * (lane & 3) + h;
+            if (n0 + n < N) Rp[r_base + rowR[m] + colR[n]] = acc[i][j][h];
+          }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int m = wm + i * 8 + (lane >> 2);
+        if (m0 + m >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int n = wn + j * 8 + 2 * (lane & 3) + h;
+            if (n0 + n >= N) continue;
+            double* dst = Rp + r_base + rowR[m] + colR[n];
+            const double v = acc[i][j][h];
+            *dst = g.bmode == 0 ? g.alpha * v : g.alpha * v + g.beta * *dst;
+          }
       }
     }
   }
@@ -232,7 +246,9 @@ constexpr int SK_THREADS = 256, SK_RPT = 2, SK_ROWS = SK_THREADS * SK_RPT, SK_MA
 
 // One row chunk of one group with exactly NN output columns (no predicated FMAs:
 // the FP64 pipe is the bound for these pairs on GB300).
-template <int NN>
+// MODE (uniform, resolved at compile time so the store path carries no FP64 work):
+// 0: R = acc, 1: R = alpha acc, 2: R = alpha acc + beta R.
+template <int NN, int MODE>
 __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& wi, PairDesc& pd,
                                             double (*Bs)[SK_MAXN], int64_t* kA, int64_t* colR) {
   const int tid = threadIdx.x;
@@ -298,7 +314,8 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
     for (int j = 0; j < NN; ++j) {
       double* dst = Rp + rrow[r] + colR[j];
       const double v = acc[r][j];
-      if (g.bmode == 0) *dst = g.amode ? g.alpha * v : v;
+      if (MODE == 0) *dst = v;
+      else if (MODE == 1) *dst = g.alpha * v;
       else *dst = g.alpha * v + g.beta * *dst;
     }
   }
@@ -312,16 +329,28 @@ __global__ void __launch_bounds__(SK_THREADS, 4) gemm_skinny_f64(GemmArgs g) {
   for (int it = blockIdx.x; it < g.nitems; it += gridDim.x) {
     const WorkItem wi = g.items[it];
     const int N = __ldg(&g.pairs[wi.pair_begin].N);
+    const int mode = g.bmode ? 2 : (g.amode ? 1 : 0);
+#define ND_SKINNY_CASE(NN)                                              \
+  case NN:                                                              \
+    if (mode == 0) skinny_item<NN, 0>(g, wi, pd, Bs, kA, colR);         \
+    else if (mode == 1) skinny_item<NN, 1>(g, wi, pd, Bs, kA, colR);    \
+    else skinny_item<NN, 2>(g, wi, pd, Bs, kA, colR);                   \
+    break;
     switch (N) {
-      case 1: skinny_item<1>(g, wi, pd, Bs, kA, colR); break;
-      case 2: skinny_item<2>(g, wi, pd, Bs, kA, colR); break;
-      case 3: skinny_item<3>(g, wi, pd, Bs, kA, colR); break;
-      case 4: skinny_item<4>(g, wi, pd, Bs, kA, colR); break;
-      case 5: skinny_item<5>(g, wi, pd, Bs, kA, colR); break;
-      case 6: skinny_item<6>(g, wi, pd, Bs, kA, colR); break;
-      case 7: skinny_item<7>(g, wi, pd, Bs, kA, colR); break;
-      default: skinny_item<8>(g, wi, pd, Bs, kA, colR); break;
+      ND_SKINNY_CASE(1)
+      ND_SKINNY_CASE(2)
+      ND_SKINNY_CASE(3)
+      ND_SKINNY_CASE(4)
+      ND_SKINNY_CASE(5)
+      ND_SKINNY_CASE(6)
+      ND_SKINNY_CASE(7)
+      default:
+        if (mode == 0) skinny_item<8, 0>(g, wi, pd, Bs, kA, colR);
+        else if (mode == 1) skinny_item<8, 1>(g, wi, pd, Bs, kA, colR);
+        else skinny_item<8, 2>(g, wi, pd, Bs, kA, colR);
+        break;
     }
+#undef ND_SKINNY_CASE
   }
 }
 }  // namespace

@@ -642,16 +642,22 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
           const int Ei = S > 2 ? g.exps[oa.exp_off + gm] : 0;
           const int32_t* Fj = g.exps + ob.exp_off + wi.nt * BN + cg * EPI_COLS;
           const bool first = pd.first != 0;
+          // the uniform store choice is made outside the column loop: the common overwrite
+          // (first pair, alpha = 1, beta = 0) carries no FP64 arithmetic
+          if (first && g.bmode == 0 && g.amode == 0) {
 #pragma unroll
-          for (int c = 0; c < EPI_COLS; ++c) {
-            if (c < ncols) {
-              double v = (S > 2) ? i64_scaled_to_f64(acc[c], Ei + __ldg(Fj + c) - 38) : (double)facc[c];
-              double* dst = Rb + colR_s[cg * EPI_COLS + c];
-              if (first) {
-                if (g.bmode == 0) *dst = g.amode ? g.alpha * v : v;
-                else *dst = g.alpha * v + g.beta * *dst;
-              } else {
-                *dst = g.amode ? *dst + g.alpha * v : *dst + v;
+            for (int c = 0; c < EPI_COLS; ++c)
+              if (c < ncols)
+                Rb[colR_s[cg * EPI_COLS + c]] =
+                    (S > 2) ? i64_scaled_to_f64(acc[c], Ei + __ldg(Fj + c) - 38) : (double)facc[c];
+          } else {
+#pragma unroll
+            for (int c = 0; c < EPI_COLS; ++c) {
+              if (c < ncols) {
+                double v = (S > 2) ? i64_scaled_to_f64(acc[c], Ei + __ldg(Fj + c) - 38) : (double)facc[c];
+                double* dst = Rb + colR_s[cg * EPI_COLS + c];
+                if (first) *dst = g.bmode == 0 ? g.alpha * v : g.alpha * v + g.beta * *dst;
+                else *dst = g.amode ? *dst + g.alpha * v : *dst + v;
               }
             }
           }

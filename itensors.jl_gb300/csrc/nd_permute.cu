@@ -63,7 +63,12 @@ void fast_divisor(int64_t d, uint32_t& mul, uint32_t& shr) {
   mul = (uint32_t)((((1ull << 32) * ((1ull << shr) - (uint64_t)d)) / (uint64_t)d) + 1ull);
 }
 
+// COPY: mode 0 resolved at compile time, so the plain copy carries no FP64 arithmetic
+// (the compiler would otherwise turn the runtime switch into selects and evaluate a * t
+// for every element on GB300's narrow FP64 pipe).
+template <bool COPY>
 __device__ __forceinline__ double combine(const PermParams& p, double a, double t, const double* rp) {
+  if (COPY) return t;
   switch (p.mode) {
     case 0: return t;
     case 1: return a * t;
@@ -110,6 +115,7 @@ constexpr int BOX_I = 16;                       // 16 doubles = 128 bytes (swizz
 constexpr int TILE_BYTES = TI * TJ * 8;         // 16 KB
 constexpr int BOX_BYTES = BOX_I * TJ * 8;       // 8 KB
 
+template <bool COPY>
 __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUtensorMap tmap, double* R,
                                                    const double* Rin, PermParams p, DeviceStatus* st) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -154,14 +160,14 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
       if (t < p.ntiles) issue(t, s);
     }
   }
-  uint32_t phase[STAGES] = {0, 0, 0, 0};
+  uint32_t phase = 0;                            // bit s: parity of stage s
   int s = 0;
   bool ok = true;
   for (int64_t t = first; t < p.ntiles; t += stride) {
     // one thread polls the barrier and broadcasts, so every thread leaves together
-    if (tid == 0) s_ok = mbar_wait(smem_u32(&full[s]), phase[s], st, 100) ? 1 : 0;
+    if (tid == 0) s_ok = mbar_wait(smem_u32(&full[s]), (phase >> s) & 1u, st, 100) ? 1 : 0;
     __syncthreads();
-    phase[s] ^= 1;
+    phase ^= 1u << s;
     ok = s_ok != 0;
     if (!ok) break;
     int64_t rest = pdiv(p, t, p.ntile_j, p.mul_j, p.shr_j);
@@ -187,16 +193,16 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
         double2 o;
         if (p.mode >= 2) {
           double2 old = *(const double2*)(Rin + roff);
-          o.x = combine(p, a, v0, &old.x);
-          o.y = combine(p, a, v1, &old.y);
+          o.x = combine<COPY>(p, a, v0, &old.x);
+          o.y = combine<COPY>(p, a, v1, &old.y);
         } else {
-          o.x = combine(p, a, v0, nullptr);
-          o.y = combine(p, a, v1, nullptr);
+          o.x = combine<COPY>(p, a, v0, nullptr);
+          o.y = combine<COPY>(p, a, v1, nullptr);
         }
         *(double2*)(R + roff) = o;
       } else {
-        if (jg < p.dq) R[roff] = combine(p, a, v0, Rin + roff);
-        if (jg + 1 < p.dq) R[roff + 1] = combine(p, a, v1, Rin + roff + 1);
+        if (jg < p.dq) R[roff] = combine<COPY>(p, a, v0, Rin + roff);
+        if (jg + 1 < p.dq) R[roff + 1] = combine<COPY>(p, a, v1, Rin + roff + 1);
       }
     }
     __syncthreads();   // every thread is done with stage s
@@ -209,11 +215,12 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
   // After a timeout, give copies still in flight a bounded chance to land
   // before the CTA exits (on the normal path every issued tile was consumed).
   if (!ok && tid == 0) {
-    for (int q = 0; q < STAGES; ++q) mbar_wait(smem_u32(&full[q]), phase[q], st, 101);
+    for (int q = 0; q < STAGES; ++q) mbar_wait(smem_u32(&full[q]), (phase >> q) & 1u, st, 101);
   }
 }
 
 // Same tiling, plain loads: T[i, j, batch] -> smem (padded) -> R.
+template <bool COPY>
 __global__ void __launch_bounds__(256) permute_tiles(const double* __restrict__ T, double* R,
                                                      const double* Rin, PermParams p) {
   __shared__ double tile[TJ][TI + 1];
@@ -240,7 +247,7 @@ __global__ void __launch_bounds__(256) permute_tiles(const double* __restrict__ 
         int64_t j = j0 + jj;
         if (j < p.dq) {
           int64_t roff = ro + i * p.rs_i + j;
-          R[roff] = combine(p, a, tile[jj][ii], Rin + roff);
+          R[roff] = combine<COPY>(p, a, tile[jj][ii], Rin + roff);
         }
       }
     }
@@ -249,6 +256,7 @@ __global__ void __launch_bounds__(256) permute_tiles(const double* __restrict__ 
 }
 
 // Shared contiguous dimension: copy rows of length d0 (i) for every batch index.
+template <bool COPY>
 __global__ void __launch_bounds__(256) permute_rows(const double* __restrict__ T, double* R,
                                                     const double* Rin, PermParams p) {
   const double a = eff_alpha(p);
@@ -265,22 +273,22 @@ __global__ void __launch_bounds__(256) permute_rows(const double* __restrict__ T
         double2 o;
         if (p.mode >= 2) {
           double2 old = *((const double2*)(Rin + ro) + c);
-          o.x = combine(p, a, v.x, &old.x);
-          o.y = combine(p, a, v.y, &old.y);
+          o.x = combine<COPY>(p, a, v.x, &old.x);
+          o.y = combine<COPY>(p, a, v.y, &old.y);
         } else {
-          o.x = combine(p, a, v.x, nullptr);
-          o.y = combine(p, a, v.y, nullptr);
+          o.x = combine<COPY>(p, a, v.x, nullptr);
+          o.y = combine<COPY>(p, a, v.y, nullptr);
         }
         *((double2*)(R + ro) + c) = o;
       }
     } else {
-      for (int64_t c = lane; c < p.d0; c += 32) R[ro + c] = combine(p, a, __ldg(T + to + c), Rin + ro + c);
+      for (int64_t c = lane; c < p.d0; c += 32) R[ro + c] = combine<COPY>(p, a, __ldg(T + to + c), Rin + ro + c);
     }
   }
 }
 
 __global__ void permute_scalar(const double* T, double* R, PermParams p) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) R[0] = combine(p, eff_alpha(p), T[0], R);
+  if (threadIdx.x == 0 && blockIdx.x == 0) R[0] = combine<false>(p, eff_alpha(p), T[0], R);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -365,7 +373,8 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
     p.vec = al ? 1 : 0;
     int64_t blocks = std::min<int64_t>((p.ntiles + 7) / 8, (int64_t)h->num_sms * 8);
     nd_prof_begin(h, "permute_rows");
-    permute_rows<<<(unsigned)std::max<int64_t>(blocks, 1), threads, 0, h->stream>>>(T, R, Rin, p);
+    if (p.mode == 0) permute_rows<true><<<(unsigned)std::max<int64_t>(blocks, 1), threads, 0, h->stream>>>(T, R, Rin, p);
+    else permute_rows<false><<<(unsigned)std::max<int64_t>(blocks, 1), threads, 0, h->stream>>>(T, R, Rin, p);
     nd_prof_end(h);
     ND_LAUNCHED(h);
     return nd_cuda_check(h, cudaGetLastError(), "permute_rows");
@@ -417,12 +426,14 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
       size_t smem = STAGES * TILE_BYTES + 1024;
       static bool attr_set = false;
       if (!attr_set) {
-        cudaFuncSetAttribute(permute_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(permute_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(permute_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr_set = true;
       }
       int64_t blocks = std::min<int64_t>(p.ntiles, (int64_t)h->num_sms * 3);
       nd_prof_begin(h, "permute_tma");
-      permute_tma<<<(unsigned)blocks, threads, smem, h->stream>>>(tmap, R, Rin, p, h->d_status);
+      if (p.mode == 0) permute_tma<true><<<(unsigned)blocks, threads, smem, h->stream>>>(tmap, R, Rin, p, h->d_status);
+      else permute_tma<false><<<(unsigned)blocks, threads, smem, h->stream>>>(tmap, R, Rin, p, h->d_status);
       nd_prof_end(h);
       ND_LAUNCHED(h);
       return nd_cuda_check(h, cudaGetLastError(), "permute_tma");
@@ -430,7 +441,8 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
   }
   int64_t blocks = std::min<int64_t>(p.ntiles, (int64_t)h->num_sms * 8);
   nd_prof_begin(h, "permute_tiles");
-  permute_tiles<<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
+  if (p.mode == 0) permute_tiles<true><<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
+  else permute_tiles<false><<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "permute_tiles");
