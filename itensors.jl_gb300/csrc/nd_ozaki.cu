@@ -93,28 +93,6 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(b)) : "memory");
 }
 
-// Balanced base-256 digits of the fixed-point integer X (|X| <= 2^(8S-1)).
-// digit[0] is the most significant.
-__device__ __forceinline__ void balanced_digits(int64_t X, int S, int* d) {
-  for (int p = S - 1; p >= 1; --p) {
-    int lo = (int)(((X + 128) & 255)) - 128;
-    d[p] = lo;
-    X = (X - lo) >> 8;
-  }
-  d[0] = (int)X;
-}
-
-// Round |x| * 2^(8S-1-E) to an integer using only integer instructions.
-__device__ __forceinline__ int64_t fixed_point(uint64_t bits, int E, int S) {
-  int ex = (int)((bits >> 52) & 0x7ff);
-  uint64_t m = bits & 0xfffffffffffffull;
-  if (ex) m |= (1ull << 52); else ex = 1;
-  int sh = 1075 - ex - (8 * S - 1) + E;   // >= 5 because |x| < 2^E and 8S-1 <= 47
-  uint64_t mag = 0;
-  if (sh < 64 && m) mag = (sh > 0) ? ((m + (1ull << (sh - 1))) >> sh) : (m << (-sh));
-  return (bits >> 63) ? -(int64_t)mag : (int64_t)mag;
-}
-
 // FP64 -> FP32 with round-to-nearest-even using integer instructions only.
 // Values beyond the FP32 range saturate to +-Inf / flush to zero.
 __device__ __forceinline__ float f64_to_f32_int(uint64_t bits) {
@@ -162,16 +140,6 @@ __device__ __forceinline__ double i64_scaled_to_f64(long long v, int e) {
   return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (mant & 0xfffffffffffffull)));
 }
 
-__device__ __forceinline__ uint16_t bf16_bits_of_int(int d) {
-  // |d| <= 256: exact in bf16
-  return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
-}
-
-// byte offset of element (r, k) inside one [rows][32] BF16 slice, 64-byte swizzle
-__device__ __forceinline__ int swz64(int r, int k) {
-  return r * 64 + ((((k >> 3) ^ (r >> 1)) & 3) << 4) + (k & 7) * 2;
-}
-
 // ---- pack kernels ----------------------------------------------------------
 // Two launches over fine-grained items (operand, row tile, chunk of PACK_KC
 // k-steps), so every SM has work: pack_rowmax folds |x| maxima of its chunk
@@ -200,51 +168,49 @@ struct PackArgs2 {
   DeviceStatus* st;
 };
 
-// Digits of one element.  |x| * 2^(8S-1-E) is rounded to an integer with at
-// most 8S-1 <= 47 bits, split into two 32-bit halves, and read byte by byte
-// from the least significant end; a carry pass turns bytes in [0, 255] into
-// balanced digits in [-128, 128] (digit >= 128 becomes digit - 256, carry 1).
-// The sign of x is applied to every digit.  All arithmetic is 32-bit.
-__device__ __forceinline__ void pack_unit_digits(uint64_t bits, int E, int S, uint16_t* hh) {
-  if (S > 2) {
+// Digits of one element as floats d_q * 2^(-8q), q = 0 most significant.
+// S > 2: X = round(x * 2^(8S-1-E)) (signed, |X| <= 2^(8S-1)) in balanced base 256.
+// Adding C = 0x80 in each of the S-1 low byte positions makes every low byte y_i of
+// X + C equal to d_i + 128 (the adder does the carries); the top digit is the
+// arithmetic shift of X + C, so all digits lie in [-128, 128].  Integer -> float is
+// the exact magic-constant addition: the bits of 1.5 * 2^(23-8q) plus d, read as a
+// float, minus 1.5 * 2^(23-8q), equal d * 2^(-8q) for |d| < 2^22.
+// S == 2 (3xBF16): the FP32 rounding of x split into a BF16 head and its remainder.
+template <int S>
+__device__ __forceinline__ void unit_digits_f(uint64_t bits, int E, float* f) {
+  if constexpr (S > 2) {
     const uint32_t hi_w = (uint32_t)(bits >> 32);
     const int ex = (int)((hi_w >> 20) & 0x7ff);
-    uint32_t mag_lo = 0, mag_hi = 0;
+    uint64_t mag = 0;
     if (ex != 0x7ff && (bits << 1) != 0) {
       const uint64_t m = (bits & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
       const int sh = 1075 - (ex ? ex : 1) - (8 * S - 1) + E;   // >= 5
-      if (sh < 64) {
-        const uint64_t mag = (m + (1ull << (sh - 1))) >> sh;
-        mag_lo = (uint32_t)mag;
-        mag_hi = (uint32_t)(mag >> 32);
-      }
+      if (sh < 64) mag = (m + (1ull << (sh - 1))) >> sh;
     }
-    const bool neg = (hi_w >> 31) != 0;
-    int carry = 0;
-    int d[6];
+    const long long X = (hi_w >> 31) ? -(long long)mag : (long long)mag;
+    constexpr unsigned long long C = 0x8080808080808080ull & ((1ull << (8 * (S - 1))) - 1ull);
+    const long long Y = X + (long long)C;
+    const uint32_t ylo = (uint32_t)Y, yhi = (uint32_t)((unsigned long long)Y >> 32);
 #pragma unroll
-    for (int p = 5; p >= 0; --p) {
-      const int byte_idx = 5 - p;                           // 0 = least significant
-      if (p >= S) continue;
-      const int lsb = (S - 1 - p);                          // byte position of digit p
-      const uint32_t byte = lsb < 4 ? ((mag_lo >> (8 * lsb)) & 0xffu) : ((mag_hi >> (8 * (lsb - 4))) & 0xffu);
-      (void)byte_idx;
-      int v = (int)byte + carry;
-      carry = (p > 0 && v >= 128) ? 1 : 0;
-      d[p] = v - 256 * carry;
+    for (int q = 0; q < S; ++q) {
+      const int i = S - 1 - q;                                 // byte position of slice q
+      int d;
+      if (i == S - 1) d = (int)(Y >> (8 * i));
+      else d = (int)(i < 4 ? __byte_perm(ylo, 0, 0x4440 + i) : __byte_perm(yhi, 0, 0x4440 + (i - 4))) - 128;
+      const int mq = 0x4B400000 - ((8 * q) << 23);             // bits of 1.5 * 2^(23-8q)
+      f[q] = __int_as_float(mq + d) - __int_as_float(mq);
     }
-#pragma unroll
-    for (int q = 0; q < 6; ++q)
-      if (q < S) {
-        const int dq = neg ? -d[q] : d[q];
-        hh[q] = __bfloat16_as_ushort(__float2bfloat16_rn((float)dq * __int_as_float((127 - 8 * q) << 23)));
-      }
   } else {
-    float xf = f64_to_f32_int(bits);
-    __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-    hh[0] = __bfloat16_as_ushort(hi);
-    hh[1] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(hi)));
+    const float xf = f64_to_f32_int(bits);
+    const float hd = __bfloat162float(__float2bfloat16_rn(xf));
+    f[0] = hd;
+    f[1] = xf - hd;
   }
+}
+
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
 }
 
 // shared set-up of one pack item: row offsets and k offsets of the chunk
@@ -287,34 +253,35 @@ __global__ void __launch_bounds__(256) pack_rowmax(PackArgs2 a) {
       if (j >= units) continue;
       const int r = (lane >> 2) + 8 * warp + 64 * j;
       const bool rv = pi.rt * ROWS + r < op.rows;
-      unsigned long long mx = 0ull;
+      // only the exponent of the row maximum is used: max of the high words' exponent field
+      uint32_t mx = 0u;
       if (rv) {
-        const double* rowp = src + rowoff[r];
+        const unsigned int* rowp = (const unsigned int*)(src + rowoff[r]) + 1;   // high 32 bits of each double
         for (int ks = 0; ks < ks1 - ks0; ++ks) {
 #pragma unroll
           for (int e = 0; e < 8; ++e) {
             const int64_t ko = koff[ks * BK + c * 8 + e];
             if (ko >= 0) {
-              uint64_t b = (uint64_t)__double_as_longlong(__ldg(rowp + ko)) & 0x7fffffffffffffffull;
-              if (b >= 0x7ff0000000000000ull) { bad = true; b = 0; }
-              mx = b > mx ? b : mx;
+              const uint32_t hw = __ldg(rowp + 2 * ko) & 0x7ff00000u;
+              if (hw == 0x7ff00000u) bad = true;
+              else mx = max(mx, hw);
             }
           }
         }
       }
-      unsigned long long w = __shfl_xor_sync(0xffffffffu, mx, 1); mx = w > mx ? w : mx;
-      w = __shfl_xor_sync(0xffffffffu, mx, 2); mx = w > mx ? w : mx;
-      if (c == 0 && rv && mx) atomicMax(&a.rowmax[op.exp_off + pi.rt * ROWS + r], mx);
+      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+      if (c == 0 && rv && mx) atomicMax(&a.rowmax[op.exp_off + pi.rt * ROWS + r], (unsigned long long)mx << 32);
     }
     if (bad && atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
   }
 }
 
+template <int S>
 __global__ void __launch_bounds__(256) pack_digits(PackArgs2 a) {
   __shared__ int64_t rowoff[BM];
   __shared__ int64_t koff[PACK_KC * BK];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, c = lane & 3;
-  const int S = a.slices;
   for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
     const PackItem2 pi = a.items[it];
     const SplitOp& op = a.ops[pi.op];
@@ -339,22 +306,21 @@ __global__ void __launch_bounds__(256) pack_digits(PackArgs2 a) {
       const double* rowp = src + rowoff[r];
       for (int ks = ks0; ks < ks1; ++ks) {
         unsigned char* tile = a.pack + op.pack_off + ((int64_t)(pi.rt * op.k_steps + ks) * S) * (ROWS * 64);
-        uint32_t w[6][4];
+        uint32_t w[S][4];
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
-          uint16_t h0[6], h1[6];
+          float f0[S], f1[S];
           const int64_t k0 = koff[(ks - ks0) * BK + c * 8 + e], k1 = koff[(ks - ks0) * BK + c * 8 + e + 1];
           const uint64_t b0 = (rv && k0 >= 0) ? (uint64_t)__double_as_longlong(__ldg(rowp + k0)) : 0ull;
           const uint64_t b1 = (rv && k1 >= 0) ? (uint64_t)__double_as_longlong(__ldg(rowp + k1)) : 0ull;
-          pack_unit_digits(b0, E, S, h0);
-          pack_unit_digits(b1, E, S, h1);
+          unit_digits_f<S>(b0, E, f0);
+          unit_digits_f<S>(b1, E, f1);
 #pragma unroll
-          for (int q = 0; q < 6; ++q) w[q][e / 2] = (uint32_t)h0[q] | ((uint32_t)h1[q] << 16);
+          for (int q = 0; q < S; ++q) w[q][e / 2] = bf16x2_bits(f0[q], f1[q]);
         }
         const int so = r * 64 + (((c ^ (r >> 1)) & 3) << 4);
 #pragma unroll
-        for (int q = 0; q < 6; ++q)
-          if (q < S) *(uint4*)(tile + q * ROWS * 64 + so) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+        for (int q = 0; q < S; ++q) *(uint4*)(tile + q * ROWS * 64 + so) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
       }
     }
   }
@@ -788,7 +754,13 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
       ND_LAUNCHED(h);
     }
     nd_prof_begin(h, "pack_digits");
-    pack_digits<<<pblocks, 256, 0, h->stream>>>(pa);
+    switch (S) {
+      case 2: pack_digits<2><<<pblocks, 256, 0, h->stream>>>(pa); break;
+      case 3: pack_digits<3><<<pblocks, 256, 0, h->stream>>>(pa); break;
+      case 4: pack_digits<4><<<pblocks, 256, 0, h->stream>>>(pa); break;
+      case 5: pack_digits<5><<<pblocks, 256, 0, h->stream>>>(pa); break;
+      default: pack_digits<6><<<pblocks, 256, 0, h->stream>>>(pa); break;
+    }
     nd_prof_end(h);
     ND_LAUNCHED(h);
     ND_CUDA(h, cudaGetLastError());
