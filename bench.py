@@ -171,6 +171,11 @@ def matvec_flops_oracle(net, steps_labels):
     return tot
 
 
+# DRAM traffic of split_gemm per launch from one ncu capture of this workload at S = 5
+# (dram__bytes_read.sum + dram__bytes_write.sum: L*psi 361.3 MB, *R 647.5 MB; mean of the two)
+NCU_SPLIT_GEMM_TRAFFIC = {4096: 504.4e6}
+
+
 def split_routed_flops(shapes):
     """2MNK of the block pairs that run on split_gemm: every output block except those
     whose pairs all have N <= 8 and K <= 32 (those run on the FP64 skinny kernel)."""
@@ -299,7 +304,10 @@ def run_ours(args):
         tensor_flops_per_launch = npair_levels * split_flops * args.steps / gemm_n
         achieved = tensor_flops_per_launch / (per_launch_ms * 1e-3) / 1e12
         roof = {"bound": "tensor", "achieved": round(achieved, 2), "peak": pk["bf16"], "unit": "TFLOP/s",
-                "frac": round(achieved / pk["bf16"], 4), "traffic": None,
+                "frac": round(achieved / pk["bf16"], 4),
+                "traffic": NCU_SPLIT_GEMM_TRAFFIC.get(args.chi) if S == 5 else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, mean of the L*psi "
+                                  "and *R launches (one capture of this workload)",
                 "kernel": "split_gemm (tcgen05 kind::f16, TMEM accumulators)",
                 "peak_source": f"{pk['src']} bf16 dense burst",
                 "units": f"{npair_levels} BF16 slice-pair products x 2MNK per block pair",

@@ -12,11 +12,14 @@
 // SVD algorithm: one-sided (Hestenes) Jacobi on the columns of every block at
 // once (transposed when a block is wide).  Column pairs follow a round-robin
 // tournament, so the n/2 rotations of a round are independent; all blocks
-// advance round by round inside one persistent cooperative kernel whose CTAs
-// meet at a grid barrier (bounded spin) between rounds.  Each sweep records
-// the largest |a_i . a_j| / (|a_i| |a_j|) per block; the host stops when every
-// block is below tolerance and reports ND_ERR_NOCONV after the sweep limit
-// (the reference returns `nothing` when LAPACK fails).  FP64 throughout.
+// advance round by round inside one persistent cooperative kernel (one warp per
+// pair) whose CTAs meet at a grid barrier (bounded spin) between rounds.  Each
+// sweep records the largest |a_i . a_j| / (|a_i| |a_j|) per block; blocks whose
+// sweep rotated nothing are done, and the host reports ND_ERR_NOCONV after the
+// sweep limit (the reference returns `nothing` when LAPACK fails).  Larger
+// problems first run the sweeps in FP32 and re-orthogonalise that V in FP64
+// (Newton-Schulz), then finish with FP64 sweeps on W V, so the result is an
+// FP64 Jacobi SVD.
 #include "nd_plan.h"
 #include <cooperative_groups.h>
 #include <algorithm>
