@@ -99,6 +99,7 @@ nd_status nd_destroy(nd_handle h) {
   if (!h) return ND_OK;
   cudaSetDevice(h->device);
   cudaStreamSynchronize(h->stream);
+  nd_dense_cache_clear(h);
   if (h->ws) cudaFree(h->ws);
   if (h->d_status) cudaFree(h->d_status);
   for (auto& r : h->prof) { cudaEventDestroy(r.e0); cudaEventDestroy(r.e1); }

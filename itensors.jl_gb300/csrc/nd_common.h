@@ -54,7 +54,13 @@ struct nd_context {
   // autotuner
   bool tuning = false;
   std::map<std::string, TuneEntry> tune;
+  // device state of recent dense contractions, keyed by their GEMM descriptor and
+  // precision (owned by nd_contract.cu; released by nd_dense_cache_clear)
+  std::map<std::string, void*> dense_cache;
+  std::vector<std::string> dense_order;   // insertion order, for eviction
 };
+
+void nd_dense_cache_clear(nd_handle h);
 
 // Host helpers -------------------------------------------------------------
 nd_status nd_fail(nd_handle h, nd_status code, const char* fmt, ...);

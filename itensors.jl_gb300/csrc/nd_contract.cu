@@ -15,6 +15,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <new>
 
 nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups, int precision);
 nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double alpha, double beta);
@@ -321,6 +322,55 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
 // ---------------------------------------------------------------------------
 // Dense contract!
 // ---------------------------------------------------------------------------
+constexpr size_t kDenseCacheEntries = 64;
+
+static void append_mixed(std::string& k, const Mixed& m) {
+  k.append((const char*)&m.n, sizeof m.n);
+  for (int d = 0; d < m.n; ++d) {
+    k.append((const char*)&m.dim[d], sizeof m.dim[d]);
+    k.append((const char*)&m.st0[d], sizeof m.st0[d]);
+    k.append((const char*)&m.st1[d], sizeof m.st1[d]);
+  }
+}
+
+// Cached execution state of a dense contraction (one block pair), oldest evicted first.
+static ExecCache* dense_exec(nd_handle h, const PairDesc& pd, int precision) {
+  std::string key;
+  const int32_t head[4] = {precision, h->ozaki_slices, pd.M, pd.N};
+  key.append((const char*)head, sizeof head);
+  key.append((const char*)&pd.K, sizeof pd.K);
+  append_mixed(key, pd.rows);
+  append_mixed(key, pd.cols);
+  append_mixed(key, pd.ks);
+  auto it = h->dense_cache.find(key);
+  if (it != h->dense_cache.end()) return (ExecCache*)it->second;
+  if (h->capturing) return nullptr;
+  if (h->dense_cache.size() >= kDenseCacheEntries) {
+    const std::string old = h->dense_order.front();
+    h->dense_order.erase(h->dense_order.begin());
+    cudaStreamSynchronize(h->stream);               // the evicted state may still be in use
+    ExecCache* e = (ExecCache*)h->dense_cache[old];
+    e->free_all();
+    delete e;
+    h->dense_cache.erase(old);
+  }
+  ExecCache* c = new (std::nothrow) ExecCache();
+  if (!c) return nullptr;
+  h->dense_cache[key] = c;
+  h->dense_order.push_back(key);
+  return c;
+}
+
+void nd_dense_cache_clear(nd_handle h) {
+  for (auto& e : h->dense_cache) {
+    ExecCache* c = (ExecCache*)e.second;
+    c->free_all();
+    delete c;
+  }
+  h->dense_cache.clear();
+  h->dense_order.clear();
+}
+
 extern "C" nd_status nd_contract_dense_f64(nd_handle h, double* R, int32_t rankR, const int64_t* dimsR,
                                            const int32_t* labelsR, const double* A, int32_t rankA,
                                            const int64_t* dimsA, const int32_t* labelsA, const double* B,
@@ -378,13 +428,18 @@ extern "C" nd_status nd_contract_dense_f64(nd_handle h, double* R, int32_t rankR
     return nd_launch_permute(h, R, R, 1, &n, &p0, 0.0, beta, nullptr);
   }
   std::vector<PairDesc> pairs{pd};
-  ExecCache c;
+  // the device state (descriptors, work list, split-K / split-operand scratch) of a
+  // dense contraction is kept per handle and reused by later calls of the same shape,
+  // so repeated small contractions cost no allocation and can be graph-captured
+  ExecCache* c = dense_exec(h, pd, precision);
+  if (!c && h->capturing)
+    return nd_fail(h, ND_ERR_ARG, "contract: run this shape once before graph capture (its state is built then)");
+  if (!c) return nd_fail(h, ND_ERR_OOM, "contract: host allocation failed");
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
-  nd_status s = nd_execute_cached(h, c, pairs, 1, ptrs, alpha, beta, precision);
-  ND_CUDA(h, cudaStreamSynchronize(h->stream));
-  c.free_all();
+  nd_status s = nd_execute_cached(h, *c, pairs, 1, ptrs, alpha, beta, precision);
   if (s != ND_OK) return s;
-  return nd_check_device_status(h, "contract");
+  if (h->capturing) return ND_OK;
+  return nd_check_device_status(h, "contract");   // synchronises the stream
 }
 
 // ---------------------------------------------------------------------------

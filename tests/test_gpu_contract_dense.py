@@ -131,3 +131,49 @@ def test_bad_labels_rejected(nd):
     with pytest.raises(nd.NDError):
         nd.contract_(nd.DenseTensor.from_numpy(np.ones((2, 4))), (1, 2), a, (1, -1),
                      nd.DenseTensor.from_numpy(np.ones((4, 4))), (-1, 2))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_dense_state_reuse_and_capture(nd, precision):
+    """Repeated dense contractions of one shape reuse the cached device state: results
+    are identical, other shapes interleave freely, and after one eager call the
+    contraction can be captured into a CUDA graph and replayed."""
+    import ctypes as C
+    import torch
+    rng = np.random.default_rng(31)
+    a, b = rng.standard_normal((96, 3, 80)), rng.standard_normal((80, 3, 70))
+    la, lb, lr = (1, 2, -1), (-1, 3, 4), (1, 2, 3, 4)
+    ref = odense.contract(a, la, b, lb, lr)
+    A, B = nd.DenseTensor.from_numpy(a), nd.DenseTensor.from_numpy(b)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        R = nd.DenseTensor.empty(ref.shape)
+        nd.contract_(R, lr, A, la, B, lb, precision=precision)
+        first = R.to_numpy()
+        assert odense.rel_frobenius_error(first, ref) <= TOL[precision]
+        other, oref = _run(nd, a[:50], la, b, lb, lr, precision)           # a second shape in between
+        assert odense.rel_frobenius_error(other, oref) <= TOL[precision]
+        nd.contract_(R, lr, A, la, B, lb, precision=precision)
+        np.testing.assert_array_equal(R.to_numpy(), first)
+        h = nd.handle(0)
+        R.data.zero_()
+        torch.cuda.synchronize()
+        h.call("nd_graph_begin")
+        nd.contract_(R, lr, A, la, B, lb, precision=precision)
+        ge = C.c_void_p()
+        h.call("nd_graph_end", C.byref(ge))
+        for _ in range(2):
+            R.data.zero_()
+            h.call("nd_graph_launch", ge)
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(R.to_numpy(), first)
+        h.lib.nd_graph_destroy(ge)
+        # a shape never run eagerly cannot be built inside a capture
+        R2 = nd.DenseTensor.empty((96, 3, 3, 71))
+        B2 = nd.DenseTensor.from_numpy(rng.standard_normal((80, 3, 71)))
+        h.call("nd_graph_begin")
+        with pytest.raises(nd.NDError):
+            nd.contract_(R2, lr, A, la, B2, lb, precision=precision)
+        h.call("nd_graph_end", C.byref(ge))
+        if ge.value:
+            h.lib.nd_graph_destroy(ge)
