@@ -94,14 +94,34 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def dist_init():
+def dist_init(need_group=True):
+    """(rank, world size, local rank, torch.distributed or None).  Replicas only: the
+    group is used for the barrier and the max-over-ranks timing (NCCL with GPUs, gloo
+    without); the reference arm needs no group at all."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
-    if ws > 1:
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1 and need_group:
+        import torch
         import torch.distributed as dist
-        backend = "nccl"
-        dist.init_process_group(backend)
-        return dist.get_rank(), ws, int(os.environ.get("LOCAL_RANK", "0")), dist
-    return 0, 1, 0, None
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        return dist.get_rank(), ws, local, dist
+    return rank, ws, local, None
+
+
+def max_over_ranks(ms, dist, device=None):
+    """The slowest rank's time per step (every rank gets the same value)."""
+    if not dist:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(flops_per_step, ms, world_size):
+    """Aggregate GFLOP/s of all replicas: every rank processes one step's work per step."""
+    return world_size * flops_per_step / (ms * 1e-3) / 1e9
 
 
 def oracle_matvec(net, steps_labels):
@@ -127,7 +147,7 @@ def cpu_threads():
 
 
 def run_reference(args):
-    rank, ws, _, dist = dist_init()
+    rank, ws, _, dist = dist_init(need_group=False)
     if rank != 0:
         return
     from ndtensors_gb300 import workloads as wl
@@ -281,12 +301,8 @@ def run_ours(args):
     h.profile(False)
     launches = h.launches() - launches0
     torch.cuda.synchronize()
-    ms = float(np.sum(ts)) / args.steps
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * flops / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(float(np.sum(ts)) / args.steps, dist, dev)
+    value = whole_job_rate(flops, ms, ws)
 
     # plain FP64 path in the same run (fewer steps: it is ~50x slower)
     k64 = max(1, min(3, args.steps))
