@@ -52,8 +52,8 @@ def sector_dims(chi, sigma=3.0, qmax=8, dmin=8):
     d = np.round(chi * phi / phi.sum()).astype(np.int64)
     d = np.maximum(d, dmin)
     d[qmax] += chi - int(d.sum())
-    if d[qmax] < dmin:
-        raise ValueError(f"chi = {chi} is too small for {2 * qmax + 1} sectors of at least {dmin} states")
+    if d[qmax] < 1:
+        raise ValueError(f"chi = {chi} leaves no states for the q = 0 sector ({2 * qmax + 1} sectors, min {dmin})")
     return [(int(q), int(x)) for q, x in zip(qs, d)]
 
 
