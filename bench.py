@@ -662,7 +662,9 @@ def cfg_gradient(args):
 
 
 def cfg_sweep_step(args):
-    """C4 sweep step at chi = 4096: 10 H_eff matvecs + matricize + truncated blockwise SVD."""
+    """C4 sweep step at chi = 4096: Lanczos with 10 Krylov vectors on the two-site H_eff
+    (10 matvecs + full re-orthogonalisation, one CUDA graph), then matricize + truncated
+    blockwise SVD of the Ritz vector."""
     import torch
     import ndtensors_gb300 as nd
     from ndtensors_gb300 import workloads as wl
@@ -672,28 +674,27 @@ def cfg_sweep_step(args):
     G = {k: nd.BlockSparseTensor.from_host(net[k]) for k in ("L", "psi", "W1", "W2", "R")}
     sec = net["sectors"]
     qinds = [(sec, 1), (wl.SPIN_SECTORS, 1), (wl.SPIN_SECTORS, 1), (sec, -1)]
-
-    def matvec(v, prec):
-        x = nd.contract(G["L"], st[0][0], v, st[0][1], st[0][2], precision=prec)
-        for (a, b, c), key in zip(st[1:], ("W1", "W2", "R")):
-            x = nd.contract(x, a, G[key], b, c, precision=prec)
-        x.data /= torch.linalg.norm(x.data)
-        return x
-
-    def chain(prec):
-        v = G["psi"]
-        for _ in range(10):
-            v = matvec(v, prec)
-        return v
+    psi = G["psi"]
 
     res = {}
-    finals = {}
+    ritz = {}
     for prec in ("fp64", "ozaki"):
-        chain(prec)                      # builds and caches the plans of both block orders
+        op = nd.HeffOperator(G["L"], G["W1"], G["W2"], G["R"], psi, st, precision=prec)
+        eager = nd.Lanczos(op.apply, op.n, krylovdim=10)
+        graph = nd.Lanczos(op.apply, op.n, krylovdim=10, graph=True)
+        eager.run(psi.data)                              # builds plans and caches
+        graph.run(psi.data)                              # captures the graph
         torch.cuda.synchronize()
-        ts = _events_ms(lambda: chain(prec), 3)
-        v = chain(prec)
-        finals[prec] = v
+        t0 = time.perf_counter()
+        for _ in range(3):
+            r = eager.run(psi.data)
+        eager_ms = (time.perf_counter() - t0) * 1e3 / 3
+        t0 = time.perf_counter()
+        for _ in range(3):
+            r = graph.run(psi.data)
+        graph_ms = (time.perf_counter() - t0) * 1e3 / 3
+        ritz[prec] = r
+        v = nd.BlockSparseTensor(list(psi.inds), list(psi.blocks), list(psi.offsets), r.vector.contiguous())
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         hd = nd.handle(0)
         hd.profile(True)
@@ -708,36 +709,40 @@ def cfg_sweep_step(args):
         rows = [M.inds[0][b[0] - 1] for b in M.blocks]
         cols = [M.inds[1][b[1] - 1] for b in M.blocks]
         svd_flops = sum(22 * m * n * min(m, n) for m, n in zip(rows, cols))
-        res[prec] = {"matvecs_ms": round(float(np.median(ts)), 3), "svd_ms": round(svd_ms, 3),
-                     "svd_blocks": len(M.blocks), "svd_GFLOP/s_rule_of_thumb": round(svd_flops / (svd_ms * 1e-3) / 1e9, 1),
+        res[prec] = {"lanczos_graph_ms": round(graph_ms, 3), "lanczos_eager_ms": round(eager_ms, 3),
+                     "ritz_value": r.value, "ritz_residual": r.residual,
+                     "svd_ms": round(svd_ms, 3), "svd_blocks": len(M.blocks),
+                     "svd_GFLOP/s_rule_of_thumb": round(svd_flops / (svd_ms * 1e-3) / 1e9, 1),
                      "truncerr": spec.truncerr, "kept_total": int(sum(kept)),
-                     "svd_kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in svd_prof.items()}}
+                     "svd_kernels": {k: {"launches": v_[0], "ms": round(v_[1], 3)} for k, v_ in svd_prof.items()},
+                     "matricized": M}
     # CPU baseline for the truncation step: the oracle's per-block LAPACK gesdd + truncate! on the same blocks
     from oracle import linalg as olin
-    M, _, _ = nd.matricize(finals["ozaki"], qinds, (0, 1), (2, 3))
+    M = res["ozaki"].pop("matricized")
+    res["fp64"].pop("matricized")
     host = M.data_numpy()
     mats = []
     for i, b in enumerate(M.blocks):
-        r, c = M.inds[0][b[0] - 1], M.inds[1][b[1] - 1]
-        mats.append(host[M.offsets[i]:M.offsets[i] + r * c].reshape((r, c), order="F"))
+        r_, c_ = M.inds[0][b[0] - 1], M.inds[1][b[1] - 1]
+        mats.append(host[M.offsets[i]:M.offsets[i] + r_ * c_].reshape((r_, c_), order="F"))
     t0 = time.perf_counter()
     ref = olin.svd_blocks(mats, maxdim=4096, cutoff=1e-10)
     cpu_svd_ms = (time.perf_counter() - t0) * 1e3
-    oz, f64 = finals["ozaki"], finals["fp64"]
-    same_structure = oz.blocks == f64.blocks and oz.offsets == f64.offsets
-    err = float(torch.linalg.norm(oz.data - f64.data) / torch.linalg.norm(f64.data)) if same_structure else None
-    step_ms = res["ozaki"]["matvecs_ms"] + res["ozaki"]["svd_ms"]
-    _line("two-site sweep step time (10 H_eff matvecs + blockwise SVD), chi=4096", round(step_ms, 3), "ms", False,
-          "qn_sweep_step_chi4096", {"precisions": res, "matvec_rel_err_ozaki_vs_fp64_after_10": err,
-                                     "truncerr_abs_diff": abs(res["ozaki"]["truncerr"] - res["fp64"]["truncerr"]),
-                                     "svd": "maxdim 4096, cutoff 1e-10; one-sided Jacobi, FP32-preconditioned, "
-                                            "all blocks per launch",
-                                     "cpu_baseline": {"value": round(cpu_svd_ms, 1), "unit": "ms (svd + truncate only)",
-                                                      "cores": cpu_threads(), "kind": "port",
-                                                      "sample": "oracle: LAPACK gesdd per block + truncate! on the "
-                                                                "same 19 blocks",
-                                                      "truncerr": ref["truncerr"]},
-                                     "matvec_chain": "v <- H v / |H v|, plans cached by structure"},
+    a, b = ritz["ozaki"], ritz["fp64"]
+    step_ms = res["ozaki"]["lanczos_graph_ms"] + res["ozaki"]["svd_ms"]
+    _line("two-site sweep step time (Lanczos, 10 Krylov vectors in one CUDA graph, + blockwise SVD), chi=4096",
+          round(step_ms, 3), "ms", False, "qn_sweep_step_chi4096",
+          {"precisions": res,
+           "ritz_value_rel_diff_ozaki_vs_fp64": abs(a.value - b.value) / abs(b.value),
+           "lanczos_coeff_max_rel_diff_ozaki_vs_fp64": float(np.max(np.abs(a.alpha - b.alpha)) / np.max(np.abs(b.alpha))),
+           "truncerr_abs_diff": abs(res["ozaki"]["truncerr"] - res["fp64"]["truncerr"]),
+           "svd": "maxdim 4096, cutoff 1e-10; one-sided Jacobi, FP32-preconditioned, all blocks per launch",
+           "lanczos": "full re-orthogonalisation (classical Gram-Schmidt twice); H_eff plans cached; graph replay "
+                      "includes the host tridiagonal solve and Ritz vector",
+           "cpu_baseline": {"value": round(cpu_svd_ms, 1), "unit": "ms (svd + truncate only)",
+                            "cores": cpu_threads(), "kind": "port",
+                            "sample": "oracle: LAPACK gesdd per block + truncate! on the same 19 blocks",
+                            "truncerr": ref["truncerr"]}},
           3, 1)
 
 

@@ -28,7 +28,7 @@ nd_status nd_cuda_check(nd_handle h, cudaError_t e, const char* what) {
 nd_status nd_workspace(nd_handle h, size_t bytes, void** out) {
   if (bytes == 0) bytes = 256;
   if (bytes > h->ws_size) {
-    if (h->capturing)
+    if (nd_capturing(h))
       return nd_fail(h, ND_ERR_ARG, "workspace must grow during graph capture: run the call once before capture");
     if (h->ws) {
       ND_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -44,8 +44,15 @@ nd_status nd_workspace(nd_handle h, size_t bytes, void** out) {
   return ND_OK;
 }
 
+bool nd_capturing(nd_handle h) {
+  if (h->capturing) return true;
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->stream, &st) != cudaSuccess) return false;
+  return st == cudaStreamCaptureStatusActive;
+}
+
 nd_status nd_check_device_status(nd_handle h, const char* what) {
-  if (h->capturing) return ND_OK;   // read after replay via nd_sync
+  if (nd_capturing(h)) return ND_OK;   // read after replay via nd_sync
   DeviceStatus st{};
   ND_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
   ND_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -114,7 +121,7 @@ const char* nd_last_error(nd_handle h) { return h ? h->last_error.c_str() : g_no
 nd_status nd_set_stream(nd_handle h, void* s) {
   if (!h) return ND_ERR_ARG;
   if ((cudaStream_t)s == h->stream) return ND_OK;
-  if (h->capturing) return nd_fail(h, ND_ERR_ARG, "nd_set_stream: cannot change streams during graph capture");
+  if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "nd_set_stream: cannot change streams during graph capture");
   if (h->own_stream) {
     ND_CUDA(h, cudaStreamSynchronize(h->stream));
     cudaStreamDestroy(h->stream);
@@ -314,7 +321,7 @@ nd_status nd_graph_destroy(void* exec) {
 }  // extern "C"
 
 void nd_prof_begin(nd_handle h, const char* name) {
-  if (!h->profiling || h->capturing) return;
+  if (!h->profiling || nd_capturing(h)) return;
   auto get = [&]() {
     if (!h->event_pool.empty()) { cudaEvent_t e = h->event_pool.back(); h->event_pool.pop_back(); return e; }
     cudaEvent_t e; cudaEventCreate(&e); return e;
@@ -325,7 +332,7 @@ void nd_prof_begin(nd_handle h, const char* name) {
 }
 
 void nd_prof_end(nd_handle h) {
-  if (!h->profiling || h->capturing || h->prof.empty()) return;
+  if (!h->profiling || nd_capturing(h) || h->prof.empty()) return;
   cudaEventRecord(h->prof.back().e1, h->stream);
 }
 

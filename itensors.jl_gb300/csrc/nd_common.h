@@ -62,6 +62,11 @@ struct nd_context {
 
 void nd_dense_cache_clear(nd_handle h);
 
+// True while the handle's stream is being captured into a CUDA graph, whether the
+// capture was opened by nd_graph_begin or by the caller (e.g. torch.cuda.graph):
+// the library then allocates, uploads and synchronises nothing.
+bool nd_capturing(nd_handle h);
+
 // Host helpers -------------------------------------------------------------
 nd_status nd_fail(nd_handle h, nd_status code, const char* fmt, ...);
 nd_status nd_cuda_check(nd_handle h, cudaError_t e, const char* what);

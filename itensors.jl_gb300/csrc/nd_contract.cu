@@ -301,7 +301,7 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
     return nd_fail(h, ND_ERR_ARG, "unknown precision %d", precision);
   const int want_slices = precision == ND_PREC_OZAKI ? h->ozaki_slices : (precision == ND_PREC_BF16X3 ? 2 : 0);
   if (!c.built || c.precision != precision || c.slices != want_slices) {
-    if (h->capturing) return nd_fail(h, ND_ERR_ARG, "contraction state must be built before graph capture (run once first)");
+    if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "contraction state must be built before graph capture (run once first)");
     const std::string key = tune_key(h, pairs, precision, want_slices);
     auto it = h->tune.find(key);
     nd_status s;
@@ -344,7 +344,7 @@ static ExecCache* dense_exec(nd_handle h, const PairDesc& pd, int precision) {
   append_mixed(key, pd.ks);
   auto it = h->dense_cache.find(key);
   if (it != h->dense_cache.end()) return (ExecCache*)it->second;
-  if (h->capturing) return nullptr;
+  if (nd_capturing(h)) return nullptr;
   if (h->dense_cache.size() >= kDenseCacheEntries) {
     const std::string old = h->dense_order.front();
     h->dense_order.erase(h->dense_order.begin());
@@ -432,13 +432,13 @@ extern "C" nd_status nd_contract_dense_f64(nd_handle h, double* R, int32_t rankR
   // dense contraction is kept per handle and reused by later calls of the same shape,
   // so repeated small contractions cost no allocation and can be graph-captured
   ExecCache* c = dense_exec(h, pd, precision);
-  if (!c && h->capturing)
+  if (!c && nd_capturing(h))
     return nd_fail(h, ND_ERR_ARG, "contract: run this shape once before graph capture (its state is built then)");
   if (!c) return nd_fail(h, ND_ERR_OOM, "contract: host allocation failed");
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
   nd_status s = nd_execute_cached(h, *c, pairs, 1, ptrs, alpha, beta, precision);
   if (s != ND_OK) return s;
-  if (h->capturing) return ND_OK;
+  if (nd_capturing(h)) return ND_OK;
   return nd_check_device_status(h, "contract");   // synchronises the stream
 }
 
@@ -638,7 +638,7 @@ extern "C" nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan p, const do
     for (int b = 0; b < p->B.nnzblocks; ++b) if (!tB[b]) ranges.insert(ranges.end(), {1, p->B.offsets[b], p->B.block_elems(b)});
   }
   if (!ranges.empty()) {
-    if (h->capturing) return nd_fail(h, ND_ERR_ARG, "adjoint with untouched blocks cannot be captured");
+    if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "adjoint with untouched blocks cannot be captured");
     int64_t* d = nullptr;
     ND_CUDA(h, cudaMallocAsync(&d, ranges.size() * 8, h->stream));
     ND_CUDA(h, cudaMemcpyAsync(d, ranges.data(), ranges.size() * 8, cudaMemcpyHostToDevice, h->stream));

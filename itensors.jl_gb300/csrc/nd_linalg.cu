@@ -767,7 +767,7 @@ extern "C" nd_status nd_bs_svd_f64(nd_handle h, int32_t nb, const int64_t* rows,
                                    int32_t use_relative_cutoff, int32_t min_blockdim, int32_t* kept, double* spectrum,
                                    int32_t* spectrum_len, double* truncerr, double* docut) {
   if (!h) return ND_ERR_ARG;
-  if (h->capturing) return nd_fail(h, ND_ERR_ARG, "svd returns kept dimensions to the host and cannot be captured");
+  if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd returns kept dimensions to the host and cannot be captured");
   if (nb < 0 || (nb > 0 && (!rows || !cols || !offsets || !A || !U || !S || !V || !kept)))
     return nd_fail(h, ND_ERR_ARG, "svd: NULL argument");
   if (nb == 0) { if (spectrum_len) *spectrum_len = 0; if (truncerr) *truncerr = 0; if (docut) *docut = 0; return ND_OK; }

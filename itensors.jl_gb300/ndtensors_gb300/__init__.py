@@ -13,6 +13,8 @@ from .autodiff import contract_autograd, contract_rrule, dense_structure
 from .linalg import Spectrum, matricize, qr, svd, truncate
 from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
+from . import krylov
+from .krylov import HeffOperator, Lanczos, lanczos
 
 __all__ = [
     "workloads", "NDError", "NoConvergence", "PRECISIONS", "handle", "load", "LIB_PATH",
@@ -21,4 +23,5 @@ __all__ = [
     "permutedims", "permutedims_", "permutedims_blocksparse",
     "linalg", "Spectrum", "matricize", "qr", "svd", "truncate",
     "autodiff", "contract_autograd", "contract_rrule", "dense_structure",
+    "krylov", "HeffOperator", "Lanczos", "lanczos",
 ]

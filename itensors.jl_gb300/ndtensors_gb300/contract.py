@@ -174,6 +174,7 @@ def contract_blocksparse(T1, l1, T2, l2, lr=None, alpha=1.0, precision="fp64", p
         data = torch.empty(max(plan.nnzR, 1), dtype=torch.float64, device=T1.data.device)[:plan.nnzR]
         R = BlockSparseTensor(list(plan.indsR), list(plan.blocksR), list(plan.offsetsR), data)
     if plan.npairs:
+        handle(T1.data.device.index or 0)          # bind the handle to torch's current stream
         plan.h.call("nd_bs_contract_f64", plan.ptr, C.c_void_p(R.data.data_ptr()), C.c_void_p(T1.data.data_ptr()),
                     C.c_void_p(T2.data.data_ptr()), float(alpha), _prec(precision))
     return R
