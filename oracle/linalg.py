@@ -54,6 +54,43 @@ def svd_blocks(mats, mindim=None, maxdim=None, cutoff=None, use_absolute_cutoff=
                 docut=docut)
 
 
+def eigen_blocks(mats, mindim=None, maxdim=None, cutoff=None, use_absolute_cutoff=None,
+                 use_relative_cutoff=None, min_blockdim=None):
+    """Blockwise Hermitian eigendecomposition (NDTensors/src/blocksparse/linearalgebra.jl:221-348).
+
+    Per block a dense Hermitian eigen with eigenpairs sorted by |lambda| descending
+    (NDTensors/src/linearalgebra/linearalgebra.jl:162-213), all |lambda| pooled and
+    sorted descending, truncate!!, per block the leading eigenpairs with |lambda| > docut
+    (_truncated_blockdim with singular_values = false, :8-33).  Returns dict with D
+    (kept eigenvalues per surviving block), V, kept, spectrum (pooled |lambda| after
+    truncation), truncerr, docut.
+    """
+    Ds, Vs, d = [], [], []
+    for m in mats:
+        lam, vec = np.linalg.eigh(m)
+        order = np.argsort(-np.abs(lam), kind="stable")
+        Ds.append(lam[order])
+        Vs.append(vec[:, order])
+        d.extend(np.abs(lam).tolist())
+    d = sorted(d, reverse=True)
+    kept = [len(x) for x in Ds]
+    truncerr, docut = 0.0, 0.0
+    if maxdim is not None or cutoff is not None:
+        d, truncerr, docut = truncate(d, mindim=mindim, maxdim=maxdim, cutoff=cutoff,
+                                      use_absolute_cutoff=use_absolute_cutoff,
+                                      use_relative_cutoff=use_relative_cutoff)
+        for n, lam in enumerate(Ds):
+            kept[n] = truncated_blockdim(lam, docut, singular_values=False, min_blockdim=min_blockdim)
+    out_d, out_v = [], []
+    for n in range(len(mats)):
+        k = kept[n]
+        if k == 0:
+            continue
+        out_d.append(Ds[n][:k])
+        out_v.append(Vs[n][:, :k])
+    return dict(D=out_d, V=out_v, kept=kept, spectrum=d, truncerr=truncerr, docut=docut)
+
+
 def qr_positive(m):
     """QR with non-negative diag(R) (linearalgebra.jl:374-381)."""
     q, r = np.linalg.qr(m, mode="reduced")

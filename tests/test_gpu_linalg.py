@@ -218,3 +218,42 @@ def test_two_site_step(nd, precision):
     assert kept == ref["kept"]
     np.testing.assert_allclose(spec.eigs, ref["spectrum"], rtol=1e-8, atol=1e-13 * ref["spectrum"][0])
     assert abs(spec.truncerr - ref["truncerr"]) <= 1e-8 * ref["truncerr"] + 1e-16
+
+
+@pytest.mark.parametrize("case", ["full", "truncated", "min_blockdim"])
+def test_eigen_blockwise_matches_oracle(nd, case):
+    """Blockwise Hermitian eigen (linearalgebra.jl:221-348) vs the oracle (numpy eigh per
+    block, |lambda|-sorted, pooled truncate!, per-block kept dims)."""
+    rng = np.random.default_rng({"full": 61, "truncated": 62, "min_blockdim": 63}[case])
+    dims = [40, 130, 7, 260]
+    mats = []
+    for n in dims:
+        q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        lam = rng.standard_normal(n) * np.exp(rng.uniform(-12, 0, n))     # both signs, wide range
+        mats.append((q * lam) @ q.T)
+    mats.append(np.zeros((5, 5)))                                          # a zero block
+    mats.append(-np.outer(np.ones(6), np.ones(6)))                         # rank one, negative
+    dims = [m.shape[0] for m in mats]
+    offs, o = [], 0
+    for m in mats:
+        offs.append(o)
+        o += m.size
+    A = obs.BlockSparseTensor([dims, dims], [(i + 1, i + 1) for i in range(len(dims))], offs,
+                              np.concatenate([m.reshape(-1, order="F") for m in mats]))
+    kw = {"full": {}, "truncated": {"maxdim": 150, "cutoff": 1e-9},
+          "min_blockdim": {"cutoff": 1e-3, "min_blockdim": 2}}[case]
+    ref = olin.eigen_blocks(mats, **kw)
+    D, V, spec, kept = nd.eigen(_gpu(nd, A), **kw)
+    assert kept == ref["kept"]
+    # error scale of lambda = sigma - c with c ~ ||A_b||_F: eps-level multiples of ||A_b||_F
+    fro = max(np.linalg.norm(m) for m in mats)
+    np.testing.assert_allclose(spec.eigs, ref["spectrum"], rtol=0, atol=1e-12 * fro)
+    assert abs(spec.truncerr - ref["truncerr"]) <= 1e-10 * max(ref["truncerr"], 1e-300) + 1e-15
+    Vb = _blocks(nd, V)
+    surv = [n for n in range(len(mats)) if kept[n] > 0]
+    for i, n in enumerate(surv):
+        m, lam, vec = mats[n], D[i].cpu().numpy(), Vb[i]
+        scale = max(np.linalg.norm(m), 1e-300)
+        np.testing.assert_allclose(lam, ref["D"][i], rtol=0, atol=1e-12 * scale)
+        np.testing.assert_allclose(vec.T @ vec, np.eye(len(lam)), atol=1e-12)
+        np.testing.assert_allclose(m @ vec, vec * lam, rtol=0, atol=1e-11 * scale)   # eigenpairs
