@@ -5,7 +5,7 @@ interface, calling libndtensors_gb300.so through its C ABI.  No CPU fallback:
 every operation runs in the library's CUDA kernels.
 """
 from ._lib import NDError, NoConvergence, PRECISIONS, handle, load, LIB_PATH
-from .tensors import BlockSparseTensor, DenseTensor, blockoffsets
+from .tensors import BlockSparseTensor, DenseTensor, DiagBlockSparseTensor, blockoffsets
 from . import workloads
 from . import linalg
 from . import autodiff
@@ -18,7 +18,7 @@ from .krylov import HeffOperator, Lanczos, lanczos
 
 __all__ = [
     "workloads", "NDError", "NoConvergence", "PRECISIONS", "handle", "load", "LIB_PATH",
-    "BlockSparseTensor", "DenseTensor", "blockoffsets",
+    "BlockSparseTensor", "DenseTensor", "DiagBlockSparseTensor", "blockoffsets",
     "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
     "permutedims", "permutedims_", "permutedims_blocksparse",
     "linalg", "Spectrum", "eigen", "matricize", "qr", "svd", "truncate",

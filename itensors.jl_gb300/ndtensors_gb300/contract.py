@@ -181,8 +181,21 @@ def contract_blocksparse(T1, l1, T2, l2, lr=None, alpha=1.0, precision="fp64", p
 
 
 def contract(T1, labels1, T2, labels2, labelsR=None, precision="fp64"):
-    """contract(T1, labelsT1, T2, labelsT2[, labelsR]) for Dense or BlockSparse storage."""
+    """contract(T1, labelsT1, T2, labelsT2[, labelsR]) for Dense, BlockSparse or
+    BlockSparse x DiagBlockSparse storage.
+
+    A DiagBlockSparse operand follows NDTensors' default dense conversion
+    (diag/tensoralgebra/contract.jl:103-214; blocksparse/diagblocksparse.jl:601-696): its
+    diagonal blocks are expanded on the device and the contraction is one grouped
+    launch whose block plan and output structure are those of contraction_output."""
+    from .tensors import DiagBlockSparseTensor
     l1, l2 = tuple(labels1), tuple(labels2)
+    if isinstance(T1, DiagBlockSparseTensor):
+        return contract(T2, l2, T1, l1, contract_labels(l2, l1) if labelsR is None else labelsR, precision)
+    if isinstance(T2, DiagBlockSparseTensor):
+        if not isinstance(T1, BlockSparseTensor):
+            raise TypeError("contract: a DiagBlockSparse operand needs a BlockSparse partner")
+        T2 = T2.dense()
     lr = contract_labels(l1, l2) if labelsR is None else tuple(labelsR)
     if isinstance(T1, BlockSparseTensor) and isinstance(T2, BlockSparseTensor):
         return contract_blocksparse(T1, l1, T2, l2, lr, precision=precision)

@@ -140,3 +140,53 @@ class BlockSparseTensor:
         d = BsDesc(self.rank, nb, bd, len(self.blocks), bl, of)
         d._keep = (nb, bd, bl, of)
         return d
+
+
+@dataclass
+class DiagBlockSparseTensor:
+    """DiagBlockSparse storage (NDTensors/src/blocksparse/diagblocksparse.jl): block-diagonal
+    blocks (every block number equal), each storing only its diagonal, min(blockdims)
+    entries, at `offsets` into one flat vector."""
+    inds: list
+    blocks: list
+    offsets: list
+    data: object          # torch.float64 CUDA 1-D
+
+    @property
+    def rank(self):
+        return len(self.inds)
+
+    def blockdims(self, block):
+        return tuple(self.inds[k][block[k] - 1] for k in range(self.rank))
+
+    @classmethod
+    def from_diagonals(cls, inds, blocks, diags):
+        """From per-block diagonal vectors (torch CUDA tensors), in block order."""
+        torch = _torch()
+        for b in blocks:
+            if len(set(b)) != 1:
+                raise ValueError("DiagBlockSparse blocks must be block diagonal (all block numbers equal)")
+        offs, o = [], 0
+        for d in diags:
+            offs.append(o)
+            o += int(d.numel())
+        data = torch.cat([d.reshape(-1).to(torch.float64) for d in diags]) if diags else torch.empty(0)
+        return cls([tuple(i) for i in inds], [tuple(b) for b in blocks], offs, data)
+
+    def dense(self):
+        """The equal-structure BlockSparseTensor with the diagonals expanded (on the device),
+        as NDTensors' default dense(D) conversion (diag/tensoralgebra/contract.jl:103-214)."""
+        torch = _torch()
+        offs, nnz = blockoffsets(self.blocks, self.inds)
+        out = torch.zeros(max(nnz, 1), dtype=torch.float64, device=self.data.device)[:nnz]
+        for b, o, do in zip(self.blocks, offs, self.offsets):
+            dims = self.blockdims(b)
+            k = min(dims) if dims else 1
+            stride = 0                                # column-major offset of (i, i, ..., i)
+            s = 1
+            for d in dims:
+                stride += s
+                s *= d
+            idx = torch.arange(k, device=self.data.device) * stride + o
+            out.index_copy_(0, idx, self.data[do:do + k])
+        return BlockSparseTensor(list(self.inds), list(self.blocks), offs, out)

@@ -257,3 +257,34 @@ def test_eigen_blockwise_matches_oracle(nd, case):
         np.testing.assert_allclose(lam, ref["D"][i], rtol=0, atol=1e-12 * scale)
         np.testing.assert_allclose(vec.T @ vec, np.eye(len(lam)), atol=1e-12)
         np.testing.assert_allclose(m @ vec, vec * lam, rtol=0, atol=1e-11 * scale)   # eigenpairs
+
+
+def test_diag_blocksparse_contraction_rebuilds_svd(nd):
+    """BlockSparse x DiagBlockSparse (blocksparse/diagblocksparse.jl:601-696): U * S * V^T
+    rebuilt from the blockwise SVD equals the input; the output structure is the plan's
+    (contraction_output) and matches the oracle's contraction with the expanded diagonal."""
+    import torch
+    rng = np.random.default_rng(72)
+    dims = [50, 80, 33]
+    mats = [rng.standard_normal((d, d + 7)) for d in dims]
+    inds = [dims, [d + 7 for d in dims]]
+    blocks = [(i + 1, i + 1) for i in range(len(dims))]
+    offs, nnz = obs.blockoffsets(blocks, inds)
+    A = obs.BlockSparseTensor(inds, blocks, offs, np.concatenate([m.reshape(-1, order="F") for m in mats]))
+    U, S, V, spec, kept = nd.svd(_gpu(nd, A))
+    u_ind = U.inds[1]
+    D = nd.DiagBlockSparseTensor.from_diagonals([u_ind, u_ind], [(i + 1, i + 1) for i in range(len(S))], S)
+    US = nd.contract(U, (1, -1), D, (-1, 2))                # diag operand second
+    SU = nd.contract(D, (-1, 2), U, (1, -1))                 # diag operand first: labels (1, 2) by default
+    assert SU.blocks == US.blocks and SU.offsets == US.offsets
+    np.testing.assert_array_equal(SU.data_numpy(), US.data_numpy())
+    R = nd.contract(US, (1, -1), V, (2, -1))                 # (l, r)
+    out = obs.BlockSparseTensor(R.inds, R.blocks, R.offsets, R.data_numpy()).to_dense()
+    assert odense.rel_frobenius_error(out, A.to_dense()) <= 1e-12
+    # oracle: the same contraction with the diagonal expanded to dense blocks
+    Dd = D.dense()
+    Do = obs.BlockSparseTensor([list(u_ind), list(u_ind)], Dd.blocks, Dd.offsets, Dd.data_numpy())
+    Uo = obs.BlockSparseTensor([list(U.inds[0]), list(u_ind)], U.blocks, U.offsets, U.data_numpy())
+    ref, _ = obs.contract(Uo, (1, -1), Do, (-1, 2), (1, 2))
+    assert US.blocks == [tuple(b) for b in ref.blocks] and US.offsets == list(ref.offsets)
+    assert odense.rel_frobenius_error(US.data_numpy(), ref.data) <= 1e-14
