@@ -23,25 +23,29 @@
 //
 // Levels: level t = p+q carries weight 2^(-8(t-2)).  Slices are stored
 // pre-scaled (slice p holds d_p * 2^(-8(p-1)), still exact in BF16), so every
-// product already carries its level weight.  Levels 2 and 3 must be exact:
-// they accumulate in an "X" accumulator pair (L2 | L3) in FP32 TMEM over
-// chunks of 512 of K (|sum| <= 2^24 units), and the epilogue warps drain each
-// chunk into int64 fixed point (unit 2^-24 of a level-2 unit).  Levels >= 4
-// go to a "T" pair (T4 | T5+) in FP32 over the whole K of a block pair: their
-// rounding is below 2^-40 of the leading term.  X slots alternate per chunk
-// and T slots per block pair, both double buffered in the 512 TMEM columns,
-// so the epilogue of one pair overlaps the MMAs of the next.
+// product already carries its level weight.  All levels accumulate in FP32 TMEM
+// over chunks of 512 of K and are drained per chunk into int64 fixed point (unit
+// 2^-24 of a level-2 unit): levels 2 and 3 are exact there (|sum| <= 2^24 units),
+// levels 4 and >= 5 are rounded once per chunk, below 2^-40 of the leading term.
+// A slot is [L2 | L3 | T4 | T5+] (64 columns each); two slots alternate per chunk
+// in the 512 TMEM columns, so the drain of one chunk overlaps the MMAs of the next.
+// The drains convert with FP32 magic-constant splits, not float->int
+// instructions, which sm_103a runs on its narrow FP64 pipe.
 //
 // Each A-slice stage is [S][128 rows][32 k] BF16 and each B-slice stage is
 // [S][64 rows][32 k], pre-swizzled (64-byte swizzle) by the pack kernel, so one
 // cp.async.bulk per operand brings a whole stage and the slices of B sit in
-// consecutive rows: A_p x [B_q, B_q+1] is ONE tcgen05.mma with N = 128 whose
-// two 64-column halves land in adjacent accumulator blocks (L2|L3 or T4|T5+).
+// consecutive rows.  Level t sits in block t - 2 of a slot, so A_p x [B_1 .. B_r]
+// is ONE tcgen05.mma with N = 64 r whose 64-column parts land in consecutive
+// blocks (for S = 5: N = 256, 192, 128, 64 for p = 1..4); the few products past
+// the last block go to T5+ with N = 64.  Consecutive MMAs that share A_p reuse it
+// through the A collector.  9 MMAs per 16 of K for S = 5.
 //
 // Warp roles (576 threads): warp 0 = bulk-copy producer, warp 1 = TMEM
 // allocator + MMA issuer, warps 2..17 = epilogue (TMEM lane quarter = warp % 4,
-// 16-column group = (warp-2)/4).  Persistent CTAs walk a cost-sorted list of
-// output tiles; each tile loops over the block pairs of its output block.
+// 16-column group = (warp-2)/4).  Persistent CTAs walk a list of output tiles
+// balanced across them by longest-processing-time assignment; each tile loops
+// over the block pairs of its output block.
 #include "nd_plan.h"
 #include <cuda_bf16.h>
 #include <algorithm>
@@ -353,13 +357,34 @@ __device__ __forceinline__ uint32_t idesc(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
 
+// The MMA warp runs its loop on all 32 lanes (warp-uniform values stay in uniform
+// registers); one elected lane issues each tcgen05 instruction.
+// CU selects the A-collector use: 0 none, 1 fill, 2 use, 3 lastuse (consecutive MMAs
+// that share A_p read it from shared memory once).
+#define ND_ELECT " .reg .pred e;\n elect.sync _|e, 0xffffffff;\n @e "
+template <int CU>
 __device__ __forceinline__ void mma(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t id, uint32_t acc) {
-  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
-               :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+  if constexpr (CU == 1)
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n" ND_ELECT
+                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+  else if constexpr (CU == 2)
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n" ND_ELECT
+                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+  else if constexpr (CU == 3)
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n" ND_ELECT
+                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+  else
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n" ND_ELECT
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
 }
 
 __device__ __forceinline__ void commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(bar)) : "memory");
+  asm volatile("{\n" ND_ELECT "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}"
+               :: "r"(smem_u32(bar)) : "memory");
 }
 
 #define TMEM_LD16(taddr, r)                                                                                   \
@@ -384,18 +409,41 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, %0;" :: "r"(EPI_WARPS * 32) : "memory"); }
 
+// Round-to-nearest-even of v (|v| < 2^33) to an integer on the FP32 and integer
+// pipes (sm_103a runs float->int conversions on its narrow FP64 pipe).  Magic-
+// constant splitting: v + 1.5*2^35 rounds v to a multiple of 2^12 whose count sits
+// in the low mantissa bits (hi); h = that multiple is exact, lo = v - h is exact
+// with |lo| <= 2^11, and lo + 1.5*2^23 rounds lo to an integer the same way (li).
+// v rounds to hi * 2^12 + li; ties go to even because h is even.
+__device__ __forceinline__ void f32_round_split(float v, int& hi, int& li) {
+  const float C12 = 51539607552.0f;   // 1.5 * 2^35, bits 0x51400000
+  const float C0 = 12582912.0f;       // 1.5 * 2^23, bits 0x4B400000
+  const float t = __fadd_rn(v, C12);
+  const float h = __fsub_rn(t, C12);
+  const float tl = __fadd_rn(__fsub_rn(v, h), C0);
+  hi = __float_as_int(t) - 0x51400000;
+  li = __float_as_int(tl) - 0x4B400000;
+}
+
+// One vote per wait: every lane of the MMA warp polls, and the warp leaves the loop
+// together if any lane gave up.
+__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, DeviceStatus* st, int site,
+                                               volatile int* abort_flag) {
+  return __all_sync(0xffffffffu, mbar_wait(bar, parity, st, site, abort_flag));
+}
+
 template <int S>
 struct Cfg {
   static constexpr int STAGE = S * (A_SLICE + B_SLICE);
   static constexpr int STAGES = (SMEM_BUDGET - 1024) / STAGE;
   static constexpr int TBLK = S >= 4 ? 2 : (S == 3 ? 1 : 0);   // tail blocks (T4, T5+)
-  static constexpr int TMEM_COLS = 512;                        // X0 T0 X1 T1, 128 columns each
+  static constexpr int TMEM_COLS = 512;                        // two slots of [L2 L3 T4 T5+]
   static constexpr int SMEM = STAGES * STAGE + 1024;
 };
 
-// TMEM column of X slot x / T slot t
+// TMEM column of slot x (levels 2, 3) and of its tail blocks (levels 4, >= 5)
 __device__ __forceinline__ uint32_t xcol(uint32_t x) { return x * 256u; }
-__device__ __forceinline__ uint32_t tcol(uint32_t t) { return t * 256u + 128u; }
+__device__ __forceinline__ uint32_t tcol(uint32_t x) { return x * 256u + 128u; }
 
 template <int S>
 __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
@@ -462,60 +510,65 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
     }
   } else if (warp == 1) {
     // ------------------------------- MMA issuer ----------------------------
-    if (lane == 0) {
+    {
       uint32_t n = 0, chunk = 0;
       bool ok = true;
       const uint32_t smem_base = smem_u32(smem);
-      const uint32_t i64 = idesc(BN), i128 = idesc(2 * BN);
+      const uint32_t i64 = idesc(BN);
+      constexpr int NBLK = 2 + C::TBLK;     // accumulator blocks of a slot: L2 L3 [T4 [T5+]]
       for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
         const WorkItem wi = g.items[it];
         for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
           const PairDesc& pd = g.pairs[wi.pair_begin + pi];
           const int nks = g.ops[pd.a_op].k_steps;
           const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
-          uint32_t X = tmem, T = tmem + tcol(0);
+          uint32_t X = tmem;
           for (int ks = 0; ks < nks; ++ks, ++n) {
             const bool cstart = (ks % chunk_steps) == 0;
             const bool cend = ((ks % chunk_steps) == chunk_steps - 1) || ks == nks - 1;
             if (cstart) {
-              // every level is drained per chunk: slot xs holds both X and T of this chunk
+              // every level is drained per chunk: slot xs holds all levels of this chunk
               const uint32_t xs = chunk & 1, xu = chunk >> 1;
-              if (xu >= 1 && !mbar_wait(smem_u32(&xempty[xs]), (xu - 1) & 1, g.st, 411, &abort_flag)) { ok = false; break; }
+              if (xu >= 1 && !mbar_wait_warp(smem_u32(&xempty[xs]), (xu - 1) & 1, g.st, 411, &abort_flag)) { ok = false; break; }
               X = tmem + xcol(xs);
-              T = tmem + tcol(xs);
             }
             const uint32_t s = n % C::STAGES, u = n / C::STAGES;
-            if (!mbar_wait(smem_u32(&full[s]), u & 1, g.st, 412, &abort_flag)) { ok = false; break; }
+            if (!mbar_wait_warp(smem_u32(&full[s]), u & 1, g.st, 412, &abort_flag)) { ok = false; break; }
             fence_after();
+            // descriptors of one stage differ only in the start-address field (addr >> 4)
             const uint32_t a0 = smem_base + s * C::STAGE;
-            const uint32_t b0 = a0 + S * A_SLICE;
+            const uint64_t adesc0 = sdesc(a0), bdesc0 = sdesc(a0 + S * A_SLICE);
 #pragma unroll
             for (int kk = 0; kk < 2; ++kk) {
               const uint32_t accx = (cstart && kk == 0) ? 0u : 1u;
-              const uint32_t acct = accx;
               const uint32_t ko = kk * 32;
-              auto A = [&](int p) { return sdesc(a0 + (p - 1) * A_SLICE + ko); };
-              auto B = [&](int q) { return sdesc(b0 + (q - 1) * B_SLICE + ko); };
-              // exact levels: A1 x [B1 B2] -> (L2 | L3), A2 x B1 -> L3
-              mma(X, A(1), B(1), i128, accx);
-              mma(X + BN, A(2), B(1), i64, 1u);
-              if (S == 3) {
-                mma(T, A(1), B(3), i64, acct);
-                mma(T, A(2), B(2), i64, 1u);
-                mma(T, A(3), B(1), i64, 1u);
-              } else if (S >= 4) {
-                // level 4 -> T4, levels >= 5 -> T5+ : A_p x [B_(4-p), B_(5-p)] is one N = 128 MMA for p <= 3
-                mma(T, A(1), B(3), i128, acct);
-                mma(T, A(2), B(2), i128, 1u);
-                mma(T, A(3), B(1), i128, 1u);
+              auto A = [&](int p) { return adesc0 + (uint64_t)((((p - 1) * A_SLICE) + ko) >> 4); };
+              auto B = [&](int q) { return bdesc0 + (uint64_t)((((q - 1) * B_SLICE) + ko) >> 4); };
+              // A slot is [L2 | L3 | T4 | T5+], 64 columns each, and level t = p + q sits in
+              // block t - 2.  A_p x [B_1 .. B_r] therefore lands in consecutive blocks: ONE
+              // MMA of N = 64 r at column 64 (p - 1).  The remaining products of A_p (levels
+              // past the last block) accumulate into T5+.  The first MMA of a chunk covers
+              // every block, so it alone starts the accumulation.
 #pragma unroll
-                for (int p = 1; p <= S; ++p)
+              for (int p = 1; p <= S; ++p) {
+                const int r = (S + 1 - p) < (NBLK + 1 - p) ? (S + 1 - p) : (NBLK + 1 - p);
+                const int r0 = r > 0 ? r : 0;
+                const int nm = (r0 > 0 ? 1 : 0) + (S + 1 - p - r0);    // MMAs sharing A_p
+                int m = 0;
+                if (r0 > 0) {
+                  const uint32_t d = X + (p - 1) * BN, id = idesc(r0 * BN), ac = p == 1 ? accx : 1u;
+                  if (nm > 1) mma<1>(d, A(p), B(1), id, ac);
+                  else mma<0>(d, A(p), B(1), id, ac);
+                  ++m;
+                }
 #pragma unroll
-                  for (int q = 1; q <= S + 1 - p; ++q) {
-                    const int lv = p + q;
-                    const bool covered = (p <= 3) && (q == 4 - p || q == 5 - p);
-                    if (lv >= 5 && !covered) mma(T + BN, A(p), B(q), i64, 1u);
-                  }
+                for (int q = r0 + 1; q <= S + 1 - p; ++q, ++m) {
+                  const uint32_t d = X + (NBLK - 1) * BN;
+                  if (nm == 1) mma<0>(d, A(p), B(q), i64, 1u);
+                  else if (m == 0) mma<1>(d, A(p), B(q), i64, 1u);
+                  else if (m == nm - 1) mma<3>(d, A(p), B(q), i64, 1u);
+                  else mma<2>(d, A(p), B(q), i64, 1u);
+                }
               }
             }
             commit(&empty[s]);
@@ -577,9 +630,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
 #pragma unroll
               for (int c = 0; c < EPI_COLS; ++c) {
                 // L2: integer units; L3 was computed with pre-scaled slices: an integer multiple of 2^-8
-                long long x2 = (long long)__float2int_rn(__uint_as_float(l2[c]));
-                long long x3 = (long long)__float2int_rn(__uint_as_float(l3[c]) * 256.0f);
-                acc[c] += (x2 << 24) + (x3 << 16);
+                // |L2| <= 2^23, |256 L3| <= 2^24: hi parts fit 2^11 and 2^12, li parts 2^11
+                int h2, i2, h3, i3;
+                f32_round_split(__uint_as_float(l2[c]), h2, i2);
+                f32_round_split(__uint_as_float(l3[c]) * 256.0f, h3, i3);
+                acc[c] += ((long long)(h2 * 256 + h3) << 28) + ((long long)(i2 * 256 + i3) << 16);
               }
             } else {
 #pragma unroll
@@ -594,8 +649,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
             tmem_wait_ld();
 #pragma unroll
             for (int c = 0; c < EPI_COLS; ++c) {
-              acc[c] += __float2ll_rn(__uint_as_float(t4[c]) * 16777216.0f);                    // x 2^24
-              if (C::TBLK > 1) acc[c] += __float2ll_rn(__uint_as_float(t5[c]) * 16777216.0f);
+              // x 2^24: |T4| < 2^9 and |T5+| < 2^2 per chunk, inside the split's 2^33 range
+              int h4, i4, h5 = 0, i5 = 0;
+              f32_round_split(__uint_as_float(t4[c]) * 16777216.0f, h4, i4);
+              if (C::TBLK > 1) f32_round_split(__uint_as_float(t5[c]) * 16777216.0f, h5, i5);
+              acc[c] += ((long long)(h4 + h5) << 12) + (long long)(i4 + i5);
             }
           }
           fence_before();
@@ -654,6 +712,38 @@ nd_status launch_gemm(nd_handle h, const GemmArgs& g) {
   return nd_cuda_check(h, cudaGetLastError(), "split_gemm");
 }
 
+// Persistent-CTA schedule.  Items (cost, tile) are assigned longest first to the
+// least-loaded of G = min(#items, SMs) CTAs, and laid out so that the kernels'
+// stride-G walk (item = blockIdx.x + r G) visits exactly each CTA's list; shorter
+// lists are padded with empty items (pair_count 0), which every role skips.
+std::vector<WorkItem> balance_items(std::vector<std::pair<int64_t, WorkItem>> tmp, int num_sms) {
+  std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+  std::vector<WorkItem> items;
+  if (tmp.empty()) return items;
+  const int G = std::max(1, std::min((int)tmp.size(), num_sms));
+  std::vector<std::vector<WorkItem>> lists(G);
+  std::vector<std::pair<int64_t, int>> heap;
+  for (int b = 0; b < G; ++b) heap.push_back({0, b});
+  auto later = [](const auto& x, const auto& y) { return x.first > y.first || (x.first == y.first && x.second > y.second); };
+  std::make_heap(heap.begin(), heap.end(), later);
+  for (auto& t : tmp) {
+    std::pop_heap(heap.begin(), heap.end(), later);
+    lists[heap.back().second].push_back(t.second);
+    heap.back().first += t.first;
+    std::push_heap(heap.begin(), heap.end(), later);
+  }
+  size_t L = 0;
+  for (auto& l : lists) L = std::max(L, l.size());
+  const WorkItem empty{tmp[0].second.group, tmp[0].second.pair_begin, 0, 0, 0};
+  for (size_t r = 0; r < L; ++r)
+    for (int b = 0; b < G; ++b) items.push_back(r < lists[b].size() ? lists[b][r] : empty);
+  return items;
+}
+
+// Cost of one output tile in k-steps: its MMA steps plus a per-pair and per-tile
+// epilogue share.
+int64_t tile_cost(int64_t ksteps, int pairs) { return ksteps + 2 * (int64_t)pairs + 2; }
+
 }  // namespace
 
 // Build operand list, packed layout and work items (host; once per plan/precision).
@@ -697,25 +787,23 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
   for (int i = 0; i < (int)ops.size(); ++i)
     for (int t = 0; t < ops[i].row_tiles; ++t)
       for (int kc = 0; kc * PACK_KC < ops[i].k_steps; ++kc) pitems.push_back({i, t, kc});
-  // work items: 128 x 64 tiles, biggest first
-  struct G { int begin, count; int64_t cost; };
+  // work items: 128 x 64 output tiles, balanced over the persistent CTAs
   std::vector<std::pair<int64_t, WorkItem>> tmp;
   for (size_t i = 0; i < pairs.size();) {
     size_t j = i;
-    int64_t ksum = 0;
+    int64_t ksteps = 0;
     while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) {
-      ksum += ((pairs[j].K + BK - 1) / BK) * BK;
+      ksteps += (pairs[j].K + BK - 1) / BK;
       ++j;
     }
     const PairDesc& p = pairs[i];
     int mt = (p.M + BM - 1) / BM, nt = (p.N + BN - 1) / BN;
     for (int a = 0; a < mt; ++a)
-      for (int b = 0; b < nt; ++b) tmp.push_back({ksum, WorkItem{p.group, (int)i, (int)(j - i), a, b}});
+      for (int b = 0; b < nt; ++b)
+        tmp.push_back({tile_cost(ksteps, (int)(j - i)), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
     i = j;
   }
-  std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
-  std::vector<WorkItem> items;
-  for (auto& t : tmp) items.push_back(t.second);
+  const std::vector<WorkItem> items = balance_items(std::move(tmp), h->num_sms);
   // upload
   auto up = [&](void** dst, const void* src, size_t bytes) -> nd_status {
     ND_CUDA(h, cudaMalloc(dst, std::max<size_t>(bytes, 16)));
@@ -819,15 +907,21 @@ nd_status nd_split_layout_into(nd_handle h, ExecCache& c, const std::vector<Pair
   for (int i = 0; i < (int)ops.size(); ++i)
     for (int t = 0; t < ops[i].row_tiles; ++t)
       for (int kc = 0; kc * PACK_KC < ops[i].k_steps; ++kc) pitems.push_back({i, t, kc});
-  std::vector<WorkItem> items;
+  std::vector<std::pair<int64_t, WorkItem>> tmp;
   for (size_t i = 0; i < pairs.size();) {
     size_t j = i;
-    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) ++j;
+    int64_t ksteps = 0;
+    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) {
+      ksteps += (pairs[j].K + BK - 1) / BK;
+      ++j;
+    }
     const PairDesc& p = pairs[i];
     for (int a = 0; a < (p.M + BM - 1) / BM; ++a)
-      for (int b = 0; b < (p.N + BN - 1) / BN; ++b) items.push_back(WorkItem{p.group, (int)i, (int)(j - i), a, b});
+      for (int b = 0; b < (p.N + BN - 1) / BN; ++b)
+        tmp.push_back({tile_cost(ksteps, (int)(j - i)), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
     i = j;
   }
+  const std::vector<WorkItem> items = balance_items(std::move(tmp), h->num_sms);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t o_pairs = 0;
   const size_t o_items = al(o_pairs + pairs.size() * sizeof(PairDesc));

@@ -114,6 +114,22 @@ def test_ozaki_adversarial_digits(nd):
     assert odense.rel_frobenius_error(out, ref) <= 2.0 ** -36
 
 
+@pytest.mark.parametrize("slices,tol", [(3, 1e-5), (4, 1e-8), (5, 1e-10), (6, 1e-10)])
+def test_ozaki_slice_counts(nd, slices, tol):
+    """Every slice count the library accepts (3..6): each lays its levels into the
+    [L2 | L3 | T4 | T5+] accumulator slot with a different MMA schedule (N = 64 r
+    runs per A slice, A-collector reuse for the products that share a slice)."""
+    rng = np.random.default_rng(30 + slices)
+    a, b = rng.standard_normal((300, 700)), rng.standard_normal((700, 200))
+    h = nd.handle(0)
+    h.call("nd_set_ozaki_slices", slices)
+    try:
+        out, ref = _run(nd, a, (1, -1), b, (-1, 2), (1, 2), "ozaki")
+    finally:
+        h.call("nd_set_ozaki_slices", 5)
+    assert odense.rel_frobenius_error(out, ref) <= tol
+
+
 def test_ozaki_wide_dynamic_range(nd):
     rng = np.random.default_rng(8)
     a = rng.standard_normal((200, 300)) * np.exp(rng.uniform(-20, 20, (200, 1)))
