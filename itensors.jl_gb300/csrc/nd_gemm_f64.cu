@@ -244,13 +244,24 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
 namespace {
 constexpr int SK_THREADS = 256, SK_RPT = 2, SK_ROWS = SK_THREADS * SK_RPT, SK_MAXN = 8, SK_MAXK = 32;
 
+constexpr int SK_BATCH = 4;           // pairs staged per round
+
+// Shared staging area of one round: the pairs' descriptors, B blocks and k offsets.
+struct SkStage {
+  PairDesc pd[SK_BATCH];
+  double B[SK_BATCH][SK_MAXK][SK_MAXN];
+  int64_t kA[SK_BATCH][SK_MAXK];
+  int64_t colR[SK_MAXN];
+};
+
 // One row chunk of one group with exactly NN output columns (no predicated FMAs:
-// the FP64 pipe is the bound for these pairs on GB300).
+// the FP64 pipe is the bound for these pairs on GB300).  The pairs of the group are
+// staged SK_BATCH at a time (two barriers per round, not per pair), so the rows of
+// consecutive pairs run back to back and the warps' loads overlap across pairs.
 // MODE (uniform, resolved at compile time so the store path carries no FP64 work):
 // 0: R = acc, 1: R = alpha acc, 2: R = alpha acc + beta R.
 template <int NN, int MODE>
-__device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& wi, PairDesc& pd,
-                                            double (*Bs)[SK_MAXN], int64_t* kA, int64_t* colR) {
+__device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& wi, SkStage& sh) {
   const int tid = threadIdx.x;
   constexpr int PD_VECS = (int)(sizeof(PairDesc) / 16);
   double acc[SK_RPT][NN];
@@ -258,61 +269,72 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
   for (int r = 0; r < SK_RPT; ++r)
 #pragma unroll
     for (int j = 0; j < NN; ++j) acc[r][j] = 0.0;
-  int64_t rrow[SK_RPT] = {};
-  bool rok[SK_RPT];
-  double* Rp = nullptr;
   const int i0 = wi.mt * SK_ROWS + tid;
-  for (int pi = 0; pi < wi.pair_count; ++pi) {
+  for (int p0 = 0; p0 < wi.pair_count; p0 += SK_BATCH) {
+    const int nb = min(SK_BATCH, wi.pair_count - p0);
+    __syncthreads();                            // the previous round is done with the staging area
+    for (int e = tid; e < nb * PD_VECS; e += SK_THREADS)
+      ((int4*)sh.pd)[e] = __ldg((const int4*)(g.pairs + wi.pair_begin + p0) + e);
     __syncthreads();
-    if (tid < PD_VECS) ((int4*)&pd)[tid] = __ldg((const int4*)(g.pairs + wi.pair_begin + pi) + tid);
-    __syncthreads();
-    const int K = pd.K, M = pd.M;
-    const double* B = g.ptrs.B[pd.job] + pd.b_off;
-    if (tid < K * NN) {
-      int k = tid % K, j = tid / K;
-      int64_t ka, kb, cb, cr;
-      mixed_offsets32(pd.ks, k, ka, kb);
-      mixed_offsets32(pd.cols, j, cb, cr);
-      Bs[k][j] = __ldg(B + kb + cb);
+    // B blocks (k, j) and the k offsets of every staged pair, one element per thread
+    for (int e = tid; e < nb * SK_MAXK * SK_MAXN; e += SK_THREADS) {
+      const int q = e / (SK_MAXK * SK_MAXN), k = (e / SK_MAXN) % SK_MAXK, j = e % SK_MAXN;
+      const PairDesc& pd = sh.pd[q];
+      if (k < pd.K && j < NN) {
+        int64_t ka, kb, cb, cr;
+        mixed_offsets32(pd.ks, k, ka, kb);
+        mixed_offsets32(pd.cols, j, cb, cr);
+        sh.B[q][k][j] = __ldg(g.ptrs.B[pd.job] + pd.b_off + kb + cb);
+        if (j == 0) sh.kA[q][k] = ka;
+        if (q == 0 && k == 0) sh.colR[j] = cr;
+      }
     }
-    if (tid < K) { int64_t ka, kb; mixed_offsets32(pd.ks, tid, ka, kb); kA[tid] = ka; }
-    if (tid >= 64 && tid < 64 + NN) { int64_t cb, cr; mixed_offsets32(pd.cols, tid - 64, cb, cr); colR[tid - 64] = cr; }
     __syncthreads();
-    Rp = g.ptrs.R[pd.job] + pd.r_off;
-    const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
-    const double* Ar[SK_RPT];
+    for (int q = 0; q < nb; ++q) {
+      const PairDesc& pd = sh.pd[q];
+      const int K = pd.K, M = pd.M;
+      const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
+      const double* Ar[SK_RPT];
+      bool rok[SK_RPT];
 #pragma unroll
-    for (int r = 0; r < SK_RPT; ++r) {
-      const int i = i0 + r * SK_THREADS;
-      rok[r] = i < M;
-      int64_t ra = 0, rr = 0;
-      if (rok[r]) mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
-      rrow[r] = rr;
-      Ar[r] = Ab + ra;
-    }
-    for (int k0 = 0; k0 < K; k0 += 4) {
-      double av[4][SK_RPT];
+      for (int r = 0; r < SK_RPT; ++r) {
+        const int i = i0 + r * SK_THREADS;
+        rok[r] = i < M;
+        int64_t ra = 0, rr = 0;
+        if (rok[r]) mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
+        Ar[r] = Ab + ra;
+      }
+      for (int k0 = 0; k0 < K; k0 += 4) {
+        double av[4][SK_RPT];
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
+        for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-        for (int r = 0; r < SK_RPT; ++r)
-          av[kk][r] = (k0 + kk < K && rok[r]) ? __ldg(Ar[r] + kA[k0 + kk]) : 0.0;
+          for (int r = 0; r < SK_RPT; ++r)
+            av[kk][r] = (k0 + kk < K && rok[r]) ? __ldg(Ar[r] + sh.kA[q][k0 + kk]) : 0.0;
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        if (k0 + kk >= K) break;
+        for (int kk = 0; kk < 4; ++kk) {
+          if (k0 + kk >= K) break;
 #pragma unroll
-        for (int r = 0; r < SK_RPT; ++r)
+          for (int r = 0; r < SK_RPT; ++r)
 #pragma unroll
-          for (int j = 0; j < NN; ++j) acc[r][j] = fma(av[kk][r], Bs[k0 + kk][j], acc[r][j]);
+            for (int j = 0; j < NN; ++j) acc[r][j] = fma(av[kk][r], sh.B[q][k0 + kk][j], acc[r][j]);
+        }
       }
     }
   }
+  // every pair of the group writes the same output block: its row map comes from pair 0
+  // of the last round (staged descriptors share the output block's row strides)
+  const PairDesc& pd = sh.pd[0];
+  double* Rp = g.ptrs.R[pd.job] + pd.r_off;
 #pragma unroll
   for (int r = 0; r < SK_RPT; ++r) {
-    if (!rok[r]) continue;
+    const int i = i0 + r * SK_THREADS;
+    if (i >= pd.M) continue;
+    int64_t ra, rrow;
+    mixed_offsets32(pd.rows, (uint32_t)i, ra, rrow);
 #pragma unroll
     for (int j = 0; j < NN; ++j) {
-      double* dst = Rp + rrow[r] + colR[j];
+      double* dst = Rp + rrow + sh.colR[j];
       const double v = acc[r][j];
       if (MODE == 0) *dst = v;
       else if (MODE == 1) *dst = g.alpha * v;
@@ -322,19 +344,17 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
 }
 
 __global__ void __launch_bounds__(SK_THREADS, 4) gemm_skinny_f64(GemmArgs g) {
-  __shared__ double Bs[SK_MAXK][SK_MAXN];
-  __shared__ int64_t kA[SK_MAXK], colR[SK_MAXN];
-  __shared__ __align__(16) PairDesc pd;
+  __shared__ __align__(16) SkStage sh;
   static_assert(sizeof(PairDesc) % 16 == 0, "PairDesc must be a multiple of 16 bytes");
   for (int it = blockIdx.x; it < g.nitems; it += gridDim.x) {
     const WorkItem wi = g.items[it];
     const int N = __ldg(&g.pairs[wi.pair_begin].N);
     const int mode = g.bmode ? 2 : (g.amode ? 1 : 0);
-#define ND_SKINNY_CASE(NN)                                              \
-  case NN:                                                              \
-    if (mode == 0) skinny_item<NN, 0>(g, wi, pd, Bs, kA, colR);         \
-    else if (mode == 1) skinny_item<NN, 1>(g, wi, pd, Bs, kA, colR);    \
-    else skinny_item<NN, 2>(g, wi, pd, Bs, kA, colR);                   \
+#define ND_SKINNY_CASE(NN)                              \
+  case NN:                                              \
+    if (mode == 0) skinny_item<NN, 0>(g, wi, sh);       \
+    else if (mode == 1) skinny_item<NN, 1>(g, wi, sh);  \
+    else skinny_item<NN, 2>(g, wi, sh);                 \
     break;
     switch (N) {
       ND_SKINNY_CASE(1)
@@ -345,9 +365,9 @@ __global__ void __launch_bounds__(SK_THREADS, 4) gemm_skinny_f64(GemmArgs g) {
       ND_SKINNY_CASE(6)
       ND_SKINNY_CASE(7)
       default:
-        if (mode == 0) skinny_item<8, 0>(g, wi, pd, Bs, kA, colR);
-        else if (mode == 1) skinny_item<8, 1>(g, wi, pd, Bs, kA, colR);
-        else skinny_item<8, 2>(g, wi, pd, Bs, kA, colR);
+        if (mode == 0) skinny_item<8, 0>(g, wi, sh);
+        else if (mode == 1) skinny_item<8, 1>(g, wi, sh);
+        else skinny_item<8, 2>(g, wi, sh);
         break;
     }
 #undef ND_SKINNY_CASE

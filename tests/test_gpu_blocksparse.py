@@ -133,3 +133,15 @@ def test_plan_rejects_mismatched_blocks(nd):
     with pytest.raises(nd.NDError):
         nd.get_plan(nd.BlockSparseTensor.from_oracle(A), (1, -1), nd.BlockSparseTensor.from_oracle(B), (-1, 2),
                     (1, 2))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_skinny_group_with_many_pairs(nd, precision):
+    """One output block fed by 12 skinny pairs (K = 2 each, N = 3): more pairs than one
+    staging round of the skinny kernel holds, operands spread over 2^+-40."""
+    rng = np.random.default_rng(9)
+    A = obs.random_blocksparse(rng, [(5000,), (2,) * 12], [(1, k) for k in range(1, 13)])
+    B = obs.random_blocksparse(rng, [(2,) * 12, (3,)], [(k, 1) for k in range(1, 13)])
+    A.data[:] *= 2.0 ** rng.integers(-40, 40, A.data.shape)
+    p = _check(nd, A, (1, -1), B, (-1, 2), (1, 2), precision)
+    assert (p.npairs, p.nblocksR) == (12, 1)

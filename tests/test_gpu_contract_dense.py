@@ -193,3 +193,35 @@ def test_dense_state_reuse_and_capture(nd, precision):
         h.call("nd_graph_end", C.byref(ge))
         if ge.value:
             h.lib.nd_graph_destroy(ge)
+
+
+@pytest.mark.parametrize("precision", ["ozaki", "bf16x3"])
+@pytest.mark.parametrize("alpha,beta", [(1.0, 0.0), (2.0, 0.0), (-0.5, 2.0)])
+def test_skinny_split_precision_dynamic_range(nd, precision, alpha, beta):
+    """Skinny pairs (N <= 8, K <= 32) in the split precisions run on the FP64 CUDA-core
+    kernel: rows spanning 2^-300 .. 2^300, a B column of tiny values, zeros, and the
+    alpha / beta store modes, held row by row to 1e-12."""
+    rng = np.random.default_rng(40)
+    a = rng.standard_normal((3000, 7, 3)) * 2.0 ** rng.integers(-300, 300, (3000, 1, 1))
+    a[::17, 2, :] = 0.0
+    b = rng.standard_normal((3, 7, 5))
+    b[:, :, 4] *= 2.0 ** -200
+    r0 = rng.standard_normal((3000, 5))
+    out, ref = _run(nd, a, (1, -1, -2), b, (-2, -1, 2), (1, 2), precision, alpha, beta, r0)
+    # per output row: the row scales differ by up to 2^600, so compare row by row
+    num = np.linalg.norm(out - ref, axis=1)
+    den = np.linalg.norm(ref, axis=1) + 1e-300
+    assert np.max(num / den) <= 1e-12
+
+
+@pytest.mark.parametrize("k", [4, 20])
+def test_skinny_propagates_inf_nan(nd, k):
+    """Inf and NaN operands of skinny pairs propagate as in FP64 BLAS."""
+    a = np.ones((600, k))
+    a[3, 1], a[7, 2] = np.nan, np.inf
+    b = np.ones((k, 3))
+    out, ref = _run(nd, a, (1, -1), b, (-1, 2), (1, 2), "ozaki")
+    assert np.isnan(out[3]).all() and np.isinf(out[7]).all()
+    mask = np.ones(600, bool)
+    mask[[3, 7]] = False
+    np.testing.assert_allclose(out[mask], ref[mask], rtol=1e-15)
