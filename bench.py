@@ -192,8 +192,8 @@ def matvec_flops_oracle(net, steps_labels):
 
 
 # DRAM traffic of split_gemm per launch from one ncu capture of this workload at S = 5
-# (dram__bytes_read.sum + dram__bytes_write.sum: L*psi 361.3 MB, *R 647.5 MB; mean of the two)
-NCU_SPLIT_GEMM_TRAFFIC = {4096: 504.4e6}
+# (dram__bytes_read.sum + dram__bytes_write.sum: L*psi 361.6 MB, *R 642.4 MB; mean of the two)
+NCU_SPLIT_GEMM_TRAFFIC = {4096: 502.0e6}
 
 
 def split_routed_flops(shapes):
