@@ -242,7 +242,7 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
 // pair staged in shared memory, the group's pairs accumulated in registers.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int SK_THREADS = 256, SK_RPT = 2, SK_ROWS = SK_THREADS * SK_RPT, SK_MAXN = 8, SK_MAXK = 32;
+constexpr int SK_THREADS = 256, SK_ROWS = 8 * SK_THREADS, SK_MAXN = 8, SK_MAXK = 32;
 
 constexpr int SK_BATCH = 4;           // pairs staged per round
 
@@ -254,91 +254,99 @@ struct SkStage {
   int64_t colR[SK_MAXN];
 };
 
-// One row chunk of one group with exactly NN output columns (no predicated FMAs:
-// the FP64 pipe is the bound for these pairs on GB300).  The pairs of the group are
-// staged SK_BATCH at a time (two barriers per round, not per pair), so the rows of
-// consecutive pairs run back to back and the warps' loads overlap across pairs.
-// MODE (uniform, resolved at compile time so the store path carries no FP64 work):
-// 0: R = acc, 1: R = alpha acc, 2: R = alpha acc + beta R.
-template <int NN, int MODE>
+// One item = SK_ROWS rows of one group with exactly NN output columns (no predicated
+// FMAs: the FP64 pipe is the bound for these pairs on GB300).  These contractions are
+// bound by load latency (a few loads per output), so a thread keeps RPT rows in
+// flight: 8 for NN = 1 (one pass), 4 for NN <= 3, 2 above; a pass loads KC = 8 / RPT
+// operands per row at once.  The pairs of the group are staged SK_BATCH at a time (two
+// barriers per round, not per pair); when they fit one round they are staged once per
+// item.  MODE (uniform, resolved at compile time so the store path carries no FP64
+// work): 0: R = acc, 1: R = alpha acc, 2: R = alpha acc + beta R.
+template <int NN, int MODE, int RPT>
 __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& wi, SkStage& sh) {
   const int tid = threadIdx.x;
   constexpr int PD_VECS = (int)(sizeof(PairDesc) / 16);
-  double acc[SK_RPT][NN];
+  constexpr int KC = RPT >= 8 ? 1 : 8 / RPT;
+  const bool whole = wi.pair_count <= SK_BATCH;
+  for (int pass = 0; pass < SK_ROWS / (SK_THREADS * RPT); ++pass) {
+    const int i0 = wi.mt * SK_ROWS + pass * SK_THREADS * RPT + tid;
+    double acc[RPT][NN];
 #pragma unroll
-  for (int r = 0; r < SK_RPT; ++r)
+    for (int r = 0; r < RPT; ++r)
 #pragma unroll
-    for (int j = 0; j < NN; ++j) acc[r][j] = 0.0;
-  const int i0 = wi.mt * SK_ROWS + tid;
-  for (int p0 = 0; p0 < wi.pair_count; p0 += SK_BATCH) {
-    const int nb = min(SK_BATCH, wi.pair_count - p0);
-    __syncthreads();                            // the previous round is done with the staging area
-    for (int e = tid; e < nb * PD_VECS; e += SK_THREADS)
-      ((int4*)sh.pd)[e] = __ldg((const int4*)(g.pairs + wi.pair_begin + p0) + e);
-    __syncthreads();
-    // B blocks (k, j) and the k offsets of every staged pair, one element per thread
-    for (int e = tid; e < nb * SK_MAXK * SK_MAXN; e += SK_THREADS) {
-      const int q = e / (SK_MAXK * SK_MAXN), k = (e / SK_MAXN) % SK_MAXK, j = e % SK_MAXN;
-      const PairDesc& pd = sh.pd[q];
-      if (k < pd.K && j < NN) {
-        int64_t ka, kb, cb, cr;
-        mixed_offsets32(pd.ks, k, ka, kb);
-        mixed_offsets32(pd.cols, j, cb, cr);
-        sh.B[q][k][j] = __ldg(g.ptrs.B[pd.job] + pd.b_off + kb + cb);
-        if (j == 0) sh.kA[q][k] = ka;
-        if (q == 0 && k == 0) sh.colR[j] = cr;
+      for (int j = 0; j < NN; ++j) acc[r][j] = 0.0;
+    for (int p0 = 0; p0 < wi.pair_count; p0 += SK_BATCH) {
+      const int nb = min(SK_BATCH, wi.pair_count - p0);
+      if (!whole || pass == 0) {
+        __syncthreads();                          // the previous round is done with the staging area
+        for (int e = tid; e < nb * PD_VECS; e += SK_THREADS)
+          ((int4*)sh.pd)[e] = __ldg((const int4*)(g.pairs + wi.pair_begin + p0) + e);
+        __syncthreads();
+        // B blocks (k, j) and the k offsets of every staged pair, one element per thread
+        for (int e = tid; e < nb * SK_MAXK * SK_MAXN; e += SK_THREADS) {
+          const int q = e / (SK_MAXK * SK_MAXN), k = (e / SK_MAXN) % SK_MAXK, j = e % SK_MAXN;
+          const PairDesc& pd = sh.pd[q];
+          if (k < pd.K && j < NN) {
+            int64_t ka, kb, cb, cr;
+            mixed_offsets32(pd.ks, k, ka, kb);
+            mixed_offsets32(pd.cols, j, cb, cr);
+            sh.B[q][k][j] = __ldg(g.ptrs.B[pd.job] + pd.b_off + kb + cb);
+            if (j == 0) sh.kA[q][k] = ka;
+            if (q == 0 && k == 0) sh.colR[j] = cr;
+          }
+        }
+        __syncthreads();
       }
-    }
-    __syncthreads();
-    for (int q = 0; q < nb; ++q) {
-      const PairDesc& pd = sh.pd[q];
-      const int K = pd.K, M = pd.M;
-      const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
-      const double* Ar[SK_RPT];
-      bool rok[SK_RPT];
+      for (int q = 0; q < nb; ++q) {
+        const PairDesc& pd = sh.pd[q];
+        const int K = pd.K, M = pd.M;
+        const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
+        const double* Ar[RPT];
+        bool rok[RPT];
 #pragma unroll
-      for (int r = 0; r < SK_RPT; ++r) {
-        const int i = i0 + r * SK_THREADS;
-        rok[r] = i < M;
-        int64_t ra = 0, rr = 0;
-        if (rok[r]) mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
-        Ar[r] = Ab + ra;
-      }
-      for (int k0 = 0; k0 < K; k0 += 4) {
-        double av[4][SK_RPT];
+        for (int r = 0; r < RPT; ++r) {
+          const int i = i0 + r * SK_THREADS;
+          rok[r] = i < M;
+          int64_t ra = 0, rr = 0;
+          if (rok[r]) mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
+          Ar[r] = Ab + ra;
+        }
+        for (int k0 = 0; k0 < K; k0 += KC) {
+          double av[KC][RPT];
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk)
+          for (int kk = 0; kk < KC; ++kk)
 #pragma unroll
-          for (int r = 0; r < SK_RPT; ++r)
-            av[kk][r] = (k0 + kk < K && rok[r]) ? __ldg(Ar[r] + sh.kA[q][k0 + kk]) : 0.0;
+            for (int r = 0; r < RPT; ++r)
+              av[kk][r] = (k0 + kk < K && rok[r]) ? __ldg(Ar[r] + sh.kA[q][k0 + kk]) : 0.0;
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          if (k0 + kk >= K) break;
+          for (int kk = 0; kk < KC; ++kk) {
+            if (k0 + kk >= K) break;
 #pragma unroll
-          for (int r = 0; r < SK_RPT; ++r)
+            for (int r = 0; r < RPT; ++r)
 #pragma unroll
-            for (int j = 0; j < NN; ++j) acc[r][j] = fma(av[kk][r], sh.B[q][k0 + kk][j], acc[r][j]);
+              for (int j = 0; j < NN; ++j) acc[r][j] = fma(av[kk][r], sh.B[q][k0 + kk][j], acc[r][j]);
+          }
         }
       }
     }
-  }
-  // every pair of the group writes the same output block: its row map comes from pair 0
-  // of the last round (staged descriptors share the output block's row strides)
-  const PairDesc& pd = sh.pd[0];
-  double* Rp = g.ptrs.R[pd.job] + pd.r_off;
+    // every pair of the group writes the same output block: its row map comes from pair 0
+    // of the last round (staged descriptors share the output block's row strides)
+    const PairDesc& pd = sh.pd[0];
+    double* Rp = g.ptrs.R[pd.job] + pd.r_off;
 #pragma unroll
-  for (int r = 0; r < SK_RPT; ++r) {
-    const int i = i0 + r * SK_THREADS;
-    if (i >= pd.M) continue;
-    int64_t ra, rrow;
-    mixed_offsets32(pd.rows, (uint32_t)i, ra, rrow);
+    for (int r = 0; r < RPT; ++r) {
+      const int i = i0 + r * SK_THREADS;
+      if (i >= pd.M) continue;
+      int64_t ra, rrow;
+      mixed_offsets32(pd.rows, (uint32_t)i, ra, rrow);
 #pragma unroll
-    for (int j = 0; j < NN; ++j) {
-      double* dst = Rp + rrow + sh.colR[j];
-      const double v = acc[r][j];
-      if (MODE == 0) *dst = v;
-      else if (MODE == 1) *dst = g.alpha * v;
-      else *dst = g.alpha * v + g.beta * *dst;
+      for (int j = 0; j < NN; ++j) {
+        double* dst = Rp + rrow + sh.colR[j];
+        const double v = acc[r][j];
+        if (MODE == 0) *dst = v;
+        else if (MODE == 1) *dst = g.alpha * v;
+        else *dst = g.alpha * v + g.beta * *dst;
+      }
     }
   }
 }
@@ -350,11 +358,11 @@ __global__ void __launch_bounds__(SK_THREADS, 4) gemm_skinny_f64(GemmArgs g) {
     const WorkItem wi = g.items[it];
     const int N = __ldg(&g.pairs[wi.pair_begin].N);
     const int mode = g.bmode ? 2 : (g.amode ? 1 : 0);
-#define ND_SKINNY_CASE(NN)                              \
-  case NN:                                              \
-    if (mode == 0) skinny_item<NN, 0>(g, wi, sh);       \
-    else if (mode == 1) skinny_item<NN, 1>(g, wi, sh);  \
-    else skinny_item<NN, 2>(g, wi, sh);                 \
+#define ND_SKINNY_CASE(NN)                                               \
+  case NN:                                                               \
+    if (mode == 0) skinny_item<NN, 0, (NN == 1 ? 8 : NN <= 3 ? 4 : 2)>(g, wi, sh);     \
+    else if (mode == 1) skinny_item<NN, 1, (NN == 1 ? 8 : NN <= 3 ? 4 : 2)>(g, wi, sh);\
+    else skinny_item<NN, 2, (NN == 1 ? 8 : NN <= 3 ? 4 : 2)>(g, wi, sh);               \
     break;
     switch (N) {
       ND_SKINNY_CASE(1)
@@ -365,9 +373,9 @@ __global__ void __launch_bounds__(SK_THREADS, 4) gemm_skinny_f64(GemmArgs g) {
       ND_SKINNY_CASE(6)
       ND_SKINNY_CASE(7)
       default:
-        if (mode == 0) skinny_item<8, 0>(g, wi, sh);
-        else if (mode == 1) skinny_item<8, 1>(g, wi, sh);
-        else skinny_item<8, 2>(g, wi, sh);
+        if (mode == 0) skinny_item<8, 0, 2>(g, wi, sh);
+        else if (mode == 1) skinny_item<8, 1, 2>(g, wi, sh);
+        else skinny_item<8, 2, 2>(g, wi, sh);
         break;
     }
 #undef ND_SKINNY_CASE
