@@ -268,7 +268,9 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
   constexpr int PD_VECS = (int)(sizeof(PairDesc) / 16);
   constexpr int KC = RPT >= 8 ? 1 : 8 / RPT;
   const bool whole = wi.pair_count <= SK_BATCH;
+  const int M = __ldg(&g.pairs[wi.pair_begin].M);   // every pair of the group has the output's rows
   for (int pass = 0; pass < SK_ROWS / (SK_THREADS * RPT); ++pass) {
+    if (wi.mt * SK_ROWS + pass * SK_THREADS * RPT >= M) break;   // uniform: no rows left in this item
     const int i0 = wi.mt * SK_ROWS + pass * SK_THREADS * RPT + tid;
     double acc[RPT][NN];
 #pragma unroll
@@ -299,7 +301,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
       }
       for (int q = 0; q < nb; ++q) {
         const PairDesc& pd = sh.pd[q];
-        const int K = pd.K, M = pd.M;
+        const int K = pd.K;
         const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
         const double* Ar[RPT];
         bool rok[RPT];
