@@ -336,11 +336,23 @@ def run_ours(args):
     out_host = torch.empty(outs[-1].nnz, dtype=torch.float64).pin_memory()
     d2h = int(out_host.numel()) * 8
 
+    side = torch.cuda.Stream()
+
     def e2e_step(cold_plans=False):
+        # R is needed by the last contraction only: its upload runs on a side stream under
+        # the first three contractions (every copy stays inside the timed step)
+        cur = torch.cuda.current_stream()
         D = {k: nd.BlockSparseTensor(G[k].inds, G[k].blocks, G[k].offsets,
-                                     pinned[k].to(dev, non_blocking=True)) for k in pinned}
+                                     pinned[k].to(dev, non_blocking=True)) for k in ("L", "psi", "W1", "W2")}
+        side.wait_stream(cur)                 # after the other uploads: R shares the link with compute only
+        with torch.cuda.stream(side):
+            r_dev = pinned["R"].to(dev, non_blocking=True)
         x = D["L"]
         for (a, b, c), key in zip(steps_labels, ("psi", "W1", "W2", "R")):
+            if key == "R":
+                cur.wait_stream(side)
+                r_dev.record_stream(cur)
+                D["R"] = nd.BlockSparseTensor(G["R"].inds, G["R"].blocks, G["R"].offsets, r_dev)
             if cold_plans:
                 p = nd.ContractionPlan(x, a, D[key], b, c)
                 x = nd.contract_blocksparse(x, a, D[key], b, c, precision=args.precision, plan=p)
@@ -377,8 +389,9 @@ def run_ours(args):
             "roofline": roof,
             "e2e": {"value": round(e2e_v, 2), "unit": "GFLOP/s", "ms_per_step": round(e2e_ms, 3),
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "note": "public contract() per step: pinned-host inputs copied in, block plans from the "
-                            "structure-keyed plan cache (built by the untimed first call), result copied back",
+                    "note": "public contract() per step: pinned-host inputs copied in (R on a side stream under the "
+                            "first three contractions), block plans from the structure-keyed plan cache (built by "
+                            "the untimed first call), result copied back",
                     "plans_rebuilt_each_step": {"value": round(ws * flops / (e2e_cold_ms * 1e-3) / 1e9, 2),
                                                 "ms_per_step": round(e2e_cold_ms, 3)}},
             "gpu_launches": launches,
