@@ -35,7 +35,7 @@ enum {
   ND_ERR_NOCONV = 3,       /* an SVD did not converge within the sweep limit    */
   ND_ERR_TIMEOUT = 4,      /* a device-side wait ran past its iteration limit   */
   ND_ERR_CUDA = 5,         /* a CUDA runtime/driver call failed                 */
-  ND_ERR_UNSUPPORTED = 6,  /* shape/feature outside what this build supports    */
+  ND_ERR_UNSUPPORTED = 6,  /* shape/feature outside what the library supports  */
   ND_ERR_NONFINITE = 7     /* split-precision GEMM met Inf/NaN input            */
 };
 

@@ -1,7 +1,7 @@
 """Write tests/golden/reference_kats.json.
 
-The reference (ITensors.jl / NDTensors.jl, Julia) cannot run in this build
-environment, and its test suite stores no numeric golden vectors for the
+The reference (ITensors.jl / NDTensors.jl, Julia) cannot run here (there is no
+Julia toolchain), and its test suite stores no numeric golden vectors for the
 contraction path.  Its known-answer tests are literals inside the Julia test
 files; this script records those literals, each with the file:line it comes
 from, so the oracle can be pinned against them.  Only the reference's stated
