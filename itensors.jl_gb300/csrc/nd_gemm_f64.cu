@@ -246,6 +246,31 @@ constexpr int SK_THREADS = 256, SK_ROWS = 8 * SK_THREADS, SK_MAXN = 8, SK_MAXK =
 
 constexpr int SK_BATCH = 4;           // pairs staged per round
 
+// Row index -> (A offset, R offset).  Row maps of at most two dimensions (the MPO
+// contractions' blocks) take one multiply-high division and four multiply-adds with
+// the map's parameters held in registers; longer maps take mixed_offsets32.
+struct SkRowMap {
+  bool fast;
+  uint32_t d0, mul0, shr0;
+  int64_t a0, a1, b0, b1;
+  __device__ __forceinline__ void load(const Mixed& m) {
+    fast = m.n >= 1 && m.n <= 2 && m.mul[0] != 0u;
+    d0 = (uint32_t)m.dim[0]; mul0 = m.mul[0]; shr0 = m.shr[0];
+    a0 = m.st0[0]; b0 = m.st1[0];
+    a1 = m.n > 1 ? m.st0[1] : 0; b1 = m.n > 1 ? m.st1[1] : 0;
+  }
+  __device__ __forceinline__ void offsets(const Mixed& m, uint32_t i, int64_t& ra, int64_t& rr) const {
+    if (fast) {
+      const uint32_t q = (__umulhi(i, mul0) + i) >> shr0;   // i / d0 (q = 0 for one-dimensional maps)
+      const int64_t r = (int64_t)(i - q * d0);
+      ra = r * a0 + (int64_t)q * a1;
+      rr = r * b0 + (int64_t)q * b1;
+    } else {
+      mixed_offsets32(m, i, ra, rr);
+    }
+  }
+};
+
 // Shared staging area of one round: the pairs' descriptors, B blocks and k offsets.
 struct SkStage {
   PairDesc pd[SK_BATCH];
@@ -305,12 +330,14 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
         const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
         const double* Ar[RPT];
         bool rok[RPT];
+        SkRowMap rm;
+        rm.load(pd.rows);
 #pragma unroll
         for (int r = 0; r < RPT; ++r) {
           const int i = i0 + r * SK_THREADS;
           rok[r] = i < M;
           int64_t ra = 0, rr = 0;
-          if (rok[r]) mixed_offsets32(pd.rows, (uint32_t)i, ra, rr);
+          if (rok[r]) rm.offsets(pd.rows, (uint32_t)i, ra, rr);
           Ar[r] = Ab + ra;
         }
         for (int k0 = 0; k0 < K; k0 += KC) {
@@ -335,12 +362,14 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
     // of the last round (staged descriptors share the output block's row strides)
     const PairDesc& pd = sh.pd[0];
     double* Rp = g.ptrs.R[pd.job] + pd.r_off;
+    SkRowMap rm;
+    rm.load(pd.rows);
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       const int i = i0 + r * SK_THREADS;
       if (i >= pd.M) continue;
       int64_t ra, rrow;
-      mixed_offsets32(pd.rows, (uint32_t)i, ra, rrow);
+      rm.offsets(pd.rows, (uint32_t)i, ra, rrow);
 #pragma unroll
       for (int j = 0; j < NN; ++j) {
         double* dst = Rp + rrow + sh.colR[j];
