@@ -247,24 +247,27 @@ constexpr int SK_THREADS = 256, SK_ROWS = 8 * SK_THREADS, SK_MAXN = 8, SK_MAXK =
 constexpr int SK_BATCH = 4;           // pairs staged per round
 
 // Row index -> (A offset, R offset).  Row maps of at most two dimensions (the MPO
-// contractions' blocks) take one multiply-high division and four multiply-adds with
-// the map's parameters held in registers; longer maps take mixed_offsets32.
+// contractions' blocks) whose A and output blocks hold fewer than 2^31 elements take
+// one multiply-high division and four 32-bit multiply-adds with the map's parameters
+// held in registers; other maps take mixed_offsets32.
 struct SkRowMap {
   bool fast;
   uint32_t d0, mul0, shr0;
-  int64_t a0, a1, b0, b1;
-  __device__ __forceinline__ void load(const Mixed& m) {
-    fast = m.n >= 1 && m.n <= 2 && m.mul[0] != 0u;
+  int32_t a0, a1, b0, b1;
+  __device__ __forceinline__ void load(const PairDesc& pd) {
+    const Mixed& m = pd.rows;
+    fast = m.n >= 1 && m.n <= 2 && m.mul[0] != 0u && (int64_t)pd.M * pd.K < (1ll << 31) &&
+           (int64_t)pd.M * pd.N < (1ll << 31);
     d0 = (uint32_t)m.dim[0]; mul0 = m.mul[0]; shr0 = m.shr[0];
-    a0 = m.st0[0]; b0 = m.st1[0];
-    a1 = m.n > 1 ? m.st0[1] : 0; b1 = m.n > 1 ? m.st1[1] : 0;
+    a0 = (int32_t)m.st0[0]; b0 = (int32_t)m.st1[0];
+    a1 = m.n > 1 ? (int32_t)m.st0[1] : 0; b1 = m.n > 1 ? (int32_t)m.st1[1] : 0;
   }
   __device__ __forceinline__ void offsets(const Mixed& m, uint32_t i, int64_t& ra, int64_t& rr) const {
     if (fast) {
       const uint32_t q = (__umulhi(i, mul0) + i) >> shr0;   // i / d0 (q = 0 for one-dimensional maps)
-      const int64_t r = (int64_t)(i - q * d0);
-      ra = r * a0 + (int64_t)q * a1;
-      rr = r * b0 + (int64_t)q * b1;
+      const int32_t r = (int32_t)(i - q * d0);
+      ra = r * a0 + (int32_t)q * a1;
+      rr = r * b0 + (int32_t)q * b1;
     } else {
       mixed_offsets32(m, i, ra, rr);
     }
@@ -331,7 +334,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
         const double* Ar[RPT];
         bool rok[RPT];
         SkRowMap rm;
-        rm.load(pd.rows);
+        rm.load(pd);
 #pragma unroll
         for (int r = 0; r < RPT; ++r) {
           const int i = i0 + r * SK_THREADS;
@@ -363,7 +366,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
     const PairDesc& pd = sh.pd[0];
     double* Rp = g.ptrs.R[pd.job] + pd.r_off;
     SkRowMap rm;
-    rm.load(pd.rows);
+    rm.load(pd);
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
       const int i = i0 + r * SK_THREADS;
