@@ -250,6 +250,14 @@ struct JobPtrs {
   double* R[2];
 };
 
+#ifdef __CUDACC__
+// Base pointers of a job's operands as selects: indexing a kernel-parameter array with
+// a run-time value makes the compiler copy the parameters to local memory.
+__device__ __forceinline__ const double* job_A(const JobPtrs& p, int j) { return j ? p.A[1] : p.A[0]; }
+__device__ __forceinline__ const double* job_B(const JobPtrs& p, int j) { return j ? p.B[1] : p.B[0]; }
+__device__ __forceinline__ double* job_R(const JobPtrs& p, int j) { return j ? p.R[1] : p.R[0]; }
+#endif
+
 nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkItem* d_items,
                              int nitems, const JobPtrs& ptrs, double alpha, double beta, double* ws,
                              const ReduceItem* d_red, int nred);

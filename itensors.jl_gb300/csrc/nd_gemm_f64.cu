@@ -79,9 +79,9 @@ __global__ void __launch_bounds__(128) gemm_f64_grouped(GemmArgs g) {
         if (n0 + c < N) mixed_offsets32(pd.cols, (uint32_t)(n0 + c), o0, o1);
         colB[c] = o0; colR[c] = o1;
       }
-      const double* A = g.ptrs.A[pd.job] + pd.a_off;
-      const double* B = g.ptrs.B[pd.job] + pd.b_off;
-      Rp = g.ptrs.R[pd.job];
+      const double* A = job_A(g.ptrs, pd.job) + pd.a_off;
+      const double* B = job_B(g.ptrs, pd.job) + pd.b_off;
+      Rp = job_R(g.ptrs, pd.job);
       r_base = pd.r_off;
       const bool a_rows_contig = pd.rows.n > 0 && pd.rows.st0[0] == 1;
       const bool b_cols_contig = pd.cols.n > 0 && pd.cols.st0[0] == 1;
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256) splitk_reduce(const PairDesc* pairs, cons
     colR[j] = r;
   }
   __syncthreads();
-  double* R = ptrs.R[pd.job] + pd.r_off;
+  double* R = job_R(ptrs, pd.job) + pd.r_off;
   for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
     const int m = e % BM, n = e / BM;
     if (m0 + m >= pd.M || n0 + n >= pd.N) continue;
@@ -320,7 +320,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
             int64_t ka, kb, cb, cr;
             mixed_offsets32(pd.ks, k, ka, kb);
             mixed_offsets32(pd.cols, j, cb, cr);
-            sh.B[q][k][j] = __ldg(g.ptrs.B[pd.job] + pd.b_off + kb + cb);
+            sh.B[q][k][j] = __ldg(job_B(g.ptrs, pd.job) + pd.b_off + kb + cb);
             if (j == 0) sh.kA[q][k] = ka;
             if (q == 0 && k == 0) sh.colR[j] = cr;
           }
@@ -330,7 +330,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
       for (int q = 0; q < nb; ++q) {
         const PairDesc& pd = sh.pd[q];
         const int K = pd.K;
-        const double* Ab = g.ptrs.A[pd.job] + pd.a_off;
+        const double* Ab = job_A(g.ptrs, pd.job) + pd.a_off;
         const double* Ar[RPT];
         bool rok[RPT];
         SkRowMap rm;
@@ -364,7 +364,7 @@ __device__ __forceinline__ void skinny_item(const GemmArgs& g, const WorkItem& w
     // every pair of the group writes the same output block: its row map comes from pair 0
     // of the last round (staged descriptors share the output block's row strides)
     const PairDesc& pd = sh.pd[0];
-    double* Rp = g.ptrs.R[pd.job] + pd.r_off;
+    double* Rp = job_R(g.ptrs, pd.job) + pd.r_off;
     SkRowMap rm;
     rm.load(pd);
 #pragma unroll

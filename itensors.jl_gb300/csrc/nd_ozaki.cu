@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(256) pack_rowmax(PackArgs2 a) {
     const SplitOp& op = a.ops[pi.op];
     const int ROWS = op.is_b ? BN : BM;
     const int units = ROWS / 64;
-    const double* src = (op.is_b ? a.ptrs.B[op.job] : a.ptrs.A[op.job]) + op.src_off;
+    const double* src = (op.is_b ? job_B(a.ptrs, op.job) : job_A(a.ptrs, op.job)) + op.src_off;
     int ks0, ks1;
     __syncthreads();
     pack_setup(op, pi, ROWS, rowoff, koff, ks0, ks1);
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256) pack_digits(PackArgs2 a) {
     const SplitOp& op = a.ops[pi.op];
     const int ROWS = op.is_b ? BN : BM;
     const int units = ROWS / 64;
-    const double* src = (op.is_b ? a.ptrs.B[op.job] : a.ptrs.A[op.job]) + op.src_off;
+    const double* src = (op.is_b ? job_B(a.ptrs, op.job) : job_A(a.ptrs, op.job)) + op.src_off;
     int ks0, ks1;
     __syncthreads();
     pack_setup(op, pi, ROWS, rowoff, koff, ks0, ks1);
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
         colR_s[etid] = co;
       }
       epi_sync();
-      double* Rb = g.ptrs.R[p0.job] + p0.r_off + roff;
+      double* Rb = job_R(g.ptrs, p0.job) + p0.r_off + roff;
       const int ncols = min(EPI_COLS, p0.N - (wi.nt * BN + cg * EPI_COLS));
       for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
         const PairDesc& pd = g.pairs[wi.pair_begin + pi];
