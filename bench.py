@@ -124,19 +124,45 @@ def whole_job_rate(flops_per_step, ms, world_size):
     return world_size * flops_per_step / (ms * 1e-3) / 1e9
 
 
-def oracle_matvec(net, steps_labels):
-    """One H_eff matvec with the oracle (reference algorithm restated on the CPU)."""
+def _oracle_tensors(net):
     from oracle import blocksparse as obs
     def conv(t):
         return obs.BlockSparseTensor([tuple(i) for i in t.inds], [tuple(b) for b in t.blocks], list(t.offsets),
                                      t.data)
-    L, psi, W1, W2, R = (conv(net[k]) for k in ("L", "psi", "W1", "W2", "R"))
-    (l1, l2, lr), (m1, m2, mr), (n1, n2, nr), (o1, o2, orr) = steps_labels
-    t, _ = obs.contract(L, l1, psi, l2, lr)
-    t, _ = obs.contract(t, m1, W1, m2, mr)
-    t, _ = obs.contract(t, n1, W2, n2, nr)
-    t, _ = obs.contract(t, o1, R, o2, orr)
-    return t
+    return {k: conv(net[k]) for k in ("L", "psi", "W1", "W2", "R")}
+
+
+def oracle_matvec(net, steps_labels, with_plans=False):
+    """One H_eff matvec with the oracle (reference algorithm restated on the CPU): the
+    result and, with with_plans, each contraction's (output blocks, offsets, pair list)."""
+    from oracle import blocksparse as obs
+    T = _oracle_tensors(net)
+    t = T["L"]
+    plans = []
+    for (a, b, c), key in zip(steps_labels, ("psi", "W1", "W2", "R")):
+        t, plan = obs.contract(t, a, T[key], b, c)
+        plans.append((list(t.blocks), list(t.offsets), [tuple(q) for q in plan]))
+    return (t, plans) if with_plans else t
+
+
+def headline_config(args, block_pairs, flops):
+    """The workload's config dict, identical in both arms of the benchmark."""
+    return {"workload": f"qn_heff_matvec_chi{args.chi}", "chi": args.chi, "d": 2, "w": 5, "charges": 17,
+            "contractions_per_step": 4, "block_pairs": list(block_pairs), "flops_per_step": flops,
+            "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{args.gpus}"}
+
+
+def oracle_sample_1thread(chi):
+    """Seconds of one oracle H_eff matvec with single-threaded BLAS (the reference's test
+    default), in a child process whose BLAS thread pools are pinned to 1 before numpy loads."""
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1",
+               RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    try:
+        r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--oracle-sample", "--chi", str(chi)], env=env,
+                           capture_output=True, text=True, timeout=600)
+        return float(r.stdout.strip().splitlines()[-1])
+    except Exception:
+        return None
 
 
 def cpu_threads():
@@ -154,21 +180,23 @@ def run_reference(args):
     net = wl.qn_heff(chi=args.chi)
     steps_labels = wl.heff_steps()
     cores = cpu_threads()
-    # flops of one matvec (algorithmic, from the oracle's own plans)
-    from oracle import blocksparse as obs
-    flops = matvec_flops_oracle(net, steps_labels)
+    # flops and block pairs of one matvec (algorithmic, from the oracle's own plans)
+    flops, npairs = matvec_plan_oracle(net, steps_labels)
+    flush = np.empty(256 * 1024 * 1024 // 8)           # 256 MB written between steps, as the GPU arm does
     for _ in range(args.warmup):
         oracle_matvec(net, steps_labels)
-    t0 = time.perf_counter()
+    dts = []
     for _ in range(args.steps):
+        flush.fill(1.0)
+        t0 = time.perf_counter()
         oracle_matvec(net, steps_labels)
-    dt = (time.perf_counter() - t0) / args.steps
+        dts.append(time.perf_counter() - t0)
+    dt = float(np.sum(dts)) / args.steps
     v = flops / dt / 1e9
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "GFLOP/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"qn_heff_matvec_chi{args.chi}", "chi": args.chi, "d": 2, "w": 5, "charges": 17,
-                       "flops_per_step": flops},
+            "config": headline_config(args, npairs, flops),
             "cpu_baseline": {"value": round(v, 3), "unit": "GFLOP/s", "cores": cores, "kind": "port",
                              "sample": f"{args.steps} full H_eff matvecs (oracle, numpy/OpenBLAS dgemm per block pair, "
                                        f"reference sequential plan order)"},
@@ -176,19 +204,28 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def matvec_flops_oracle(net, steps_labels):
+def matvec_plan_oracle(net, steps_labels):
+    """(flops, block pairs per contraction) of one matvec from the oracle's sequential plans."""
     from oracle import blocksparse as obs
-    def conv(t):
-        return obs.BlockSparseTensor([tuple(i) for i in t.inds], [tuple(b) for b in t.blocks], list(t.offsets),
-                                     t.data)
-    cur = conv(net["L"])
-    others = [conv(net["psi"]), conv(net["W1"]), conv(net["W2"]), conv(net["R"])]
-    tot = 0
-    for (a, b, c), T in zip(steps_labels, others):
-        indsr, blocks_r, offs_r, nnz_r, plan = obs.contract_blockoffsets(cur, a, T, b, c)
-        tot += obs.flops_of_plan(cur, a, T, b, plan)
+    T = _oracle_tensors(net)
+    cur = T["L"]
+    tot, npairs = 0, []
+    for (a, b, c), key in zip(steps_labels, ("psi", "W1", "W2", "R")):
+        indsr, blocks_r, offs_r, nnz_r, plan = obs.contract_blockoffsets(cur, a, T[key], b, c)
+        tot += obs.flops_of_plan(cur, a, T[key], b, plan)
+        npairs.append(len(plan))
         cur = obs.BlockSparseTensor(indsr, blocks_r, offs_r, np.zeros(nnz_r))
-    return tot
+    return tot, npairs
+
+
+def run_oracle_sample(args):
+    """One oracle matvec, its seconds printed (child process of oracle_sample_1thread)."""
+    from ndtensors_gb300 import workloads as wl
+    net = wl.qn_heff(chi=args.chi)
+    steps_labels = wl.heff_steps()
+    t0 = time.perf_counter()
+    oracle_matvec(net, steps_labels)
+    print(time.perf_counter() - t0, flush=True)
 
 
 # DRAM traffic of split_gemm per launch from one ncu capture of this workload at S = 5
@@ -282,10 +319,27 @@ def run_ours(args):
         torch.cuda.synchronize()
         return [a.elapsed_time(b) for a, b in ts]
 
-    # accuracy: Ozaki vs FP64 on the same inputs
-    ref64 = step("fp64").data.clone()
-    oz = step(args.precision).data.clone()
-    rel_err = float(torch.linalg.norm(oz - ref64) / torch.linalg.norm(ref64))
+    # accuracy against the oracle (the reference's algorithm on the CPU, same inputs): the
+    # four block plans compared element for element, then both GPU precisions' values.
+    # Rank 0 at N = 1 also times this oracle run as the CPU baseline.
+    want_oracle = rank == 0 and ws == 1 and not args.no_cpu
+    oracle_out = None
+    if rank == 0:
+        t0 = time.perf_counter()
+        oracle_out, oracle_plans = oracle_matvec(net, steps_labels, with_plans=True)
+        oracle_s = time.perf_counter() - t0
+        structure_exact = all(list(p.blocksR) == ob and list(p.offsetsR) == oo and list(p.pairs) == opairs
+                              for p, (ob, oo, opairs) in zip(plans, oracle_plans))
+    gpu64 = step("fp64").data.clone()
+    gpu_oz = step(args.precision).data.clone()
+    rel_err = float(torch.linalg.norm(gpu_oz - gpu64) / torch.linalg.norm(gpu64))
+    if oracle_out is not None:
+        ref = torch.from_numpy(np.ascontiguousarray(oracle_out.data)).to(dev)
+        rn = torch.linalg.norm(ref)
+        err_oracle = {"fp64": float(torch.linalg.norm(gpu64 - ref) / rn),
+                      args.precision: float(torch.linalg.norm(gpu_oz - ref) / rn)}
+        del ref
+    del gpu64, gpu_oz
 
     for _ in range(args.warmup):
         step(args.precision)
@@ -379,10 +433,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "precision": f"ozaki-{S}slices" if args.precision == "ozaki" else args.precision,
             "data": "synthetic",
-            "config": {"workload": f"qn_heff_matvec_chi{args.chi}", "chi": args.chi, "d": 2, "w": 5, "charges": 17,
-                       "contractions_per_step": 4, "block_pairs": [p.npairs for p in plans],
-                       "flops_per_step": flops, "l2": "flushed between steps (256 MB write)",
-                       "parallelism": f"replicas x{ws}"},
+            "config": headline_config(args, [p.npairs for p in plans], flops),
             "rel_err_vs_fp64": rel_err,
             "fp64": {"value": round(v64, 2), "unit": "GFLOP/s", "ms_per_step": round(ms64, 3)},
             "speedup_vs_fp64": round(value / ws / v64, 2),
@@ -398,14 +449,23 @@ def run_ours(args):
             "autotune": tune_summary(h),
             "clocks": cs.summary()}
 
-    # CPU baseline: the oracle on the same workload, one matvec (rank 0, N=1 only)
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        t0 = time.perf_counter()
-        oracle_matvec(net, steps_labels)
-        dt = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": round(flops / dt / 1e9, 3), "unit": "GFLOP/s", "cores": cpu_threads(),
+    if rank == 0:
+        line["parity_vs_oracle"] = {
+            "structure_bit_exact": bool(structure_exact),
+            "rel_err_vs_oracle": {k: v for k, v in err_oracle.items()},
+            "bars": {"fp64": 1e-13, args.precision: 1e-10 if args.precision == "ozaki" else 1e-4},
+            "what": "all four block plans (pairs, output blocks, offsets) compared with the oracle's sequential "
+                    "plans; GPU FP64 and split-precision results vs the oracle's matvec, relative Frobenius"}
+    # CPU baseline: the oracle matvec timed above (all host threads), plus one matvec with
+    # single-threaded BLAS (rank 0, N = 1 only)
+    if want_oracle:
+        one = oracle_sample_1thread(args.chi)
+        line["cpu_baseline"] = {"value": round(flops / oracle_s / 1e9, 3), "unit": "GFLOP/s", "cores": cpu_threads(),
                                 "kind": "port", "sample": "1 full H_eff matvec (oracle: numpy/OpenBLAS dgemm per "
-                                                          "block pair, sequential plan order)"}
+                                                          "block pair, sequential plan order)",
+                                "single_thread": None if one is None else
+                                {"value": round(flops / one / 1e9, 3), "unit": "GFLOP/s", "cores": 1,
+                                 "sample": "1 full H_eff matvec, OPENBLAS_NUM_THREADS=1"}}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -784,7 +844,11 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default execution parameters (no autotuning runs)")
     ap.add_argument("--config", default="heff", choices=["heff", "all"] + list(CONFIGS),
                     help="heff (default): the headline line; others: one line per workload")
+    ap.add_argument("--oracle-sample", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.oracle_sample:
+        run_oracle_sample(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

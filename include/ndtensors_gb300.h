@@ -65,6 +65,18 @@ nd_status nd_free(nd_handle h, void *dptr);
 nd_status nd_h2d(nd_handle h, void *dst, const void *host_src, size_t bytes);
 nd_status nd_d2h(nd_handle h, void *host_dst, const void *src, size_t bytes);
 nd_status nd_memset0(nd_handle h, void *dst, size_t bytes);
+/* Poll limit of the library's device-side waits (mbarrier waits of the TMA and
+ * tensor-core pipelines, grid barriers of the SVD).  A wait that runs past it
+ * makes the call return ND_ERR_TIMEOUT instead of hanging; copies and MMAs
+ * already issued are still waited for before a kernel exits, and the handle stays
+ * usable.  0 restores the default (2^26 polls).  Synchronises the handle's stream.
+ * No counterpart in the reference (its CPU path has no device waits). */
+nd_status nd_set_spin_limit(nd_handle h, uint32_t polls);
+/* FP64 Jacobi sweep limit of nd_bs_svd_f64 (default 60; negative restores it).  A
+ * block that has not converged within it makes the SVD return ND_ERR_NOCONV, the
+ * case where the reference's svd returns `nothing`
+ * (NDTensors/src/linearalgebra/linearalgebra.jl:91-127). */
+nd_status nd_set_svd_max_sweeps(nd_handle h, int32_t sweeps);
 /* Number of slice digits used by ND_PREC_OZAKI (3..6, default 5). */
 nd_status nd_set_ozaki_slices(nd_handle h, int32_t slices);
 /* Count of kernel launches this handle enqueued so far (diagnostics). */
@@ -108,10 +120,12 @@ nd_status nd_contract_dense_f64(nd_handle h,
  * synchronisation).  It allocates nothing: its scratch is a fixed 32 MiB device
  * array inside the library, held by every GPU that loads the library until exit.
  * Its address is looked up on the first call per device; make that first call
- * before any stream capture.  Contractions needing more scratch are rejected with
- * ND_ERR_ARG.  All calls share the array, so calls whose GPU work overlaps race.
- * No counterpart in the reference: NDTensors always allocates its outputs and
- * BLAS manages its own workspace. */
+ * before any stream capture.  Each call uploads its descriptors from host memory
+ * and synchronises the handle's stream before it returns, so calls made while
+ * that stream is being captured are refused with ND_ERR_ARG.  Contractions
+ * needing more scratch are rejected with ND_ERR_ARG.  All calls share the array,
+ * so calls whose GPU work overlaps race.  No counterpart in the reference:
+ * NDTensors always allocates its outputs and BLAS manages its own workspace. */
 nd_status nd_contract_dense_ozaki_noalloc_f64(nd_handle h,
                                               double *R, int32_t rankR, const int64_t *dimsR, const int32_t *labelsR,
                                               const double *A, int32_t rankA, const int64_t *dimsA, const int32_t *labelsA,

@@ -57,8 +57,8 @@ nd_status nd_check_device_status(nd_handle h, const char* what) {
   ND_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
   ND_CUDA(h, cudaStreamSynchronize(h->stream));
   if (st.code != ND_OK) {
-    DeviceStatus z{};
-    cudaMemcpy(h->d_status, &z, sizeof(z), cudaMemcpyHostToDevice);
+    const int32_t z[2] = {0, 0};              // clear code and site; keep the spin limit
+    cudaMemcpy(h->d_status, z, sizeof(z), cudaMemcpyHostToDevice);
     if (st.code == ND_ERR_TIMEOUT)
       return nd_fail(h, ND_ERR_TIMEOUT, "%s: device wait exceeded its iteration limit (site %d)", what, st.where);
     if (st.code == ND_ERR_NONFINITE)
@@ -96,7 +96,10 @@ nd_status nd_create(int32_t device, nd_handle* out) {
   h->own_stream = true;
   e = cudaMalloc(&h->d_status, sizeof(DeviceStatus));
   if (e != cudaSuccess) { cudaStreamDestroy(h->stream); delete h; return nd_fail(nullptr, ND_ERR_OOM, "status word"); }
-  cudaMemset(h->d_status, 0, sizeof(DeviceStatus));
+  {
+    const DeviceStatus init{0, 0, ND_SPIN_LIMIT, 0};
+    cudaMemcpy(h->d_status, &init, sizeof(init), cudaMemcpyHostToDevice);
+  }
   cudaDeviceSynchronize();
   *out = h;
   return ND_OK;
@@ -175,6 +178,21 @@ nd_status nd_d2h(nd_handle h, void* dst, const void* src, size_t bytes) {
 nd_status nd_memset0(nd_handle h, void* dst, size_t bytes) {
   if (!h || (bytes && !dst)) return nd_fail(h, ND_ERR_ARG, "nd_memset0: NULL argument");
   if (bytes) ND_CUDA(h, cudaMemsetAsync(dst, 0, bytes, h->stream));
+  return ND_OK;
+}
+
+nd_status nd_set_spin_limit(nd_handle h, uint32_t polls) {
+  if (!h) return ND_ERR_ARG;
+  if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "nd_set_spin_limit: not during graph capture");
+  const uint32_t v = polls ? polls : ND_SPIN_LIMIT;
+  ND_CUDA(h, cudaStreamSynchronize(h->stream));
+  ND_CUDA(h, cudaMemcpy(&h->d_status->spin_limit, &v, sizeof(v), cudaMemcpyHostToDevice));
+  return ND_OK;
+}
+
+nd_status nd_set_svd_max_sweeps(nd_handle h, int32_t sweeps) {
+  if (!h) return ND_ERR_ARG;
+  h->svd_max_sweeps = sweeps < 0 ? -1 : sweeps;
   return ND_OK;
 }
 

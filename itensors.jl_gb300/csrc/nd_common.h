@@ -11,15 +11,28 @@
 
 #define ND_HOSTDEV __host__ __device__ __forceinline__
 
-// Bounded device-side waits: a spin that runs past this many polls records
+// Bounded device-side waits: a spin that runs past its limit records
 // ND_ERR_TIMEOUT in the status word and returns instead of hanging the GPU.
+// ND_SPIN_LIMIT is the default limit of the waits that make progress (set per
+// handle with nd_set_spin_limit) and the fixed limit of the clean-up waits that
+// let issued copies and MMAs land before a CTA exits after a timeout.
 #define ND_SPIN_LIMIT (1u << 26)
 
-// device status word layout (int32): [0] = first error code, [1] = where it was raised
+// Device status word of a handle: [code] = first error code, [where] = the site
+// that raised it, [spin_limit] = poll limit of the progress waits (0 = default).
 struct DeviceStatus {
   int32_t code;
   int32_t where;
+  uint32_t spin_limit;
+  uint32_t reserved;
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t nd_spin_limit(const DeviceStatus* st) {
+  const uint32_t l = *(const volatile uint32_t*)&st->spin_limit;
+  return l ? l : ND_SPIN_LIMIT;
+}
+#endif
 
 // Execution parameters chosen by the autotuner (per block-size histogram).
 struct TuneChoice {
@@ -37,6 +50,7 @@ struct nd_context {
   bool own_stream = false;
   int num_sms = 0;
   int ozaki_slices = 5;
+  int svd_max_sweeps = -1;            // FP64 Jacobi sweep limit of the SVD (-1 = default 60)
   std::string last_error;
   DeviceStatus* d_status = nullptr;   // device status word
   int64_t launches = 0;

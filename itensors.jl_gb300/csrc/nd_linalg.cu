@@ -94,8 +94,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, volatile unsig
       atomicAdd((unsigned int*)gen, 1u);
     } else {
       unsigned int it = 0;
+      const unsigned int lim = nd_spin_limit(st);
       while (*gen == g) {
-        if (++it > ND_SPIN_LIMIT) {
+        if (++it > lim) {
           if (atomicCAS(&st->code, 0, ND_ERR_TIMEOUT) == 0) st->where = 500;
           ok = 0;
           break;
@@ -429,9 +430,11 @@ struct BlockCopyDev {
 __global__ void block_copy(const BlockCopyDev* list, int n, const double* src, double* dst) {
   for (int r = blockIdx.y; r < n; r += gridDim.y) {
     const BlockCopyDev& c = list[r];
+    const bool small = c.count < (1ll << 31);   // multiply-high division of 32-bit indices
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < c.count; e += (int64_t)gridDim.x * blockDim.x) {
       int64_t so, d;
-      mixed_offsets(c.idx, e, so, d);
+      if (small) mixed_offsets32(c.idx, (uint32_t)e, so, d);
+      else mixed_offsets(c.idx, e, so, d);
       dst[c.dst_off + d] = src[c.src_off + so];
     }
   }
@@ -688,6 +691,9 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
   // (quadratic: 1e-6 -> 1e-12 -> roundoff), then W0 = W Q.  The FP64 sweeps that
   // follow start nearly orthogonal and converge in a few sweeps; the result is
   // the FP64 one-sided Jacobi SVD of W0, so accuracy is unchanged.
+  // FP64 sweep limit (the reference's LAPACK call has no such knob; a limit of 0 makes
+  // every block with more than one column report ND_ERR_NOCONV, which tests use)
+  const int max_sweeps = h->svd_max_sweeps < 0 ? 60 : h->svd_max_sweeps;
   double work = 0.0;
   for (auto& b : blocks) work += (double)b.mm * b.nn * b.nn;
   bool converged = false;
@@ -715,8 +721,8 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
     ND_LAUNCHED(h);
     ND_LAUNCHED(h);
     bool c32 = false;
-    st = run_sweeps<float>(h, dblk, nb, task0, maxr, soff, W32, V32, offmax, bar, 5.9604644775390625e-08, 40, c32,
-                           sweeps32);
+    st = run_sweeps<float>(h, dblk, nb, task0, maxr, soff, W32, V32, offmax, bar, 5.9604644775390625e-08,
+                           std::min(40, max_sweeps), c32, sweeps32);
     if (!st) {
       to_f64_and_identity<<<gv, 256, 0, s>>>(dblk, V32, V, Y);
       ND_LAUNCHED(h);
@@ -733,9 +739,8 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
     cudaFreeAsync(W32, s); cudaFreeAsync(V32, s); cudaFreeAsync(Y, s); cudaFreeAsync(Vn, s);
     cudaFreeAsync(W0, s); cudaFreeAsync(bmax, s);
   }
-  if (!st) st = run_sweeps<double>(h, dblk, nb, task0, maxr, soff, W, V, offmax, bar, 2.220446049250313e-16, 60,
-                                   converged, sweeps64);
-  const int max_sweeps = 60;
+  if (!st) st = run_sweeps<double>(h, dblk, nb, task0, maxr, soff, W, V, offmax, bar, 2.220446049250313e-16,
+                                   max_sweeps, converged, sweeps64);
   if (st) {
     cudaFreeAsync(W, s); cudaFreeAsync(V, s); cudaFreeAsync(sig, s); cudaFreeAsync(order, s);
     cudaFreeAsync(dblk, s); cudaFreeAsync(offmax, s); cudaFreeAsync(bar, s);

@@ -12,7 +12,10 @@
 // (32 MiB).  Every GPU that loads this library holds it until the process
 // exits.  Its device address is looked up once per device, on the first call
 // made with a handle on that device (that device is made current for the
-// lookup); make that first call before any stream capture.  Problems whose
+// lookup); make that first call before any stream capture.  Every call uploads
+// its descriptors from host memory and waits for its own work to finish, so a
+// call made while the handle's stream is being captured is refused with
+// ND_ERR_ARG instead of being recorded into the caller's graph.  Problems whose
 // split operands, descriptors and exponents need more than the array holds are
 // rejected with ND_ERR_ARG and a message giving the size.
 //
@@ -62,6 +65,9 @@ extern "C" nd_status nd_contract_dense_ozaki_noalloc_f64(nd_handle h,
                                                          const double* B, int32_t rankB, const int64_t* dimsB,
                                                          const int32_t* labelsB, double alpha, double beta) {
   if (!h) return ND_ERR_ARG;
+  if (nd_capturing(h))
+    return nd_fail(h, ND_ERR_ARG, "noalloc contract: the handle's stream is being captured; this entry point uploads "
+                                  "host descriptors and synchronises, call it outside the capture");
   if (rankA < 0 || rankB < 0 || rankR < 0 || rankA > ND_MAX_RANK || rankB > ND_MAX_RANK || rankR > ND_MAX_RANK)
     return nd_fail(h, ND_ERR_ARG, "noalloc contract: rank out of range (max %d)", ND_MAX_RANK);
   int64_t nA = 1, nB = 1, nR = 1;
@@ -103,6 +109,5 @@ extern "C" nd_status nd_contract_dense_ozaki_noalloc_f64(nd_handle h,
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
   s = nd_split_run(h, c, ptrs, alpha, beta);
   if (s) return s;
-  ND_CUDA(h, cudaStreamSynchronize(h->stream));
-  return nd_check_device_status(h, "noalloc contract");
+  return nd_check_device_status(h, "noalloc contract");   // synchronises the stream
 }

@@ -76,9 +76,12 @@ struct SplitOp {
 // ---- helpers ---------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+// Progress waits pass the CTA's abort flag and the handle's spin limit; clean-up
+// waits (copies or MMAs already issued) pass no flag and wait up to ND_SPIN_LIMIT.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, DeviceStatus* st, int site,
-                                          volatile int* abort_flag) {
-  for (uint32_t it = 0; it < ND_SPIN_LIMIT; ++it) {
+                                          volatile int* abort_flag, uint32_t lim = ND_SPIN_LIMIT) {
+  if (!abort_flag) lim = ND_SPIN_LIMIT;
+  for (uint32_t it = 0; it < lim; ++it) {
     uint32_t ok;
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
                  : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
@@ -428,8 +431,8 @@ __device__ __forceinline__ void f32_round_split(float v, int& hi, int& li) {
 // One vote per wait: every lane of the MMA warp polls, and the warp leaves the loop
 // together if any lane gave up.
 __device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, DeviceStatus* st, int site,
-                                               volatile int* abort_flag) {
-  return __all_sync(0xffffffffu, mbar_wait(bar, parity, st, site, abort_flag));
+                                               volatile int* abort_flag, uint32_t lim) {
+  return __all_sync(0xffffffffu, mbar_wait(bar, parity, st, site, abort_flag, lim));
 }
 
 template <int S>
@@ -456,6 +459,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   __shared__ volatile int abort_flag;
   __shared__ int64_t colR_s[BN];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t lim = nd_spin_limit(g.st);
 
   if (tid == 0) {
     for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -488,7 +492,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
           const unsigned char* srcB = g.pack + ob.pack_off + (int64_t)wi.nt * ob.k_steps * S * B_SLICE;
           for (int ks = 0; ks < oa.k_steps; ++ks, ++n) {
             const uint32_t s = n % C::STAGES, u = n / C::STAGES;
-            if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (u - 1) & 1, g.st, 400, &abort_flag)) { ok = false; break; }
+            if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (u - 1) & 1, g.st, 400, &abort_flag, lim)) { ok = false; break; }
             unsigned char* dA = smem + s * C::STAGE;
             unsigned char* dB = dA + S * A_SLICE;
             const uint32_t fb = smem_u32(&full[s]);
@@ -529,11 +533,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
             if (cstart) {
               // every level is drained per chunk: slot xs holds all levels of this chunk
               const uint32_t xs = chunk & 1, xu = chunk >> 1;
-              if (xu >= 1 && !mbar_wait_warp(smem_u32(&xempty[xs]), (xu - 1) & 1, g.st, 411, &abort_flag)) { ok = false; break; }
+              if (xu >= 1 && !mbar_wait_warp(smem_u32(&xempty[xs]), (xu - 1) & 1, g.st, 411, &abort_flag, lim)) { ok = false; break; }
               X = tmem + xcol(xs);
             }
             const uint32_t s = n % C::STAGES, u = n / C::STAGES;
-            if (!mbar_wait_warp(smem_u32(&full[s]), u & 1, g.st, 412, &abort_flag)) { ok = false; break; }
+            if (!mbar_wait_warp(smem_u32(&full[s]), u & 1, g.st, 412, &abort_flag, lim)) { ok = false; break; }
             fence_after();
             // descriptors of one stage differ only in the start-address field (addr >> 4)
             const uint32_t a0 = smem_base + s * C::STAGE;
@@ -619,7 +623,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
         for (int c = 0; c < EPI_COLS; ++c) { acc[c] = 0; facc[c] = 0.f; }
         for (int ch = 0; ch < nchunks; ++ch, ++chunk) {
           const uint32_t xs = chunk & 1, xu = chunk >> 1;
-          if (!mbar_wait(smem_u32(&xfull[xs]), xu & 1, g.st, 420, &abort_flag)) { ok = false; break; }
+          if (!mbar_wait(smem_u32(&xfull[xs]), xu & 1, g.st, 420, &abort_flag, lim)) { ok = false; break; }
           fence_after();
           {
             uint32_t l2[EPI_COLS], l3[EPI_COLS];
@@ -746,14 +750,24 @@ int64_t tile_cost(int64_t ksteps, int pairs) { return ksteps + 2 * (int64_t)pair
 
 }  // namespace
 
-// Build operand list, packed layout and work items (host; once per plan/precision).
-nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs_in, int ngroups, int precision) {
-  (void)ngroups;
-  const int S = precision == ND_PREC_OZAKI ? h->ozaki_slices : 2;
-  std::vector<PairDesc> pairs = pairs_in;
+// Host layout of one split-precision launch: the operand list (one entry per
+// distinct A block and B block), the pairs pointing at their operands, the pack
+// work list and the balanced output-tile list, with the packed-slice and exponent
+// sizes.  Both the allocating path (nd_split_build) and the allocation-free one
+// (nd_split_layout_into) place exactly this layout.
+struct SplitLayout {
+  std::vector<PairDesc> pairs;
   std::vector<SplitOp> ops;
-  std::map<std::pair<int, int64_t>, int> amap, bmap;   // (job, offset) -> op
+  std::vector<PackItem2> pitems;
+  std::vector<WorkItem> items;
   int64_t pack_bytes = 0, exp_count = 0;
+  int nops_a = 0, nops_b = 0;
+};
+
+static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int S, SplitLayout& L) {
+  L = SplitLayout{};
+  L.pairs = pairs_in;
+  std::map<std::pair<int, int64_t>, int> amap, bmap;   // (job, offset) -> op
   auto add_op = [&](bool is_b, const PairDesc& pd) -> int {
     auto& mp = is_b ? bmap : amap;
     auto key = std::make_pair(pd.job, is_b ? pd.b_off : pd.a_off);
@@ -771,60 +785,72 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
     const int rows_per_tile = is_b ? BN : BM;
     o.row_tiles = (o.rows + rows_per_tile - 1) / rows_per_tile;
     o.k_steps = (o.kdim + BK - 1) / BK;
-    o.pack_off = pack_bytes;
-    pack_bytes += (int64_t)o.row_tiles * o.k_steps * S * (is_b ? B_SLICE : A_SLICE);
-    o.exp_off = exp_count;
-    exp_count += (int64_t)o.row_tiles * rows_per_tile;
-    ops.push_back(o);
-    mp[key] = (int)ops.size() - 1;
-    return (int)ops.size() - 1;
+    o.pack_off = L.pack_bytes;
+    L.pack_bytes += (int64_t)o.row_tiles * o.k_steps * S * (is_b ? B_SLICE : A_SLICE);
+    o.exp_off = L.exp_count;
+    L.exp_count += (int64_t)o.row_tiles * rows_per_tile;
+    L.ops.push_back(o);
+    mp[key] = (int)L.ops.size() - 1;
+    return (int)L.ops.size() - 1;
   };
-  for (auto& pd : pairs) {
+  for (auto& pd : L.pairs) {
     pd.a_op = add_op(false, pd);
     pd.b_op = add_op(true, pd);
   }
-  std::vector<PackItem2> pitems;
-  for (int i = 0; i < (int)ops.size(); ++i)
-    for (int t = 0; t < ops[i].row_tiles; ++t)
-      for (int kc = 0; kc * PACK_KC < ops[i].k_steps; ++kc) pitems.push_back({i, t, kc});
-  // work items: 128 x 64 output tiles, balanced over the persistent CTAs
+  L.nops_a = (int)amap.size();
+  L.nops_b = (int)bmap.size();
+  for (int i = 0; i < (int)L.ops.size(); ++i)
+    for (int t = 0; t < L.ops[i].row_tiles; ++t)
+      for (int kc = 0; kc * PACK_KC < L.ops[i].k_steps; ++kc) L.pitems.push_back({i, t, kc});
+  // work items: BM x BN output tiles, balanced over the persistent CTAs
   std::vector<std::pair<int64_t, WorkItem>> tmp;
-  for (size_t i = 0; i < pairs.size();) {
+  for (size_t i = 0; i < L.pairs.size();) {
     size_t j = i;
     int64_t ksteps = 0;
-    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) {
-      ksteps += (pairs[j].K + BK - 1) / BK;
+    while (j < L.pairs.size() && L.pairs[j].group == L.pairs[i].group && L.pairs[j].job == L.pairs[i].job) {
+      ksteps += (L.pairs[j].K + BK - 1) / BK;
       ++j;
     }
-    const PairDesc& p = pairs[i];
-    int mt = (p.M + BM - 1) / BM, nt = (p.N + BN - 1) / BN;
+    const PairDesc& p = L.pairs[i];
+    const int mt = (p.M + BM - 1) / BM, nt = (p.N + BN - 1) / BN;
     for (int a = 0; a < mt; ++a)
       for (int b = 0; b < nt; ++b)
         tmp.push_back({tile_cost(ksteps, (int)(j - i)), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
     i = j;
   }
-  const std::vector<WorkItem> items = balance_items(std::move(tmp), h->num_sms);
-  // upload
+  L.items = balance_items(std::move(tmp), h->num_sms);
+}
+
+static void split_adopt(ExecCache& c, const SplitLayout& L, int S) {
+  c.nsplit_items = (int)L.items.size();
+  c.npack_items = (int)L.pitems.size();
+  c.nops_a = L.nops_a;
+  c.nops_b = L.nops_b;
+  c.pack_bytes = L.pack_bytes;
+  c.exp_count = L.exp_count;
+  c.slices = S;
+}
+
+// Build operand list, packed layout and work items (host; once per plan/precision).
+nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs_in, int ngroups, int precision) {
+  (void)ngroups;
+  const int S = precision == ND_PREC_OZAKI ? h->ozaki_slices : 2;
+  SplitLayout L;
+  split_layout(h, pairs_in, S, L);
   auto up = [&](void** dst, const void* src, size_t bytes) -> nd_status {
     ND_CUDA(h, cudaMalloc(dst, std::max<size_t>(bytes, 16)));
     if (bytes) ND_CUDA(h, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
     return ND_OK;
   };
   nd_status s;
-  if ((s = up((void**)&c.d_split_pairs, pairs.data(), pairs.size() * sizeof(PairDesc)))) return s;
-  if ((s = up((void**)&c.d_split_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
-  if ((s = up(&c.d_operands, ops.data(), ops.size() * sizeof(SplitOp)))) return s;
-  if ((s = up(&c.d_pack_items, pitems.data(), pitems.size() * sizeof(PackItem2)))) return s;
-  ND_CUDA(h, cudaMalloc((void**)&c.d_rowmax, std::max<int64_t>(exp_count, 1) * 8));
-  ND_CUDA(h, cudaMalloc(&c.d_pack, std::max<int64_t>(pack_bytes, 16)));
-  ND_CUDA(h, cudaMalloc((void**)&c.d_exp, std::max<int64_t>(exp_count, 4) * 4));
-  c.pack_bytes = pack_bytes;
-  c.exp_count = exp_count;
-  c.nsplit_items = (int)items.size();
-  c.npack_items = (int)pitems.size();
-  c.nops_a = (int)amap.size();
-  c.nops_b = (int)bmap.size();
-  c.slices = S;
+  if ((s = up((void**)&c.d_split_pairs, L.pairs.data(), L.pairs.size() * sizeof(PairDesc)))) return s;
+  if ((s = up((void**)&c.d_split_items, L.items.data(), L.items.size() * sizeof(WorkItem)))) return s;
+  if ((s = up(&c.d_operands, L.ops.data(), L.ops.size() * sizeof(SplitOp)))) return s;
+  if ((s = up(&c.d_pack_items, L.pitems.data(), L.pitems.size() * sizeof(PackItem2)))) return s;
+  ND_CUDA(h, cudaMalloc((void**)&c.d_rowmax, std::max<int64_t>(L.exp_count, 1) * 8));
+  ND_CUDA(h, cudaMalloc(&c.d_pack, std::max<int64_t>(L.pack_bytes, 16)));
+  ND_CUDA(h, cudaMalloc((void**)&c.d_exp, std::max<int64_t>(L.exp_count, 4) * 4));
+  split_adopt(c, L, S);
   return ND_OK;
 }
 
@@ -868,90 +894,37 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
 }
 
 // Lay out one split-precision launch inside caller-provided device memory
-// instead of allocating: computes the same operand / pack / tile lists as
-// nd_split_build, reports the bytes needed, and when `base` holds enough,
-// uploads the descriptors there and points the cache's fields into it.
+// instead of allocating: the same layout as nd_split_build (split_layout), the
+// bytes it needs reported in *needed, and when `base` holds enough, the
+// descriptors uploaded there and the cache's fields pointed into it.
 nd_status nd_split_layout_into(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs_in, int S,
                                unsigned char* base, size_t capacity, size_t* needed) {
-  std::vector<PairDesc> pairs = pairs_in;
-  std::vector<SplitOp> ops;
-  std::map<std::pair<int, int64_t>, int> amap, bmap;
-  int64_t pack_bytes = 0, exp_count = 0;
-  auto add_op = [&](bool is_b, const PairDesc& pd) -> int {
-    auto& mp = is_b ? bmap : amap;
-    auto key = std::make_pair(pd.job, is_b ? pd.b_off : pd.a_off);
-    auto f = mp.find(key);
-    if (f != mp.end()) return f->second;
-    SplitOp o{};
-    o.src_off = key.second;
-    o.is_b = is_b;
-    o.job = pd.job;
-    o.rows = is_b ? pd.N : pd.M;
-    o.kdim = pd.K;
-    o.rk = is_b ? pd.cols : pd.rows;
-    o.kk = pd.ks;
-    if (is_b) for (int d = 0; d < o.kk.n; ++d) o.kk.st0[d] = pd.ks.st1[d];
-    const int rpt = is_b ? BN : BM;
-    o.row_tiles = (o.rows + rpt - 1) / rpt;
-    o.k_steps = (o.kdim + BK - 1) / BK;
-    o.pack_off = pack_bytes;
-    pack_bytes += (int64_t)o.row_tiles * o.k_steps * S * (is_b ? B_SLICE : A_SLICE);
-    o.exp_off = exp_count;
-    exp_count += (int64_t)o.row_tiles * rpt;
-    ops.push_back(o);
-    mp[key] = (int)ops.size() - 1;
-    return (int)ops.size() - 1;
-  };
-  for (auto& pd : pairs) { pd.a_op = add_op(false, pd); pd.b_op = add_op(true, pd); }
-  std::vector<PackItem2> pitems;
-  for (int i = 0; i < (int)ops.size(); ++i)
-    for (int t = 0; t < ops[i].row_tiles; ++t)
-      for (int kc = 0; kc * PACK_KC < ops[i].k_steps; ++kc) pitems.push_back({i, t, kc});
-  std::vector<std::pair<int64_t, WorkItem>> tmp;
-  for (size_t i = 0; i < pairs.size();) {
-    size_t j = i;
-    int64_t ksteps = 0;
-    while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) {
-      ksteps += (pairs[j].K + BK - 1) / BK;
-      ++j;
-    }
-    const PairDesc& p = pairs[i];
-    for (int a = 0; a < (p.M + BM - 1) / BM; ++a)
-      for (int b = 0; b < (p.N + BN - 1) / BN; ++b)
-        tmp.push_back({tile_cost(ksteps, (int)(j - i)), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
-    i = j;
-  }
-  const std::vector<WorkItem> items = balance_items(std::move(tmp), h->num_sms);
+  SplitLayout L;
+  split_layout(h, pairs_in, S, L);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t o_pairs = 0;
-  const size_t o_items = al(o_pairs + pairs.size() * sizeof(PairDesc));
-  const size_t o_ops = al(o_items + items.size() * sizeof(WorkItem));
-  const size_t o_pit = al(o_ops + ops.size() * sizeof(SplitOp));
-  const size_t o_exp = al(o_pit + pitems.size() * sizeof(PackItem2));
-  const size_t o_rmx = al(o_exp + (size_t)exp_count * 4);
-  const size_t o_pack = al(o_rmx + (size_t)exp_count * 8);
-  const size_t total = o_pack + (size_t)pack_bytes;
+  const size_t o_items = al(o_pairs + L.pairs.size() * sizeof(PairDesc));
+  const size_t o_ops = al(o_items + L.items.size() * sizeof(WorkItem));
+  const size_t o_pit = al(o_ops + L.ops.size() * sizeof(SplitOp));
+  const size_t o_exp = al(o_pit + L.pitems.size() * sizeof(PackItem2));
+  const size_t o_rmx = al(o_exp + (size_t)L.exp_count * 4);
+  const size_t o_pack = al(o_rmx + (size_t)L.exp_count * 8);
+  const size_t total = o_pack + (size_t)L.pack_bytes;
   if (needed) *needed = total;
   if (!base) return ND_OK;
   if (total > capacity) return ND_ERR_ARG;
   cudaStream_t s = h->stream;
-  ND_CUDA(h, cudaMemcpyAsync(base + o_pairs, pairs.data(), pairs.size() * sizeof(PairDesc), cudaMemcpyHostToDevice, s));
-  ND_CUDA(h, cudaMemcpyAsync(base + o_items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
-  ND_CUDA(h, cudaMemcpyAsync(base + o_ops, ops.data(), ops.size() * sizeof(SplitOp), cudaMemcpyHostToDevice, s));
-  ND_CUDA(h, cudaMemcpyAsync(base + o_pit, pitems.data(), pitems.size() * sizeof(PackItem2), cudaMemcpyHostToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(base + o_pairs, L.pairs.data(), L.pairs.size() * sizeof(PairDesc), cudaMemcpyHostToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(base + o_items, L.items.data(), L.items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(base + o_ops, L.ops.data(), L.ops.size() * sizeof(SplitOp), cudaMemcpyHostToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(base + o_pit, L.pitems.data(), L.pitems.size() * sizeof(PackItem2), cudaMemcpyHostToDevice, s));
   c.d_split_pairs = (PairDesc*)(base + o_pairs);
   c.d_split_items = (WorkItem*)(base + o_items);
-  c.nsplit_items = (int)items.size();
   c.d_operands = base + o_ops;
-  c.nops_a = (int)amap.size();
-  c.nops_b = (int)bmap.size();
   c.d_pack_items = base + o_pit;
-  c.npack_items = (int)pitems.size();
   c.d_exp = (int32_t*)(base + o_exp);
-  c.exp_count = exp_count;
   c.d_rowmax = base + o_rmx;
   c.d_pack = base + o_pack;
-  c.pack_bytes = pack_bytes;
-  c.slices = S;
+  split_adopt(c, L, S);
   return ND_OK;
 }

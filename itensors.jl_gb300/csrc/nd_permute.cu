@@ -98,13 +98,18 @@ __device__ __forceinline__ void batch_offsets(const PermParams& p, int64_t b, in
 // ---- mbarrier / TMA helpers (bounded waits) -------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, DeviceStatus* st, int site) {
-  for (uint32_t it = 0; it < ND_SPIN_LIMIT; ++it) {
+// Progress wait (drain == false): gives up after the handle's spin limit, or early
+// once another CTA has recorded a timeout.  Clean-up wait (drain == true): waits for
+// copies already issued with the fixed ND_SPIN_LIMIT and no early exit.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, DeviceStatus* st, int site, bool drain,
+                                          uint32_t lim) {
+  if (drain) lim = ND_SPIN_LIMIT;
+  for (uint32_t it = 0; it < lim; ++it) {
     uint32_t ok;
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
                  : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
     if (ok) return true;
-    if ((it & 1023) == 1023 && *(volatile int32_t*)&st->code == ND_ERR_TIMEOUT) return false;
+    if (!drain && (it & 1023) == 1023 && *(volatile int32_t*)&st->code == ND_ERR_TIMEOUT) return false;
   }
   if (atomicCAS(&st->code, 0, ND_ERR_TIMEOUT) == 0) st->where = site;
   return false;
@@ -124,6 +129,7 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
   __shared__ int s_ok;
   const int tid = threadIdx.x;
   const double a = eff_alpha(p);
+  const uint32_t lim = tid == 0 ? nd_spin_limit(st) : 0u;   // only thread 0 waits
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&full[s])), "r"(1));
@@ -160,16 +166,17 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
       if (t < p.ntiles) issue(t, s);
     }
   }
-  uint32_t phase = 0;                            // bit s: parity of stage s
+  uint32_t phase = 0;                            // bit s: parity of the next completion of stage s
   int s = 0;
   bool ok = true;
+  int64_t t_stop = 0;                            // tile whose wait gave up
   for (int64_t t = first; t < p.ntiles; t += stride) {
     // one thread polls the barrier and broadcasts, so every thread leaves together
-    if (tid == 0) s_ok = mbar_wait(smem_u32(&full[s]), (phase >> s) & 1u, st, 100) ? 1 : 0;
+    if (tid == 0) s_ok = mbar_wait(smem_u32(&full[s]), (phase >> s) & 1u, st, 100, false, lim) ? 1 : 0;
     __syncthreads();
-    phase ^= 1u << s;
     ok = s_ok != 0;
-    if (!ok) break;
+    if (!ok) { t_stop = t; break; }
+    phase ^= 1u << s;                            // stage s consumed
     int64_t rest = pdiv(p, t, p.ntile_j, p.mul_j, p.shr_j);
     int64_t tj = t - rest * p.ntile_j;
     int64_t b = pdiv(p, rest, p.ntile_i, p.mul_i, p.shr_i);
@@ -212,10 +219,18 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
     }
     s = (s + 1) % STAGES;
   }
-  // After a timeout, give copies still in flight a bounded chance to land
-  // before the CTA exits (on the normal path every issued tile was consumed).
+  // After a timeout, wait for the copies still in flight before the CTA exits (on
+  // the normal path every issued tile was consumed).  Issued and not consumed are
+  // the tiles t_stop, t_stop + stride, ... (at most STAGES of them, the ring ahead
+  // of the consumer), in stages s, s + 1, ...; none of those stages has flipped its
+  // phase bit since the copy was issued.
   if (!ok && tid == 0) {
-    for (int q = 0; q < STAGES; ++q) mbar_wait(smem_u32(&full[q]), (phase >> q) & 1u, st, 101);
+    for (int k = 0; k < STAGES; ++k) {
+      const int64_t tk = t_stop + (int64_t)k * stride;
+      if (tk >= p.ntiles) break;
+      const int q = (s + k) % STAGES;
+      mbar_wait(smem_u32(&full[q]), (phase >> q) & 1u, st, 101, true, lim);
+    }
   }
 }
 

@@ -9,9 +9,15 @@
 #   permutedims!(R, T, perm)                                      (NDTensors/ext/NDTensorsCUDAExt/permutedims.jl:4-23)
 #   contract(::BlockSparseTensor, ...) via contract_blockoffsets /
 #   contract! with the plan built on the device                   (NDTensors/src/blocksparse/contract.jl:3-76)
-#   svd(::BlockSparseMatrix) / qr(::BlockSparseMatrix)            (NDTensors/src/blocksparse/linearalgebra.jl:45-415)
-#   rrule(contract, ::ITensor, ::ITensor)                         (ext/ITensorsChainRulesCoreExt/itensor.jl:94-103)
+#   svd(::BlockSparseMatrix)                                      (NDTensors/src/blocksparse/linearalgebra.jl:45-215)
+#   qr(::BlockSparseMatrix) through qx                            (NDTensors/src/blocksparse/linearalgebra.jl:351-415)
+#   truncate!!(::Type{<:GB300Vector}, P)                          (NDTensors/src/truncate.jl:15-20)
+#   rrule(contract, T1, labels1, T2, labels2, labelsR) on block-sparse
+#   storage, and the pullback contract_pullback_gb300 that
+#   rrule(contract, ::ITensor, ::ITensor) hands GB300 storage to  (ext/ITensorsChainRulesCoreExt/itensor.jl:94-103)
 #
+# Fermionic sign fixes of the reference's svd (right_arrow_sign / left_arrow_sign) are
+# not applied: auto-fermion is off by default and this backend is bosonic (real FP64).
 # Status: written against the C ABI in include/ndtensors_gb300.h; it has not been
 # run (no Julia toolchain was available where this library was built and tested).
 module NDTensorsGB300Ext
@@ -20,10 +26,13 @@ using NDTensors
 using NDTensors: BlockSparseTensor, DenseTensor, Tensor, inds, data, blockoffsets, nzblocks,
     BlockOffsets, Block, blockdim, contract_labels
 using NDTensors.Expose: Exposed, unexpose, expose
+using NDTensors: DiagBlockSparseTensor, Spectrum, ind, dag, sim, setblock!, block, resize
 using LinearAlgebra
+using ChainRulesCore: ChainRulesCore, NoTangent
 
 const LIB = get(ENV, "NDTENSORS_GB300_LIB", joinpath(@__DIR__, "..", "ndtensors_gb300", "libndtensors_gb300.so"))
 
+const ND_ERR_NOCONV = Int32(3)
 const ND_PREC_FP64 = Int32(0)
 const ND_PREC_OZAKI = Int32(1)
 const ND_PREC_BF16X3 = Int32(2)
@@ -72,6 +81,20 @@ function gb300(a::AbstractVector{Float64})
   v = GB300Vector(undef, length(a))
   check(ccall((:nd_h2d, LIB), Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Csize_t), handle(), v.ptr, collect(a), length(a) * 8))
   return v
+end
+
+# a view of the first n elements that shares (and keeps alive) the parent's memory
+mutable struct GB300View <: AbstractVector{Float64}
+  parent::GB300Vector
+  ptr::Ptr{Float64}
+  len::Int
+end
+Base.size(v::GB300View) = (v.len,)
+Base.getindex(::GB300View, ::Int) = error("scalar indexing of a GB300View: copy to the host with Array(v)")
+function Base.Array(v::GB300View)
+  a = Vector{Float64}(undef, v.len)
+  check(ccall((:nd_d2h, LIB), Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Csize_t), handle(), a, v.ptr, v.len * 8))
+  return a
 end
 
 # ---- dense ----------------------------------------------------------------
@@ -126,16 +149,7 @@ end
 function NDTensors.contract(T1::BlockSparseTensor{Float64,N1,<:NDTensors.BlockSparse{Float64,<:GB300Vector}}, labels1,
                             T2::BlockSparseTensor{Float64,N2,<:NDTensors.BlockSparse{Float64,<:GB300Vector}}, labels2,
                             labelsR=contract_labels(labels1, labels2)) where {N1,N2}
-  a1 = desc_arrays(T1)
-  a2 = desc_arrays(T2)
-  GC.@preserve a1 a2 begin
-    d1 = Ref(BsDesc(length(a1[1]), pointer(a1[1]), pointer(a1[2]), a1[5], pointer(a1[3]), pointer(a1[4])))
-    d2 = Ref(BsDesc(length(a2[1]), pointer(a2[1]), pointer(a2[2]), a2[5], pointer(a2[3]), pointer(a2[4])))
-    plan = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:nd_bs_plan_create, LIB), Int32,
-                (Ptr{Cvoid}, Ref{BsDesc}, Ptr{Int32}, Ref{BsDesc}, Ptr{Int32}, Int32, Ptr{Int32}, Ref{Ptr{Cvoid}}),
-                handle(), d1, Int32[labels1...], d2, Int32[labels2...], length(labelsR), Int32[labelsR...], plan))
-  end
+  plan = Ref(bs_plan(T1, labels1, T2, labels2, labelsR))
   np, nr, nnz = Ref{Int32}(0), Ref{Int32}(0), Ref{Int64}(0)
   check(ccall((:nd_bs_plan_sizes, LIB), Int32, (Ptr{Cvoid}, Ref{Int32}, Ref{Int32}, Ref{Int64}), plan[], np, nr, nnz))
   NR = length(labelsR)
@@ -154,6 +168,161 @@ function NDTensors.contract(T1::BlockSparseTensor{Float64,N1,<:NDTensors.BlockSp
   end
   ccall((:nd_bs_plan_destroy, LIB), Int32, (Ptr{Cvoid},), plan[])
   return R
+end
+
+const GB300BlockSparseMatrix = Tensor{Float64,2,<:NDTensors.BlockSparse{Float64,<:GB300Vector}}
+isgb300(T::Tensor) = data(T) isa Union{GB300Vector,GB300View}
+isgb300(x) = isgb300(NDTensors.tensor(x))        # an ITensor: its storage
+const GB300BlockSparseTensor = BlockSparseTensor{Float64,N,<:NDTensors.BlockSparse{Float64,<:GB300Vector}} where {N}
+
+# rows, columns and offsets of the nonzero blocks of a block-sparse matrix, in block order
+function matrix_blocks(T)
+  i1, i2 = ind(T, 1), ind(T, 2)
+  nzb = collect(nzblocks(T))
+  rows = Int64[blockdim(i1, b[1]) for b in nzb]
+  cols = Int64[blockdim(i2, b[2]) for b in nzb]
+  offs = Int64[NDTensors.offset(T, b) for b in nzb]
+  return nzb, rows, cols, offs
+end
+
+# truncate! on the device (NDTensors/src/truncate.jl:15-20 copies GPU spectra to the
+# CPU instead): the kept prefix of P is returned as a view of P.
+function NDTensors.truncate!!(::Type{<:Union{GB300Vector,GB300View}}, P::AbstractVector;
+                              mindim=nothing, maxdim=nothing, cutoff=nothing,
+                              use_absolute_cutoff=nothing, use_relative_cutoff=nothing)
+  n, terr, dcut = Ref{Int32}(0), Ref{Float64}(0), Ref{Float64}(0)
+  check(ccall((:nd_truncate_f64, LIB), Int32,
+              (Ptr{Cvoid}, Ptr{Float64}, Int32, Int32, Int32, Float64, Int32, Int32, Ref{Int32}, Ref{Float64}, Ref{Float64}),
+              handle(), P.ptr, length(P), Int32(something(mindim, 1)), Int32(something(maxdim, -1)),
+              Float64(something(cutoff, -1.0)), Int32(something(use_absolute_cutoff, false)),
+              Int32(something(use_relative_cutoff, true)), n, terr, dcut))
+  parent = P isa GB300View ? P.parent : P
+  return GB300View(parent, P.ptr, Int(n[])), terr[], dcut[]
+end
+
+# Blockwise SVD with truncation (NDTensors/src/blocksparse/linearalgebra.jl:45-215): one
+# batched device call computes every block's SVD, the pooled sort, truncate! and the kept
+# dimensions; this method builds the reference's output structure from them.  Returns
+# `nothing` when a block does not converge, as the reference does.
+function LinearAlgebra.svd(T::GB300BlockSparseMatrix; min_blockdim=nothing, mindim=nothing, maxdim=nothing,
+                           cutoff=nothing, alg=nothing, use_absolute_cutoff=nothing, use_relative_cutoff=nothing)
+  nzb, rows, cols, offs = matrix_blocks(T)
+  nb = length(nzb)
+  ks = min.(rows, cols)
+  U = GB300Vector(undef, sum(rows .* ks))
+  S = GB300Vector(undef, sum(ks))
+  V = GB300Vector(undef, sum(cols .* ks))
+  kept = zeros(Int32, max(nb, 1))
+  spec = Vector{Float64}(undef, max(sum(ks), 1))
+  slen, terr, dcut = Ref{Int32}(0), Ref{Float64}(0), Ref{Float64}(0)
+  st = ccall((:nd_bs_svd_f64, LIB), Int32,
+             (Ptr{Cvoid}, Int32, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+              Ptr{Float64}, Int32, Int32, Float64, Int32, Int32, Int32, Ptr{Int32}, Ptr{Float64}, Ref{Int32},
+              Ref{Float64}, Ref{Float64}),
+             handle(), nb, rows, cols, offs, data(T).ptr, U.ptr, S.ptr, V.ptr,
+             Int32(something(mindim, 1)), Int32(something(maxdim, -1)), Float64(something(cutoff, -1.0)),
+             Int32(something(use_absolute_cutoff, false)), Int32(something(use_relative_cutoff, true)),
+             Int32(something(min_blockdim, 0)), kept, spec, slen, terr, dcut)
+  st == ND_ERR_NOCONV && return nothing
+  check(st)
+  # blocks whose kept dimension is 0 are dropped (linearalgebra.jl:86-114)
+  surv = [n for n in 1:nb if kept[n] > 0]
+  i1, i2 = ind(T, 1), ind(T, 2)
+  uind = dag(sim(i1))
+  vind = dag(sim(i2))
+  resize!(uind, length(surv))
+  resize!(vind, length(surv))
+  for (n, m) in enumerate(surv)
+    setblock!(uind, resize(block(i1, nzb[m][1]), Int(kept[m])), n)
+    setblock!(vind, resize(block(i2, nzb[m][2]), Int(kept[m])), n)
+  end
+  nzblocksU = [Block(nzb[m][1], UInt(n)) for (n, m) in enumerate(surv)]
+  nzblocksS = [Block(UInt(n), UInt(n)) for n in 1:length(surv)]
+  nzblocksV = [Block(nzb[m][2], UInt(n)) for (n, m) in enumerate(surv)]
+  indsU = NDTensors.setindex(inds(T), uind, 2)
+  indsV = NDTensors.permute(NDTensors.setindex(inds(T), vind, 1), (2, 1))
+  indsS = NDTensors.setindex(NDTensors.setindex(inds(T), dag(uind), 1), dag(vind), 2)
+  # the library wrote the kept blocks in this order, each column-major m x k / n x k,
+  # which is exactly the BlockOffsets layout of nzblocksU / nzblocksV
+  bU, _ = NDTensors.blockoffsets(nzblocksU, indsU)
+  bV, _ = NDTensors.blockoffsets(nzblocksV, indsV)
+  bS = BlockOffsets{2}()
+  o = 0
+  for (n, m) in enumerate(surv)
+    insert!(bS, nzblocksS[n], o)
+    o += Int(kept[m])
+  end
+  Ut = BlockSparseTensor(NDTensors.BlockSparse(U, bU), indsU)
+  St = DiagBlockSparseTensor(NDTensors.DiagBlockSparse(S, bS), indsS)
+  Vt = BlockSparseTensor(NDTensors.BlockSparse(V, bV), indsV)
+  return Ut, St, Vt, Spectrum(spec[1:slen[]], terr[])
+end
+
+# Blockwise QR through qx (NDTensors/src/blocksparse/linearalgebra.jl:351-415): one batched
+# Householder launch; Q blocks (b1, n) of m x k, R blocks (n, b2) of k x n_cols.
+function qx_gb300(T::GB300BlockSparseMatrix; positive=nothing)
+  nzb, rows, cols, offs = matrix_blocks(T)
+  nb = length(nzb)
+  ks = min.(rows, cols)
+  Q = GB300Vector(undef, sum(rows .* ks))
+  X = GB300Vector(undef, sum(cols .* ks))
+  check(ccall((:nd_bs_qr_f64, LIB), Int32,
+              (Ptr{Cvoid}, Int32, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32),
+              handle(), nb, rows, cols, offs, data(T).ptr, Q.ptr, X.ptr, Int32(something(positive, false))))
+  itl = ind(T, 1)
+  iq = dag(sim(itl))
+  resize!(iq, nb)
+  for (n, b) in enumerate(nzb)
+    setblock!(iq, resize(block(itl, b[1]), ks[n]), n)
+  end
+  indsQ = NDTensors.setindex(inds(T), iq, 2)
+  indsX = NDTensors.setindex(inds(T), dag(iq), 1)
+  nzblocksQ = [Block(b[1], UInt(n)) for (n, b) in enumerate(nzb)]
+  nzblocksX = [Block(UInt(n), b[2]) for (n, b) in enumerate(nzb)]
+  bQ, _ = NDTensors.blockoffsets(nzblocksQ, indsQ)
+  bX, _ = NDTensors.blockoffsets(nzblocksX, indsX)
+  return BlockSparseTensor(NDTensors.BlockSparse(Q, bQ), indsQ), BlockSparseTensor(NDTensors.BlockSparse(X, bX), indsX)
+end
+LinearAlgebra.qr(T::GB300BlockSparseMatrix; kwargs...) = qx_gb300(T; kwargs...)
+
+# plan of one block-sparse contraction (kept by the pullback)
+function bs_plan(T1, labels1, T2, labels2, labelsR)
+  a1 = desc_arrays(T1)
+  a2 = desc_arrays(T2)
+  plan = Ref{Ptr{Cvoid}}(C_NULL)
+  GC.@preserve a1 a2 begin
+    d1 = Ref(BsDesc(length(a1[1]), pointer(a1[1]), pointer(a1[2]), a1[5], pointer(a1[3]), pointer(a1[4])))
+    d2 = Ref(BsDesc(length(a2[1]), pointer(a2[1]), pointer(a2[2]), a2[5], pointer(a2[3]), pointer(a2[4])))
+    check(ccall((:nd_bs_plan_create, LIB), Int32,
+                (Ptr{Cvoid}, Ref{BsDesc}, Ptr{Int32}, Ref{BsDesc}, Ptr{Int32}, Int32, Ptr{Int32}, Ref{Ptr{Cvoid}}),
+                handle(), d1, Int32[labels1...], d2, Int32[labels2...], length(labelsR), Int32[labelsR...], plan))
+  end
+  return plan[]
+end
+
+# Pullback of R = contract(T1, T2): both cotangents (R̄ * T2 over T2's free labels and
+# T1 * R̄) in one grouped launch, with the structures of T1 and T2
+# (ext/ITensorsChainRulesCoreExt/itensor.jl:94-103; real FP64, so dag is the identity).
+function contract_pullback_gb300(T1, labels1, T2, labels2, labelsR, R̄)
+  plan = bs_plan(T1, labels1, T2, labels2, labelsR)
+  T̄1 = BlockSparseTensor(NDTensors.BlockSparse(GB300Vector(undef, length(data(T1))), blockoffsets(T1)), inds(T1))
+  T̄2 = BlockSparseTensor(NDTensors.BlockSparse(GB300Vector(undef, length(data(T2))), blockoffsets(T2)), inds(T2))
+  st = ccall((:nd_bs_contract_adjoint_f64, LIB), Int32,
+             (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32),
+             handle(), plan, data(R̄).ptr, data(T1).ptr, data(T2).ptr, data(T̄1).ptr, data(T̄2).ptr, PRECISION[])
+  ccall((:nd_bs_plan_destroy, LIB), Int32, (Ptr{Cvoid},), plan)
+  check(st)
+  return T̄1, T̄2
+end
+
+function ChainRulesCore.rrule(::typeof(NDTensors.contract), T1::GB300BlockSparseTensor, labels1,
+                              T2::GB300BlockSparseTensor, labels2, labelsR=contract_labels(labels1, labels2))
+  R = NDTensors.contract(T1, labels1, T2, labels2, labelsR)
+  function contract_pullback(R̄)
+    T̄1, T̄2 = contract_pullback_gb300(T1, labels1, T2, labels2, labelsR, ChainRulesCore.unthunk(R̄))
+    return (NoTangent(), T̄1, NoTangent(), T̄2, NoTangent(), NoTangent())
+  end
+  return R, contract_pullback
 end
 
 end # module

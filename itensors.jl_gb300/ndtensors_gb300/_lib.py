@@ -64,6 +64,8 @@ SIGNATURES = {
     "nd_d2h": [_P, _P, _P, C.c_size_t],
     "nd_memset0": [_P, _P, C.c_size_t],
     "nd_set_ozaki_slices": [_P, _I32],
+    "nd_set_spin_limit": [_P, C.c_uint32],
+    "nd_set_svd_max_sweeps": [_P, _I32],
     "nd_launch_count": [_P, _PI64],
     "nd_profile_enable": [_P, _I32],
     "nd_profile_read": [_P, _I32, C.c_char_p, _PI64, _PD, _PI32],

@@ -7,6 +7,7 @@ Mirrors:
   truncate!(P; ...)                             NDTensors/src/truncate.jl:23-107
   combiner matricization (permutedims_combine)  NDTensors/src/blocksparse/blocksparsetensor.jl:537-638,
                                                 src/qn/qnindex.jl:359-426
+  uncombine                                     NDTensors/src/blocksparse/blocksparsetensor.jl:664-791
 The factorizations, the spectrum sort and truncate! run on the device; only
 the block structure (which blocks survive, their new dims) is host logic.
 """
@@ -43,7 +44,9 @@ def _matrix_blocks(T: BlockSparseTensor):
 
 def svd(T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absolute_cutoff=None,
         use_relative_cutoff=None, min_blockdim=None):
-    """Returns (U, S, V, Spectrum, kept) or raises NoConvergence (the reference returns nothing).
+    """Returns (U, S, V, Spectrum, kept), or None when a block's SVD did not converge within
+    the sweep limit (ND_ERR_NOCONV), as the reference's svd returns `nothing`
+    (NDTensors/src/linearalgebra/linearalgebra.jl:120-127, blocksparse/linearalgebra.jl:65-67).
 
     U has inds (T.inds[0], u), S is a list of per-block singular values (Diag),
     V has inds (T.inds[1], v); u and v carry one block per surviving nz block.
@@ -60,12 +63,15 @@ def svd(T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absolut
     kept = (C.c_int32 * max(1, nb))()
     spec = (C.c_double * max(1, sum(ks)))()
     slen, terr, dcut = C.c_int32(), C.c_double(), C.c_double()
-    h.call("nd_bs_svd_f64", nb, i64arr(rows), i64arr(cols), i64arr(T.offsets), C.c_void_p(T.data.data_ptr()),
-           C.c_void_p(U.data_ptr()), C.c_void_p(S.data_ptr()), C.c_void_p(V.data_ptr()),
-           int(_opt(mindim, 1)), int(_opt(maxdim, -1)), float(_opt(cutoff, -1.0)),
-           int(bool(use_absolute_cutoff)) if use_absolute_cutoff is not None else 0,
-           int(bool(use_relative_cutoff)) if use_relative_cutoff is not None else 1,
-           int(_opt(min_blockdim, 0)), kept, spec, C.byref(slen), C.byref(terr), C.byref(dcut))
+    try:
+        h.call("nd_bs_svd_f64", nb, i64arr(rows), i64arr(cols), i64arr(T.offsets), C.c_void_p(T.data.data_ptr()),
+               C.c_void_p(U.data_ptr()), C.c_void_p(S.data_ptr()), C.c_void_p(V.data_ptr()),
+               int(_opt(mindim, 1)), int(_opt(maxdim, -1)), float(_opt(cutoff, -1.0)),
+               int(bool(use_absolute_cutoff)) if use_absolute_cutoff is not None else 0,
+               int(bool(use_relative_cutoff)) if use_relative_cutoff is not None else 1,
+               int(_opt(min_blockdim, 0)), kept, spec, C.byref(slen), C.byref(terr), C.byref(dcut))
+    except NoConvergence:
+        return None
     kept = list(kept[:nb])
     surv = [n for n in range(nb) if kept[n] > 0]
     kdims = [kept[n] for n in surv]
@@ -113,7 +119,10 @@ def eigen(T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absol
         c = 1.01 * nrm if nrm > 0.0 else 1.0
         blk.view(r, r).diagonal().add_(c)            # column-major: the diagonal is the same either way
         shifts.append(c)
-    _, S, Vt, _, _ = svd(BlockSparseTensor(T.inds, T.blocks, T.offsets, W))
+    out = svd(BlockSparseTensor(T.inds, T.blocks, T.offsets, W))
+    if out is None:
+        return None                                  # a block did not converge (the reference returns nothing)
+    _, S, Vt, _, _ = out
     lams, vecs = [], []
     for n, (off, r) in enumerate(zip(Vt.offsets, rows)):
         lam = S[n] - shifts[n]
@@ -284,3 +293,75 @@ def matricize(T: BlockSparseTensor, qinds, row_dims, col_dims):
         handle(T.data.device.index or 0).call("nd_block_copy_f64", len(copies), arr, C.c_void_p(T.data.data_ptr()),
                                               C.c_void_p(data.data_ptr()))
     return M, (rsec, rplace), (csec, cplace)
+
+
+def uncombine(T: BlockSparseTensor, combdim, group, info):
+    """Split the fused dimension ``combdim`` of T back into the indices of ``group``
+    (NDTensors/src/blocksparse/blocksparsetensor.jl:693-791: uncombine_output +
+    uncombine, with uncombine_blocks :664-678).
+
+    ``group``: the (sectors, arrow) of the fused indices, in fusion order; ``info``:
+    the (combined sectors, place) that ``matricize`` returned for that group.  Every
+    block of T, in T's order, yields one block per uncombined sector of its combined
+    sector, in the combined index's sorted order (the reference's block order); the
+    sub-block is the slice [off, off + dim) of T's block along ``combdim``, copied on
+    the device (nd_block_copy_f64) into its own column-major block.
+    """
+    import torch
+    _, place = info
+    subs = {}
+    for orig, (cb, off) in place.items():
+        subs.setdefault(cb, []).append((off, orig))
+    for v in subs.values():
+        v.sort()
+    gdims = [tuple(d for _, d in sec) for sec, _ in group]
+    nbs = [len(d) for d in gdims]
+    if T.rank - 1 + len(gdims) > MAX_RANK:
+        raise ValueError(f"uncombine: result rank exceeds {MAX_RANK}")
+
+    def split(lin0):
+        out = []
+        for n in nbs:
+            out.append(lin0 % n + 1)
+            lin0 //= n
+        return tuple(out)
+
+    inds = list(T.inds[:combdim]) + gdims + list(T.inds[combdim + 1:])
+    blocks, pieces = [], []
+    for i, b in enumerate(T.blocks):
+        for off, orig in subs[b[combdim]]:
+            blocks.append(tuple(b[:combdim]) + split(orig) + tuple(b[combdim + 1:]))
+            pieces.append((i, off))
+    offs, nnz = blockoffsets(blocks, inds)
+    data = torch.empty(max(nnz, 1), dtype=torch.float64, device=T.data.device)[:nnz]
+    R = BlockSparseTensor([tuple(x) for x in inds], blocks, offs, data)
+    copies = []
+    ng = len(gdims)
+    for j, (i, off) in enumerate(pieces):
+        tb = T.blockdims(T.blocks[i])
+        tst = [1]
+        for d in tb[:-1]:
+            tst.append(tst[-1] * d)
+        rb = R.blockdims(blocks[j])
+        c = BlockCopy()
+        c.src_off = T.offsets[i] + off * tst[combdim]
+        c.dst_off = offs[j]
+        c.rank = len(rb)
+        src = list(tst[:combdim])
+        g = tst[combdim]
+        for k in range(ng):                      # the fused dimension splits first index fastest
+            src.append(g)
+            g *= rb[combdim + k]
+        src += tst[combdim + 1:]
+        dst = 1
+        for k in range(len(rb)):
+            c.dims[k] = rb[k]
+            c.src_strides[k] = src[k]
+            c.dst_strides[k] = dst
+            dst *= rb[k]
+        copies.append(c)
+    if copies:
+        arr = (BlockCopy * len(copies))(*copies)
+        handle(T.data.device.index or 0).call("nd_block_copy_f64", len(copies), arr, C.c_void_p(T.data.data_ptr()),
+                                              C.c_void_p(data.data_ptr()))
+    return R

@@ -267,3 +267,54 @@ def matricize(t, qinds, row_dims, col_dims):
                 (rdim, cdim), order="F")
             view[roff:roff + rdim, coff:coff + cdim] = mat
     return m, (rsec, rplace), (csec, cplace)
+
+
+def uncombine(t, combdim, group_dims, group_info):
+    """Split the fused dimension ``combdim`` of ``t`` back into the indices of its group.
+
+    Restates ``uncombine_output`` / ``uncombine`` (blocksparsetensor.jl:693-791, with
+    ``uncombine_blocks`` :664-678 and ``perm_blocks`` :510-517): every block of ``t``,
+    in ``t``'s block order, yields one block per uncombined sector of its combined
+    sector, in the combined index's sorted order; the sorted position is mapped back
+    to the fused product block through the combiner's permutation, and the fused
+    block number is split into the group's block numbers column-major (first index
+    fastest, ``reshape(::Block, indsT, indsR)``).  The data of sub-block j is the
+    slice [off_j, off_j + dim_j) of the combined block along ``combdim``, reshaped.
+
+    ``group_dims``: per group index, its tuple of sector dims (uncombined, original
+    order).  ``group_info``: (combined sectors, place) as returned by ``matricize``
+    for that group, place[orig] = (combined block, offset) with orig the 1-based
+    fused product block.
+    """
+    _, place = group_info
+    subs = {}
+    for orig, (cb, off) in place.items():
+        subs.setdefault(cb, []).append((off, orig))
+    for v in subs.values():
+        v.sort()
+    nbs = [len(d) for d in group_dims]
+
+    def split(lin0):
+        out = []
+        for n in nbs:
+            out.append(lin0 % n + 1)
+            lin0 //= n
+        return tuple(out)
+
+    inds = list(t.inds[:combdim]) + [tuple(d) for d in group_dims] + list(t.inds[combdim + 1:])
+    blocks, pieces = [], []
+    for i, b in enumerate(t.blocks):
+        for off, orig in subs[b[combdim]]:
+            sub = split(orig - 1)
+            blocks.append(tuple(b[:combdim]) + sub + tuple(b[combdim + 1:]))
+            pieces.append((i, off))
+    offs, nnz = blockoffsets(blocks, inds)
+    r = BlockSparseTensor(inds, blocks, offs, np.empty(nnz))
+    for j, (i, off) in enumerate(pieces):
+        dst = r.blockview(j)
+        gsize = int(np.prod([dst.shape[combdim + k] for k in range(len(group_dims))]))
+        src = t.blockview(i)
+        sl = [slice(None)] * t.rank
+        sl[combdim] = slice(off, off + gsize)
+        dst[...] = src[tuple(sl)].reshape(dst.shape, order="F")
+    return r

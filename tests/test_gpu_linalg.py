@@ -288,3 +288,28 @@ def test_diag_blocksparse_contraction_rebuilds_svd(nd):
     ref, _ = obs.contract(Uo, (1, -1), Do, (-1, 2), (1, 2))
     assert US.blocks == [tuple(b) for b in ref.blocks] and US.offsets == list(ref.offsets)
     assert odense.rel_frobenius_error(US.data_numpy(), ref.data) <= 1e-14
+
+
+def test_uncombine_inverts_matricize(nd):
+    """combine -> uncombine is the identity up to block order (blocksparsetensor.jl:537-638 and
+    :693-791), and the uncombined structure, offsets and data are those of the oracle."""
+    net = networks.qn_heff(chi=256, seed=14)
+    psi = net["psi"]
+    qi = net["qinds"]["psi"]
+    qp = [(q.sectors, q.arrow) for q in qi]
+    M, rinfo, cinfo = nd.matricize(_gpu(nd, psi), qp, (0, 1), (2, 3))
+    rows = nd.uncombine(M, 0, qp[:2], rinfo)                 # (l, s1, (s2 r))
+    back = nd.uncombine(rows, 2, qp[2:], cinfo)             # (l, s1, s2, r)
+    Mo, orinfo, ocinfo = obs.matricize(psi, qi, (0, 1), (2, 3))
+    ro = obs.uncombine(Mo, 0, [qi[0].dims, qi[1].dims], orinfo)
+    bo = obs.uncombine(ro, 2, [qi[2].dims, qi[3].dims], ocinfo)
+    for got, want in ((rows, ro), (back, bo)):
+        assert got.blocks == [tuple(b) for b in want.blocks]
+        assert got.offsets == list(want.offsets)
+        np.testing.assert_array_equal(got.data_numpy(), want.data)
+    data = back.data_numpy()
+    assert sorted(back.blocks) == sorted(tuple(b) for b in psi.blocks)
+    for i, b in enumerate(psi.blocks):
+        j = back.blocks.index(tuple(b))
+        n = int(np.prod(psi.blockdims(b)))
+        np.testing.assert_array_equal(data[back.offsets[j]:back.offsets[j] + n], psi.data[psi.offsets[i]:psi.offsets[i] + n])

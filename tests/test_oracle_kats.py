@@ -233,3 +233,14 @@ def test_package_workloads_match_oracle_generators():
     for k in ("L", "psi", "W1", "R"):
         assert [tuple(b) for b in net[k].blocks] == pnet[k].blocks
         np.testing.assert_array_equal(net[k].data, pnet[k].data)
+
+
+def test_uncombine_roundtrip_oracle():
+    """Oracle uncombine (blocksparsetensor.jl:693-791) undoes matricize's combiners."""
+    net = networks.qn_heff(chi=256, seed=3)
+    psi, qi = net["psi"], net["qinds"]["psi"]
+    m, rinfo, cinfo = bs.matricize(psi, qi, (0, 1), (2, 3))
+    u = bs.uncombine(bs.uncombine(m, 0, [qi[0].dims, qi[1].dims], rinfo), 2, [qi[2].dims, qi[3].dims], cinfo)
+    assert sorted(u.blocks) == sorted(psi.blocks) and u.nnz == psi.nnz
+    for i, b in enumerate(psi.blocks):
+        assert np.array_equal(u.blockview(u.blocks.index(tuple(b))), psi.blockview(i))
