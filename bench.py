@@ -256,11 +256,12 @@ def tune_summary(h):
         for line in path.read_text().splitlines():
             if line.startswith("#") or not line.strip():
                 continue
-            key, mult, skinny, best, dflt = line.split("\t")
+            key, mult, skinny, pair2, best, dflt = line.split("\t")
             prec = key.split("/")[1]
             npairs = sum(int(b.split("x")[1]) for b in key.split("/")[3].split(","))
             out.append({"precision": {"p0": "fp64", "p1": "ozaki", "p2": "bf16x3"}.get(prec, prec),
                         "block_pairs": npairs, "splitk_mult": int(mult), "skinny_fp64": int(skinny),
+                        "split_tile": "256x64 (CTA pair)" if int(pair2) else "128x64",
                         "best_ms": round(float(best), 4), "default_ms": round(float(dflt), 4)})
     return {"entries": len(out), "choices": out}
 

@@ -77,6 +77,11 @@ nd_status nd_set_spin_limit(nd_handle h, uint32_t polls);
  * case where the reference's svd returns `nothing`
  * (NDTensors/src/linearalgebra/linearalgebra.jl:91-127). */
 nd_status nd_set_svd_max_sweeps(nd_handle h, int32_t sweeps);
+/* Output tile of the split-precision (Ozaki / 3xBF16) GEMM when the autotuner has no
+ * entry for a contraction: 0 (default) = 128 x 64 tiles on single CTAs, 1 = 256 x 64
+ * tiles on pairs of CTAs (tcgen05.mma.cta_group::2).  With tuning on, both are timed
+ * and the faster is cached.  No counterpart in the reference. */
+nd_status nd_set_split_tile(nd_handle h, int32_t shape);
 /* Number of slice digits used by ND_PREC_OZAKI (3..6, default 5). */
 nd_status nd_set_ozaki_slices(nd_handle h, int32_t slices);
 /* Count of kernel launches this handle enqueued so far (diagnostics). */
@@ -161,6 +166,12 @@ nd_status nd_bs_plan_sizes(nd_plan plan, int32_t *npairs, int32_t *nnzblocksR, i
  * positions in the respective block lists.  Any pointer may be NULL. */
 nd_status nd_bs_plan_get(nd_plan plan, int32_t *blocksR, int64_t *offsetsR, int32_t *pairs);
 nd_status nd_bs_plan_destroy(nd_plan plan);
+/* Write the plan's output blocks at these element offsets (host, nnzblocksR entries)
+ * instead of the reference's first-appearance offsets: the contraction then lands
+ * directly in a caller's layout (e.g. an H_eff apply writing back into psi's block
+ * order, which a Krylov solver needs).  The caller guarantees the blocks do not
+ * overlap.  No counterpart in the reference (its result is always a fresh tensor). */
+nd_status nd_bs_plan_set_output_offsets(nd_plan plan, const int64_t *offsetsR);
 
 /* R = alpha * contract(A, B) executed as ONE grouped-GEMM launch over all
  * block pairs: pairs are grouped by output block, the first pair of a group
@@ -168,6 +179,16 @@ nd_status nd_bs_plan_destroy(nd_plan plan);
  * with compute_alpha == 1, contract_utilities.jl:2-15). */
 nd_status nd_bs_contract_f64(nd_handle h, nd_plan plan, double *R, const double *A,
                              const double *B, double alpha, int32_t precision);
+
+/* R = alpha * contract(T, D) for a block-sparse T and a block-diagonal DiagBlockSparse D
+ * (NDTensors/src/blocksparse/diagblocksparse.jl:601-696; per pair the diagonal
+ * contraction of NDTensors/src/diag/tensoralgebra/contract.jl:103-214).  The plan is
+ * built with nd_bs_plan_create from T and D's block structure (every D block has equal
+ * block numbers); D's data is the diagonal of each of its blocks, block b's
+ * min(block dims) values starting at diag_offsets[b] (host).  Output structure and
+ * block order are the plan's; elements off the diagonal of D's indices are zero. */
+nd_status nd_bs_contract_diag_f64(nd_handle h, nd_plan plan, double *R, const double *T, const double *Ddiag,
+                                  const int64_t *diag_offsets, double alpha);
 
 /* Pullback of R = contract(A, B) for the same plan (ext/ITensorsChainRulesCoreExt/itensor.jl:94-103):
  * Abar = Rbar * B (contract over B's free labels), Bbar = A * Rbar.  Both
@@ -203,6 +224,20 @@ nd_status nd_bs_svd_f64(nd_handle h, int32_t nblocks, const int64_t *rows, const
                         int32_t *kept, double *spectrum, int32_t *spectrum_len,
                         double *truncerr, double *docut);
 
+/* Blockwise eigendecomposition of a real symmetric block-diagonal matrix with
+ * truncation (eigen(::Hermitian{<:BlockSparseMatrix}), NDTensors/src/blocksparse/
+ * linearalgebra.jl:221-348; per block the dense Hermitian eigen sorted by |lambda|
+ * descending, NDTensors/src/linearalgebra/linearalgebra.jl:162-213).  Block b is
+ * dims[b] x dims[b] at offsets[b] in A.  Outputs for the kept blocks in input order:
+ * D, the concatenated kept eigenvalues (|lambda| descending within a block), and V,
+ * the concatenated dims[b] x kept[b] column-major eigenvector blocks; kept[b] = 0 for
+ * a dropped block.  Size D and V for the untruncated case.  spectrum (host) receives
+ * the truncated pooled |lambda| (sorted descending).  ND_ERR_NOCONV as nd_bs_svd_f64. */
+nd_status nd_bs_eigen_f64(nd_handle h, int32_t nblocks, const int64_t *dims, const int64_t *offsets, const double *A,
+                          double *D, double *V, int32_t mindim, int32_t maxdim, double cutoff,
+                          int32_t use_absolute_cutoff, int32_t use_relative_cutoff, int32_t min_blockdim,
+                          int32_t *kept, double *spectrum, int32_t *spectrum_len, double *truncerr, double *docut);
+
 /* Blockwise QR (NDTensors/src/blocksparse/linearalgebra.jl:351-415, dense qr /
  * qr_positive NDTensors/src/linearalgebra/linearalgebra.jl:321-381).  Q blocks
  * m_b x k_b, R blocks k_b x n_b, k_b = min(m_b, n_b), concatenated in order. */
@@ -230,6 +265,30 @@ typedef struct {
 } nd_block_copy;
 nd_status nd_block_copy_f64(nd_handle h, int32_t n, const nd_block_copy *list /* host */, const double *src,
                             double *dst);
+
+/* ---- vector-space operations (Krylov solvers) ---------------------------------
+ * The VectorInterface methods the reference defines for ITensors
+ * (ext/ITensorsVectorInterfaceExt/ITensorsVectorInterfaceExt.jl:5-84) on flat FP64
+ * device vectors of length n, plus the two block forms of classical Gram-Schmidt
+ * against k <= 32 basis vectors stored ldv apart.  Results and scalars are DEVICE
+ * pointers and nothing synchronises, so a Krylov iteration built from these calls and
+ * contractions can be captured into one CUDA graph (make one eager call per handle
+ * before capturing: the first reduction allocates its fixed partial-sum buffer).
+ * Reductions run in a fixed order: replays reproduce eager results bit for bit. */
+nd_status nd_vec_inner_f64(nd_handle h, int64_t n, const double *x, const double *y, double *out);   /* inner(x, y)     */
+nd_status nd_vec_norm_f64(nd_handle h, int64_t n, const double *x, double *out);                     /* norm(x)         */
+/* y = alpha * x, times (invert = 0) or divided by (invert = 1) the device scalar *s when s != NULL:
+ * scale(x, alpha) / scale!(y, x, alpha) */
+nd_status nd_vec_scale_f64(nd_handle h, int64_t n, const double *x, double *y, double alpha, const double *s,
+                           int32_t invert);
+/* y = beta * y + alpha * x (beta == 0 overwrites y): add!(y, x, alpha, beta) */
+nd_status nd_vec_add_f64(nd_handle h, int64_t n, const double *x, double *y, double alpha, double beta);
+/* out[j] = inner(V_j, x), V_j = V + j * ldv, j < k */
+nd_status nd_vec_dots_f64(nd_handle h, int64_t n, int32_t k, const double *V, int64_t ldv, const double *x,
+                          double *out);
+/* y += sign * sum_j coef[j] * V_j, j < k (coef a device array) */
+nd_status nd_vec_update_f64(nd_handle h, int64_t n, int32_t k, const double *V, int64_t ldv, const double *coef,
+                            double sign, double *y);
 
 /* ---- autotuner -------------------------------------------------------------
  * Execution parameters of a contraction (today: the split-K target of the FP64

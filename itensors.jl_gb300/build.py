@@ -18,7 +18,7 @@ CSRC = HERE / "csrc"
 OUT = HERE / "ndtensors_gb300" / "libndtensors_gb300.so"
 BUILD = HERE / "_build"
 SOURCES = ["nd_api.cu", "nd_permute.cu", "nd_plan.cu", "nd_contract.cu", "nd_gemm_f64.cu",
-           "nd_ozaki.cu", "nd_linalg.cu", "nd_noalloc.cu"]
+           "nd_ozaki.cu", "nd_linalg.cu", "nd_noalloc.cu", "nd_vector.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -44,6 +44,12 @@ nd_status nd_workspace(nd_handle h, size_t bytes, void** out) {
   return ND_OK;
 }
 
+nd_status nd_dalloc(nd_handle h, void** p, size_t bytes) {
+  *p = nullptr;
+  ND_CUDA(h, cudaMallocAsync(p, std::max<size_t>(bytes, 16), h->stream));
+  return ND_OK;
+}
+
 bool nd_capturing(nd_handle h) {
   if (h->capturing) return true;
   cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
@@ -100,6 +106,16 @@ nd_status nd_create(int32_t device, nd_handle* out) {
     const DeviceStatus init{0, 0, ND_SPIN_LIMIT, 0};
     cudaMemcpy(h->d_status, &init, sizeof(init), cudaMemcpyHostToDevice);
   }
+  {
+    // execution state is allocated stream-ordered from the default pool: keep freed
+    // blocks in the pool instead of returning them to the system at every sync
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   cudaDeviceSynchronize();
   *out = h;
   return ND_OK;
@@ -111,6 +127,9 @@ nd_status nd_destroy(nd_handle h) {
   cudaStreamSynchronize(h->stream);
   nd_dense_cache_clear(h);
   if (h->ws) cudaFree(h->ws);
+  if (h->pin) cudaFreeHost(h->pin);
+  if (h->order_ev) cudaEventDestroy(h->order_ev);
+  if (h->vec_part) cudaFree(h->vec_part);
   if (h->d_status) cudaFree(h->d_status);
   for (auto& r : h->prof) { cudaEventDestroy(r.e0); cudaEventDestroy(r.e1); }
   for (auto e : h->event_pool) cudaEventDestroy(e);
@@ -196,6 +215,13 @@ nd_status nd_set_svd_max_sweeps(nd_handle h, int32_t sweeps) {
   return ND_OK;
 }
 
+nd_status nd_set_split_tile(nd_handle h, int32_t shape) {
+  if (!h) return ND_ERR_ARG;
+  if (shape != 0 && shape != 1) return nd_fail(h, ND_ERR_ARG, "split tile shape must be 0 (128x64) or 1 (256x64 on CTA pairs)");
+  h->split_pair2 = shape;
+  return ND_OK;
+}
+
 nd_status nd_set_ozaki_slices(nd_handle h, int32_t s) {
   if (!h) return ND_ERR_ARG;
   if (s < 3 || s > 6) return nd_fail(h, ND_ERR_ARG, "ozaki slices must be in 3..6 (got %d)", s);
@@ -205,7 +231,8 @@ nd_status nd_set_ozaki_slices(nd_handle h, int32_t s) {
 
 // ---- autotuner cache ---------------------------------------------------------
 // File format: '#' comment lines, then one line per entry:
-//   <key> TAB <splitk_mult> TAB <skinny> TAB <best_ms> TAB <default_ms>
+//   <key> TAB <splitk_mult> TAB <skinny> TAB <pair2> TAB <best_ms> TAB <default_ms>
+// (version 1 files, without the pair2 column, load with the default tile shape)
 nd_status nd_tune_enable(nd_handle h, int32_t enable) {
   if (!h) return ND_ERR_ARG;
   h->tuning = enable != 0;
@@ -223,10 +250,10 @@ nd_status nd_tune_save(nd_handle h, const char* path) {
   if (!path) return nd_fail(h, ND_ERR_ARG, "tune_save: NULL path");
   FILE* f = std::fopen(path, "w");
   if (!f) return nd_fail(h, ND_ERR_ARG, "tune_save: cannot open %s", path);
-  std::fprintf(f, "# ndtensors_gb300 autotune cache v1: key splitk_mult skinny best_ms default_ms\n");
+  std::fprintf(f, "# ndtensors_gb300 autotune cache v2: key splitk_mult skinny pair2 best_ms default_ms\n");
   for (const auto& e : h->tune)
-    std::fprintf(f, "%s\t%d\t%d\t%.6f\t%.6f\n", e.first.c_str(), e.second.choice.splitk_mult,
-                 e.second.choice.skinny, e.second.best_ms, e.second.default_ms);
+    std::fprintf(f, "%s\t%d\t%d\t%d\t%.6f\t%.6f\n", e.first.c_str(), e.second.choice.splitk_mult,
+                 e.second.choice.skinny, e.second.choice.pair2, e.second.best_ms, e.second.default_ms);
   const bool ok = std::fclose(f) == 0;
   return ok ? ND_OK : nd_fail(h, ND_ERR_ARG, "tune_save: write to %s failed", path);
 }
@@ -249,9 +276,21 @@ nd_status nd_tune_load(nd_handle h, const char* path) {
     char* tab = std::strchr(line, '\t');
     TuneEntry e;
     int used = 0;
-    if (!tab || std::sscanf(tab + 1, "%d\t%d\t%lf\t%lf%n", &e.choice.splitk_mult, &e.choice.skinny, &e.best_ms,
-                            &e.default_ms, &used) != 4 || tab[1 + used] != 0 || e.choice.splitk_mult < 0 ||
-        e.choice.splitk_mult > 64 || (e.choice.skinny != 0 && e.choice.skinny != 1)) {
+    bool parsed = false;
+    if (tab) {
+      int nf = 0;
+      int ntabs = 0;
+      for (const char* c = tab + 1; *c; ++c) ntabs += *c == '\t';
+      if (ntabs == 4)
+        nf = std::sscanf(tab + 1, "%d\t%d\t%d\t%lf\t%lf%n", &e.choice.splitk_mult, &e.choice.skinny,
+                         &e.choice.pair2, &e.best_ms, &e.default_ms, &used) == 5;
+      else if (ntabs == 3)
+        nf = std::sscanf(tab + 1, "%d\t%d\t%lf\t%lf%n", &e.choice.splitk_mult, &e.choice.skinny, &e.best_ms,
+                         &e.default_ms, &used) == 4;
+      parsed = nf && tab[1 + used] == 0;
+    }
+    if (!parsed || e.choice.splitk_mult < 0 || e.choice.splitk_mult > 64 ||
+        (e.choice.skinny != 0 && e.choice.skinny != 1) || (e.choice.pair2 != 0 && e.choice.pair2 != 1)) {
       st = nd_fail(h, ND_ERR_ARG, "tune_load: malformed entry at %s:%d", path, lineno);
       break;
     }

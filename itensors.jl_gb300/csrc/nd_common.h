@@ -38,6 +38,7 @@ __device__ __forceinline__ uint32_t nd_spin_limit(const DeviceStatus* st) {
 struct TuneChoice {
   int32_t splitk_mult = 4;   // FP64 tile kernel: split-K balances work over splitk_mult x SMs CTAs (0 = off)
   int32_t skinny = 1;        // 1: skinny groups (N <= 8, K <= 32) on the FP64 CUDA-core kernel
+  int32_t pair2 = 0;         // split GEMM tile shape: 1 = 256 x 64 on CTA pairs, 0 = 128 x 64 per CTA
 };
 struct TuneEntry {
   TuneChoice choice;
@@ -51,12 +52,17 @@ struct nd_context {
   int num_sms = 0;
   int ozaki_slices = 5;
   int svd_max_sweeps = -1;            // FP64 Jacobi sweep limit of the SVD (-1 = default 60)
+  int split_pair2 = 0;                // untuned split-GEMM tile shape (TuneChoice::pair2)
   std::string last_error;
   DeviceStatus* d_status = nullptr;   // device status word
   int64_t launches = 0;
-  // grow-only scratch arena (device)
+  // grow-only scratch arena (device) and its pinned host staging buffer (the planner's)
   void* ws = nullptr;
   size_t ws_size = 0;
+  void* pin = nullptr;
+  size_t pin_size = 0;
+  cudaEvent_t order_ev = nullptr;     // orders state used on a previous stream before the current one
+  void* vec_part = nullptr;           // per-CTA partial sums of the vector reductions (fixed size)
   // graph capture
   cudaGraph_t graph = nullptr;
   bool capturing = false;
@@ -85,6 +91,11 @@ bool nd_capturing(nd_handle h);
 nd_status nd_fail(nd_handle h, nd_status code, const char* fmt, ...);
 nd_status nd_cuda_check(nd_handle h, cudaError_t e, const char* what);
 nd_status nd_workspace(nd_handle h, size_t bytes, void** out);
+// Device memory for a contraction's execution state: stream-ordered allocations on
+// the handle's stream from the device's default pool, which nd_create keeps from
+// returning freed memory to the system, so rebuilding state per plan costs no
+// device-wide synchronisation.
+nd_status nd_dalloc(nd_handle h, void** p, size_t bytes);
 nd_status nd_check_device_status(nd_handle h, const char* what);  // syncs
 
 #define ND_CUDA(h, call)                                              \

@@ -16,23 +16,17 @@
 #include <map>
 #include <string>
 #include <new>
+#include <climits>
 
-nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups, int precision);
+nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups, int precision,
+                         int pair2);
 nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double alpha, double beta);
 
-void ExecCache::free_all() {
-  if (d_pairs) cudaFree(d_pairs);
-  if (d_items) cudaFree(d_items);
-  if (d_operands) cudaFree(d_operands);
-  if (d_pack) cudaFree(d_pack);
-  if (d_exp) cudaFree(d_exp);
-  if (d_pack_items) cudaFree(d_pack_items);
-  if (d_rowmax) cudaFree(d_rowmax);
-  if (d_sk_items) cudaFree(d_sk_items);
-  if (d_split_pairs) cudaFree(d_split_pairs);
-  if (d_split_items) cudaFree(d_split_items);
-  if (d_ws) cudaFree(d_ws);
-  if (d_red) cudaFree(d_red);
+void ExecCache::free_all(nd_handle h) {
+  if (stream && stream != h->stream) cudaDeviceSynchronize();
+  for (void* p : {(void*)d_pairs, (void*)d_items, d_operands, d_pack, (void*)d_exp, d_pack_items, d_rowmax,
+                  (void*)d_sk_items, (void*)d_split_pairs, (void*)d_split_items, (void*)d_ws, (void*)d_red})
+    if (p) cudaFreeAsync(p, h->stream);
   *this = ExecCache{};
 }
 
@@ -103,8 +97,9 @@ bool nd_make_pair(const Roles& ro, const int64_t* dA, const int64_t* dB, const i
 }
 
 static nd_status upload(nd_handle h, void** dst, const void* src, size_t bytes) {
-  if (*dst) { cudaFree(*dst); *dst = nullptr; }
-  ND_CUDA(h, cudaMalloc(dst, std::max<size_t>(bytes, 16)));
+  if (*dst) { cudaFreeAsync(*dst, h->stream); *dst = nullptr; }
+  nd_status s = nd_dalloc(h, dst, bytes);
+  if (s) return s;
   if (bytes) ND_CUDA(h, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
   return ND_OK;
 }
@@ -179,8 +174,9 @@ static nd_status plan_split_k(nd_handle h, const std::vector<PairDesc>& pairs, s
   }
   if (red.empty()) return ND_OK;
   items.swap(out);
-  if (c.d_ws) { cudaFree(c.d_ws); c.d_ws = nullptr; }
-  ND_CUDA(h, cudaMalloc((void**)&c.d_ws, (size_t)slot * nd_gemm_f64_tile_elems() * sizeof(double)));
+  if (c.d_ws) { cudaFreeAsync(c.d_ws, h->stream); c.d_ws = nullptr; }
+  nd_status s0 = nd_dalloc(h, (void**)&c.d_ws, (size_t)slot * nd_gemm_f64_tile_elems() * sizeof(double));
+  if (s0) return s0;
   nd_status st = upload(h, (void**)&c.d_red, red.data(), red.size() * sizeof(ReduceItem));
   if (st) return st;
   c.nred = (int)red.size();
@@ -197,9 +193,11 @@ static bool group_skinny(const std::vector<PairDesc>& pairs, size_t i) {
 // Device state of one contraction for one set of execution parameters.
 static nd_status build_exec(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups,
                             int precision, int slices, const TuneChoice& tc) {
-  c.free_all();
+  c.free_all(h);
+  c.stream = h->stream;
   c.precision = precision;
   c.slices = slices;
+  c.req_pair2 = h->split_pair2;
   nd_status s = upload(h, (void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc));
   if (s) return s;
   // which pairs sit in skinny groups (routed to the FP64 CUDA-core kernel)
@@ -222,7 +220,7 @@ static nd_status build_exec(nd_handle h, ExecCache& c, const std::vector<PairDes
   } else {
     std::vector<PairDesc> regular;
     for (size_t i = 0; i < pairs.size(); ++i) if (!sk[i]) regular.push_back(pairs[i]);
-    if (!regular.empty() && (s = nd_split_build(h, c, regular, ngroups, precision))) return s;
+    if (!regular.empty() && (s = nd_split_build(h, c, regular, ngroups, precision, tc.pair2))) return s;
   }
   c.built = true;
   return ND_OK;
@@ -259,10 +257,10 @@ static nd_status tune_exec(nd_handle h, ExecCache& c, const std::vector<PairDesc
   std::vector<TuneChoice> cands;
   if (precision == ND_PREC_FP64) {
     for (int sk = 1; sk >= 0; --sk)
-      for (int m : {4, 0, 2, 8}) cands.push_back(TuneChoice{m, sk});
+      for (int m : {4, 0, 2, 8}) cands.push_back(TuneChoice{m, sk, 1});
   } else {
-    cands.push_back(TuneChoice{4, 1});
-    cands.push_back(TuneChoice{4, 0});
+    for (int sk = 1; sk >= 0; --sk)
+      for (int p2 : {h->split_pair2, 1 - h->split_pair2}) cands.push_back(TuneChoice{4, sk, p2});
   }
   cudaEvent_t e0, e1;
   ND_CUDA(h, cudaEventCreate(&e0));
@@ -300,7 +298,8 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
   if (precision != ND_PREC_FP64 && precision != ND_PREC_OZAKI && precision != ND_PREC_BF16X3)
     return nd_fail(h, ND_ERR_ARG, "unknown precision %d", precision);
   const int want_slices = precision == ND_PREC_OZAKI ? h->ozaki_slices : (precision == ND_PREC_BF16X3 ? 2 : 0);
-  if (!c.built || c.precision != precision || c.slices != want_slices) {
+  if (!c.built || c.precision != precision || c.slices != want_slices ||
+      (precision != ND_PREC_FP64 && c.req_pair2 != h->split_pair2)) {
     if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "contraction state must be built before graph capture (run once first)");
     const std::string key = tune_key(h, pairs, precision, want_slices);
     auto it = h->tune.find(key);
@@ -312,9 +311,19 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
       s = tune_exec(h, c, pairs, ngroups, ptrs, alpha, precision, want_slices, e);
       if (!s) h->tune[key] = e;
     } else {
-      s = build_exec(h, c, pairs, ngroups, precision, want_slices, TuneChoice{});
+      TuneChoice dflt;
+      dflt.pair2 = h->split_pair2;
+      s = build_exec(h, c, pairs, ngroups, precision, want_slices, dflt);
     }
     if (s) return s;
+  }
+  if (c.stream != h->stream && !nd_capturing(h)) {
+    // the state was last used on another stream: order that work before this launch, so
+    // the state's release (on the handle's stream) follows every use
+    if (!h->order_ev) ND_CUDA(h, cudaEventCreateWithFlags(&h->order_ev, cudaEventDisableTiming));
+    ND_CUDA(h, cudaEventRecord(h->order_ev, c.stream));
+    ND_CUDA(h, cudaStreamWaitEvent(h->stream, h->order_ev, 0));
+    c.stream = h->stream;
   }
   return launch_exec(h, c, ptrs, alpha, beta);
 }
@@ -336,7 +345,7 @@ static void append_mixed(std::string& k, const Mixed& m) {
 // Cached execution state of a dense contraction (one block pair), oldest evicted first.
 static ExecCache* dense_exec(nd_handle h, const PairDesc& pd, int precision) {
   std::string key;
-  const int32_t head[4] = {precision, h->ozaki_slices, pd.M, pd.N};
+  const int32_t head[5] = {precision, h->ozaki_slices, pd.M, pd.N, h->split_pair2};
   key.append((const char*)head, sizeof head);
   key.append((const char*)&pd.K, sizeof pd.K);
   append_mixed(key, pd.rows);
@@ -350,7 +359,7 @@ static ExecCache* dense_exec(nd_handle h, const PairDesc& pd, int precision) {
     h->dense_order.erase(h->dense_order.begin());
     cudaStreamSynchronize(h->stream);               // the evicted state may still be in use
     ExecCache* e = (ExecCache*)h->dense_cache[old];
-    e->free_all();
+    e->free_all(h);
     delete e;
     h->dense_cache.erase(old);
   }
@@ -364,7 +373,7 @@ static ExecCache* dense_exec(nd_handle h, const PairDesc& pd, int precision) {
 void nd_dense_cache_clear(nd_handle h) {
   for (auto& e : h->dense_cache) {
     ExecCache* c = (ExecCache*)e.second;
-    c->free_all();
+    c->free_all(h);
     delete c;
   }
   h->dense_cache.clear();
@@ -504,11 +513,27 @@ extern "C" nd_status nd_bs_plan_get(nd_plan plan, int32_t* blocksR, int64_t* off
   return ND_OK;
 }
 
+extern "C" nd_status nd_bs_plan_set_output_offsets(nd_plan p, const int64_t* offsetsR) {
+  if (!p) return ND_ERR_ARG;
+  nd_handle h = p->h;
+  if (!offsetsR && p->res.nR > 0) return nd_fail(h, ND_ERR_ARG, "plan_set_output_offsets: NULL offsets");
+  if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "plan_set_output_offsets: not during graph capture");
+  for (int32_t g = 0; g < p->res.nR; ++g)
+    if (offsetsR[g] < 0) return nd_fail(h, ND_ERR_ARG, "plan_set_output_offsets: negative offset for block %d", g);
+  p->res.offsetsR.assign(offsetsR, offsetsR + p->res.nR);
+  // execution state carries the old offsets: rebuild it on the next call
+  for (auto& c : p->cache) c.free_all(h);
+  for (auto& c : p->adj_cache) c.free_all(h);
+  p->descs.clear();
+  p->adj_descs.clear();
+  p->adj_built = false;
+  return ND_OK;
+}
+
 extern "C" nd_status nd_bs_plan_destroy(nd_plan plan) {
   if (!plan) return ND_OK;
-  cudaStreamSynchronize(plan->h->stream);
-  for (auto& c : plan->cache) c.free_all();
-  for (auto& c : plan->adj_cache) c.free_all();
+  for (auto& c : plan->cache) c.free_all(plan->h);      // stream-ordered after the plan's last launch
+  for (auto& c : plan->adj_cache) c.free_all(plan->h);
   delete plan;
   return ND_OK;
 }
@@ -652,6 +677,159 @@ extern "C" nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan p, const do
   if (p->adj_descs.empty()) return ND_OK;
   JobPtrs ptrs{{Rbar, A}, {B, Rbar}, {Abar, Bbar}};
   return nd_execute_cached(h, p->adj_cache[precision], p->adj_descs, p->adj_ngroups, ptrs, 1.0, 0.0, precision);
+}
+
+// ---------------------------------------------------------------------------
+// Block-sparse x block-diagonal DiagBlockSparse
+// (NDTensors/src/blocksparse/diagblocksparse.jl:601-696; per block pair the
+// diagonal contraction of NDTensors/src/diag/tensoralgebra/contract.jl:103-214)
+// ---------------------------------------------------------------------------
+// Every index of a diagonal block carries the same coordinate i < min(block dims),
+// d_i its value.  So an output element whose D-index coordinates are all equal to i
+// is alpha * sum over the group's pairs of d_i * T(x, i, ..., i) (x the T-free
+// coordinates; with no D index in the output, the sum also runs over i), and every
+// other output element is zero.  One thread per output element, each written once:
+// T is read once and R written once, 16 bytes per element.
+namespace {
+struct DiagGroupDesc {
+  int64_t r_off, count;
+  int32_t rank, pair_begin, pair_count, dmask;     // dmask: output positions holding a D index
+  int32_t dims[ND_MAX_RANK];
+  uint32_t mul[ND_MAX_RANK], shr[ND_MAX_RANK];     // multiply-high division by dims (counts < 2^31)
+};
+struct DiagPairDesc {
+  int64_t t_off, d_off, t_istride;                 // t_istride: sum of T strides of the contracted indices
+  int64_t tst[ND_MAX_RANK];                        // T stride of each output position (0 for D positions)
+  int32_t mind, pad;
+};
+struct DiagItem {
+  int32_t group, pad;
+  int64_t e0, e1;
+};
+
+__global__ void __launch_bounds__(256) bs_diag_contract(const DiagGroupDesc* groups, const DiagPairDesc* pairs,
+                                                        const DiagItem* items, int nitems, const double* __restrict__ T,
+                                                        const double* __restrict__ D, double* R, double alpha) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const DiagItem wi = items[it];
+    const DiagGroupDesc& g = groups[wi.group];
+    for (int64_t e = wi.e0 + threadIdx.x; e < wi.e1; e += blockDim.x) {
+      uint32_t rem = (uint32_t)e;
+      int32_t cd[ND_MAX_RANK];
+      int iy = -1;
+      bool diag = true;
+      for (int k = 0; k < g.rank; ++k) {
+        const uint32_t q = (nd_umulhi(rem, g.mul[k]) + rem) >> g.shr[k];
+        const int c = (int)(rem - q * (uint32_t)g.dims[k]);
+        rem = q;
+        cd[k] = c;
+        if ((g.dmask >> k) & 1) {
+          if (iy < 0) iy = c;
+          else diag = diag && (c == iy);
+        }
+      }
+      double v = 0.0;
+      if (diag) {
+        for (int pi = 0; pi < g.pair_count; ++pi) {
+          const DiagPairDesc& p = pairs[g.pair_begin + pi];
+          int64_t toff = 0;
+          for (int k = 0; k < g.rank; ++k) toff += (int64_t)cd[k] * p.tst[k];
+          if (iy >= 0) {
+            if (iy < p.mind) v = fma(__ldg(D + p.d_off + iy), __ldg(T + p.t_off + toff + iy * p.t_istride), v);
+          } else {
+            for (int i = 0; i < p.mind; ++i) v = fma(__ldg(D + p.d_off + i), __ldg(T + p.t_off + toff + i * p.t_istride), v);
+          }
+        }
+      }
+      R[g.r_off + e] = alpha * v;
+    }
+  }
+}
+}  // namespace
+
+extern "C" nd_status nd_bs_contract_diag_f64(nd_handle h, nd_plan p, double* R, const double* T, const double* Ddiag,
+                                             const int64_t* diag_offsets, double alpha) {
+  if (!h || !p) return ND_ERR_ARG;
+  if (p->res.npairs == 0) return ND_OK;
+  if (!R || !T || !Ddiag || !diag_offsets) return nd_fail(h, ND_ERR_ARG, "bs_contract_diag: NULL argument");
+  if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "bs_contract_diag: not during graph capture");
+  const Roles& ro = p->roles;
+  const BsDesc& A = p->A;
+  const BsDesc& Dd = p->B;
+  // D must be block diagonal (the reference's requirement, diagblocksparse.jl:652-657)
+  for (int b = 0; b < Dd.nnzblocks; ++b)
+    for (int d = 1; d < Dd.rank; ++d)
+      if (Dd.blocks[(size_t)b * Dd.rank + d] != Dd.blocks[(size_t)b * Dd.rank]) 
+        return nd_fail(h, ND_ERR_ARG, "bs_contract_diag: the DiagBlockSparse operand must be block diagonal");
+  const PlanResult& r = p->res;
+  const int rankR = p->rankR;
+  int dmask = 0;
+  for (int t = 0; t < ro.nfb; ++t) dmask |= 1 << ro.r_bfree[t];
+  std::vector<std::vector<int>> by_group(r.nR);
+  for (int q = 0; q < r.npairs; ++q) by_group[r.pairs[3 * q + 2]].push_back(q);
+  std::vector<DiagGroupDesc> groups;
+  std::vector<DiagPairDesc> pairs;
+  std::vector<DiagItem> items;
+  constexpr int64_t ITEM = 8192;
+  for (int g = 0; g < r.nR; ++g) {
+    DiagGroupDesc gd{};
+    gd.r_off = r.offsetsR[g];
+    gd.rank = rankR;
+    gd.dmask = dmask;
+    gd.pair_begin = (int32_t)pairs.size();
+    gd.pair_count = (int32_t)by_group[g].size();
+    int64_t count = 1;
+    for (int k = 0; k < rankR; ++k) {
+      const int64_t d = p->r_blockdims[k][r.blocksR[(size_t)g * rankR + k] - 1];
+      gd.dims[k] = (int32_t)d;
+      count *= d;
+    }
+    if (count >= (1ll << 31)) return nd_fail(h, ND_ERR_UNSUPPORTED, "bs_contract_diag: output block beyond 2^31 elements");
+    Mixed m{};
+    m.n = rankR;
+    for (int k = 0; k < rankR; ++k) m.dim[k] = gd.dims[k] > 0 ? gd.dims[k] : 1;
+    mixed_finalize(m);
+    for (int k = 0; k < rankR; ++k) { gd.mul[k] = m.mul[k]; gd.shr[k] = m.shr[k]; }
+    gd.count = count;
+    for (int q : by_group[g]) {
+      const int iA = r.pairs[3 * q], iD = r.pairs[3 * q + 1];
+      int64_t sT[ND_MAX_RANK + 1];
+      sT[0] = 1;
+      for (int k = 0; k < A.rank; ++k) sT[k + 1] = sT[k] * A.bdim(iA, k);
+      DiagPairDesc pd{};
+      pd.t_off = A.offsets[iA];
+      pd.d_off = diag_offsets[iD];
+      int64_t mind = INT64_MAX;
+      for (int k = 0; k < Dd.rank; ++k) mind = std::min(mind, Dd.bdim(iD, k));
+      pd.mind = Dd.rank ? (int32_t)mind : 1;
+      for (int t = 0; t < ro.nk; ++t) pd.t_istride += sT[ro.a_k[t]];
+      for (int t = 0; t < ro.nfa; ++t) pd.tst[ro.r_afree[t]] = sT[ro.a_free[t]];
+      pairs.push_back(pd);
+    }
+    groups.push_back(gd);
+    for (int64_t e = 0; e < count; e += ITEM) items.push_back(DiagItem{g, 0, e, std::min(count, e + ITEM)});
+  }
+  if (items.empty()) return ND_OK;
+  // one upload of the three descriptor lists, stream-ordered scratch
+  const size_t bg = groups.size() * sizeof(DiagGroupDesc), bp = pairs.size() * sizeof(DiagPairDesc),
+               bi = items.size() * sizeof(DiagItem);
+  std::vector<unsigned char> host(bg + bp + bi);
+  memcpy(host.data(), groups.data(), bg);
+  memcpy(host.data() + bg, pairs.data(), bp);
+  memcpy(host.data() + bg + bp, items.data(), bi);
+  void* d = nullptr;
+  nd_status st = nd_dalloc(h, &d, host.size());
+  if (st) return st;
+  ND_CUDA(h, cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, h->stream));
+  const int grid = (int)std::min<size_t>(items.size(), (size_t)h->num_sms * 8);
+  nd_prof_begin(h, "bs_diag_contract");
+  bs_diag_contract<<<grid, 256, 0, h->stream>>>((const DiagGroupDesc*)d, (const DiagPairDesc*)((unsigned char*)d + bg),
+                                                (const DiagItem*)((unsigned char*)d + bg + bp), (int)items.size(), T,
+                                                Ddiag, R, alpha);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  cudaFreeAsync(d, h->stream);
+  return nd_cuda_check(h, cudaGetLastError(), "bs_diag_contract");
 }
 
 extern "C" nd_status nd_bs_permutedims_f64(nd_handle h, const nd_bs_desc* T, const double* Tdata,

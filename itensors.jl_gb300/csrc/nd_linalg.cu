@@ -403,8 +403,9 @@ __global__ void __launch_bounds__(1024) sort_truncate(const double* sig, int n, 
 }
 
 // kept dims per block (_truncated_blockdim, NDTensors/src/blocksparse/linearalgebra.jl:8-33)
+// squared = 1: singular values (s^2 > docut); 0: eigenvalues (|lambda| > docut)
 __global__ void kept_dims(const SvdBlock* blocks, int nb, const double* sig, const double* docut, int min_blockdim,
-                          int truncate, int32_t* kept) {
+                          int truncate, int32_t* kept, int squared = 1) {
   const int bi = blockIdx.x * blockDim.x + threadIdx.x;
   if (bi >= nb) return;
   const SvdBlock b = blocks[bi];
@@ -414,7 +415,7 @@ __global__ void kept_dims(const SvdBlock* blocks, int nb, const double* sig, con
   int k = 0;
   while (k < full) {
     const double v = sig[b.s_off + k];
-    if (!(v * v > *docut)) break;
+    if (!((squared ? v * v : fabs(v)) > *docut)) break;
     ++k;
   }
   if (k < mb) k = mb;
@@ -540,6 +541,56 @@ __global__ void set_identity(const SvdBlock* blocks, double* Y) {
     Y[b.v_off + e] = (e % b.nn == e / b.nn) ? 1.0 : 0.0;
 }
 
+// ---- blockwise Hermitian eigen -------------------------------------------------
+// A_b + c_b I with c_b = 1.01 ||A_b||_F (1 for a zero block) is positive definite, so
+// its one-sided Jacobi SVD gives the eigenvectors of A_b (left = right singular
+// vectors) and lambda = sigma - c_b.
+__global__ void eig_shift(const SvdBlock* blocks, const double* A, double* As, double* shift) {
+  const SvdBlock b = blocks[blockIdx.x];
+  __shared__ double red[8];
+  const int64_t n = b.n, tot = n * n;
+  const double* a = A + b.a_off;
+  double ss = 0.0;
+  for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) ss = fma(a[e], a[e], ss);
+  ss = block_reduce_sum(ss, red);
+  __shared__ double c;
+  if (threadIdx.x == 0) c = ss > 0.0 ? 1.01 * sqrt(ss) : 1.0;
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) As[b.a_off + e] = a[e] + ((e % (n + 1)) == 0 ? c : 0.0);
+  if (threadIdx.x == 0) shift[blockIdx.x] = c;
+}
+
+// per block: lambda_j = sigma_j - c_b, re-ordered by |lambda| descending (ties by the
+// sigma order): values, their |lambda| (pooled for truncate!) and the Jacobi column
+// of each (NDTensors/src/linearalgebra/linearalgebra.jl:183-186: sortperm(rev, by = abs))
+__global__ void eig_finish(const SvdBlock* blocks, const double* sig, const int32_t* order, const double* shift,
+                           double* lam, double* absl, int32_t* vcol) {
+  const SvdBlock b = blocks[blockIdx.x];
+  const double c = shift[blockIdx.x];
+  for (int j = threadIdx.x; j < b.nn; j += blockDim.x) {
+    const double v = sig[b.s_off + j] - c, av = fabs(v);
+    int rank = 0;
+    for (int k = 0; k < b.nn; ++k) {
+      const double u = fabs(sig[b.s_off + k] - c);
+      rank += (u > av) || (u == av && k < j);
+    }
+    lam[b.s_off + rank] = v;
+    absl[b.s_off + rank] = av;
+    vcol[b.s_off + rank] = order[b.s_off + j];
+  }
+}
+
+// eigenvectors (n x n per block, columns in |lambda| order) from the Jacobi V
+__global__ void eig_vectors(const SvdBlock* blocks, const double* Vw, const int32_t* vcol, double* Vfull,
+                            const int64_t* v_off) {
+  const SvdBlock b = blocks[blockIdx.y];
+  const int64_t tot = (int64_t)b.nn * b.nn;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % b.nn, c = e / b.nn;
+    Vfull[v_off[blockIdx.y] + e] = Vw[b.v_off + (int64_t)vcol[b.s_off + c] * b.nn + i];
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -634,7 +685,7 @@ static nd_status block_gemm(nd_handle h, const std::vector<SvdBlock>& blocks, in
   ExecCache c;
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
   nd_status st = nd_execute_cached(h, c, pairs, (int)blocks.size(), ptrs, alpha, beta, ND_PREC_FP64);
-  c.free_all();
+  c.free_all(h);
   return st;
 }
 
@@ -852,6 +903,122 @@ extern "C" nd_status nd_bs_svd_f64(nd_handle h, int32_t nb, const int64_t* rows,
     cudaFreeAsync(p, s);
   ND_CUDA(h, cudaStreamSynchronize(s));
   return nd_check_device_status(h, "svd");
+}
+
+extern "C" nd_status nd_bs_eigen_f64(nd_handle h, int32_t nb, const int64_t* dims, const int64_t* offsets,
+                                     const double* A, double* D, double* V, int32_t mindim, int32_t maxdim,
+                                     double cutoff, int32_t use_absolute_cutoff, int32_t use_relative_cutoff,
+                                     int32_t min_blockdim, int32_t* kept, double* spectrum, int32_t* spectrum_len,
+                                     double* truncerr, double* docut) {
+  if (!h) return ND_ERR_ARG;
+  if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "eigen returns kept dimensions to the host and cannot be captured");
+  if (nb < 0 || (nb > 0 && (!dims || !offsets || !A || !D || !V || !kept)))
+    return nd_fail(h, ND_ERR_ARG, "eigen: NULL argument");
+  if (nb == 0) { if (spectrum_len) *spectrum_len = 0; if (truncerr) *truncerr = 0; if (docut) *docut = 0; return ND_OK; }
+  cudaStream_t s = h->stream;
+  int64_t span = 0;
+  for (int i = 0; i < nb; ++i) {
+    if (dims[i] <= 0) return nd_fail(h, ND_ERR_ARG, "eigen: block %d has dimension %lld", i, (long long)dims[i]);
+    span = std::max(span, offsets[i] + dims[i] * dims[i]);
+  }
+  // shifted copy (same layout as A), then the batched Jacobi SVD of every block
+  std::vector<SvdBlock> hb(nb);
+  for (int i = 0; i < nb; ++i) { hb[i] = SvdBlock{}; hb[i].a_off = offsets[i]; hb[i].n = (int)dims[i]; }
+  double *As = nullptr, *shift = nullptr;
+  SvdBlock* dpre = nullptr;
+  ND_CUDA(h, cudaMallocAsync(&As, std::max<int64_t>(span, 1) * 8, s));
+  ND_CUDA(h, cudaMallocAsync(&shift, nb * 8, s));
+  ND_CUDA(h, cudaMallocAsync(&dpre, nb * sizeof(SvdBlock), s));
+  ND_CUDA(h, cudaMemcpyAsync(dpre, hb.data(), nb * sizeof(SvdBlock), cudaMemcpyHostToDevice, s));
+  nd_prof_begin(h, "eig_shift");
+  eig_shift<<<nb, 256, 0, s>>>(dpre, A, As, shift);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  std::vector<SvdBlock> blocks;
+  double *sig = nullptr, *W = nullptr, *Vw = nullptr;
+  int32_t* order = nullptr;
+  SvdBlock* dblk = nullptr;
+  int total = 0;
+  nd_status st = svd_core(h, nb, dims, dims, offsets, As, blocks, &sig, &order, &W, &Vw, &dblk, total);
+  cudaFreeAsync(As, s);
+  cudaFreeAsync(dpre, s);
+  if (st) { cudaFreeAsync(shift, s); return st; }
+  std::vector<int64_t> vo(nb);
+  int64_t vt = 0;
+  for (int i = 0; i < nb; ++i) { vo[i] = vt; vt += dims[i] * dims[i]; }
+  int npow2 = 1;
+  while (npow2 < total) npow2 <<= 1;
+  double *lam = nullptr, *absl = nullptr, *Vf = nullptr, *P = nullptr, *res = nullptr;
+  int32_t *vcol = nullptr, *dkept = nullptr;
+  int64_t* dvo = nullptr;
+  int* dlen = nullptr;
+  auto cleanup = [&]() {
+    for (void* p : {(void*)lam, (void*)absl, (void*)Vf, (void*)P, (void*)res, (void*)vcol, (void*)dkept, (void*)dvo,
+                    (void*)dlen, (void*)sig, (void*)order, (void*)W, (void*)Vw, (void*)dblk, (void*)shift})
+      if (p) cudaFreeAsync(p, s);
+  };
+  if ((size_t)npow2 * 8 > 200 * 1024) { cleanup(); return nd_fail(h, ND_ERR_UNSUPPORTED, "eigen: %d eigenvalues exceed the on-chip sort", total); }
+  cudaError_t e = cudaSuccess;
+  for (auto pr : {std::make_pair((void**)&lam, (size_t)total * 8), std::make_pair((void**)&absl, (size_t)total * 8),
+                  std::make_pair((void**)&Vf, (size_t)std::max<int64_t>(vt, 1) * 8),
+                  std::make_pair((void**)&P, (size_t)total * 8), std::make_pair((void**)&res, (size_t)32),
+                  std::make_pair((void**)&vcol, (size_t)total * 4), std::make_pair((void**)&dkept, (size_t)nb * 4),
+                  std::make_pair((void**)&dvo, (size_t)nb * 8), std::make_pair((void**)&dlen, (size_t)8)})
+    if (e == cudaSuccess) e = cudaMallocAsync(pr.first, std::max<size_t>(pr.second, 8), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dvo, vo.data(), nb * 8, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) { cleanup(); return nd_cuda_check(h, e, "eigen buffers"); }
+  nd_prof_begin(h, "eig_finish");
+  eig_finish<<<nb, 256, 0, s>>>(dblk, sig, order, shift, lam, absl, vcol);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  {
+    int64_t maxe = 1;
+    for (int i = 0; i < nb; ++i) maxe = std::max(maxe, dims[i] * dims[i]);
+    dim3 grid((unsigned)std::min<int64_t>((maxe + 255) / 256, 1024), nb);
+    nd_prof_begin(h, "eig_vectors");
+    eig_vectors<<<grid, 256, 0, s>>>(dblk, Vw, vcol, Vf, dvo);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+  }
+  // pooled |lambda|: sort + truncate! on the device, then the kept dims per block
+  TruncParams tp{mindim < 1 ? 1 : mindim, maxdim, cutoff, cutoff >= 0.0 ? 1 : 0, use_absolute_cutoff, use_relative_cutoff};
+  const bool trunc = maxdim >= 0 || cutoff >= 0.0;
+  static bool attr = false;
+  if (!attr) { cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+  nd_prof_begin(h, "sort_truncate");
+  sort_truncate<<<1, 1024, npow2 * 8, s>>>(absl, total, npow2, 0, 1, tp, P, dlen, res, res + 1);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  nd_prof_begin(h, "kept_dims");
+  kept_dims<<<(nb + 127) / 128, 128, 0, s>>>(dblk, nb, absl, res + 1, min_blockdim < 0 ? 0 : min_blockdim, trunc ? 1 : 0,
+                                             dkept, 0);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  int len = 0;
+  double hres[2];
+  e = cudaMemcpyAsync(kept, dkept, nb * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&len, dlen, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hres, res, 16, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && spectrum) e = cudaMemcpy(spectrum, P, (size_t)len * 8, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) { cleanup(); return nd_cuda_check(h, e, "eigen results"); }
+  if (spectrum_len) *spectrum_len = len;
+  if (truncerr) *truncerr = hres[0];
+  if (docut) *docut = hres[1];
+  // kept prefixes: D values and V columns (column-major prefixes are contiguous)
+  int64_t cd = 0, cv = 0;
+  for (int i = 0; i < nb && e == cudaSuccess; ++i) {
+    const int k = kept[i];
+    if (k == 0) continue;
+    e = cudaMemcpyAsync(D + cd, lam + blocks[i].s_off, (size_t)k * 8, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(V + cv, Vf + vo[i], (size_t)dims[i] * k * 8, cudaMemcpyDeviceToDevice, s);
+    cd += k;
+    cv += dims[i] * k;
+  }
+  cleanup();
+  if (e != cudaSuccess) return nd_cuda_check(h, e, "eigen outputs");
+  ND_CUDA(h, cudaStreamSynchronize(s));
+  return nd_check_device_status(h, "eigen");
 }
 
 extern "C" nd_status nd_truncate_f64(nd_handle h, const double* Pin, int32_t n, int32_t mindim, int32_t maxdim,

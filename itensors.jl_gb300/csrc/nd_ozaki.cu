@@ -156,7 +156,10 @@ __device__ __forceinline__ double i64_scaled_to_f64(long long v, int e) {
 // K-major SW64 layout.  A thread owns (row, 8-wide k chunk) units: the four
 // lanes of a row read its 32 k values (coalesced whether rows or k are
 // contiguous in the tensor) and each writes one 16-byte chunk per slice, so
-// four lanes fill a 64-byte row and a warp a 512-byte run.
+// four lanes fill a 64-byte row and a warp a 512-byte run.  (One exponent per
+// (row, 512-wide chunk), digitised in a single pack pass that reads its chunk
+// twice, was measured too: the second, L2-resident read made pack_digits 1.5-1.8x
+// slower, more than the row-maximum pass it removes.)
 constexpr int PACK_KC = 8;                 // k-steps (of 32) per pack item
 
 struct PackItem2 {
@@ -232,11 +235,11 @@ __device__ __forceinline__ void pack_setup(const SplitOp& op, const PackItem2& p
     if (r0 + tid < op.rows) mixed_offsets32(op.rk, r0 + tid, o, dummy);
     rowoff[tid] = o;
   }
-  {
-    const int k = ks0 * BK + tid;          // 256 threads = PACK_KC * 32 k values
+  for (int t = tid; t < PACK_KC * BK; t += blockDim.x) {
+    const int k = ks0 * BK + t;
     int64_t o = -1, dummy;
-    if (k < op.kdim && tid < (ks1 - ks0) * BK) mixed_offsets32(op.kk, k, o, dummy);
-    koff[tid] = o;                         // -1 marks padding
+    if (k < op.kdim && t < (ks1 - ks0) * BK) mixed_offsets32(op.kk, k, o, dummy);
+    koff[t] = o;                           // -1 marks padding
   }
 }
 
@@ -390,11 +393,9 @@ __device__ __forceinline__ void commit(uint64_t* bar) {
                :: "r"(smem_u32(bar)) : "memory");
 }
 
-#define TMEM_LD16(taddr, r)                                                                                   \
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),          \
-                 "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),       \
-                 "=r"(r[14]), "=r"(r[15])                                                                      \
+#define TMEM_LD8(taddr, r)                                                                                    \
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"                           \
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])  \
                : "r"(taddr))
 
 #define TMEM_LD32(taddr, r)                                                                                   \
@@ -625,39 +626,41 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
           const uint32_t xs = chunk & 1, xu = chunk >> 1;
           if (!mbar_wait(smem_u32(&xfull[xs]), xu & 1, g.st, 420, &abort_flag, lim)) { ok = false; break; }
           fence_after();
-          {
-            uint32_t l2[EPI_COLS], l3[EPI_COLS];
-            TMEM_LD16(lane_addr + xcol(xs), l2);
-            TMEM_LD16(lane_addr + xcol(xs) + BN, l3);
+          // 8 columns at a time: L2 and L3 (exact) then the FP32 tail levels T4 and T5+
+#pragma unroll
+          for (int hb = 0; hb < EPI_COLS; hb += 8) {
+            uint32_t l2[8], l3[8];
+            TMEM_LD8(lane_addr + xcol(xs) + hb, l2);
+            TMEM_LD8(lane_addr + xcol(xs) + BN + hb, l3);
             tmem_wait_ld();
             if (S > 2) {
 #pragma unroll
-              for (int c = 0; c < EPI_COLS; ++c) {
+              for (int c = 0; c < 8; ++c) {
                 // L2: integer units; L3 was computed with pre-scaled slices: an integer multiple of 2^-8
                 // |L2| <= 2^23, |256 L3| <= 2^24: hi parts fit 2^11 and 2^12, li parts 2^11
                 int h2, i2, h3, i3;
                 f32_round_split(__uint_as_float(l2[c]), h2, i2);
                 f32_round_split(__uint_as_float(l3[c]) * 256.0f, h3, i3);
-                acc[c] += ((long long)(h2 * 256 + h3) << 28) + ((long long)(i2 * 256 + i3) << 16);
+                acc[hb + c] += ((long long)(h2 * 256 + h3) << 28) + ((long long)(i2 * 256 + i3) << 16);
               }
             } else {
 #pragma unroll
-              for (int c = 0; c < EPI_COLS; ++c) facc[c] += __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
+              for (int c = 0; c < 8; ++c) facc[hb + c] += __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
             }
-          }
-          if (C::TBLK) {
-            // levels >= 4 of this chunk (FP32, rounded once per chunk into the fixed point)
-            uint32_t t4[EPI_COLS], t5[EPI_COLS];
-            TMEM_LD16(lane_addr + tcol(xs), t4);
-            if (C::TBLK > 1) TMEM_LD16(lane_addr + tcol(xs) + BN, t5);
-            tmem_wait_ld();
+            if (C::TBLK) {
+              // levels >= 4 of this chunk (FP32, rounded once per chunk into the fixed point)
+              uint32_t t4[8], t5[8];
+              TMEM_LD8(lane_addr + tcol(xs) + hb, t4);
+              if (C::TBLK > 1) TMEM_LD8(lane_addr + tcol(xs) + BN + hb, t5);
+              tmem_wait_ld();
 #pragma unroll
-            for (int c = 0; c < EPI_COLS; ++c) {
-              // x 2^24: |T4| < 2^9 and |T5+| < 2^2 per chunk, inside the split's 2^33 range
-              int h4, i4, h5 = 0, i5 = 0;
-              f32_round_split(__uint_as_float(t4[c]) * 16777216.0f, h4, i4);
-              if (C::TBLK > 1) f32_round_split(__uint_as_float(t5[c]) * 16777216.0f, h5, i5);
-              acc[c] += ((long long)(h4 + h5) << 12) + (long long)(i4 + i5);
+              for (int c = 0; c < 8; ++c) {
+                // x 2^24: |T4| < 2^9 and |T5+| < 2^2 per chunk, inside the split's 2^33 range
+                int h4, i4, h5 = 0, i5 = 0;
+                f32_round_split(__uint_as_float(t4[c]) * 16777216.0f, h4, i4);
+                if (C::TBLK > 1) f32_round_split(__uint_as_float(t5[c]) * 16777216.0f, h5, i5);
+                acc[hb + c] += ((long long)(h4 + h5) << 12) + (long long)(i4 + i5);
+              }
             }
           }
           fence_before();
@@ -716,15 +719,428 @@ nd_status launch_gemm(nd_handle h, const GemmArgs& g) {
   return nd_cuda_check(h, cudaGetLastError(), "split_gemm");
 }
 
+// ---- 2-CTA variant (tcgen05.mma.cta_group::2, M = 256) -----------------------
+// A CTA pair (a cluster of 2) computes a 256 x 64 output tile.  CTA c stages the 128 rows
+// of A of row tile 2 m + c and one half (32 rows) of every B slice; one tcgen05.mma of
+// M = 256 reads A from each CTA's own shared memory and the two B halves from both, so
+// each SM reads half the B bytes the 1-CTA kernel reads per product and a stage is
+// S x 10 KB (4 stages for S = 5 instead of 3).  The products run as separate N = 64 MMAs
+// (15 per 16 of K for S = 5; the two B halves break the 1-CTA kernel's concatenation of
+// B slices), consecutive ones sharing A_p through the A collector.  The even CTA issues
+// the MMAs; the odd CTA's MMA warp relays each landed stage to the even CTA (a
+// cluster-scope mbarrier arrive).  Completion of a stage's MMAs and of a chunk's
+// accumulation is multicast to both CTAs.  Accumulators are per CTA (its 128 rows of the
+// pair tile in its own TMEM), so the chunk drains and the epilogue are the 1-CTA kernel's;
+// the odd CTA's epilogue warps release a slot with remote arrivals on the even CTA.
+constexpr int B_HALF = B_SLICE / 2;   // 32 rows x 32 k, 2048 bytes
+
+template <int S>
+struct Cfg2 {
+  static constexpr int STAGE = S * (A_SLICE + B_HALF);
+  static constexpr int STAGES = (SMEM_BUDGET - 1024) / STAGE;
+  static constexpr int TBLK = Cfg<S>::TBLK;
+  static constexpr int TMEM_COLS = 512;
+  static constexpr int SMEM = STAGES * STAGE + 1024;
+};
+
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_addr(const void* p, uint32_t rank) {
+  uint32_t o;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(o) : "r"(smem_u32(p)), "r"(rank));
+  return o;
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" :: "r"(addr) : "memory");
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// mbarrier wait with cluster-scope acquire: the arrivals come from the other CTA
+__device__ __forceinline__ bool mbar_wait_cl(uint32_t bar, uint32_t parity, DeviceStatus* st, int site,
+                                             volatile int* abort_flag, uint32_t lim) {
+  if (!abort_flag) lim = ND_SPIN_LIMIT;
+  for (uint32_t it = 0; it < lim; ++it) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    if (ok) return true;
+    if ((it & 255) == 255 && abort_flag && *abort_flag) return false;
+  }
+  if (atomicCAS(&st->code, 0, ND_ERR_TIMEOUT) == 0) st->where = site;
+  if (abort_flag) *abort_flag = 1;
+  return false;
+}
+
+template <int CU>
+__device__ __forceinline__ void mma2(uint32_t dt, uint64_t ad, uint64_t bd, uint32_t id, uint32_t acc) {
+  if constexpr (CU == 1)
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n" ND_ELECT
+                 "tcgen05.mma.cta_group::2.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+  else if constexpr (CU == 2)
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n" ND_ELECT
+                 "tcgen05.mma.cta_group::2.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+  else if constexpr (CU == 3)
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n" ND_ELECT
+                 "tcgen05.mma.cta_group::2.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+  else
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n" ND_ELECT
+                 "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
+}
+
+// arrive on the mbarrier at this offset in both CTAs once the issued MMAs complete
+__device__ __forceinline__ void commit2_both(uint64_t* bar) {
+  asm volatile("{\n" ND_ELECT "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;\n}"
+               :: "r"(smem_u32(bar)), "h"((unsigned short)3) : "memory");
+}
+__device__ __forceinline__ void commit2_local(uint64_t* bar) {
+  asm volatile("{\n" ND_ELECT "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}"
+               :: "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ uint32_t idesc2(int n) {
+  // as idesc, with M = 256 (the CTA pair)
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+}
+
+template <int S>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1) split_gemm2(GemmArgs g) {
+  using C = Cfg2<S>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[C::STAGES], empty[C::STAGES], pfull[C::STAGES];
+  __shared__ __align__(8) uint64_t xfull[2], xempty[2], done_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  __shared__ int64_t colR_s[BN];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t lim = nd_spin_limit(g.st);
+  const uint32_t crank = cluster_ctarank();            // 0 issues the MMAs, 1 relays
+  const int pair_id = blockIdx.x >> 1, npairs = gridDim.x >> 1;
+
+  if (tid == 0) {
+    for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); mbar_init(&pfull[s], 1); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&xfull[b], 1); mbar_init(&xempty[b], 2 * EPI_WARPS); }
+    mbar_init(&done_bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(&tmem_slot)), "r"(C::TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  cluster_sync_all();                                   // both CTAs' barriers exist before any remote arrive
+  fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------- producer (both CTAs) --------------------
+    if (lane == 0) {
+      uint32_t n = 0;
+      bool ok = true;
+      for (int it = pair_id; it < g.nitems && ok; it += npairs) {
+        const WorkItem wi = g.items[it];
+        const int mt = 2 * wi.mt + (int)crank;
+        for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+          const PairDesc& pd = g.pairs[wi.pair_begin + pi];
+          const SplitOp& oa = g.ops[pd.a_op];
+          const SplitOp& ob = g.ops[pd.b_op];
+          const unsigned char* srcA = g.pack + oa.pack_off + (int64_t)mt * oa.k_steps * S * A_SLICE;
+          const unsigned char* srcB = g.pack + ob.pack_off + (int64_t)wi.nt * ob.k_steps * S * B_SLICE + crank * B_HALF;
+          for (int ks = 0; ks < oa.k_steps; ++ks, ++n) {
+            const uint32_t s = n % C::STAGES, u = n / C::STAGES;
+            if (u >= 1 && !mbar_wait_cl(smem_u32(&empty[s]), (u - 1) & 1, g.st, 430, &abort_flag, lim)) { ok = false; break; }
+            unsigned char* dA = smem + s * C::STAGE;
+            unsigned char* dB = dA + S * A_SLICE;
+            const uint32_t fb = smem_u32(&full[s]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(fb), "r"(C::STAGE) : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         :: "r"(smem_u32(dA)), "l"(srcA + (int64_t)ks * S * A_SLICE), "r"(S * A_SLICE), "r"(fb) : "memory");
+            const unsigned char* sb = srcB + (int64_t)ks * S * B_SLICE;
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+              asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                           :: "r"(smem_u32(dB + q * B_HALF)), "l"(sb + q * B_SLICE), "r"(B_HALF), "r"(fb) : "memory");
+          }
+        }
+      }
+      if (ok) {
+        // tail: every multicast release of this CTA's stages has landed before it can exit
+        for (uint32_t q = 0; q < C::STAGES && q < n; ++q) {
+          const uint32_t m = n - 1 - q;
+          mbar_wait_cl(smem_u32(&empty[m % C::STAGES]), (m / C::STAGES) & 1, g.st, 431, nullptr, lim);
+        }
+      } else {
+        // let copies already issued land before the CTA can exit
+        for (uint32_t q = 0; q < C::STAGES && q < n; ++q) {
+          const uint32_t m = n - 1 - q;
+          mbar_wait(smem_u32(&full[m % C::STAGES]), (m / C::STAGES) & 1, g.st, 432, nullptr);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (crank == 0) {
+      // ----------------------------- MMA issuer (even CTA) --------------------
+      uint32_t n = 0, chunk = 0;
+      bool ok = true;
+      const uint32_t smem_base = smem_u32(smem);
+      const uint32_t i64 = idesc2(BN);
+      constexpr int NBLK = 2 + C::TBLK;
+      for (int it = pair_id; it < g.nitems && ok; it += npairs) {
+        const WorkItem wi = g.items[it];
+        for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+          const PairDesc& pd = g.pairs[wi.pair_begin + pi];
+          const int nks = g.ops[pd.a_op].k_steps;
+          const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
+          uint32_t X = tmem;
+          for (int ks = 0; ks < nks; ++ks, ++n) {
+            const bool cstart = (ks % chunk_steps) == 0;
+            const bool cend = ((ks % chunk_steps) == chunk_steps - 1) || ks == nks - 1;
+            if (cstart) {
+              const uint32_t xs = chunk & 1, xu = chunk >> 1;
+              if (xu >= 1 && !__all_sync(0xffffffffu, mbar_wait_cl(smem_u32(&xempty[xs]), (xu - 1) & 1, g.st, 441, &abort_flag, lim))) { ok = false; break; }
+              X = tmem + xcol(xs);
+            }
+            const uint32_t s = n % C::STAGES, u = n / C::STAGES;
+            if (!__all_sync(0xffffffffu, mbar_wait(smem_u32(&full[s]), u & 1, g.st, 442, &abort_flag, lim))) { ok = false; break; }
+            if (!__all_sync(0xffffffffu, mbar_wait_cl(smem_u32(&pfull[s]), u & 1, g.st, 443, &abort_flag, lim))) { ok = false; break; }
+            fence_after();
+            const uint32_t a0 = smem_base + s * C::STAGE;
+            const uint64_t adesc0 = sdesc(a0), bdesc0 = sdesc(a0 + S * A_SLICE);
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+              const uint32_t ko = kk * 32;
+              auto A = [&](int p) { return adesc0 + (uint64_t)((((p - 1) * A_SLICE) + ko) >> 4); };
+              auto B = [&](int q) { return bdesc0 + (uint64_t)((((q - 1) * B_HALF) + ko) >> 4); };
+              // product (p, q) accumulates into level block min(p + q - 2, NBLK - 1); the
+              // p = 1 products are the first writes of every block of a chunk
+#pragma unroll
+              for (int p = 1; p <= S; ++p) {
+                const int nm = S + 1 - p;                     // MMAs sharing A_p
+#pragma unroll
+                for (int q = 1; q <= S + 1 - p; ++q) {
+                  const int blk = (p + q - 2) < (NBLK - 1) ? (p + q - 2) : (NBLK - 1);
+                  const uint32_t d = X + blk * BN;
+                  const uint32_t ac = (cstart && kk == 0 && p == 1 && q <= NBLK) ? 0u : 1u;
+                  if (nm == 1) mma2<0>(d, A(p), B(q), i64, ac);
+                  else if (q == 1) mma2<1>(d, A(p), B(q), i64, ac);
+                  else if (q == nm) mma2<3>(d, A(p), B(q), i64, ac);
+                  else mma2<2>(d, A(p), B(q), i64, ac);
+                }
+              }
+            }
+            commit2_both(&empty[s]);
+            if (cend) { commit2_both(&xfull[chunk & 1]); ++chunk; }
+          }
+          if (!ok) break;
+        }
+      }
+      commit2_local(&done_bar);
+      mbar_wait(smem_u32(&done_bar), 0, g.st, 444, nullptr);
+    } else {
+      // ----------------------------- stage relay (odd CTA) --------------------
+      if (lane == 0) {
+        uint32_t n = 0;
+        bool ok = true;
+        const uint32_t leader_pfull0 = cluster_addr(&pfull[0], 0);
+        for (int it = pair_id; it < g.nitems && ok; it += npairs) {
+          const WorkItem wi = g.items[it];
+          for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+            const int nks = g.ops[g.pairs[wi.pair_begin + pi].a_op].k_steps;
+            for (int ks = 0; ks < nks; ++ks, ++n) {
+              const uint32_t s = n % C::STAGES, u = n / C::STAGES;
+              if (!mbar_wait(smem_u32(&full[s]), u & 1, g.st, 445, &abort_flag, lim)) { ok = false; break; }
+              mbar_arrive_cluster(leader_pfull0 + s * 8u);
+            }
+          }
+        }
+      }
+    }
+  } else {
+    // ------------------------------- epilogue (both CTAs) --------------------
+    const int q = warp & 3;
+    const int cg = (warp - 2) >> 2;
+    const int row = q * 32 + lane;
+    const int etid = tid - 64;
+    const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + cg * EPI_COLS;
+    const uint32_t leader_xempty0 = cluster_addr(&xempty[0], 0);
+    uint32_t chunk = 0;
+    bool ok = true;
+    for (int it = pair_id; it < g.nitems && ok; it += npairs) {
+      const WorkItem wi = g.items[it];
+      if (wi.pair_count == 0) continue;
+      const PairDesc& p0 = g.pairs[wi.pair_begin];
+      const int gm = (2 * wi.mt + (int)crank) * BM + row;
+      const bool row_ok = gm < p0.M;
+      int64_t roff = 0, dummy;
+      if (row_ok) mixed_offsets32(p0.rows, (uint32_t)gm, dummy, roff);
+      epi_sync();
+      if (etid < BN) {
+        int64_t co = 0, d2;
+        const int gn = wi.nt * BN + etid;
+        if (gn < p0.N) mixed_offsets32(p0.cols, (uint32_t)gn, d2, co);
+        colR_s[etid] = co;
+      }
+      epi_sync();
+      double* Rb = job_R(g.ptrs, p0.job) + p0.r_off + roff;
+      const int ncols = min(EPI_COLS, p0.N - (wi.nt * BN + cg * EPI_COLS));
+      for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
+        const PairDesc& pd = g.pairs[wi.pair_begin + pi];
+        const SplitOp& oa = g.ops[pd.a_op];
+        const SplitOp& ob = g.ops[pd.b_op];
+        const int nks = oa.k_steps;
+        const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
+        const int nchunks = (nks + chunk_steps - 1) / chunk_steps;
+        long long acc[EPI_COLS];
+        float facc[EPI_COLS];
+#pragma unroll
+        for (int c = 0; c < EPI_COLS; ++c) { acc[c] = 0; facc[c] = 0.f; }
+        for (int ch = 0; ch < nchunks; ++ch, ++chunk) {
+          const uint32_t xs = chunk & 1, xu = chunk >> 1;
+          if (!mbar_wait_cl(smem_u32(&xfull[xs]), xu & 1, g.st, 450, &abort_flag, lim)) { ok = false; break; }
+          fence_after();
+          // 8 columns at a time: L2 and L3 (exact) then the FP32 tail levels T4 and T5+
+#pragma unroll
+          for (int hb = 0; hb < EPI_COLS; hb += 8) {
+            uint32_t l2[8], l3[8];
+            TMEM_LD8(lane_addr + xcol(xs) + hb, l2);
+            TMEM_LD8(lane_addr + xcol(xs) + BN + hb, l3);
+            tmem_wait_ld();
+            if (S > 2) {
+#pragma unroll
+              for (int c = 0; c < 8; ++c) {
+                // L2: integer units; L3 was computed with pre-scaled slices: an integer multiple of 2^-8
+                // |L2| <= 2^23, |256 L3| <= 2^24: hi parts fit 2^11 and 2^12, li parts 2^11
+                int h2, i2, h3, i3;
+                f32_round_split(__uint_as_float(l2[c]), h2, i2);
+                f32_round_split(__uint_as_float(l3[c]) * 256.0f, h3, i3);
+                acc[hb + c] += ((long long)(h2 * 256 + h3) << 28) + ((long long)(i2 * 256 + i3) << 16);
+              }
+            } else {
+#pragma unroll
+              for (int c = 0; c < 8; ++c) facc[hb + c] += __uint_as_float(l2[c]) + __uint_as_float(l3[c]);
+            }
+            if (C::TBLK) {
+              // levels >= 4 of this chunk (FP32, rounded once per chunk into the fixed point)
+              uint32_t t4[8], t5[8];
+              TMEM_LD8(lane_addr + tcol(xs) + hb, t4);
+              if (C::TBLK > 1) TMEM_LD8(lane_addr + tcol(xs) + BN + hb, t5);
+              tmem_wait_ld();
+#pragma unroll
+              for (int c = 0; c < 8; ++c) {
+                // x 2^24: |T4| < 2^9 and |T5+| < 2^2 per chunk, inside the split's 2^33 range
+                int h4, i4, h5 = 0, i5 = 0;
+                f32_round_split(__uint_as_float(t4[c]) * 16777216.0f, h4, i4);
+                if (C::TBLK > 1) f32_round_split(__uint_as_float(t5[c]) * 16777216.0f, h5, i5);
+                acc[hb + c] += ((long long)(h4 + h5) << 12) + (long long)(i4 + i5);
+              }
+            }
+          }
+          fence_before();
+          __syncwarp();
+          if (lane == 0) {
+            if (crank == 0) mbar_arrive(&xempty[xs]);
+            else mbar_arrive_cluster(leader_xempty0 + xs * 8u);
+          }
+        }
+        if (!ok) break;
+        if (row_ok && ncols > 0) {
+          const int Ei = S > 2 ? g.exps[oa.exp_off + gm] : 0;
+          const int32_t* Fj = g.exps + ob.exp_off + wi.nt * BN + cg * EPI_COLS;
+          const bool first = pd.first != 0;
+          if (first && g.bmode == 0 && g.amode == 0) {
+#pragma unroll
+            for (int c = 0; c < EPI_COLS; ++c)
+              if (c < ncols)
+                Rb[colR_s[cg * EPI_COLS + c]] =
+                    (S > 2) ? i64_scaled_to_f64(acc[c], Ei + __ldg(Fj + c) - 38) : (double)facc[c];
+          } else {
+#pragma unroll
+            for (int c = 0; c < EPI_COLS; ++c) {
+              if (c < ncols) {
+                double v = (S > 2) ? i64_scaled_to_f64(acc[c], Ei + __ldg(Fj + c) - 38) : (double)facc[c];
+                double* dst = Rb + colR_s[cg * EPI_COLS + c];
+                if (first) *dst = g.bmode == 0 ? g.alpha * v : g.alpha * v + g.beta * *dst;
+                else *dst = g.amode ? *dst + g.alpha * v : *dst + v;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  cluster_sync_all();                 // no MMA, copy or remote arrival of the pair is in flight
+  fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(C::TMEM_COLS));
+}
+
+// Shared-memory attribute of split_gemm2<S> (set once) and the number of CTA pairs that
+// can be resident at once, which is the persistent grid (SMs of a GPC pair up, so an odd
+// count leaves one idle).  Returns 0 on failure.
+template <int S>
+int pair_slots_for(nd_handle h) {
+  using C = Cfg2<S>;
+  static int slots = -1;
+  if (slots < 0) {
+    slots = 0;
+    if (cudaFuncSetAttribute(split_gemm2<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) == cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * std::max(1, h->num_sms / 2));
+      cfg.blockDim = dim3(NTHREADS);
+      cfg.dynamicSmemBytes = C::SMEM;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, (void*)split_gemm2<S>, &cfg) == cudaSuccess && n > 0) slots = n;
+      else cudaGetLastError();
+    } else {
+      cudaGetLastError();
+    }
+  }
+  return slots;
+}
+
+int pair_slots(nd_handle h, int S) {
+  switch (S) {
+    case 2: return pair_slots_for<2>(h);
+    case 3: return pair_slots_for<3>(h);
+    case 4: return pair_slots_for<4>(h);
+    case 5: return pair_slots_for<5>(h);
+    default: return pair_slots_for<6>(h);
+  }
+}
+
+template <int S>
+nd_status launch_gemm2(nd_handle h, const GemmArgs& g, int slots) {
+  if (pair_slots_for<S>(h) <= 0) return nd_fail(h, ND_ERR_CUDA, "split_gemm2: no CTA pair can be resident");
+  nd_prof_begin(h, "split_gemm");
+  using C = Cfg2<S>;
+  split_gemm2<S><<<2 * slots, NTHREADS, C::SMEM, h->stream>>>(g);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "split_gemm2");
+}
+
 // Persistent-CTA schedule.  Items (cost, tile) are assigned longest first to the
 // least-loaded of G = min(#items, SMs) CTAs, and laid out so that the kernels'
 // stride-G walk (item = blockIdx.x + r G) visits exactly each CTA's list; shorter
 // lists are padded with empty items (pair_count 0), which every role skips.
-std::vector<WorkItem> balance_items(std::vector<std::pair<int64_t, WorkItem>> tmp, int num_sms) {
+std::vector<WorkItem> balance_items(std::vector<std::pair<int64_t, WorkItem>> tmp, int num_slots, int* slots_out) {
   std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
   std::vector<WorkItem> items;
+  if (slots_out) *slots_out = 0;
   if (tmp.empty()) return items;
-  const int G = std::max(1, std::min((int)tmp.size(), num_sms));
+  const int G = std::max(1, std::min((int)tmp.size(), num_slots));
+  if (slots_out) *slots_out = G;
   std::vector<std::vector<WorkItem>> lists(G);
   std::vector<std::pair<int64_t, int>> heap;
   for (int b = 0; b < G; ++b) heap.push_back({0, b});
@@ -762,10 +1178,16 @@ struct SplitLayout {
   std::vector<WorkItem> items;
   int64_t pack_bytes = 0, exp_count = 0;
   int nops_a = 0, nops_b = 0;
+  int pair2 = 0;     // 1: 256 x 64 tiles on CTA pairs (split_gemm2); 0: 128 x 64 tiles (split_gemm)
+  int slots = 0;     // persistent CTAs (1-CTA tiles) or CTA pairs (2-CTA tiles)
 };
 
-static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int S, SplitLayout& L) {
+// pair2: tiles for CTA pairs.  A operands then hold an even number of 128-row tiles
+// (the odd CTA of a pair whose rows run past M stages zero digits, and the epilogue
+// stores nothing for those rows); work item mt is the index of a pair of row tiles.
+static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int S, int pair2, SplitLayout& L) {
   L = SplitLayout{};
+  L.pair2 = pair2 ? 1 : 0;
   L.pairs = pairs_in;
   std::map<std::pair<int, int64_t>, int> amap, bmap;   // (job, offset) -> op
   auto add_op = [&](bool is_b, const PairDesc& pd) -> int {
@@ -784,6 +1206,7 @@ static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int
     if (is_b) for (int d = 0; d < o.kk.n; ++d) o.kk.st0[d] = pd.ks.st1[d];
     const int rows_per_tile = is_b ? BN : BM;
     o.row_tiles = (o.rows + rows_per_tile - 1) / rows_per_tile;
+    if (L.pair2 && !is_b) o.row_tiles += o.row_tiles & 1;
     o.k_steps = (o.kdim + BK - 1) / BK;
     o.pack_off = L.pack_bytes;
     L.pack_bytes += (int64_t)o.row_tiles * o.k_steps * S * (is_b ? B_SLICE : A_SLICE);
@@ -812,13 +1235,24 @@ static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int
       ++j;
     }
     const PairDesc& p = L.pairs[i];
-    const int mt = (p.M + BM - 1) / BM, nt = (p.N + BN - 1) / BN;
+    int mt = (p.M + BM - 1) / BM;
+    const int nt = (p.N + BN - 1) / BN;
+    if (L.pair2) mt = (mt + 1) / 2;
     for (int a = 0; a < mt; ++a)
       for (int b = 0; b < nt; ++b)
         tmp.push_back({tile_cost(ksteps, (int)(j - i)), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
     i = j;
   }
-  L.items = balance_items(std::move(tmp), h->num_sms);
+  int nslots = h->num_sms;
+  if (L.pair2) {
+    nslots = pair_slots(h, S);
+    if (nslots <= 0) {            // the pair kernel cannot run here: single-CTA tiles
+      L = SplitLayout{};
+      split_layout(h, pairs_in, S, 0, L);
+      return;
+    }
+  }
+  L.items = balance_items(std::move(tmp), nslots, &L.slots);
 }
 
 static void split_adopt(ExecCache& c, const SplitLayout& L, int S) {
@@ -829,16 +1263,20 @@ static void split_adopt(ExecCache& c, const SplitLayout& L, int S) {
   c.pack_bytes = L.pack_bytes;
   c.exp_count = L.exp_count;
   c.slices = S;
+  c.split_pair2 = L.pair2;
+  c.split_slots = L.slots;
 }
 
 // Build operand list, packed layout and work items (host; once per plan/precision).
-nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs_in, int ngroups, int precision) {
+nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs_in, int ngroups, int precision,
+                         int pair2) {
   (void)ngroups;
   const int S = precision == ND_PREC_OZAKI ? h->ozaki_slices : 2;
   SplitLayout L;
-  split_layout(h, pairs_in, S, L);
+  split_layout(h, pairs_in, S, pair2, L);
   auto up = [&](void** dst, const void* src, size_t bytes) -> nd_status {
-    ND_CUDA(h, cudaMalloc(dst, std::max<size_t>(bytes, 16)));
+    nd_status e = nd_dalloc(h, dst, bytes);
+    if (e) return e;
     if (bytes) ND_CUDA(h, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
     return ND_OK;
   };
@@ -847,9 +1285,9 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
   if ((s = up((void**)&c.d_split_items, L.items.data(), L.items.size() * sizeof(WorkItem)))) return s;
   if ((s = up(&c.d_operands, L.ops.data(), L.ops.size() * sizeof(SplitOp)))) return s;
   if ((s = up(&c.d_pack_items, L.pitems.data(), L.pitems.size() * sizeof(PackItem2)))) return s;
-  ND_CUDA(h, cudaMalloc((void**)&c.d_rowmax, std::max<int64_t>(L.exp_count, 1) * 8));
-  ND_CUDA(h, cudaMalloc(&c.d_pack, std::max<int64_t>(L.pack_bytes, 16)));
-  ND_CUDA(h, cudaMalloc((void**)&c.d_exp, std::max<int64_t>(L.exp_count, 4) * 4));
+  if ((s = nd_dalloc(h, &c.d_rowmax, std::max<int64_t>(L.exp_count, 1) * 8))) return s;
+  if ((s = nd_dalloc(h, &c.d_pack, std::max<int64_t>(L.pack_bytes, 16)))) return s;
+  if ((s = nd_dalloc(h, (void**)&c.d_exp, std::max<int64_t>(L.exp_count, 4) * 4))) return s;
   split_adopt(c, L, S);
   return ND_OK;
 }
@@ -883,12 +1321,22 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
              (const unsigned char*)c.d_pack, c.d_exp, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1,
              h->d_status};
   if (c.nsplit_items == 0) return ND_OK;
-  switch (S) {
-    case 2: return launch_gemm<2>(h, g);
-    case 3: return launch_gemm<3>(h, g);
-    case 4: return launch_gemm<4>(h, g);
-    case 5: return launch_gemm<5>(h, g);
-    case 6: return launch_gemm<6>(h, g);
+  if (c.split_pair2) {
+    switch (S) {
+      case 2: return launch_gemm2<2>(h, g, c.split_slots);
+      case 3: return launch_gemm2<3>(h, g, c.split_slots);
+      case 4: return launch_gemm2<4>(h, g, c.split_slots);
+      case 5: return launch_gemm2<5>(h, g, c.split_slots);
+      case 6: return launch_gemm2<6>(h, g, c.split_slots);
+    }
+  } else {
+    switch (S) {
+      case 2: return launch_gemm<2>(h, g);
+      case 3: return launch_gemm<3>(h, g);
+      case 4: return launch_gemm<4>(h, g);
+      case 5: return launch_gemm<5>(h, g);
+      case 6: return launch_gemm<6>(h, g);
+    }
   }
   return nd_fail(h, ND_ERR_ARG, "unsupported slice count %d", S);
 }
@@ -900,7 +1348,7 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
 nd_status nd_split_layout_into(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs_in, int S,
                                unsigned char* base, size_t capacity, size_t* needed) {
   SplitLayout L;
-  split_layout(h, pairs_in, S, L);
+  split_layout(h, pairs_in, S, h->split_pair2, L);
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t o_pairs = 0;
   const size_t o_items = al(o_pairs + L.pairs.size() * sizeof(PairDesc));

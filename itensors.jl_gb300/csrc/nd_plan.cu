@@ -23,6 +23,7 @@
 namespace {
 
 constexpr int SCAN_BLOCK = 1024;
+constexpr int64_t PLAN1_MAX = 1 << 20;    // candidate pairs planned by one CTA in one launch
 
 __global__ void scan_block_sums(const int64_t* in, int64_t* block_sums, int64_t n) {
   __shared__ int64_t s[SCAN_BLOCK];
@@ -161,6 +162,134 @@ __global__ void assign_kernel(PlanKParams p, int64_t npairs, const int32_t* bloc
   }
 }
 
+// ---- one-CTA planner ---------------------------------------------------------
+// For up to PLAN1_MAX candidate pairs the whole plan is one launch of one CTA:
+// match flags and their block-wide scan compact the pairs in (A-major, B-minor)
+// order, a hash table in global scratch keeps each output key's first pair, a scan
+// of the first-appearance flags numbers the output blocks, and a last scan of their
+// sizes gives the offsets.  Every step is a fixed-order scan, so the result does not
+// depend on thread timing, and it is the same as the multi-kernel path's.
+constexpr int PLAN1_THREADS = 1024;
+
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* excl, T* wsum) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < (int)(blockDim.x >> 5) ? wsum[lane] : (T)0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  *excl = (warp ? wsum[warp - 1] : (T)0) + x - v;
+  const T total = wsum[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return total;
+}
+
+__global__ void __launch_bounds__(PLAN1_THREADS) plan_one_cta(PlanKParams p, const int32_t* blocksA,
+                                                              const int32_t* blocksB, const int64_t* rbd,
+                                                              int32_t* pairs, uint64_t* keys, int32_t* firstof,
+                                                              int32_t* blockid, uint64_t* tk, int32_t* tv,
+                                                              uint32_t mask, int32_t* blocksR, int64_t* offsR,
+                                                              int64_t* counts, DeviceStatus* st) {
+  __shared__ int wsum[32];
+  __shared__ long long wsum64[32];
+  const int tid = threadIdx.x;
+  for (uint32_t i = tid; i <= mask; i += blockDim.x) { tk[i] = ~0ull; tv[i] = 0x7fffffff; }
+  // 1. contracted pairs, compacted in the reference's order
+  const int64_t ncand = (int64_t)p.nA * p.nB;
+  int npairs = 0;
+  for (int64_t base = 0; base < ncand; base += blockDim.x) {
+    const int64_t idx = base + tid;
+    int flag = 0, i1 = 0, i2 = 0;
+    if (idx < ncand) {
+      i1 = (int)(idx / p.nB);
+      i2 = (int)(idx - (int64_t)i1 * p.nB);
+      const int32_t* bA = blocksA + (int64_t)i1 * p.rankA;
+      const int32_t* bB = blocksB + (int64_t)i2 * p.rankB;
+      flag = 1;
+      for (int t = 0; t < p.nk; ++t) flag &= (bA[p.a_k[t]] == bB[p.b_k[t]]);
+    }
+    int ex;
+    const int tot = block_exclusive_scan<int>(flag, &ex, wsum);
+    if (flag) {
+      const int q = npairs + ex;
+      int32_t c[ND_MAX_RANK];
+      blockR_coords(p, blocksA + (int64_t)i1 * p.rankA, blocksB + (int64_t)i2 * p.rankB, c);
+      pairs[3 * q] = i1;
+      pairs[3 * q + 1] = i2;
+      keys[q] = key_of(p, c);
+    }
+    npairs += tot;
+  }
+  __syncthreads();
+  // 2. the first pair of every output key
+  for (int q = tid; q < npairs; q += blockDim.x) {
+    const uint64_t key = keys[q];
+    uint32_t hsh = hash64(key) & mask;
+    bool done = false;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+      const unsigned long long prev = atomicCAS((unsigned long long*)&tk[hsh], ~0ull, (unsigned long long)key);
+      if (prev == ~0ull || prev == key) { atomicMin(&tv[hsh], q); done = true; break; }
+      hsh = (hsh + 1) & mask;
+    }
+    if (!done && atomicCAS(&st->code, 0, ND_ERR_ARG) == 0) st->where = 210;
+  }
+  __syncthreads();
+  // 3. output blocks numbered in first-appearance order, with their coordinates and sizes
+  int nR = 0;
+  for (int base = 0; base < npairs; base += blockDim.x) {
+    const int q = base + tid;
+    int first = 0;
+    if (q < npairs) {
+      const int f = table_lookup(keys[q], tk, tv, mask);
+      firstof[q] = f;
+      first = f == q;
+    }
+    int ex;
+    const int tot = block_exclusive_scan<int>(first, &ex, wsum);
+    if (first) {
+      const int id = nR + ex;
+      blockid[q] = id;
+      int32_t c[ND_MAX_RANK];
+      blockR_coords(p, blocksA + (int64_t)pairs[3 * q] * p.rankA, blocksB + (int64_t)pairs[3 * q + 1] * p.rankB, c);
+      int64_t sz = 1;
+      for (int r = 0; r < p.rankR; ++r) {
+        blocksR[(int64_t)id * p.rankR + r] = c[r];
+        sz *= rbd[p.r_bd_off[r] + c[r] - 1];
+      }
+      offsR[id] = sz;
+    }
+    nR += tot;
+  }
+  __syncthreads();
+  // 4. each pair's output block
+  for (int q = tid; q < npairs; q += blockDim.x) pairs[3 * q + 2] = blockid[firstof[q]];
+  // 5. offsets: exclusive scan of the block sizes, in block order
+  long long run = 0;
+  for (int base = 0; base < nR; base += blockDim.x) {
+    const int i = base + tid;
+    const long long v = i < nR ? (long long)offsR[i] : 0ll;
+    long long ex;
+    const long long tot = block_exclusive_scan<long long>(v, &ex, wsum64);
+    if (i < nR) offsR[i] = run + ex;
+    run += tot;
+  }
+  if (tid == 0) { counts[0] = npairs; counts[1] = nR; counts[2] = run; }
+}
+
 }  // namespace
 
 // Exclusive scan of n int64 values in place; *total_dev receives the sum.
@@ -203,6 +332,45 @@ nd_status nd_device_exclusive_scan(nd_handle h, int64_t* data, int64_t n, int64_
   return nd_cuda_check(h, cudaGetLastError(), "scan");
 }
 
+// Device buffers of the multi-kernel planner, released (stream-ordered) on every exit.
+namespace {
+struct AsyncBufs {
+  cudaStream_t s;
+  std::vector<void*> ptrs;
+  explicit AsyncBufs(cudaStream_t st) : s(st) {}
+  template <typename T>
+  cudaError_t alloc(T** p, size_t bytes) {
+    cudaError_t e = cudaMallocAsync((void**)p, bytes, s);
+    if (e == cudaSuccess) ptrs.push_back((void*)*p);
+    return e;
+  }
+  ~AsyncBufs() { for (void* p : ptrs) cudaFreeAsync(p, s); }
+};
+}  // namespace
+
+static nd_status device_plan_multi(nd_handle h, const Roles& ro, const BsDesc& A, const BsDesc& B,
+                                   const std::vector<int64_t>& r_nblocks,
+                                   const std::vector<std::vector<int64_t>>& r_blockdims, PlanResult& out);
+
+static void plan_params(const Roles& ro, const BsDesc& A, const BsDesc& B, const std::vector<int64_t>& r_nblocks,
+                        const std::vector<std::vector<int64_t>>& r_blockdims, PlanKParams& p, std::vector<int64_t>& rbd) {
+  p = PlanKParams{};
+  p.nA = A.nnzblocks; p.nB = B.nnzblocks; p.rankA = ro.rankA; p.rankB = ro.rankB; p.rankR = ro.rankR;
+  p.nk = ro.nk; p.nfa = ro.nfa; p.nfb = ro.nfb;
+  for (int t = 0; t < ro.nk; ++t) { p.a_k[t] = ro.a_k[t]; p.b_k[t] = ro.b_k[t]; }
+  for (int t = 0; t < ro.nfa; ++t) { p.a_free[t] = ro.a_free[t]; p.r_afree[t] = ro.r_afree[t]; }
+  for (int t = 0; t < ro.nfb; ++t) { p.b_free[t] = ro.b_free[t]; p.r_bfree[t] = ro.r_bfree[t]; }
+  rbd.clear();
+  for (int r = 0; r < ro.rankR; ++r) {
+    p.r_nblocks[r] = r_nblocks[r];
+    p.r_bd_off[r] = (int32_t)rbd.size();
+    rbd.insert(rbd.end(), r_blockdims[r].begin(), r_blockdims[r].end());
+  }
+  if (rbd.empty()) rbd.push_back(1);
+}
+
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
 nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const BsDesc& B,
                          const std::vector<int64_t>& r_nblocks, const std::vector<std::vector<int64_t>>& r_blockdims,
                          PlanResult& out) {
@@ -217,30 +385,91 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
     for (int r = 0; r < rankR; ++r) ks *= (long double)r_nblocks[r];
     if (ks > 1.8e19L) return nd_fail(h, ND_ERR_UNSUPPORTED, "plan: output block space exceeds 2^64");
   }
-  PlanKParams p{};
-  p.nA = nA; p.nB = nB; p.rankA = ro.rankA; p.rankB = ro.rankB; p.rankR = rankR;
-  p.nk = ro.nk; p.nfa = ro.nfa; p.nfb = ro.nfb;
-  for (int t = 0; t < ro.nk; ++t) { p.a_k[t] = ro.a_k[t]; p.b_k[t] = ro.b_k[t]; }
-  for (int t = 0; t < ro.nfa; ++t) { p.a_free[t] = ro.a_free[t]; p.r_afree[t] = ro.r_afree[t]; }
-  for (int t = 0; t < ro.nfb; ++t) { p.b_free[t] = ro.b_free[t]; p.r_bfree[t] = ro.r_bfree[t]; }
+  if (ncand > PLAN1_MAX || nd_capturing(h)) return device_plan_multi(h, ro, A, B, r_nblocks, r_blockdims, out);
+  PlanKParams p;
   std::vector<int64_t> rbd;
-  for (int r = 0; r < rankR; ++r) {
-    p.r_nblocks[r] = r_nblocks[r];
-    p.r_bd_off[r] = (int32_t)rbd.size();
-    rbd.insert(rbd.end(), r_blockdims[r].begin(), r_blockdims[r].end());
+  plan_params(ro, A, B, r_nblocks, r_blockdims, p, rbd);
+  // one device buffer: inputs (block lists, R block dims) | scratch | results (counts, pairs, blocksR, offsets)
+  uint32_t tsize = 1;
+  while (tsize < 2 * (uint64_t)ncand) tsize <<= 1;
+  const size_t szA = (size_t)nA * ro.rankA * 4, szB = (size_t)nB * ro.rankB * 4, szR = rbd.size() * 8;
+  const size_t o_A = 0, o_B = al256(o_A + szA), o_rbd = al256(o_B + szB), in_bytes = al256(o_rbd + szR);
+  const size_t o_keys = in_bytes, o_first = al256(o_keys + ncand * 8), o_bid = al256(o_first + ncand * 4);
+  const size_t o_tk = al256(o_bid + ncand * 4), o_tv = al256(o_tk + (size_t)tsize * 8);
+  const size_t o_out = al256(o_tv + (size_t)tsize * 4);
+  const size_t r_counts = 0, r_pairs = 32, r_blocks = al256(r_pairs + ncand * 12);
+  const size_t r_offs = al256(r_blocks + ncand * rankR * 4), out_bytes = r_offs + ncand * 8;
+  void* ws = nullptr;
+  nd_status s = nd_workspace(h, o_out + out_bytes, &ws);
+  if (s) return s;
+  unsigned char* d = (unsigned char*)ws;
+  if (h->pin_size < std::max(in_bytes, out_bytes)) {
+    if (h->pin) { cudaStreamSynchronize(h->stream); cudaFreeHost(h->pin); h->pin = nullptr; h->pin_size = 0; }
+    const size_t sz = std::max<size_t>(std::max(in_bytes, out_bytes), 1 << 16);
+    ND_CUDA(h, cudaHostAlloc(&h->pin, sz, cudaHostAllocDefault));
+    h->pin_size = sz;
   }
-  if (rbd.empty()) rbd.push_back(1);
+  unsigned char* hp = (unsigned char*)h->pin;
+  if (szA) memcpy(hp + o_A, A.blocks, szA);
+  if (szB) memcpy(hp + o_B, B.blocks, szB);
+  memcpy(hp + o_rbd, rbd.data(), szR);
+  cudaStream_t st = h->stream;
+  ND_CUDA(h, cudaMemcpyAsync(d, hp, in_bytes, cudaMemcpyHostToDevice, st));
+  unsigned char* r = d + o_out;
+  nd_prof_begin(h, "plan_one_cta");
+  plan_one_cta<<<1, PLAN1_THREADS, 0, st>>>(p, (const int32_t*)(d + o_A), (const int32_t*)(d + o_B),
+                                            (const int64_t*)(d + o_rbd), (int32_t*)(r + r_pairs),
+                                            (uint64_t*)(d + o_keys), (int32_t*)(d + o_first), (int32_t*)(d + o_bid),
+                                            (uint64_t*)(d + o_tk), (int32_t*)(d + o_tv), tsize - 1,
+                                            (int32_t*)(r + r_blocks), (int64_t*)(r + r_offs), (int64_t*)(r + r_counts),
+                                            h->d_status);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  ND_CUDA(h, cudaGetLastError());
+  // results: in one copy when the bound is small, else the counts first and then exact sizes
+  int64_t counts[3];
+  const bool one_copy = out_bytes <= (1u << 20);
+  ND_CUDA(h, cudaMemcpyAsync(hp, r, one_copy ? out_bytes : 32, cudaMemcpyDeviceToHost, st));
+  s = nd_check_device_status(h, "block plan");       // synchronises the stream
+  if (s) return s;
+  memcpy(counts, hp + r_counts, sizeof counts);
+  const int64_t npairs = counts[0], nR = counts[1];
+  if (!one_copy && npairs > 0) {
+    ND_CUDA(h, cudaMemcpyAsync(hp + r_pairs, r + r_pairs, npairs * 12, cudaMemcpyDeviceToHost, st));
+    ND_CUDA(h, cudaMemcpyAsync(hp + r_blocks, r + r_blocks, nR * rankR * 4, cudaMemcpyDeviceToHost, st));
+    ND_CUDA(h, cudaMemcpyAsync(hp + r_offs, r + r_offs, nR * 8, cudaMemcpyDeviceToHost, st));
+    ND_CUDA(h, cudaStreamSynchronize(st));
+  }
+  out.npairs = (int32_t)npairs;
+  out.nR = (int32_t)nR;
+  out.nnzR = counts[2];
+  out.pairs.assign((const int32_t*)(hp + r_pairs), (const int32_t*)(hp + r_pairs) + npairs * 3);
+  out.blocksR.assign((const int32_t*)(hp + r_blocks), (const int32_t*)(hp + r_blocks) + nR * rankR);
+  out.offsetsR.assign((const int64_t*)(hp + r_offs), (const int64_t*)(hp + r_offs) + nR);
+  return ND_OK;
+}
+
+// Plans with more than PLAN1_MAX candidate pairs: the same steps as plan_one_cta, one
+// grid-wide launch each, with device-wide scans.
+static nd_status device_plan_multi(nd_handle h, const Roles& ro, const BsDesc& A, const BsDesc& B,
+                                   const std::vector<int64_t>& r_nblocks,
+                                   const std::vector<std::vector<int64_t>>& r_blockdims, PlanResult& out) {
+  const int nA = A.nnzblocks, nB = B.nnzblocks, rankR = ro.rankR;
+  const int64_t ncand = (int64_t)nA * nB;
+  PlanKParams p;
+  std::vector<int64_t> rbd;
+  plan_params(ro, A, B, r_nblocks, r_blockdims, p, rbd);
   cudaStream_t s = h->stream;
-  // device buffers
+  AsyncBufs bufs(s);      // every buffer below is released on return, error paths included
   int32_t *dA = nullptr, *dB = nullptr, *pairs = nullptr, *tv = nullptr, *firstof = nullptr, *blocksR = nullptr;
   int64_t *flags = nullptr, *isfirst = nullptr, *sizeR = nullptr, *tot = nullptr, *rbd_d = nullptr;
   uint64_t *keys = nullptr, *tk = nullptr;
   size_t szA = std::max<size_t>(1, (size_t)nA * ro.rankA), szB = std::max<size_t>(1, (size_t)nB * ro.rankB);
-  ND_CUDA(h, cudaMallocAsync(&dA, szA * 4, s));
-  ND_CUDA(h, cudaMallocAsync(&dB, szB * 4, s));
-  ND_CUDA(h, cudaMallocAsync(&flags, ncand * 8, s));
-  ND_CUDA(h, cudaMallocAsync(&tot, 4 * 8, s));
-  ND_CUDA(h, cudaMallocAsync(&rbd_d, rbd.size() * 8, s));
+  ND_CUDA(h, bufs.alloc(&dA, szA * 4));
+  ND_CUDA(h, bufs.alloc(&dB, szB * 4));
+  ND_CUDA(h, bufs.alloc(&flags, ncand * 8));
+  ND_CUDA(h, bufs.alloc(&tot, 4 * 8));
+  ND_CUDA(h, bufs.alloc(&rbd_d, rbd.size() * 8));
   if (nA * (size_t)ro.rankA) ND_CUDA(h, cudaMemcpyAsync(dA, A.blocks, (size_t)nA * ro.rankA * 4, cudaMemcpyHostToDevice, s));
   if (nB * (size_t)ro.rankB) ND_CUDA(h, cudaMemcpyAsync(dB, B.blocks, (size_t)nB * ro.rankB * 4, cudaMemcpyHostToDevice, s));
   ND_CUDA(h, cudaMemcpyAsync(rbd_d, rbd.data(), rbd.size() * 8, cudaMemcpyHostToDevice, s));
@@ -252,7 +481,7 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
   ND_LAUNCHED(h);
   // positions = exclusive scan of flags (kept in a copy: flags still needed)
   int64_t* pos = nullptr;
-  ND_CUDA(h, cudaMallocAsync(&pos, ncand * 8, s));
+  ND_CUDA(h, bufs.alloc(&pos, ncand * 8));
   ND_CUDA(h, cudaMemcpyAsync(pos, flags, ncand * 8, cudaMemcpyDeviceToDevice, s));
   nd_status stt = nd_device_exclusive_scan(h, pos, ncand, tot);
   if (stt != ND_OK) return stt;
@@ -264,12 +493,12 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
     uint32_t tsize = 1;
     while (tsize < 2 * (uint64_t)npairs) tsize <<= 1;
     const uint32_t mask = tsize - 1;
-    ND_CUDA(h, cudaMallocAsync(&pairs, npairs * 3 * 4, s));
-    ND_CUDA(h, cudaMallocAsync(&keys, npairs * 8, s));
-    ND_CUDA(h, cudaMallocAsync(&tk, (size_t)tsize * 8, s));
-    ND_CUDA(h, cudaMallocAsync(&tv, (size_t)tsize * 4, s));
-    ND_CUDA(h, cudaMallocAsync(&isfirst, npairs * 8, s));
-    ND_CUDA(h, cudaMallocAsync(&firstof, npairs * 4, s));
+    ND_CUDA(h, bufs.alloc(&pairs, npairs * 3 * 4));
+    ND_CUDA(h, bufs.alloc(&keys, npairs * 8));
+    ND_CUDA(h, bufs.alloc(&tk, (size_t)tsize * 8));
+    ND_CUDA(h, bufs.alloc(&tv, (size_t)tsize * 4));
+    ND_CUDA(h, bufs.alloc(&isfirst, npairs * 8));
+    ND_CUDA(h, bufs.alloc(&firstof, npairs * 4));
     ND_CUDA(h, cudaMemsetAsync(tk, 0xff, (size_t)tsize * 8, s));
     ND_CUDA(h, cudaMemsetAsync(tv, 0x7f, (size_t)tsize * 4, s));
     nd_prof_begin(h, "compact_kernel");
@@ -283,7 +512,7 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
     ND_LAUNCHED(h);
     // block ids = exclusive scan of first-appearance flags
     int64_t* blockid = nullptr;
-    ND_CUDA(h, cudaMallocAsync(&blockid, npairs * 8, s));
+    ND_CUDA(h, bufs.alloc(&blockid, npairs * 8));
     ND_CUDA(h, cudaMemcpyAsync(blockid, isfirst, npairs * 8, cudaMemcpyDeviceToDevice, s));
     stt = nd_device_exclusive_scan(h, blockid, npairs, tot + 1);
     if (stt != ND_OK) return stt;
@@ -291,8 +520,8 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
     ND_CUDA(h, cudaMemcpyAsync(&nR, tot + 1, 8, cudaMemcpyDeviceToHost, s));
     ND_CUDA(h, cudaStreamSynchronize(s));
     out.nR = (int32_t)nR;
-    ND_CUDA(h, cudaMallocAsync(&blocksR, std::max<int64_t>(1, nR * rankR) * 4, s));
-    ND_CUDA(h, cudaMallocAsync(&sizeR, std::max<int64_t>(1, nR) * 8, s));
+    ND_CUDA(h, bufs.alloc(&blocksR, std::max<int64_t>(1, nR * rankR) * 4));
+    ND_CUDA(h, bufs.alloc(&sizeR, std::max<int64_t>(1, nR) * 8));
     nd_prof_begin(h, "assign_kernel");
     assign_kernel<<<pg, threads, 0, s>>>(p, npairs, dA, dB, pairs, isfirst, blockid, firstof, rbd_d, blocksR, sizeR);
     nd_prof_end(h);
@@ -307,12 +536,7 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
     ND_CUDA(h, cudaMemcpyAsync(out.offsetsR.data(), sizeR, nR * 8, cudaMemcpyDeviceToHost, s));
     ND_CUDA(h, cudaMemcpyAsync(&out.nnzR, tot + 2, 8, cudaMemcpyDeviceToHost, s));
     ND_CUDA(h, cudaStreamSynchronize(s));
-    cudaFreeAsync(pairs, s); cudaFreeAsync(keys, s); cudaFreeAsync(tk, s); cudaFreeAsync(tv, s);
-    cudaFreeAsync(isfirst, s); cudaFreeAsync(firstof, s); cudaFreeAsync(blockid, s);
-    cudaFreeAsync(blocksR, s); cudaFreeAsync(sizeR, s);
   }
-  cudaFreeAsync(dA, s); cudaFreeAsync(dB, s); cudaFreeAsync(flags, s); cudaFreeAsync(pos, s);
-  cudaFreeAsync(tot, s); cudaFreeAsync(rbd_d, s);
   ND_CUDA(h, cudaGetLastError());
   return nd_check_device_status(h, "block plan");
 }

@@ -62,7 +62,13 @@ struct ExecCache {
   void* d_pack_items = nullptr;    // pack work list
   int npack_items = 0;
   void* d_rowmax = nullptr;        // per-row |x| maxima (IEEE bits) of the split operands
-  void free_all();
+  int split_pair2 = 0;             // 1: split GEMM on CTA pairs (256 x 64 tiles)
+  int req_pair2 = -1;              // the handle's untuned tile shape when this state was built
+  int split_slots = 0;             // persistent CTAs / CTA pairs of the split GEMM
+  cudaStream_t stream = nullptr;   // stream of the last work that used this state
+  // Release every buffer, stream-ordered on the handle's stream (after a device-wide
+  // synchronisation when the state was last used on another stream).
+  void free_all(nd_handle h);
 };
 
 struct nd_bs_plan_s {

@@ -64,6 +64,7 @@ SIGNATURES = {
     "nd_d2h": [_P, _P, _P, C.c_size_t],
     "nd_memset0": [_P, _P, C.c_size_t],
     "nd_set_ozaki_slices": [_P, _I32],
+    "nd_set_split_tile": [_P, _I32],
     "nd_set_spin_limit": [_P, C.c_uint32],
     "nd_set_svd_max_sweeps": [_P, _I32],
     "nd_launch_count": [_P, _PI64],
@@ -82,14 +83,24 @@ SIGNATURES = {
     "nd_bs_plan_sizes": [_P, _PI32, _PI32, _PI64],
     "nd_bs_plan_get": [_P, _PI32, _PI64, _PI32],
     "nd_bs_plan_destroy": [_P],
+    "nd_bs_plan_set_output_offsets": [_P, _PI64],
     "nd_bs_contract_f64": [_P, _P, _P, _P, _P, _D, _I32],
     "nd_bs_contract_adjoint_f64": [_P, _P, _P, _P, _P, _P, _P, _I32],
+    "nd_bs_contract_diag_f64": [_P, _P, _P, _P, _P, _PI64, _D],
     "nd_bs_permutedims_f64": [_P, C.POINTER(BsDesc), _P, _PI32, _PI64, _P],
     "nd_bs_svd_f64": [_P, _I32, _PI64, _PI64, _PI64, _P, _P, _P, _P, _I32, _I32, _D, _I32, _I32, _I32,
                       _PI32, _PD, _PI32, _PD, _PD],
     "nd_bs_qr_f64": [_P, _I32, _PI64, _PI64, _PI64, _P, _P, _P, _I32],
+    "nd_bs_eigen_f64": [_P, _I32, _PI64, _PI64, _P, _P, _P, _I32, _I32, _D, _I32, _I32, _I32, _PI32, _PD, _PI32,
+                        _PD, _PD],
     "nd_truncate_f64": [_P, _P, _I32, _I32, _I32, _D, _I32, _I32, _PI32, _PD, _PD],
     "nd_block_copy_f64": [_P, _I32, C.POINTER(BlockCopy), _P, _P],
+    "nd_vec_inner_f64": [_P, _I64, _P, _P, _P],
+    "nd_vec_norm_f64": [_P, _I64, _P, _P],
+    "nd_vec_scale_f64": [_P, _I64, _P, _P, _D, _P, _I32],
+    "nd_vec_add_f64": [_P, _I64, _P, _P, _D, _D],
+    "nd_vec_dots_f64": [_P, _I64, _I32, _P, _I64, _P, _P],
+    "nd_vec_update_f64": [_P, _I64, _I32, _P, _I64, _P, _D, _P],
     "nd_graph_begin": [_P],
     "nd_graph_end": [_P, C.POINTER(_P)],
     "nd_graph_launch": [_P, _P],

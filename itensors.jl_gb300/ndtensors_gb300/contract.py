@@ -133,6 +133,15 @@ class ContractionPlan:
             out.append((m, n, k, ir))
         return out
 
+    def set_output_offsets(self, offsets):
+        """Write the output blocks at these offsets (a caller's layout, e.g. psi's block
+        order) instead of the first-appearance offsets."""
+        offs = [int(o) for o in offsets]
+        if len(offs) != self.nblocksR:
+            raise ValueError("set_output_offsets: one offset per output block")
+        self.h._check(self.h.lib.nd_bs_plan_set_output_offsets(self.ptr, i64arr(offs)))
+        self.offsetsR = offs
+
     def flops(self, T1, T2):
         return sum(2 * m * n * k for (m, n, k, _) in self.pair_shapes(T1, T2))
 
@@ -180,14 +189,36 @@ def contract_blocksparse(T1, l1, T2, l2, lr=None, alpha=1.0, precision="fp64", p
     return R
 
 
+def contract_diag(T1: BlockSparseTensor, l1, D, l2, lr=None, alpha=1.0):
+    """contract(::BlockSparseTensor, ::DiagBlockSparseTensor) (blocksparse/diagblocksparse.jl:601-696):
+    the block plan and output structure of contraction_output, then one library kernel
+    that scales / sums T1's entries by D's diagonal (no dense expansion of D)."""
+    import torch
+    l1, l2 = tuple(l1), tuple(l2)
+    lr = contract_labels(l1, l2) if lr is None else tuple(lr)
+    offs, _ = blockoffsets(D.blocks, D.inds)
+    Ds = BlockSparseTensor(list(D.inds), list(D.blocks), offs, D.data)     # D's block structure for the planner
+    plan = get_plan(T1, l1, Ds, l2, lr)
+    data = torch.empty(max(plan.nnzR, 1), dtype=torch.float64, device=T1.data.device)[:plan.nnzR]
+    R = BlockSparseTensor(list(plan.indsR), list(plan.blocksR), list(plan.offsetsR), data)
+    if plan.nnzR:
+        if not plan.npairs:
+            handle(T1.data.device.index or 0).call("nd_memset0", C.c_void_p(data.data_ptr()), 8 * plan.nnzR)
+        else:
+            handle(T1.data.device.index or 0)
+            plan.h.call("nd_bs_contract_diag_f64", plan.ptr, C.c_void_p(data.data_ptr()), C.c_void_p(T1.data.data_ptr()),
+                        C.c_void_p(D.data.data_ptr()), i64arr(D.offsets), float(alpha))
+    return R
+
+
 def contract(T1, labels1, T2, labels2, labelsR=None, precision="fp64"):
     """contract(T1, labelsT1, T2, labelsT2[, labelsR]) for Dense, BlockSparse or
     BlockSparse x DiagBlockSparse storage.
 
-    A DiagBlockSparse operand follows NDTensors' default dense conversion
-    (diag/tensoralgebra/contract.jl:103-214; blocksparse/diagblocksparse.jl:601-696): its
-    diagonal blocks are expanded on the device and the contraction is one grouped
-    launch whose block plan and output structure are those of contraction_output."""
+    A block-diagonal DiagBlockSparse operand runs on the library's diagonal kernel
+    (contract_diag; NDTensors/src/blocksparse/diagblocksparse.jl:601-696) with the block
+    plan and output structure of contraction_output; the result is exact (no
+    precision choice applies: each output element is one product or a short sum)."""
     from .tensors import DiagBlockSparseTensor
     l1, l2 = tuple(labels1), tuple(labels2)
     if isinstance(T1, DiagBlockSparseTensor):
@@ -195,7 +226,7 @@ def contract(T1, labels1, T2, labels2, labelsR=None, precision="fp64"):
     if isinstance(T2, DiagBlockSparseTensor):
         if not isinstance(T1, BlockSparseTensor):
             raise TypeError("contract: a DiagBlockSparse operand needs a BlockSparse partner")
-        T2 = T2.dense()
+        return contract_diag(T1, l1, T2, l2, labelsR)
     lr = contract_labels(l1, l2) if labelsR is None else tuple(labelsR)
     if isinstance(T1, BlockSparseTensor) and isinstance(T2, BlockSparseTensor):
         return contract_blocksparse(T1, l1, T2, l2, lr, precision=precision)

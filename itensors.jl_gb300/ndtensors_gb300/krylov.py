@@ -3,53 +3,86 @@
 A DMRG sweep solves its local eigenproblem with KrylovKit over the vector-space
 interface the reference provides for ITensors
 (ext/ITensorsVectorInterfaceExt/ITensorsVectorInterfaceExt.jl:5-84: add / add! /
-inner / scale / scale!).  Here a vector is the flat FP64 data of a
-tensor with a fixed block structure, the VectorInterface operations are torch
-ops on that data (`inner`, `norm`, `add_`, `scale_`), and the operator is a
-sequence of library contractions (`HeffOperator`: the two-site H_eff applied as
-L * psi, * W1, * W2, * R with cached plans and preallocated intermediates).
+inner / scale / scale!).  Here a vector is the flat FP64 data of a tensor with a
+fixed block structure, and every VectorInterface operation is a library call
+(nd_vec_inner_f64, nd_vec_norm_f64, nd_vec_scale_f64, nd_vec_add_f64, and the
+basis forms nd_vec_dots_f64 / nd_vec_update_f64 for Gram-Schmidt).  The operator
+is a sequence of library contractions (`HeffOperator`: the two-site H_eff applied
+as L * psi, * W1, * W2, * R with cached plans and preallocated intermediates; the
+last contraction writes straight into psi's block layout).
 
 `lanczos` builds a Krylov basis of `krylovdim` vectors with full
-re-orthogonalisation (classical Gram-Schmidt, twice).  With ``graph=True`` the
-whole basis construction -- every matvec and every orthogonalisation -- is
-captured once into one CUDA graph (torch.cuda.graph; the library detects the
-capture and only launches kernels) and replayed; the krylovdim x krylovdim
-tridiagonal problem is then solved on the host.
+re-orthogonalisation (classical Gram-Schmidt, twice).  Scalars (norms, alpha,
+beta) stay on the device, so with ``graph=True`` the whole basis construction --
+every matvec and every orthogonalisation -- is captured once into one CUDA graph
+and replayed; the krylovdim x krylovdim tridiagonal problem is then solved on the
+host.  No torch or cuBLAS kernel runs inside the loop.
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 
-from .contract import contract_blocksparse, get_plan
+from ._lib import handle
+from .contract import ContractionPlan, contract_blocksparse, get_plan
 from .tensors import BlockSparseTensor
 
 
-def inner(x, y):
-    """VectorInterface.inner on flat real data (a device scalar)."""
-    return (x * y).sum()
+def _h(x):
+    return handle(x.device.index or 0)
 
 
-def norm(x):
+def _p(t, offset=0):
+    return C.c_void_p(t.data_ptr() + 8 * offset)
+
+
+def inner(x, y, out=None):
+    """VectorInterface.inner(x, y) on flat real data: a device scalar (1-element tensor)."""
     import torch
-    return torch.linalg.vector_norm(x)
+    out = torch.empty(1, dtype=torch.float64, device=x.device) if out is None else out
+    _h(x).call("nd_vec_inner_f64", int(x.numel()), _p(x), _p(y), _p(out))
+    return out
+
+
+def norm(x, out=None):
+    """norm(x): a device scalar."""
+    import torch
+    out = torch.empty(1, dtype=torch.float64, device=x.device) if out is None else out
+    _h(x).call("nd_vec_norm_f64", int(x.numel()), _p(x), _p(out))
+    return out
 
 
 def scale_(x, a):
-    """VectorInterface.scale!(x, a)."""
-    return x.mul_(a)
+    """VectorInterface.scale!(x, a): x *= a (a a number or a device scalar)."""
+    return scale(x, a, out=x)
 
 
-def add_(y, x, a=1.0):
-    """VectorInterface.add!(y, x, a): y += a x."""
-    return y.add_(x, alpha=a)
+def scale(x, a, out=None, invert=False):
+    """VectorInterface.scale(x, a): a * x (or x / a with invert), into `out`."""
+    import torch
+    out = torch.empty_like(x) if out is None else out
+    if isinstance(a, torch.Tensor):
+        _h(x).call("nd_vec_scale_f64", int(x.numel()), _p(x), _p(out), 1.0, _p(a), 1 if invert else 0)
+    else:
+        a = float(a)
+        _h(x).call("nd_vec_scale_f64", int(x.numel()), _p(x), _p(out), 1.0 / a if invert else a, None, 0)
+    return out
+
+
+def add_(y, x, a=1.0, b=1.0):
+    """VectorInterface.add!(y, x, a, b): y = b y + a x."""
+    _h(x).call("nd_vec_add_f64", int(x.numel()), _p(x), _p(y), float(a), float(b))
+    return y
 
 
 class HeffOperator:
     """x -> H_eff x for the two-site network (L, W1, W2, R) on a fixed psi structure.
 
-    Plans and the three intermediates are built once; the result is gathered back
-    into psi's block order (the plan lists output blocks in first-appearance order),
-    so the operator maps the vector space onto itself and can be captured.
+    Plans and the intermediates are built once.  The last contraction's plan is the
+    operator's own (not the shared plan cache) and writes each output block at psi's
+    offset for that block, so the operator maps the vector space onto itself with no
+    gather and can be captured.
     """
 
     def __init__(self, L, W1, W2, R, psi: BlockSparseTensor, steps, precision="ozaki"):
@@ -61,42 +94,32 @@ class HeffOperator:
         dev = psi.data.device
         self.plans, self.outs = [], []
         x = L
-        for (a, b, c), T in zip(steps, [psi, W1, W2, R]):
-            p = get_plan(x, a, T, b, c)
-            o = BlockSparseTensor(list(p.indsR), list(p.blocksR), list(p.offsetsR),
-                                  torch.empty(max(p.nnzR, 1), dtype=torch.float64, device=dev)[:p.nnzR])
+        for i, ((a, b, c), T) in enumerate(zip(steps, [psi, W1, W2, R])):
+            last = i == len(steps) - 1
+            p = ContractionPlan(x, a, T, b, c) if last else get_plan(x, a, T, b, c)
             self.plans.append(p)
-            self.outs.append(o)
-            x = o
-        out = self.outs[-1]
-        if sorted(map(tuple, out.blocks)) != sorted(map(tuple, psi.blocks)) or out.nnz != psi.nnz:
+            if not last:
+                o = BlockSparseTensor(list(p.indsR), list(p.blocksR), list(p.offsetsR),
+                                      torch.empty(max(p.nnzR, 1), dtype=torch.float64, device=dev)[:p.nnzR])
+                self.outs.append(o)
+                x = o
+        p = self.plans[-1]
+        if sorted(map(tuple, p.blocksR)) != sorted(map(tuple, psi.blocks)) or p.nnzR != psi.nnz:
             raise ValueError("H_eff does not map psi's block structure onto itself")
-        # element gather: psi-ordered data = out.data[index]
-        index = np.empty(psi.nnz, dtype=np.int64)
-        where = {tuple(b): o for b, o in zip(out.blocks, out.offsets)}
-        for b, off in zip(psi.blocks, psi.offsets):
-            n = int(np.prod(psi.blockdims(b)))
-            src = where[tuple(b)]
-            index[off:off + n] = np.arange(src, src + n)
-        self.identity = bool(np.array_equal(index, np.arange(psi.nnz)))
-        self.index = torch.from_numpy(index).to(dev)
+        where = {tuple(b): o for b, o in zip(psi.blocks, psi.offsets)}
+        p.set_output_offsets([where[tuple(b)] for b in p.blocksR])
         self.n = psi.nnz
 
     def apply(self, x, out):
         """out = H_eff x (x, out: flat psi-ordered device data)."""
-        import torch
         psi = BlockSparseTensor(*self.psi_struct, x)
         cur = self.L
-        for (a, b, c), T, p, o in zip(self.steps, [psi] + self.rhs[1:], self.plans, self.outs):
-            if T is psi:
-                contract_blocksparse(cur, a, psi, b, c, precision=self.precision, plan=p, out=o)
-            else:
-                contract_blocksparse(cur, a, T, b, c, precision=self.precision, plan=p, out=o)
+        p = self.plans[-1]
+        res = BlockSparseTensor(list(p.indsR), list(p.blocksR), list(p.offsetsR), out)
+        dests = self.outs + [res]
+        for (a, b, c), T, pl, o in zip(self.steps, [psi] + self.rhs[1:], self.plans, dests):
+            contract_blocksparse(cur, a, T, b, c, precision=self.precision, plan=pl, out=o)
             cur = o
-        if self.identity:
-            out.copy_(self.outs[-1].data)
-        else:
-            torch.index_select(self.outs[-1].data, 0, self.index, out=out)
         return out
 
 
@@ -113,37 +136,41 @@ class Lanczos:
     def __init__(self, apply, n, krylovdim=10, device=0, graph=False):
         import torch
         self.apply, self.n, self.k, self.graph = apply, n, int(krylovdim), graph
+        if self.k + 1 > 32:
+            raise ValueError("krylovdim must be at most 31 (the library's basis operations take 32 vectors)")
         dev = torch.device("cuda", device)
         f64 = dict(dtype=torch.float64, device=dev)
-        self.V = torch.zeros((self.k + 1, n), **f64)
+        self.V = torch.zeros((self.k + 1, n), **f64)         # basis, one vector per row (ldv = n)
         self.w = torch.empty(n, **f64)
-        self.coef = torch.empty(self.k + 1, **f64)
+        self.coef = torch.empty((2, self.k + 1), **f64)       # Gram-Schmidt coefficients of the two passes
         self.alpha = torch.zeros(self.k, **f64)
         self.beta = torch.zeros(self.k, **f64)
+        self.s = torch.empty(1, **f64)
         self.start = torch.empty(n, **f64)
+        self.device = device
         self._graph = None
 
     def _body(self):
-        import torch
-        V, w, coef = self.V, self.w, self.coef
-        V[0].copy_(self.start)
-        V[0].div_(torch.linalg.vector_norm(V[0]))
+        h = handle(self.device)
+        n, V, w = self.n, self.V, self.w
+        h.call("nd_vec_norm_f64", n, _p(self.start), _p(self.s))
+        h.call("nd_vec_scale_f64", n, _p(self.start), _p(V), 1.0, _p(self.s), 1)           # V0 = start / |start|
         for j in range(self.k):
             self.apply(V[j], w)
-            basis = V[:j + 1]
-            for sweep in range(2):                      # full re-orthogonalisation
-                torch.mv(basis, w, out=coef[:j + 1])
-                if sweep == 0:
-                    self.alpha[j:j + 1].copy_(coef[j:j + 1])
-                else:
-                    self.alpha[j:j + 1].add_(coef[j:j + 1])
-                w.addmv_(basis.t(), coef[:j + 1], alpha=-1.0)
-            self.beta[j:j + 1].copy_(torch.linalg.vector_norm(w).reshape(1))
-            torch.div(w, self.beta[j], out=V[j + 1])
+            for sweep in range(2):                                                       # full re-orthogonalisation
+                c = self.coef[sweep]
+                h.call("nd_vec_dots_f64", n, j + 1, _p(V), n, _p(w), _p(c))              # c = V[:j+1] w
+                h.call("nd_vec_update_f64", n, j + 1, _p(V), n, _p(c), -1.0, _p(w))       # w -= V[:j+1]^T c
+            a = self.alpha[j:j + 1]
+            h.call("nd_vec_add_f64", 1, _p(self.coef[0], j), _p(a), 1.0, 0.0)             # alpha_j = c0_j + c1_j
+            h.call("nd_vec_add_f64", 1, _p(self.coef[1], j), _p(a), 1.0, 1.0)
+            h.call("nd_vec_norm_f64", n, _p(w), _p(self.beta, j))                          # beta_j = |w|
+            h.call("nd_vec_scale_f64", n, _p(w), _p(V, (j + 1) * n), 1.0, _p(self.beta, j), 1)   # V_{j+1} = w / beta_j
 
     def run(self, v0):
         import torch
-        self.start.copy_(v0)
+        h = handle(self.device)
+        h.call("nd_vec_scale_f64", self.n, _p(v0), _p(self.start), 1.0, None, 0)
         if not self.graph:
             self._body()
         else:
@@ -161,9 +188,12 @@ class Lanczos:
         b = self.beta.cpu().numpy()
         T = np.diag(a) + np.diag(b[:-1], 1) + np.diag(b[:-1], -1)
         vals, vecs = np.linalg.eigh(T)
-        y = vecs[:, 0]
-        x = torch.mv(self.V[:self.k].t(), torch.from_numpy(y).to(self.V.device))
-        return LanczosResult(float(vals[0]), x, float(abs(b[-1] * y[-1])), a, b, self.k)
+        y = torch.from_numpy(np.ascontiguousarray(vecs[:, 0])).to(self.V.device)
+        x = torch.empty(self.n, dtype=torch.float64, device=self.V.device)
+        h = handle(self.device)
+        h.call("nd_vec_scale_f64", self.n, _p(self.V), _p(x), 0.0, None, 0)                # x = 0
+        h.call("nd_vec_update_f64", self.n, self.k, _p(self.V), self.n, _p(y), 1.0, _p(x))  # x = V[:k]^T y
+        return LanczosResult(float(vals[0]), x, float(abs(b[-1] * y[-1].item())), a, b, self.k)
 
 
 def lanczos(apply, v0, krylovdim=10, graph=False):

@@ -94,67 +94,48 @@ def svd(T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absolut
 def eigen(T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absolute_cutoff=None,
           use_relative_cutoff=None, min_blockdim=None):
     """Blockwise eigendecomposition of a Hermitian (real symmetric) block-diagonal matrix
-    (NDTensors/src/blocksparse/linearalgebra.jl:221-348).
+    (NDTensors/src/blocksparse/linearalgebra.jl:221-348), one library call
+    (nd_bs_eigen_f64): per block the eigenpairs sorted by |lambda| descending, the pooled
+    |lambda| sorted and truncated by truncate! and the kept dimension of every block,
+    all on the device.
 
-    Returns (D, V, Spectrum, kept): D a list of per-block eigenvalues (sorted by |lambda|
-    descending, truncated), V with inds (T.inds[1], v) and one block per surviving block,
-    Spectrum of the pooled |lambda| after truncate!.  Each block A_b is shifted to
-    A_b + c_b I with c_b = ||A_b||_F, which is positive semi-definite, so the library's
-    batched Jacobi SVD gives its eigenvectors directly (left = right singular vectors)
-    and lambda = sigma - c_b; the pooled sort / truncate! also runs on the device.
+    Returns (D, V, Spectrum, kept): D a list of per-block eigenvalues (truncated), V with
+    inds (T.inds[1], v) and one block per surviving block, Spectrum of the pooled |lambda|
+    after truncate!; None if a block did not converge (the reference returns nothing).
     """
     import torch
     rows, cols = _matrix_blocks(T)
     for b, r, c in zip(T.blocks, rows, cols):
         if b[0] != b[1] or r != c:
             raise ValueError("eigen: only block-diagonal matrices with square blocks are supported")
+    nb = len(T.blocks)
     dev = T.data.device
-    W = T.data.clone()
-    shifts = []
-    for off, r in zip(T.offsets, rows):
-        blk = W[off:off + r * r]
-        # strictly positive definite after the shift (the Jacobi SVD returns zero vectors
-        # for exactly zero singular values): c = 1.01 ||A_b||_F, or 1 for a zero block
-        nrm = float(torch.linalg.vector_norm(blk)) if r else 0.0
-        c = 1.01 * nrm if nrm > 0.0 else 1.0
-        blk.view(r, r).diagonal().add_(c)            # column-major: the diagonal is the same either way
-        shifts.append(c)
-    out = svd(BlockSparseTensor(T.inds, T.blocks, T.offsets, W))
-    if out is None:
-        return None                                  # a block did not converge (the reference returns nothing)
-    _, S, Vt, _, _ = out
-    lams, vecs = [], []
-    for n, (off, r) in enumerate(zip(Vt.offsets, rows)):
-        lam = S[n] - shifts[n]
-        order = torch.argsort(-lam.abs(), stable=True)
-        lams.append(lam[order])
-        # the column-major block viewed row-major is V^T: index its rows to reorder V's columns
-        vecs.append(Vt.data[off:off + r * r].view(r, r)[order].t())
-    pooled = torch.sort(torch.cat([l.abs() for l in lams]), descending=True).values.contiguous()
-    truncerr = 0.0
-    kept = [int(l.numel()) for l in lams]
-    if maxdim is not None or cutoff is not None:
-        nkeep, truncerr, docut = truncate(pooled, mindim, maxdim, cutoff, use_absolute_cutoff, use_relative_cutoff)
-        pooled = pooled[:nkeep]
-        mb = 0 if min_blockdim is None else int(min_blockdim)
-        for n, l in enumerate(lams):
-            a = l.abs().cpu().numpy()
-            k = 0
-            while k < a.size and a[k] > docut:
-                k += 1
-            kept[n] = max(k, min(mb, a.size))
-    surv = [n for n in range(len(lams)) if kept[n] > 0]
+    Dfull = torch.empty(max(1, sum(rows)), dtype=torch.float64, device=dev)
+    Vfull = torch.empty(max(1, sum(r * r for r in rows)), dtype=torch.float64, device=dev)
+    kept = (C.c_int32 * max(1, nb))()
+    spec = (C.c_double * max(1, sum(rows)))()
+    slen, terr, dcut = C.c_int32(), C.c_double(), C.c_double()
+    h = handle(dev.index or 0)
+    try:
+        h.call("nd_bs_eigen_f64", nb, i64arr(rows), i64arr(T.offsets), C.c_void_p(T.data.data_ptr()),
+               C.c_void_p(Dfull.data_ptr()), C.c_void_p(Vfull.data_ptr()),
+               int(_opt(mindim, 1)), int(_opt(maxdim, -1)), float(_opt(cutoff, -1.0)),
+               int(bool(use_absolute_cutoff)) if use_absolute_cutoff is not None else 0,
+               int(bool(use_relative_cutoff)) if use_relative_cutoff is not None else 1,
+               int(_opt(min_blockdim, 0)), kept, spec, C.byref(slen), C.byref(terr), C.byref(dcut))
+    except NoConvergence:
+        return None
+    kept = list(kept[:nb])
+    surv = [n for n in range(nb) if kept[n] > 0]
     v_ind = tuple(kept[n] for n in surv)
     Vblocks = [(T.blocks[n][0], i + 1) for i, n in enumerate(surv)]
     Vo, nv = blockoffsets(Vblocks, [T.inds[1], v_ind])
-    Vdata = torch.empty(max(nv, 1), dtype=torch.float64, device=dev)[:nv]
-    D = []
-    for i, n in enumerate(surv):
-        k, r = kept[n], rows[n]
-        Vdata[Vo[i]:Vo[i] + r * k].copy_(vecs[n][:, :k].t().reshape(-1))   # column-major r x k
-        D.append(lams[n][:k])
-    Vt_out = BlockSparseTensor([tuple(T.inds[1]), v_ind], Vblocks, Vo, Vdata)
-    return D, Vt_out, Spectrum(pooled.cpu().numpy(), truncerr), kept
+    D, o = [], 0
+    for n in surv:
+        D.append(Dfull[o:o + kept[n]])
+        o += kept[n]
+    Vt = BlockSparseTensor([tuple(T.inds[1]), v_ind], Vblocks, Vo, Vfull[:nv])
+    return D, Vt, Spectrum(np.array(spec[:slen.value]), terr.value), kept
 
 
 def qr(T: BlockSparseTensor, positive=False):

@@ -174,19 +174,30 @@ class DiagBlockSparseTensor:
         return cls([tuple(i) for i in inds], [tuple(b) for b in blocks], offs, data)
 
     def dense(self):
-        """The equal-structure BlockSparseTensor with the diagonals expanded (on the device),
-        as NDTensors' default dense(D) conversion (diag/tensoralgebra/contract.jl:103-214)."""
+        """The equal-structure BlockSparseTensor with the diagonals expanded, as NDTensors'
+        dense(D) conversion (diag/tensoralgebra/contract.jl:103-214): a library memset and
+        one strided scatter of every diagonal (element i of block b to (i, i, ..., i))."""
+        import ctypes as C
+        from ._lib import BlockCopy, handle
         torch = _torch()
         offs, nnz = blockoffsets(self.blocks, self.inds)
-        out = torch.zeros(max(nnz, 1), dtype=torch.float64, device=self.data.device)[:nnz]
+        out = torch.empty(max(nnz, 1), dtype=torch.float64, device=self.data.device)[:nnz]
+        h = handle(self.data.device.index or 0)
+        if nnz:
+            h.call("nd_memset0", C.c_void_p(out.data_ptr()), 8 * nnz)
+        copies = []
         for b, o, do in zip(self.blocks, offs, self.offsets):
             dims = self.blockdims(b)
             k = min(dims) if dims else 1
-            stride = 0                                # column-major offset of (i, i, ..., i)
-            s = 1
+            stride, s = 0, 1                          # column-major offset step of (i, i, ..., i)
             for d in dims:
                 stride += s
                 s *= d
-            idx = torch.arange(k, device=self.data.device) * stride + o
-            out.index_copy_(0, idx, self.data[do:do + k])
+            c = BlockCopy()
+            c.src_off, c.dst_off, c.rank = do, o, 1
+            c.dims[0], c.src_strides[0], c.dst_strides[0] = k, 1, stride
+            copies.append(c)
+        if copies and nnz:
+            arr = (BlockCopy * len(copies))(*copies)
+            h.call("nd_block_copy_f64", len(copies), arr, C.c_void_p(self.data.data_ptr()), C.c_void_p(out.data_ptr()))
         return BlockSparseTensor(list(self.inds), list(self.blocks), offs, out)
