@@ -25,22 +25,37 @@ nd_status nd_cuda_check(nd_handle h, cudaError_t e, const char* what) {
   return nd_fail(h, ND_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-nd_status nd_workspace(nd_handle h, size_t bytes, void** out) {
-  if (bytes == 0) bytes = 256;
-  if (bytes > h->ws_size) {
-    if (nd_capturing(h))
-      return nd_fail(h, ND_ERR_ARG, "workspace must grow during graph capture: run the call once before capture");
-    if (h->ws) {
-      ND_CUDA(h, cudaStreamSynchronize(h->stream));
-      ND_CUDA(h, cudaFree(h->ws));
-      h->ws = nullptr;
-      h->ws_size = 0;
-    }
-    size_t sz = std::max(bytes, h->ws_size * 3 / 2);
-    ND_CUDA(h, cudaMalloc(&h->ws, sz));
-    h->ws_size = sz;
+nd_status nd_upload(nd_handle h, void* dst, const void* src, size_t bytes) {
+  if (!bytes) return ND_OK;
+  constexpr size_t kRing = 16u << 20;
+  if (bytes > kRing / 4 || nd_capturing(h)) {
+    ND_CUDA(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    return ND_OK;
   }
-  *out = h->ws;
+  if (!h->up_ring) {
+    ND_CUDA(h, cudaHostAlloc((void**)&h->up_ring, kRing, cudaHostAllocDefault));
+    h->up_cap = kRing;
+    h->up_head = 0;
+  }
+  const size_t len = (bytes + 255) & ~(size_t)255;
+  if (h->up_head + len > h->up_cap) h->up_head = 0;
+  const size_t b = h->up_head, e = b + len;
+  // wait for (and retire) the oldest uploads whose regions this one overwrites
+  while (!h->up_fifo.empty()) {
+    const nd_context::UpRec& r = h->up_fifo.front();
+    if (r.end <= b || r.begin >= e) break;
+    ND_CUDA(h, cudaEventSynchronize(r.ev));
+    h->up_events.push_back(r.ev);
+    h->up_fifo.erase(h->up_fifo.begin());
+  }
+  memcpy(h->up_ring + b, src, bytes);
+  ND_CUDA(h, cudaMemcpyAsync(dst, h->up_ring + b, bytes, cudaMemcpyHostToDevice, h->stream));
+  cudaEvent_t ev;
+  if (!h->up_events.empty()) { ev = h->up_events.back(); h->up_events.pop_back(); }
+  else ND_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  ND_CUDA(h, cudaEventRecord(ev, h->stream));
+  h->up_fifo.push_back(nd_context::UpRec{b, e, ev});
+  h->up_head = e;
   return ND_OK;
 }
 
@@ -128,8 +143,13 @@ nd_status nd_destroy(nd_handle h) {
   nd_dense_cache_clear(h);
   if (h->ws) cudaFree(h->ws);
   if (h->pin) cudaFreeHost(h->pin);
+  if (h->up_ring) cudaFreeHost(h->up_ring);
+  for (auto& r : h->up_fifo) cudaEventDestroy(r.ev);
+  for (auto e : h->up_events) cudaEventDestroy(e);
   if (h->order_ev) cudaEventDestroy(h->order_ev);
   if (h->vec_part) cudaFree(h->vec_part);
+  if (h->plan_stream) { cudaStreamSynchronize(h->plan_stream); cudaStreamDestroy(h->plan_stream); }
+  if (h->d_plan_status) cudaFree(h->d_plan_status);
   if (h->d_status) cudaFree(h->d_status);
   for (auto& r : h->prof) { cudaEventDestroy(r.e0); cudaEventDestroy(r.e1); }
   for (auto e : h->event_pool) cudaEventDestroy(e);

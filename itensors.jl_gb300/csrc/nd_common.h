@@ -63,6 +63,17 @@ struct nd_context {
   size_t pin_size = 0;
   cudaEvent_t order_ev = nullptr;     // orders state used on a previous stream before the current one
   void* vec_part = nullptr;           // per-CTA partial sums of the vector reductions (fixed size)
+  // the one-CTA planner runs on its own stream with its own status word, so building a
+  // plan waits only for the planner, not for contractions queued on the handle's stream
+  cudaStream_t plan_stream = nullptr;
+  DeviceStatus* d_plan_status = nullptr;
+  // pinned ring for descriptor uploads (nd_upload): region [begin, end) may be reused
+  // once its copy's event has completed
+  unsigned char* up_ring = nullptr;
+  size_t up_cap = 0, up_head = 0;
+  struct UpRec { size_t begin, end; cudaEvent_t ev; };
+  std::vector<UpRec> up_fifo;
+  std::vector<cudaEvent_t> up_events;
   // graph capture
   cudaGraph_t graph = nullptr;
   bool capturing = false;
@@ -90,7 +101,10 @@ bool nd_capturing(nd_handle h);
 // Host helpers -------------------------------------------------------------
 nd_status nd_fail(nd_handle h, nd_status code, const char* fmt, ...);
 nd_status nd_cuda_check(nd_handle h, cudaError_t e, const char* what);
-nd_status nd_workspace(nd_handle h, size_t bytes, void** out);
+// Host -> device copy of descriptors on the handle's stream through a pinned ring, so
+// the host never waits for the driver's pageable staging (which blocks once copies
+// queue behind running kernels).  `src` may be reused as soon as the call returns.
+nd_status nd_upload(nd_handle h, void* dst, const void* src, size_t bytes);
 // Device memory for a contraction's execution state: stream-ordered allocations on
 // the handle's stream from the device's default pool, which nd_create keeps from
 // returning freed memory to the system, so rebuilding state per plan costs no

@@ -100,8 +100,7 @@ static nd_status upload(nd_handle h, void** dst, const void* src, size_t bytes) 
   if (*dst) { cudaFreeAsync(*dst, h->stream); *dst = nullptr; }
   nd_status s = nd_dalloc(h, dst, bytes);
   if (s) return s;
-  if (bytes) ND_CUDA(h, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
-  return ND_OK;
+  return nd_upload(h, *dst, src, bytes);
 }
 
 // Work items: tiles of bm x bn over each group, biggest groups first.  Only the
@@ -820,7 +819,7 @@ extern "C" nd_status nd_bs_contract_diag_f64(nd_handle h, nd_plan p, double* R, 
   void* d = nullptr;
   nd_status st = nd_dalloc(h, &d, host.size());
   if (st) return st;
-  ND_CUDA(h, cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, h->stream));
+  if ((st = nd_upload(h, d, host.data(), host.size()))) return st;
   const int grid = (int)std::min<size_t>(items.size(), (size_t)h->num_sms * 8);
   nd_prof_begin(h, "bs_diag_contract");
   bs_diag_contract<<<grid, 256, 0, h->stream>>>((const DiagGroupDesc*)d, (const DiagPairDesc*)((unsigned char*)d + bg),

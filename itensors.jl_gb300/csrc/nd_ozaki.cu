@@ -1277,8 +1277,7 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
   auto up = [&](void** dst, const void* src, size_t bytes) -> nd_status {
     nd_status e = nd_dalloc(h, dst, bytes);
     if (e) return e;
-    if (bytes) ND_CUDA(h, cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
-    return ND_OK;
+    return nd_upload(h, *dst, src, bytes);
   };
   nd_status s;
   if ((s = up((void**)&c.d_split_pairs, L.pairs.data(), L.pairs.size() * sizeof(PairDesc)))) return s;

@@ -399,39 +399,57 @@ nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const Bs
   const size_t o_out = al256(o_tv + (size_t)tsize * 4);
   const size_t r_counts = 0, r_pairs = 32, r_blocks = al256(r_pairs + ncand * 12);
   const size_t r_offs = al256(r_blocks + ncand * rankR * 4), out_bytes = r_offs + ncand * 8;
-  void* ws = nullptr;
-  nd_status s = nd_workspace(h, o_out + out_bytes, &ws);
-  if (s) return s;
-  unsigned char* d = (unsigned char*)ws;
-  if (h->pin_size < std::max(in_bytes, out_bytes)) {
-    if (h->pin) { cudaStreamSynchronize(h->stream); cudaFreeHost(h->pin); h->pin = nullptr; h->pin_size = 0; }
-    const size_t sz = std::max<size_t>(std::max(in_bytes, out_bytes), 1 << 16);
+  if (!h->plan_stream) {
+    ND_CUDA(h, cudaStreamCreateWithFlags(&h->plan_stream, cudaStreamNonBlocking));
+    ND_CUDA(h, cudaMalloc(&h->d_plan_status, sizeof(DeviceStatus)));
+    const DeviceStatus init{0, 0, ND_SPIN_LIMIT, 0};
+    ND_CUDA(h, cudaMemcpy(h->d_plan_status, &init, sizeof(init), cudaMemcpyHostToDevice));
+  }
+  cudaStream_t st = h->plan_stream;
+  // the workspace and the pinned staging buffer belong to the planner alone, and every
+  // plan waits for its own work before returning, so growing them needs no other sync
+  if (o_out + out_bytes > h->ws_size) {
+    if (h->ws) { ND_CUDA(h, cudaFree(h->ws)); h->ws = nullptr; h->ws_size = 0; }
+    const size_t sz = std::max(o_out + out_bytes, h->ws_size * 3 / 2);
+    ND_CUDA(h, cudaMalloc(&h->ws, sz));
+    h->ws_size = sz;
+  }
+  unsigned char* d = (unsigned char*)h->ws;
+  const size_t pin_need = std::max(in_bytes, out_bytes) + sizeof(DeviceStatus);
+  if (h->pin_size < pin_need) {
+    if (h->pin) { cudaFreeHost(h->pin); h->pin = nullptr; h->pin_size = 0; }
+    const size_t sz = std::max<size_t>(pin_need, 1 << 16);
     ND_CUDA(h, cudaHostAlloc(&h->pin, sz, cudaHostAllocDefault));
     h->pin_size = sz;
   }
+  nd_status s = ND_OK;
   unsigned char* hp = (unsigned char*)h->pin;
   if (szA) memcpy(hp + o_A, A.blocks, szA);
   if (szB) memcpy(hp + o_B, B.blocks, szB);
   memcpy(hp + o_rbd, rbd.data(), szR);
-  cudaStream_t st = h->stream;
   ND_CUDA(h, cudaMemcpyAsync(d, hp, in_bytes, cudaMemcpyHostToDevice, st));
   unsigned char* r = d + o_out;
-  nd_prof_begin(h, "plan_one_cta");
   plan_one_cta<<<1, PLAN1_THREADS, 0, st>>>(p, (const int32_t*)(d + o_A), (const int32_t*)(d + o_B),
                                             (const int64_t*)(d + o_rbd), (int32_t*)(r + r_pairs),
                                             (uint64_t*)(d + o_keys), (int32_t*)(d + o_first), (int32_t*)(d + o_bid),
                                             (uint64_t*)(d + o_tk), (int32_t*)(d + o_tv), tsize - 1,
                                             (int32_t*)(r + r_blocks), (int64_t*)(r + r_offs), (int64_t*)(r + r_counts),
-                                            h->d_status);
-  nd_prof_end(h);
+                                            h->d_plan_status);
   ND_LAUNCHED(h);
   ND_CUDA(h, cudaGetLastError());
   // results: in one copy when the bound is small, else the counts first and then exact sizes
   int64_t counts[3];
   const bool one_copy = out_bytes <= (1u << 20);
+  DeviceStatus* hst = (DeviceStatus*)(hp + pin_need - sizeof(DeviceStatus));
   ND_CUDA(h, cudaMemcpyAsync(hp, r, one_copy ? out_bytes : 32, cudaMemcpyDeviceToHost, st));
-  s = nd_check_device_status(h, "block plan");       // synchronises the stream
-  if (s) return s;
+  ND_CUDA(h, cudaMemcpyAsync(hst, h->d_plan_status, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, st));
+  ND_CUDA(h, cudaStreamSynchronize(st));
+  if (hst->code != ND_OK) {
+    const int32_t code = hst->code, where = hst->where;
+    const int32_t z[2] = {0, 0};
+    cudaMemcpy(h->d_plan_status, z, sizeof(z), cudaMemcpyHostToDevice);
+    return nd_fail(h, code, "block plan: device reported error %d at site %d", code, where);
+  }
   memcpy(counts, hp + r_counts, sizeof counts);
   const int64_t npairs = counts[0], nR = counts[1];
   if (!one_copy && npairs > 0) {

@@ -234,16 +234,28 @@ class Handle:
 _handles = {}
 
 
+def _current_stream_ptr(device):
+    import torch
+    raw = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+    if raw is not None:
+        return raw(device)
+    return torch.cuda.current_stream(device).cuda_stream
+
+
 def handle(device: int = 0) -> Handle:
     """Per-device default handle, bound to torch's current CUDA stream."""
-    import torch
-    if not torch.cuda.is_available():
-        raise RuntimeError("ndtensors_gb300 needs a CUDA device (no CPU fallback)")
     h = _handles.get(device)
     if h is None:
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("ndtensors_gb300 needs a CUDA device (no CPU fallback)")
         h = Handle(device)
         _handles[device] = h
-    h.use_stream(torch.cuda.current_stream(device).cuda_stream)
+        h._stream = None
+    s = _current_stream_ptr(device)
+    if s != h._stream:
+        h.use_stream(s)
+        h._stream = s
     return h
 
 

@@ -13,6 +13,8 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
+
 from . import _lib as _libmod
 from ._lib import MAX_RANK, PRECISIONS, BsDesc, handle, i32arr, i64arr
 from .tensors import BlockSparseTensor, DenseTensor, blockoffsets
@@ -100,13 +102,15 @@ class ContractionPlan:
         self.h._check(self.h.lib.nd_bs_plan_sizes(self.ptr, C.byref(npairs), C.byref(nR), C.byref(nnzR)))
         self.npairs, self.nblocksR, self.nnzR = npairs.value, nR.value, nnzR.value
         rank = len(self.lr)
-        br = (C.c_int32 * max(1, self.nblocksR * rank))()
-        of = (C.c_int64 * max(1, self.nblocksR))()
-        pr = (C.c_int32 * max(1, 3 * self.npairs))()
-        self.h._check(self.h.lib.nd_bs_plan_get(self.ptr, br, of, pr))
-        self.blocksR = [tuple(br[i * rank:(i + 1) * rank]) for i in range(self.nblocksR)]
-        self.offsetsR = list(of[:self.nblocksR])
-        self.pairs = [tuple(pr[3 * i:3 * i + 3]) for i in range(self.npairs)]
+        br = np.empty(max(1, self.nblocksR * rank), dtype=np.int32)
+        of = np.empty(max(1, self.nblocksR), dtype=np.int64)
+        self._pairs_raw = np.empty(max(1, 3 * self.npairs), dtype=np.int32)
+        P32, P64 = C.POINTER(C.c_int32), C.POINTER(C.c_int64)
+        self.h._check(self.h.lib.nd_bs_plan_get(self.ptr, br.ctypes.data_as(P32), of.ctypes.data_as(P64),
+                                                self._pairs_raw.ctypes.data_as(P32)))
+        self.blocksR = list(map(tuple, br[:self.nblocksR * rank].reshape(self.nblocksR, rank).tolist()))
+        self.offsetsR = of[:self.nblocksR].tolist()
+        self._pairs = None
         self.indsR = [tuple(T1.inds[self.l1.index(l)]) if l in self.l1 else tuple(T2.inds[self.l2.index(l)])
                       for l in self.lr]
         self.T1_key, self.T2_key = T1.structure_key(), T2.structure_key()
@@ -132,6 +136,13 @@ class ContractionPlan:
                     n *= d
             out.append((m, n, k, ir))
         return out
+
+    @property
+    def pairs(self):
+        """(A block, B block, output block) of every contracted pair, in plan order."""
+        if self._pairs is None:
+            self._pairs = list(map(tuple, self._pairs_raw[:3 * self.npairs].reshape(self.npairs, 3).tolist()))
+        return self._pairs
 
     def set_output_offsets(self, offsets):
         """Write the output blocks at these offsets (a caller's layout, e.g. psi's block

@@ -76,6 +76,7 @@ class BlockSparseTensor:
     offsets: list
     data: object          # torch.float64 CUDA 1-D
     _key: tuple = field(default=None, repr=False)
+    _desc: object = field(default=None, repr=False)
 
     @property
     def rank(self):
@@ -131,14 +132,21 @@ class BlockSparseTensor:
         return self.data[self.offsets[i]:self.offsets[i] + n]
 
     def desc(self):
-        """nd_bs_desc for the C ABI (keeps the ctypes arrays alive on the object)."""
-        from ._lib import BsDesc, i32arr, i64arr
-        nb = i32arr([len(i) for i in self.inds])
-        bd = i64arr([d for i in self.inds for d in i])
-        bl = i32arr([x for b in self.blocks for x in b])
-        of = i64arr(self.offsets)
-        d = BsDesc(self.rank, nb, bd, len(self.blocks), bl, of)
+        """nd_bs_desc for the C ABI (arrays built once per tensor and kept on it)."""
+        import ctypes as C
+        from ._lib import BsDesc
+        cached = getattr(self, "_desc", None)
+        if cached is not None:
+            return cached
+        nb = np.array([len(i) for i in self.inds], dtype=np.int32)
+        bd = np.array([d for i in self.inds for d in i], dtype=np.int64)
+        bl = np.asarray(self.blocks, dtype=np.int32).reshape(-1) if self.blocks else np.zeros(1, np.int32)
+        of = np.asarray(self.offsets, dtype=np.int64) if self.offsets else np.zeros(1, np.int64)
+        P32, P64 = C.POINTER(C.c_int32), C.POINTER(C.c_int64)
+        d = BsDesc(self.rank, nb.ctypes.data_as(P32), bd.ctypes.data_as(P64), len(self.blocks),
+                   bl.ctypes.data_as(P32), of.ctypes.data_as(P64))
         d._keep = (nb, bd, bl, of)
+        self._desc = d
         return d
 
 
