@@ -820,8 +820,104 @@ def cfg_sweep_step(args):
           3, 1)
 
 
+def cfg_sweep_ops(args):
+    """The operations around the contraction in a chi = 4096 sweep step, each timed with CUDA
+    events (median of repetitions, L2 flushed between them): the Krylov vector kernels on the
+    psi-sized vectors (6.0 M doubles, a 11-vector basis), the block plan of each H_eff
+    contraction, the diagonal contraction U * S and the uncombine of U after the truncated
+    SVD, and blockwise eigen on the 19 square blocks of psi's matricisation."""
+    import ctypes as C
+    import torch
+    import ndtensors_gb300 as nd
+    from ndtensors_gb300 import workloads as wl
+    from oracle import blocksparse as obs
+    pk = peaks()
+    h = nd.handle(0)
+    flush = _flush_buffer()
+    reps = max(5, min(args.steps, 20))
+    out = {}
+    net = wl.qn_heff(chi=4096)
+    st = wl.heff_steps()
+    G = {k: nd.BlockSparseTensor.from_host(net[k]) for k in ("L", "psi", "W1", "W2", "R")}
+    n = G["psi"].nnz
+    k = 10
+    dev = torch.device("cuda")
+    V = torch.randn((k + 1, n), dtype=torch.float64, device=dev)
+    w = torch.randn(n, dtype=torch.float64, device=dev)
+    coef = torch.empty(k + 1, dtype=torch.float64, device=dev)
+    P = lambda t: C.c_void_p(t.data_ptr())
+
+    def gbs(nbytes, fn):
+        for _ in range(3):
+            fn()
+        ms = float(np.median(_events_ms(fn, reps, flush)))
+        return {"ms": round(ms, 4), "GB/s": round(nbytes / (ms * 1e-3) / 1e9, 1),
+                "frac_of_hbm": round(nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], 3)}
+
+    out["vec_dots_k10"] = gbs(8 * n * (k + 1), lambda: h.call("nd_vec_dots_f64", n, k, P(V), n, P(w), P(coef)))
+    out["vec_update_k10"] = gbs(8 * n * (k + 2), lambda: h.call("nd_vec_update_f64", n, k, P(V), n, P(coef), -1.0, P(w)))
+    out["vec_norm"] = gbs(8 * n, lambda: h.call("nd_vec_norm_f64", n, P(w), P(coef)))
+    out["vec_scale"] = gbs(16 * n, lambda: h.call("nd_vec_scale_f64", n, P(w), P(V), 1.0, P(coef), 1))
+    # block plans of the four H_eff contractions (device planner; oracle: the sequential loop)
+    x, pl_ms, pl_cpu = G["L"], [], []
+    for (a, b, c), key in zip(st, ("psi", "W1", "W2", "R")):
+        T = G[key]
+        nd.ContractionPlan(x, a, T, b, c).destroy()
+        t0 = time.perf_counter()
+        for _ in range(10):
+            pl = nd.ContractionPlan(x, a, T, b, c)
+            pl.destroy()
+        pl_ms.append(round((time.perf_counter() - t0) * 100, 4))
+        ox = obs.BlockSparseTensor([tuple(i) for i in x.inds], [tuple(bb) for bb in x.blocks], list(x.offsets),
+                                   np.zeros(1))
+        oT = obs.BlockSparseTensor([tuple(i) for i in T.inds], [tuple(bb) for bb in T.blocks], list(T.offsets),
+                                   np.zeros(1))
+        t0 = time.perf_counter()
+        obs.contract_blockoffsets(ox, a, oT, b, c)
+        pl_cpu.append(round((time.perf_counter() - t0) * 1e3, 4))
+        x = nd.contract(x, a, T, b, c, precision="ozaki")
+    out["block_plan_ms"] = {"device_planner_wall_ms": pl_ms, "oracle_sequential_ms": pl_cpu}
+    # truncated SVD of psi's matricisation, then U * S (diagonal contraction) and uncombine
+    sec = net["sectors"]
+    qinds = [(sec, 1), (wl.SPIN_SECTORS, 1), (wl.SPIN_SECTORS, 1), (sec, -1)]
+    M, rinfo, _ = nd.matricize(G["psi"], qinds, (0, 1), (2, 3))
+    U, S, Vt, spec, kept = nd.svd(M, maxdim=4096, cutoff=1e-10)
+    D = nd.DiagBlockSparseTensor.from_diagonals([U.inds[1], U.inds[1]], [(i + 1, i + 1) for i in range(len(S))], S)
+    nd.contract(U, (1, -1), D, (-1, 2))
+    out["diag_contract_US"] = gbs(16 * U.nnz, lambda: nd.contract(U, (1, -1), D, (-1, 2)))
+    out["uncombine_U"] = gbs(16 * U.nnz, lambda: nd.uncombine(U, 0, qinds[:2], rinfo))
+    # blockwise eigen of the 19 symmetric blocks M_b M_b^T (square, up to 1036)
+    rows = [M.inds[0][b[0] - 1] for b in M.blocks]
+    blocks, offs, o, mats = [], [], 0, []
+    host = M.data_numpy()
+    for i, b in enumerate(M.blocks):
+        r_, c_ = M.inds[0][b[0] - 1], M.inds[1][b[1] - 1]
+        m = host[M.offsets[i]:M.offsets[i] + r_ * c_].reshape((r_, c_), order="F")
+        mats.append(m @ m.T)
+        blocks.append((i + 1, i + 1))
+        offs.append(o)
+        o += r_ * r_
+    H = nd.BlockSparseTensor([tuple(rows), tuple(rows)], blocks, offs,
+                             torch.from_numpy(np.concatenate([q.reshape(-1, order="F") for q in mats])).to(dev))
+    nd.eigen(H, maxdim=4096, cutoff=1e-10)
+    e_ms = float(np.median(_events_ms(lambda: nd.eigen(H, maxdim=4096, cutoff=1e-10), 3)))
+    from oracle import linalg as olin
+    t0 = time.perf_counter()
+    olin.eigen_blocks(mats, maxdim=4096, cutoff=1e-10)
+    out["eigen_19_blocks"] = {"ms": round(e_ms, 2), "cpu_oracle_ms": round((time.perf_counter() - t0) * 1e3, 1),
+                              "blocks": len(mats), "largest": max(rows)}
+    _line("sweep-step operations around the contraction (chi=4096): kernel GB/s and times", out["vec_dots_k10"]["GB/s"],
+          "GB/s", True, "sweep_ops_chi4096",
+          {"ops": out, "roofline": {"bound": "hbm", "peak": pk["hbm_gbs"], "unit": "GB/s",
+                                    "peak_source": f"{pk['src']} copy bandwidth"},
+           "l2": "flushed between repetitions (256 MB write)",
+           "cpu_baseline": {"value": out["eigen_19_blocks"]["cpu_oracle_ms"], "unit": "ms (eigen, 19 blocks)",
+                            "cores": cpu_threads(), "kind": "port", "sample": "oracle: numpy eigh per block + truncate!"}},
+          reps, 3)
+
+
 CONFIGS = {"dense_pair": cfg_dense_pair, "permute_sweep": cfg_permute_sweep, "dense_heff": cfg_dense_heff,
-           "qn_pair": cfg_qn_pair, "gradient": cfg_gradient, "sweep_step": cfg_sweep_step}
+           "qn_pair": cfg_qn_pair, "gradient": cfg_gradient, "sweep_step": cfg_sweep_step, "sweep_ops": cfg_sweep_ops}
 
 
 def run_configs(args):

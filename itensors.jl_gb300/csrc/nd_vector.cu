@@ -26,21 +26,39 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // part[b * k + j] = sum over this CTA's slice of x_i * V[j][i], j < k; the slice of
-// CTA b is [b * chunk, (b + 1) * chunk), chunk a multiple of the block size.
+// CTA b is [b * chunk, (b + 1) * chunk), chunk a multiple of VEC_THREADS * U.  Each
+// thread keeps U elements of x and U * k of the basis in flight per iteration (U * KT
+// stays near 32 loads), which is what it takes to cover HBM latency with 2-4 CTAs per SM.
 template <int KT>
 __global__ void __launch_bounds__(VEC_THREADS) vec_dots_part(int64_t n, int k, const double* __restrict__ V,
                                                              int64_t ldv, const double* __restrict__ x,
                                                              int64_t chunk, double* __restrict__ part) {
+  constexpr int U = KT <= 1 ? 8 : KT <= 8 ? 4 : KT <= 16 ? 2 : 1;
   __shared__ double red[VEC_THREADS / 32][KT];
   double acc[KT];
 #pragma unroll
   for (int j = 0; j < KT; ++j) acc[j] = 0.0;
   const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
-  for (int64_t i = i0 + threadIdx.x; i < i1; i += VEC_THREADS) {
-    const double xi = __ldg(x + i);
+  for (int64_t base = i0 + threadIdx.x; base < i1; base += (int64_t)VEC_THREADS * U) {
+    double xv[U];
 #pragma unroll
-    for (int j = 0; j < KT; ++j)
-      if (j < k) acc[j] = fma(__ldg(V + (int64_t)j * ldv + i), xi, acc[j]);
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = base + (int64_t)u * VEC_THREADS;
+      xv[u] = i < i1 ? __ldg(x + i) : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < KT; ++j) {
+      if (j < k) {
+        double vv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int64_t i = base + (int64_t)u * VEC_THREADS;
+          vv[u] = i < i1 ? __ldg(V + (int64_t)j * ldv + i) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc[j] = fma(vv[u], xv[u], acc[j]);
+      }
+    }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -66,16 +84,28 @@ __global__ void vec_dots_final(int k, int nparts, const double* __restrict__ par
   out[j] = root ? sqrt(s) : s;
 }
 
+// Elementwise kernels: each thread handles VEC_U elements VEC_THREADS apart per
+// iteration, loads first, so VEC_U (times the basis size) loads are in flight.
+constexpr int VEC_U = 4;
+
 // y_i += sign * sum_j c_j V[j][i]
 __global__ void __launch_bounds__(VEC_THREADS) vec_update(int64_t n, int k, const double* __restrict__ V, int64_t ldv,
                                                           const double* __restrict__ coef, double sign, double* y) {
   __shared__ double c[VEC_KMAX];
   if (threadIdx.x < k) c[threadIdx.x] = sign * coef[threadIdx.x];
   __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < k; ++j) s = fma(c[j], __ldg(V + (int64_t)j * ldv + i), s);
-    y[i] += s;
+  const int64_t step = (int64_t)gridDim.x * VEC_THREADS * 2;
+  for (int64_t base = (int64_t)blockIdx.x * VEC_THREADS * 2 + threadIdx.x; base < n; base += step) {
+    const int64_t i1 = base + VEC_THREADS;
+    double s0 = 0.0, s1 = 0.0;
+    for (int j = 0; j < k; ++j) {
+      const double* v = V + (int64_t)j * ldv;
+      const double a = __ldg(v + base), b = i1 < n ? __ldg(v + i1) : 0.0;
+      s0 = fma(c[j], a, s0);
+      s1 = fma(c[j], b, s1);
+    }
+    y[base] += s0;
+    if (i1 < n) y[i1] += s1;
   }
 }
 
@@ -84,18 +114,43 @@ __global__ void __launch_bounds__(VEC_THREADS) vec_scale(int64_t n, const double
                                                          const double* s, int invert) {
   double a = alpha;
   if (s) a = invert ? alpha / __ldg(s) : alpha * __ldg(s);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = a * x[i];
+  const int64_t step = (int64_t)gridDim.x * VEC_THREADS * VEC_U;
+  for (int64_t base = (int64_t)blockIdx.x * VEC_THREADS * VEC_U + threadIdx.x; base < n; base += step) {
+    double v[VEC_U];
+#pragma unroll
+    for (int u = 0; u < VEC_U; ++u) {
+      const int64_t i = base + (int64_t)u * VEC_THREADS;
+      v[u] = i < n ? x[i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < VEC_U; ++u) {
+      const int64_t i = base + (int64_t)u * VEC_THREADS;
+      if (i < n) y[i] = a * v[u];
+    }
+  }
 }
 
 // y = beta * y + alpha * x  (beta == 0 overwrites y, so NaN in y does not propagate)
 __global__ void __launch_bounds__(VEC_THREADS) vec_add(int64_t n, const double* x, double* y, double alpha,
                                                        double beta) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = beta == 0.0 ? alpha * x[i] : fma(alpha, x[i], beta * y[i]);
+  const int64_t step = (int64_t)gridDim.x * VEC_THREADS * VEC_U;
+  for (int64_t base = (int64_t)blockIdx.x * VEC_THREADS * VEC_U + threadIdx.x; base < n; base += step) {
+    double xv[VEC_U], yv[VEC_U];
+#pragma unroll
+    for (int u = 0; u < VEC_U; ++u) {
+      const int64_t i = base + (int64_t)u * VEC_THREADS;
+      xv[u] = i < n ? x[i] : 0.0;
+      yv[u] = (i < n && beta != 0.0) ? y[i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < VEC_U; ++u) {
+      const int64_t i = base + (int64_t)u * VEC_THREADS;
+      if (i < n) y[i] = beta == 0.0 ? alpha * xv[u] : fma(alpha, xv[u], beta * yv[u]);
+    }
+  }
 }
 
-int vec_ctas(nd_handle h) { return 2 * h->num_sms; }
+int vec_ctas(nd_handle h) { return 4 * h->num_sms; }
 
 nd_status vec_partials(nd_handle h, double** part) {
   // fixed per-handle buffer: the reductions must not allocate (they are captured in graphs)
@@ -115,8 +170,10 @@ nd_status dots(nd_handle h, int64_t n, int32_t k, const double* V, int64_t ldv, 
   nd_status s = vec_partials(h, &part);
   if (s) return s;
   const int ctas = vec_ctas(h);
+  // chunk: a multiple of VEC_THREADS * 8 (every unroll factor divides it)
+  constexpr int64_t q = VEC_THREADS * 8;
   int64_t chunk = (n + ctas - 1) / ctas;
-  chunk = std::max<int64_t>(VEC_THREADS, (chunk + VEC_THREADS - 1) / VEC_THREADS * VEC_THREADS);
+  chunk = std::max<int64_t>(q, (chunk + q - 1) / q * q);
   nd_prof_begin(h, "vec_dots");
   if (k <= 1) vec_dots_part<1><<<ctas, VEC_THREADS, 0, h->stream>>>(n, k, V, ldv, x, chunk, part);
   else if (k <= 8) vec_dots_part<8><<<ctas, VEC_THREADS, 0, h->stream>>>(n, k, V, ldv, x, chunk, part);
@@ -128,8 +185,9 @@ nd_status dots(nd_handle h, int64_t n, int32_t k, const double* V, int64_t ldv, 
   return nd_cuda_check(h, cudaGetLastError(), name);
 }
 
-int grid_for(nd_handle h, int64_t n) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>((n + VEC_THREADS - 1) / VEC_THREADS, (int64_t)h->num_sms * 8));
+int grid_for(nd_handle h, int64_t n, int per_thread) {
+  const int64_t per_cta = (int64_t)VEC_THREADS * per_thread;
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + per_cta - 1) / per_cta, (int64_t)h->num_sms * 8));
 }
 
 }  // namespace
@@ -157,7 +215,7 @@ extern "C" nd_status nd_vec_update_f64(nd_handle h, int64_t n, int32_t k, const 
   if (!V || !coef || !y || (k > 1 && ldv < n)) return nd_fail(h, ND_ERR_ARG, "vec_update: NULL pointer or ldv < n");
   if (n == 0) return ND_OK;
   nd_prof_begin(h, "vec_update");
-  vec_update<<<grid_for(h, n), VEC_THREADS, 0, h->stream>>>(n, k, V, ldv, coef, sign, y);
+  vec_update<<<grid_for(h, n, 2), VEC_THREADS, 0, h->stream>>>(n, k, V, ldv, coef, sign, y);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "vec_update");
@@ -169,7 +227,7 @@ extern "C" nd_status nd_vec_scale_f64(nd_handle h, int64_t n, const double* x, d
   if (n < 0 || (n && (!x || !y))) return nd_fail(h, ND_ERR_ARG, "vec_scale: NULL pointer");
   if (n == 0) return ND_OK;
   nd_prof_begin(h, "vec_scale");
-  vec_scale<<<grid_for(h, n), VEC_THREADS, 0, h->stream>>>(n, x, y, alpha, s, invert);
+  vec_scale<<<grid_for(h, n, VEC_U), VEC_THREADS, 0, h->stream>>>(n, x, y, alpha, s, invert);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "vec_scale");
@@ -180,7 +238,7 @@ extern "C" nd_status nd_vec_add_f64(nd_handle h, int64_t n, const double* x, dou
   if (n < 0 || (n && (!x || !y))) return nd_fail(h, ND_ERR_ARG, "vec_add: NULL pointer");
   if (n == 0) return ND_OK;
   nd_prof_begin(h, "vec_add");
-  vec_add<<<grid_for(h, n), VEC_THREADS, 0, h->stream>>>(n, x, y, alpha, beta);
+  vec_add<<<grid_for(h, n, VEC_U), VEC_THREADS, 0, h->stream>>>(n, x, y, alpha, beta);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "vec_add");
