@@ -77,6 +77,14 @@ nd_status nd_set_spin_limit(nd_handle h, uint32_t polls);
  * case where the reference's svd returns `nothing`
  * (NDTensors/src/linearalgebra/linearalgebra.jl:91-127). */
 nd_status nd_set_svd_max_sweeps(nd_handle h, int32_t sweeps);
+/* How the last blockwise SVD / eigen on this handle converged (diagnostics; no
+ * counterpart in the reference, whose LAPACK calls report nothing of the kind).
+ * ints (up to nints): [0] FP32 sweeps, [1] refinement steps, [2] FP64 sweeps,
+ * [3] 1 if the sweeps ran on shared-memory panels, [4..] blocks still active at the
+ * start of each FP64 sweep.  dbls (up to ndbls): the largest first-order rotation of
+ * each refinement step, then the largest relative off-diagonal |w_i . w_j| /
+ * (|w_i| |w_j|) rotated in each FP64 sweep, then the same for each FP32 sweep. */
+nd_status nd_svd_last_info(nd_handle h, int32_t* ints, int32_t nints, double* dbls, int32_t ndbls);
 /* Output tile of the split-precision (Ozaki / 3xBF16) GEMM when the autotuner has no
  * entry for a contraction: 0 (default) = 128 x 64 tiles on single CTAs, 1 = 256 x 64
  * tiles on pairs of CTAs (tcgen05.mma.cta_group::2).  With tuning on, both are timed

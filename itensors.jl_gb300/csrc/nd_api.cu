@@ -235,6 +235,13 @@ nd_status nd_set_svd_max_sweeps(nd_handle h, int32_t sweeps) {
   return ND_OK;
 }
 
+nd_status nd_svd_last_info(nd_handle h, int32_t* ints, int32_t nints, double* dbls, int32_t ndbls) {
+  if (!h) return ND_ERR_ARG;
+  for (int32_t k = 0; ints && k < nints; ++k) ints[k] = k < (int32_t)h->svd_info_i.size() ? h->svd_info_i[k] : 0;
+  for (int32_t k = 0; dbls && k < ndbls; ++k) dbls[k] = k < (int32_t)h->svd_info_d.size() ? h->svd_info_d[k] : 0.0;
+  return ND_OK;
+}
+
 nd_status nd_set_split_tile(nd_handle h, int32_t shape) {
   if (!h) return ND_ERR_ARG;
   if (shape != 0 && shape != 1) return nd_fail(h, ND_ERR_ARG, "split tile shape must be 0 (128x64) or 1 (256x64 on CTA pairs)");
@@ -340,9 +347,16 @@ nd_status nd_profile_read(nd_handle h, int32_t cap, char* names, int64_t* counts
   std::vector<std::string> keys;
   std::vector<int64_t> cnt;
   std::vector<double> tot;
-  for (auto& r : h->prof) {
+  // a region still open (its end not recorded) counts zero time
+  std::vector<char> open(h->prof.size(), 0);
+  for (size_t i : h->prof_open) open[i] = 1;
+  for (size_t i = 0; i < h->prof.size(); ++i) {
+    const nd_context::ProfRec& r = h->prof[i];
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, r.e0, r.e1);
+    if (!open[i] && cudaEventElapsedTime(&ms, r.e0, r.e1) != cudaSuccess) {
+      (void)cudaGetLastError();
+      ms = 0.f;
+    }
     size_t k = 0;
     for (; k < keys.size(); ++k) if (keys[k] == r.name) break;
     if (k == keys.size()) { keys.push_back(r.name); cnt.push_back(0); tot.push_back(0.0); }
@@ -352,6 +366,7 @@ nd_status nd_profile_read(nd_handle h, int32_t cap, char* names, int64_t* counts
     h->event_pool.push_back(r.e1);
   }
   h->prof.clear();
+  h->prof_open.clear();
   int n = (int)keys.size();
   for (int k = 0; k < n && k < cap; ++k) {
     if (names) { strncpy(names + 64 * k, keys[k].c_str(), 63); names[64 * k + 63] = 0; }
@@ -405,12 +420,14 @@ void nd_prof_begin(nd_handle h, const char* name) {
   };
   nd_context::ProfRec r{name, get(), get()};
   cudaEventRecord(r.e0, h->stream);
+  h->prof_open.push_back(h->prof.size());
   h->prof.push_back(r);
 }
 
 void nd_prof_end(nd_handle h) {
-  if (!h->profiling || nd_capturing(h) || h->prof.empty()) return;
-  cudaEventRecord(h->prof.back().e1, h->stream);
+  if (!h->profiling || nd_capturing(h) || h->prof_open.empty()) return;
+  cudaEventRecord(h->prof[h->prof_open.back()].e1, h->stream);
+  h->prof_open.pop_back();
 }
 
 

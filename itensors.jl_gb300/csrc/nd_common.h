@@ -52,6 +52,9 @@ struct nd_context {
   int num_sms = 0;
   int ozaki_slices = 5;
   int svd_max_sweeps = -1;            // FP64 Jacobi sweep limit of the SVD (-1 = default 60)
+  // convergence record of the last SVD (nd_svd_last_info)
+  std::vector<int32_t> svd_info_i;
+  std::vector<double> svd_info_d;
   int split_pair2 = 0;                // untuned split-GEMM tile shape (TuneChoice::pair2)
   std::string last_error;
   DeviceStatus* d_status = nullptr;   // device status word
@@ -81,6 +84,7 @@ struct nd_context {
   bool profiling = false;
   struct ProfRec { const char* name; cudaEvent_t e0, e1; };
   std::vector<ProfRec> prof;
+  std::vector<size_t> prof_open;   // indices of the regions begun and not yet ended (regions nest)
   std::vector<cudaEvent_t> event_pool;
   // autotuner
   bool tuning = false;

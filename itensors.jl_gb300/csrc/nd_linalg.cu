@@ -10,23 +10,32 @@
 //                                         NDTensors/src/linearalgebra/linearalgebra.jl:321-381
 //
 // SVD algorithm: one-sided (Hestenes) Jacobi on the columns of every block at
-// once (transposed when a block is wide).  Column pairs follow a round-robin
-// tournament, so the n/2 rotations of a round are independent; all blocks
-// advance round by round inside one persistent cooperative kernel (one warp per
-// pair) whose CTAs meet at a grid barrier (bounded spin) between rounds.  Each
-// sweep records the largest |a_i . a_j| / (|a_i| |a_j|) per block; blocks whose
-// sweep rotated nothing are done, and the host reports ND_ERR_NOCONV after the
-// sweep limit (the reference returns `nothing` when LAPACK fails).  Larger
-// problems first run the sweeps in FP32 and re-orthogonalise that V in FP64
-// (Newton-Schulz), then finish with FP64 sweeps on W V, so the result is an
-// FP64 Jacobi SVD.
+// once (transposed when a block is wide).  Column groups of B follow a round-robin
+// tournament; one CTA rotates the pairs of a group pair inside shared memory
+// (bj_sweep), and all blocks advance round by round inside one persistent
+// cooperative kernel whose CTAs meet at a grid barrier (bounded spin) between
+// rounds (blocks too tall for a shared-memory panel use the scalar sweep,
+// svd_sweep: one warp per column pair, columns in global memory).  Each sweep
+// records the largest |a_i . a_j| / (|a_i| |a_j|) per block; blocks whose sweep
+// rotated nothing are done, and the host reports ND_ERR_NOCONV after the sweep
+// limit (the reference returns `nothing` when LAPACK fails).  Larger problems first
+// run the sweeps in FP32, refine that V to FP64 accuracy with split GEMMs on the
+// tensor cores (Ogita-Aishima refinement), then finish with FP64 sweeps on W V, so
+// the result is an FP64 Jacobi SVD.
 #include "nd_plan.h"
 #include <cooperative_groups.h>
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 
 namespace {
+
+inline double bits_to_double(unsigned long long u) {
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+}
 
 struct SvdBlock {
   int64_t a_off;     // offset of the block in A (column-major m x n, original orientation)
@@ -167,8 +176,8 @@ __device__ __forceinline__ void rotate_batched(T* xp, T* yp, int n, int lane, T 
 #pragma unroll
     for (int u = 0; u < CH; ++u) {
       const int i = base + 32 * u;
-      x[u] = i < n ? xp[i] : T(0);
-      y[u] = i < n ? yp[i] : T(0);
+      x[u] = i < n ? __ldcg(xp + i) : T(0);
+      y[u] = i < n ? __ldcg(yp + i) : T(0);
     }
 #pragma unroll
     for (int u = 0; u < CH; ++u) {
@@ -210,14 +219,14 @@ __global__ void __launch_bounds__(512, 2) svd_sweep(SweepArgs<T> a) {
 #pragma unroll
         for (int u = 0; u < CH; ++u) {
           const int i = base + 32 * u;
-          x[u] = i < b.mm ? wp[i] : T(0);
-          y[u] = i < b.mm ? wq[i] : T(0);
+          x[u] = i < b.mm ? __ldcg(wp + i) : T(0);   // L2: other CTAs rotate these columns too
+          y[u] = i < b.mm ? __ldcg(wq + i) : T(0);
         }
 #pragma unroll
         for (int u = 0; u < CH; ++u) ga = fma(x[u], y[u], ga);
       }
       ga = warp_sum(ga);
-      const T al = a.nrm[b.s_off + p], be = a.nrm[b.s_off + q];
+      const T al = __ldcg(a.nrm + b.s_off + p), be = __ldcg(a.nrm + b.s_off + q);
       const T nrm = sqrt(al) * sqrt(be);
       double rel = nrm > T(0) ? (double)(fabs(ga) / nrm) : 0.0;
       const double tolb = a.tol * (double)b.mm;        // m * unit roundoff, as one-sided Jacobi codes use
@@ -266,16 +275,6 @@ __global__ void to_f32_scaled(const SvdBlock* blocks, const double* W, const uns
   const int64_t tv = (int64_t)b.nn * b.nn;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tv; e += (int64_t)gridDim.x * blockDim.x)
     V32[b.v_off + e] = (e % b.nn == e / b.nn) ? 1.0f : 0.0f;
-}
-
-// V = double(V32), and Y = I (the accumulator of I - V^T V), per block.
-__global__ void to_f64_and_identity(const SvdBlock* blocks, const float* V32, double* V, double* Y) {
-  const SvdBlock b = blocks[blockIdx.y];
-  const int64_t tv = (int64_t)b.nn * b.nn;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tv; e += (int64_t)gridDim.x * blockDim.x) {
-    V[b.v_off + e] = (double)V32[b.v_off + e];
-    Y[b.v_off + e] = (e % b.nn == e / b.nn) ? 1.0 : 0.0;
-  }
 }
 
 // sigma_j = |w_j|, then per-block descending order (rank by comparison; ties by index)
@@ -541,6 +540,297 @@ __global__ void set_identity(const SvdBlock* blocks, double* Y) {
     Y[b.v_off + e] = (e % b.nn == e / b.nn) ? 1.0 : 0.0;
 }
 
+// ---- panel Jacobi: column groups of B resident in shared memory -------------------
+// The columns of a block are cut into groups of B.  A round-robin tournament over the
+// groups pairs them; one CTA loads the 2B columns of a group pair (its "panel") into
+// shared memory and rotates every cross pair (p in the first group, q in the second)
+// there, B rounds of B independent pairs, one warp per pair.  In the first round of a
+// sweep every group also rotates its own pairs (B - 1 rounds), so each column pair is
+// visited once per sweep, as in the cyclic scalar sweep.  The CTA accumulates the
+// panel's rotations in a 2B x 2B matrix Q and, if anything rotated, writes the panel
+// back and applies V[:, panel] <- V[:, panel] Q.  A sweep is one cooperative launch
+// with a grid barrier per tournament round: (#groups - 1) rounds instead of
+// (#columns - 1).
+struct BjTask {
+  int32_t block;     // block index
+  int32_t k;         // pair index within the block's tournament round
+};
+
+template <typename T>
+struct BjArgs {
+  const SvdBlock* blocks;
+  const BjTask* tasks;
+  int ntasks;
+  int nrounds;       // max over the listed blocks of (#groups rounded up to even) - 1
+  int ldp;           // leading dimension of the shared-memory panel (>= every listed mm)
+  T* W;
+  T* V;
+  unsigned long long* offmax;
+  unsigned int* bar_count;
+  unsigned int* bar_gen;
+  DeviceStatus* st;
+  double tol;        // pairs with |w_p . w_q| <= tol * mm^tol_pow |w_p||w_q| are left
+  double tol_pow;
+};
+
+// 16-byte vectors of the panel element type: a lane handles VW consecutive rows.
+template <typename T> struct PanVec;
+template <> struct PanVec<float> { using type = float4; static constexpr int W = 4; };
+template <> struct PanVec<double> { using type = double2; static constexpr int W = 2; };
+
+__device__ __forceinline__ void vdot(const float4& a, const float4& b, float& g0, float& g1) {
+  g0 = fmaf(a.x, b.x, g0); g1 = fmaf(a.y, b.y, g1); g0 = fmaf(a.z, b.z, g0); g1 = fmaf(a.w, b.w, g1);
+}
+__device__ __forceinline__ void vdot(const double2& a, const double2& b, double& g0, double& g1) {
+  g0 = fma(a.x, b.x, g0); g1 = fma(a.y, b.y, g1);
+}
+__device__ __forceinline__ void vrot(float4& x, float4& y, float c, float s) {
+  const float4 a = x, b = y;
+  x = make_float4(c * a.x - s * b.x, c * a.y - s * b.y, c * a.z - s * b.z, c * a.w - s * b.w);
+  y = make_float4(s * a.x + c * b.x, s * a.y + c * b.y, s * a.z + c * b.z, s * a.w + c * b.w);
+}
+__device__ __forceinline__ void vrot(double2& x, double2& y, double c, double s) {
+  const double2 a = x, b = y;
+  x = make_double2(c * a.x - s * b.x, c * a.y - s * b.y);
+  y = make_double2(s * a.x + c * b.x, s * a.y + c * b.y);
+}
+
+// One warp: Jacobi rotation of panel columns p and q (rotation accumulated into Q).
+// nv = rows / VW, the panel's rows padded with zeros to a whole vector.
+template <typename T, int P2>
+__device__ __forceinline__ void bj_pair(T* pan, int ldp, T* q, T* d, const int* cols, int p, int qq, int nv,
+                                        double tolb, int lane, int* any, unsigned long long* offmax) {
+  using VT = typename PanVec<T>::type;
+  if (cols[p] < 0 || cols[qq] < 0) return;
+  VT* xp = reinterpret_cast<VT*>(pan + (size_t)p * ldp);
+  VT* xq = reinterpret_cast<VT*>(pan + (size_t)qq * ldp);
+  T g0 = 0, g1 = 0, g2 = 0, g3 = 0;
+  int i = lane;
+  for (; i + 32 < nv; i += 64) {
+    vdot(xp[i], xq[i], g0, g1);
+    vdot(xp[i + 32], xq[i + 32], g2, g3);
+  }
+  if (i < nv) vdot(xp[i], xq[i], g0, g1);
+  const T g = warp_sum((g0 + g2) + (g1 + g3));
+  const T al = d[p], be = d[qq];
+  const T nrm = sqrt(al) * sqrt(be);
+  const double rel = nrm > T(0) ? (double)(fabs(g) / nrm) : 0.0;
+  if (!(rel > tolb) || g == T(0)) return;
+  const T zeta = (be - al) / (T(2) * g);
+  const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+  const T c = T(1) / sqrt(T(1) + tt * tt);
+  const T sn = c * tt;
+  for (int j = lane; j < nv; j += 32) {
+    VT x = xp[j], y = xq[j];
+    vrot(x, y, c, sn);
+    xp[j] = x;
+    xq[j] = y;
+  }
+  if (lane < P2) {
+    const T a = q[p * P2 + lane], b = q[qq * P2 + lane];
+    q[p * P2 + lane] = c * a - sn * b;
+    q[qq * P2 + lane] = sn * a + c * b;
+  }
+  if (lane == 0) {
+    d[p] = al - tt * g;
+    d[qq] = be + tt * g;
+    *any = 1;
+    atomicMax(offmax, (unsigned long long)__double_as_longlong(rel));
+  }
+}
+
+template <typename T, int B>
+__global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
+  constexpr int P2 = 2 * B;
+  extern __shared__ __align__(16) unsigned char bj_smem[];
+  T* pan = reinterpret_cast<T*>(bj_smem);            // P2 columns of ldp
+  T* q = pan + (size_t)P2 * a.ldp;                   // P2 x P2, column-major
+  T* d = q + P2 * P2;                                // |w_c|^2 of the panel columns
+  __shared__ int s_cols[P2];                         // column index in the block, -1 if none
+  __shared__ int s_any;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int r = 0; r < a.nrounds; ++r) {
+    // tasks are listed longest first; CTA i takes positions i, 2G-1-i, 2G+i, ... (a snake),
+    // so the CTAs with the longest first task get the shortest second one
+    for (int w = 0;; ++w) {
+      const int t = w * (int)gridDim.x + ((w & 1) ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x);
+      if (t >= a.ntasks) break;
+      const BjTask tk = a.tasks[t];
+      const SvdBlock b = a.blocks[tk.block];
+      const int nblk = (b.nn + B - 1) / B, nbp = nblk + (nblk & 1);
+      if (r >= nbp - 1) continue;
+      int gp, gq;
+      rr_pair(nbp, r, tk.k, gp, gq);
+      const bool rp = gp < nblk, rq = gq < nblk;
+      if (!rp && !rq) continue;
+      const bool lone = !(rp && rq);
+      if (lone && r != 0) continue;                   // a group without a partner only has its own pairs
+      const int mm = b.mm;
+      constexpr int VW = PanVec<T>::W;
+      const int mmv = (mm + VW - 1) / VW * VW;         // rows padded to whole vectors (zeros)
+      const double tolb = a.tol * (a.tol_pow == 1.0 ? (double)mm : pow((double)mm, a.tol_pow));
+      if (threadIdx.x < P2) {
+        const int g = threadIdx.x < B ? gp : gq;
+        const int col = g * B + (threadIdx.x < B ? threadIdx.x : threadIdx.x - B);
+        s_cols[threadIdx.x] = (g < nblk && col < b.nn) ? col : -1;
+      }
+      if (threadIdx.x == 0) s_any = 0;
+      for (int e = threadIdx.x; e < P2 * P2; e += blockDim.x) q[e] = (e % P2 == e / P2) ? T(1) : T(0);
+      __syncthreads();
+      for (int c = warp; c < P2; c += B) {
+        const int col = s_cols[c];
+        T* dst = pan + (size_t)c * a.ldp;
+        T acc = 0;
+        if (col >= 0) {
+          const T* src = a.W + b.w_off + (int64_t)col * mm;
+          for (int i = lane; i < mmv; i += 32) {
+            const T x = i < mm ? __ldcg(src + i) : T(0);   // L2: other CTAs rotated this column earlier
+            dst[i] = x;
+            acc = fma(x, x, acc);
+          }
+        } else {
+          for (int i = lane; i < mmv; i += 32) dst[i] = T(0);
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) d[c] = acc;
+      }
+      __syncthreads();
+      if (r == 0) {
+        // each group's own pairs: a round-robin over its B columns, both groups at once
+        for (int sr = 0; sr < B - 1; ++sr) {
+          int p, qq;
+          rr_pair(B, sr, warp % (B / 2), p, qq);
+          if (warp >= B / 2) { p += B; qq += B; }
+          bj_pair<T, P2>(pan, a.ldp, q, d, s_cols, p, qq, mmv / VW, tolb, lane, &s_any, &a.offmax[tk.block]);
+          __syncthreads();
+        }
+      }
+      if (!lone) {
+        for (int sr = 0; sr < B; ++sr) {
+          bj_pair<T, P2>(pan, a.ldp, q, d, s_cols, warp, B + (warp + sr) % B, mmv / VW, tolb, lane, &s_any,
+                         &a.offmax[tk.block]);
+          __syncthreads();
+        }
+      }
+      if (s_any) {
+        for (int c = warp; c < P2; c += B) {
+          const int col = s_cols[c];
+          if (col < 0) continue;
+          T* dst = a.W + b.w_off + (int64_t)col * mm;
+          const T* src = pan + (size_t)c * a.ldp;
+          for (int i = lane; i < mm; i += 32) dst[i] = src[i];
+        }
+        // V[:, panel] <- V[:, panel] Q, one row per thread (coalesced along each column)
+        const int nn = b.nn;
+        T* Vb = a.V + b.v_off;
+        for (int i = threadIdx.x; i < nn; i += blockDim.x) {
+          T v[P2];
+#pragma unroll
+          for (int c = 0; c < P2; ++c) v[c] = s_cols[c] >= 0 ? __ldcg(Vb + (int64_t)s_cols[c] * nn + i) : T(0);
+#pragma unroll
+          for (int c2 = 0; c2 < P2; ++c2) {
+            if (s_cols[c2] < 0) continue;
+            using VT = typename PanVec<T>::type;
+            const VT* qc = reinterpret_cast<const VT*>(q + c2 * P2);
+            T acc0 = 0, acc1 = 0;
+#pragma unroll
+            for (int c = 0; c < P2 / VW; ++c) {
+              if constexpr (VW == 4)
+                vdot(make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]), qc[c], acc0, acc1);
+              else
+                vdot(make_double2(v[2 * c], v[2 * c + 1]), qc[c], acc0, acc1);
+            }
+            Vb[(int64_t)s_cols[c2] * nn + i] = acc0 + acc1;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (!grid_barrier(a.bar_count, a.bar_gen, gridDim.x, a.st)) return;
+  }
+}
+
+// ---- mixed-precision refinement of the right singular vectors --------------------
+// Ogita and Aishima, "Iterative refinement for symmetric eigenvalue decomposition"
+// (Japan J. Indust. Appl. Math. 35, 2018), applied to W^T W without forming it:
+// with X the current V, R = I - X^T X and S = (W X)^T (W X),
+//   lambda_i = S_ii / (1 - R_ii),
+//   E_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i)   (a separated pair),
+//   E_ij = R_ij / 2                                         (diagonal, or a close pair),
+// and X <- X + X E.  A pair counts as separated when the size of its first-order
+// rotation |S_ij + (lambda_i + lambda_j) R_ij / 2| / |lambda_j - lambda_i| is at most
+// tau (decided on the unordered pair, so E_ij + E_ji = R_ij still holds); close pairs
+// are left to the FP64 Jacobi sweep that follows.  tau < 0 rotates nothing: a
+// Newton-Schulz step X <- X + X (I - X^T X) / 2.  A step rotates by first-order
+// angles and orthogonalises to first order, so it leaves X non-orthogonal by the
+// square of its largest |E_ij|.  The steps run as split GEMMs on the tensor cores
+// (which resolve a product to about 2^-38 of its largest terms) until the rotations
+// fall below 1e-10; then a step whose R, W X and S are FP64 GEMMs brings X to FP64
+// accuracy, and, if that step's E was not tiny, a Newton-Schulz step with an FP64 R
+// restores orthogonality.  In those steps E is small, so X E and (W X) E stay split
+// GEMMs.  This kernel is the O(n^2) FP64 part.  E overwrites R.
+#ifndef ND_SVD_TAU_FP64
+#define ND_SVD_TAU_FP64 3e-8
+#endif
+#ifndef ND_SVD_EXACT_STEP
+#define ND_SVD_EXACT_STEP 1
+#endif
+// FP32 sweeps leave a pair when |w_p . w_q| <= ND_SVD_TOL32 * mm^ND_SVD_TOL32_POW |w_p||w_q|:
+// 4 u sqrt(mm) (u = 2^-24), about the rounding level of an FP32 dot product of mm terms.
+#ifndef ND_SVD_TOL32
+#define ND_SVD_TOL32 2.4e-7
+#endif
+#ifndef ND_SVD_TOL32_POW
+#define ND_SVD_TOL32_POW 0.5
+#endif
+constexpr double OA_TAU = 1e-2;                   // split-GEMM steps
+constexpr double OA_TAU_FP64 = ND_SVD_TAU_FP64;   // FP64 steps: only the small corrections left at that point
+
+// emax[0]: largest first-order rotation applied; emax[1]: largest |E_ij| of any entry.
+__global__ void oa_correction(const SvdBlock* blocks, const double* S, double* RE, double tau, unsigned long long* emax) {
+  const SvdBlock b = blocks[blockIdx.y];
+  const int n = b.nn;
+  const double* Sb = S + b.v_off;
+  double* Rb = RE + b.v_off;
+  const int64_t tot = (int64_t)n * n;
+  double m = 0.0, ma = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    if (i > j) continue;                       // the thread of the upper entry writes both
+    if (i == j) { Rb[e] = 0.5 * Rb[e]; ma = fmax(ma, fabs(Rb[e])); continue; }
+    const int64_t et = (int64_t)i * n + j;     // (j, i)
+    const double rij = Rb[e];
+    const double li = Sb[(int64_t)i * n + i] / (1.0 - Rb[(int64_t)i * n + i]);
+    const double lj = Sb[(int64_t)j * n + j] / (1.0 - Rb[(int64_t)j * n + j]);
+    const double sij = 0.5 * (Sb[e] + Sb[et]);
+    const double den = lj - li;
+    const double mid = sij + 0.5 * (li + lj) * rij;
+    double eij = 0.5 * rij, eji = 0.5 * rij;
+    if (den != 0.0 && fabs(mid) <= tau * fabs(den)) {
+      eij = (sij + lj * rij) / den;
+      eji = rij - eij;
+      m = fmax(m, fabs(mid / den));
+    }
+    Rb[e] = eij;                               // E(i, j): column j of X gains E_ij x_i
+    Rb[et] = eji;
+    ma = fmax(ma, fmax(fabs(eij), fabs(eji)));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    ma = fmax(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+  }
+  if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(emax, (unsigned long long)__double_as_longlong(m));
+  if ((threadIdx.x & 31) == 0 && ma > 0.0) atomicMax(emax + 1, (unsigned long long)__double_as_longlong(ma));
+}
+
+// FP32 -> FP64 copy of V, per block
+__global__ void v_to_f64(const SvdBlock* blocks, const float* V32, double* V) {
+  const SvdBlock b = blocks[blockIdx.y];
+  const int64_t tv = (int64_t)b.nn * b.nn;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tv; e += (int64_t)gridDim.x * blockDim.x)
+    V[b.v_off + e] = (double)V32[b.v_off + e];
+}
+
 // ---- blockwise Hermitian eigen -------------------------------------------------
 // A_b + c_b I with c_b = 1.01 ||A_b||_F (1 for a zero block) is positive definite, so
 // its one-sided Jacobi SVD gives the eigenvectors of A_b (left = right singular
@@ -651,6 +941,119 @@ static nd_status run_sweeps(nd_handle h, const SvdBlock* dblk, int nb, int task0
   return st;
 }
 
+// Panel-Jacobi sweeps (bj_sweep) of element type T on (Wt, Vt).  Returns
+// ND_ERR_UNSUPPORTED without launching anything when the tallest block does not fit a
+// panel in shared memory (the caller then uses the scalar sweeps).
+template <typename T, int B>
+static nd_status launch_bj(nd_handle h, const BjArgs<T>& a, size_t smem) {
+  static size_t attr = 0;   // dynamic shared memory this instantiation is opted in to
+  if (smem > attr) {
+    nd_status st = nd_cuda_check(h, cudaFuncSetAttribute(bj_sweep<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         (int)smem), "svd panel sweep shared memory");
+    if (st) return st;
+    attr = smem;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bj_sweep<T, B>, 32 * B, smem);
+  if (per_sm < 1) return nd_fail(h, ND_ERR_UNSUPPORTED, "svd panel sweep does not fit an SM");
+  const int grid = std::max(1, std::min(a.ntasks, per_sm * h->num_sms));
+  BjArgs<T> args = a;
+  void* kargs[] = {&args};
+  return nd_cuda_check(h, cudaLaunchCooperativeKernel((void*)bj_sweep<T, B>, grid, 32 * B, kargs, smem, h->stream),
+                       "svd panel sweep (cooperative launch)");
+}
+
+// Widest column group B whose panel (2B columns of ldp) stays within ~200 KB of shared
+// memory; 0 when even the narrowest does not fit.
+template <typename T>
+static int panel_group(int ldp) {
+  ldp = (ldp + 3) / 4 * 4;
+  const size_t budget = 200 * 1024;
+  int B = sizeof(T) == 4 ? 16 : 8;
+  const int bmin = sizeof(T) == 4 ? 4 : 2;
+  while (B >= bmin && (size_t)2 * B * ldp * sizeof(T) > budget) B >>= 1;
+  return B >= bmin ? B : 0;
+}
+
+template <typename T>
+static nd_status run_panel_sweeps(nd_handle h, const std::vector<SvdBlock>& blocks, const SvdBlock* dblk, T* Wt,
+                                  T* Vt, unsigned long long* offmax, unsigned int* bar, double tol, int max_sweeps,
+                                  bool& converged, int& sweeps, std::vector<int32_t>* act_hist = nullptr,
+                                  std::vector<double>* off_hist = nullptr, double tol_pow = 1.0) {
+  cudaStream_t s = h->stream;
+  const int nb = (int)blocks.size();
+  sweeps = 0;
+  converged = false;
+  int ldp = 1;
+  for (auto& b : blocks) ldp = std::max(ldp, b.mm);
+  ldp = (ldp + 3) / 4 * 4;                  // whole 16-byte vectors per panel column
+  const int B = panel_group<T>(ldp);
+  if (!B) return ND_ERR_UNSUPPORTED;
+  const size_t smem = ((size_t)2 * B * ldp + (size_t)4 * B * B + 2 * B) * sizeof(T);
+  std::vector<unsigned long long> om(nb);
+  std::vector<int32_t> act(nb, 1);
+  // longest tasks first: blocks in decreasing mm * nn
+  std::vector<int> ord(nb);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+    return (int64_t)blocks[x].mm * blocks[x].nn > (int64_t)blocks[y].mm * blocks[y].nn;
+  });
+  int maxtasks = 0;
+  for (auto& b : blocks) { const int g = (b.nn + B - 1) / B; maxtasks += (g + (g & 1)) / 2; }
+  BjTask* dtasks = nullptr;
+  nd_status st = nd_dalloc(h, (void**)&dtasks, std::max(maxtasks, 1) * sizeof(BjTask));
+  if (st) return st;
+  std::vector<BjTask> tasks;
+  const char* name = sizeof(T) == 4 ? "svd_panel_sweep_f32" : "svd_panel_sweep";
+  for (int sw = 0; sw < max_sweeps; ++sw) {
+    tasks.clear();
+    int nrounds = 0;
+    for (int bi : ord) {
+      if (!act[bi]) continue;
+      const int g = (blocks[bi].nn + B - 1) / B, gp = g + (g & 1);
+      for (int k = 0; k < gp / 2; ++k) tasks.push_back(BjTask{bi, k});
+      nrounds = std::max(nrounds, gp - 1);
+    }
+    if (tasks.empty()) { converged = true; break; }
+    if (act_hist) act_hist->push_back((int32_t)std::count(act.begin(), act.end(), 1));
+    if ((st = nd_upload(h, dtasks, tasks.data(), tasks.size() * sizeof(BjTask)))) break;
+    if ((st = nd_cuda_check(h, cudaMemsetAsync(offmax, 0, nb * 8, s), "svd sweep set-up"))) break;
+    BjArgs<T> a{dblk, dtasks, (int)tasks.size(), nrounds, ldp, Wt, Vt, offmax, bar, bar + 1, h->d_status, tol, tol_pow};
+    nd_prof_begin(h, name);
+    if constexpr (sizeof(T) == 4) {
+      if (B == 16) st = launch_bj<T, 16>(h, a, smem);
+      else if (B == 8) st = launch_bj<T, 8>(h, a, smem);
+      else st = launch_bj<T, 4>(h, a, smem);
+    } else {
+      if (B == 8) st = launch_bj<T, 8>(h, a, smem);
+      else if (B == 4) st = launch_bj<T, 4>(h, a, smem);
+      else st = launch_bj<T, 2>(h, a, smem);
+    }
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    if (st) break;
+    cudaError_t e = cudaMemcpyAsync(om.data(), offmax, nb * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { st = nd_cuda_check(h, e, "svd panel sweep"); break; }
+    ++sweeps;
+    if ((st = nd_check_device_status(h, "svd"))) break;
+    if (off_hist) {
+      double m = 0.0;
+      for (int i = 0; i < nb; ++i) if (act[i]) m = std::max(m, bits_to_double(om[i]));
+      off_hist->push_back(m);
+    }
+    // a sweep without any rotation above mm * unit roundoff leaves its block converged
+    bool any = false;
+    for (int i = 0; i < nb; ++i) {
+      if (act[i] && om[i] == 0ull) act[i] = 0;
+      any = any || act[i];
+    }
+    if (!any) { converged = true; break; }
+  }
+  cudaFreeAsync(dtasks, s);
+  return st;
+}
+
 static Mixed mixed1(int64_t dim, int64_t st0, int64_t st1) {
   Mixed m{};
   m.n = 1;
@@ -661,32 +1064,34 @@ static Mixed mixed1(int64_t dim, int64_t st0, int64_t st1) {
   return m;
 }
 
-// R = alpha * op(A) * B + beta * R for every block in one grouped FP64 launch.
+// R = alpha * op(A) * B + beta * R for every block in one grouped launch of the given
+// precision (c: the launch state, reused while the blocks stay the same).
 //   kind 0: Y  (nn x nn) = alpha * V^T V + beta * Y
 //   kind 1: Vn (nn x nn) = alpha * V Y   + beta * Vn
 //   kind 2: W0 (mm x nn) = alpha * W Q   + beta * W0
-static nd_status block_gemm(nd_handle h, const std::vector<SvdBlock>& blocks, int kind, const double* A,
-                            const double* B, double* R, double alpha, double beta) {
+//   kind 3: S  (nn x nn) = alpha * W^T W + beta * S
+static nd_status block_gemm(nd_handle h, ExecCache& c, const std::vector<SvdBlock>& blocks, int kind, const double* A,
+                            const double* B, double* R, double alpha, double beta, int precision) {
   std::vector<PairDesc> pairs(blocks.size());
   for (size_t i = 0; i < blocks.size(); ++i) {
     const SvdBlock& b = blocks[i];
     PairDesc pd{};
-    const int64_t M = kind == 2 ? b.mm : b.nn, N = b.nn, K = b.nn;
+    const int64_t M = kind == 2 ? b.mm : b.nn, N = b.nn, K = kind == 3 ? b.mm : b.nn;
     pd.M = (int32_t)M; pd.N = (int32_t)N; pd.K = (int32_t)K;
     pd.group = (int32_t)i; pd.first = 1; pd.job = 0;
-    pd.a_off = kind == 2 ? b.w_off : b.v_off;
-    pd.b_off = b.v_off;
+    pd.a_off = (kind == 2 || kind == 3) ? b.w_off : b.v_off;
+    pd.b_off = kind == 3 ? b.w_off : b.v_off;
     pd.r_off = kind == 2 ? b.w_off : b.v_off;
-    pd.rows = mixed1(M, kind == 0 ? b.nn : 1, 1);    // A row stride, R row stride
-    pd.cols = mixed1(N, b.nn, M);                    // B column stride, R column stride
-    pd.ks = mixed1(K, kind == 0 ? 1 : M, 1);         // A k stride, B k stride
+    const int64_t a_row = kind == 0 ? b.nn : kind == 3 ? b.mm : 1;   // A(i, k) = A[i * a_row + k * a_k]
+    const int64_t a_k = (kind == 0 || kind == 3) ? 1 : M;
+    const int64_t b_col = kind == 3 ? b.mm : b.nn;                    // B(k, j) = B[k + j * b_col]
+    pd.rows = mixed1(M, a_row, 1);                   // A row stride, R row stride
+    pd.cols = mixed1(N, b_col, M);                   // B column stride, R column stride
+    pd.ks = mixed1(K, a_k, 1);                       // A k stride, B k stride
     pairs[i] = pd;
   }
-  ExecCache c;
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
-  nd_status st = nd_execute_cached(h, c, pairs, (int)blocks.size(), ptrs, alpha, beta, ND_PREC_FP64);
-  c.free_all(h);
-  return st;
+  return nd_execute_cached(h, c, pairs, (int)blocks.size(), ptrs, alpha, beta, precision);
 }
 
 static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_t* cols, const int64_t* offsets,
@@ -736,12 +1141,16 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
     nd_prof_end(h);
     ND_LAUNCHED(h);
   }
-  // Preconditioner for the larger problems: the same Jacobi sweeps in FP32 on a
-  // power-of-two scaled copy (the FP32 pipe is ~64x the FP64 one), its V
-  // re-orthogonalised in FP64 by two Newton-Schulz steps V <- V + V (I - V^T V) / 2
-  // (quadratic: 1e-6 -> 1e-12 -> roundoff), then W0 = W Q.  The FP64 sweeps that
-  // follow start nearly orthogonal and converge in a few sweeps; the result is
-  // the FP64 one-sided Jacobi SVD of W0, so accuracy is unchanged.
+  // Larger problems run in three stages.  (1) Jacobi sweeps in FP32 on a power-of-two
+  // scaled copy (the FP32 pipe is ~64x the FP64 one on this part) give an approximate V.
+  // (2) Mixed-precision refinement (oa_correction) makes V accurate and orthogonal to
+  // FP64 working accuracy; its O(n^3) products are split GEMMs with 6 slices on the
+  // tensor cores except the last orthogonality check and W V (FP64 GEMMs), its O(n^2)
+  // part is FP64.  (3) FP64 Jacobi sweeps on W V finish the
+  // pairs the refinement leaves (close singular values) and certify convergence: the
+  // result is the FP64 one-sided Jacobi SVD of W V with V orthogonal to working
+  // accuracy.  Every sweep stage uses the panel kernel when the tallest block fits a
+  // shared-memory panel and the scalar sweep otherwise.
   // FP64 sweep limit (the reference's LAPACK call has no such knob; a limit of 0 makes
   // every block with more than one column report ND_ERR_NOCONV, which tests use)
   const int max_sweeps = h->svd_max_sweeps < 0 ? 60 : h->svd_max_sweeps;
@@ -750,16 +1159,24 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
   bool converged = false;
   int sweeps32 = 0, sweeps64 = 0;
   nd_status st = ND_OK;
+  int maxmm = 1;
+  for (auto& b : blocks) maxmm = std::max(maxmm, b.mm);
+  std::vector<double> ref_angles, off64, off32;
+  std::vector<int32_t> act64, act32;
+  int nref = 0;
   if (work >= 2e8 && maxr > 0) {
     float *W32 = nullptr, *V32 = nullptr;
-    double *Y = nullptr, *Vn = nullptr, *W0 = nullptr;
-    unsigned long long* bmax = nullptr;
+    double *Y = nullptr, *Vn = nullptr, *W0 = nullptr, *W1 = nullptr, *S = nullptr;
+    unsigned long long *bmax = nullptr, *emax = nullptr;
     ND_CUDA(h, cudaMallocAsync(&W32, std::max<int64_t>(woff, 1) * 4, s));
     ND_CUDA(h, cudaMallocAsync(&V32, std::max<int64_t>(voff, 1) * 4, s));
     ND_CUDA(h, cudaMallocAsync(&Y, std::max<int64_t>(voff, 1) * 8, s));
     ND_CUDA(h, cudaMallocAsync(&Vn, std::max<int64_t>(voff, 1) * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&S, std::max<int64_t>(voff, 1) * 8, s));
     ND_CUDA(h, cudaMallocAsync(&W0, std::max<int64_t>(woff, 1) * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&W1, std::max<int64_t>(woff, 1) * 8, s));
     ND_CUDA(h, cudaMallocAsync(&bmax, nb * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&emax, 16, s));
     ND_CUDA(h, cudaMemsetAsync(bmax, 0, nb * 8, s));
     int64_t maxe = 0, maxv = 0;
     for (auto& b : blocks) { maxe = std::max(maxe, (int64_t)b.mm * b.nn); maxv = std::max(maxv, (int64_t)b.nn * b.nn); }
@@ -772,26 +1189,88 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
     ND_LAUNCHED(h);
     ND_LAUNCHED(h);
     bool c32 = false;
-    st = run_sweeps<float>(h, dblk, nb, task0, maxr, soff, W32, V32, offmax, bar, 5.9604644775390625e-08,
-                           std::min(40, max_sweeps), c32, sweeps32);
+    const double u32 = ND_SVD_TOL32;
+    const int sweeps32_max = std::min(40, max_sweeps);
+    if (panel_group<float>(maxmm))
+      st = run_panel_sweeps<float>(h, blocks, dblk, W32, V32, offmax, bar, u32, sweeps32_max, c32, sweeps32, &act32,
+                                   &off32, ND_SVD_TOL32_POW);
+    else
+      st = run_sweeps<float>(h, dblk, nb, task0, maxr, soff, W32, V32, offmax, bar, u32, sweeps32_max, c32, sweeps32);
     if (!st) {
-      to_f64_and_identity<<<gv, 256, 0, s>>>(dblk, V32, V, Y);
+      v_to_f64<<<gv, 256, 0, s>>>(dblk, V32, V);
       ND_LAUNCHED(h);
-      for (int it = 0; it < 2 && !st; ++it) {
-        if (it) { set_identity<<<gv, 256, 0, s>>>(dblk, Y); ND_LAUNCHED(h); }
-        st = block_gemm(h, blocks, 0, V, V, Y, -1.0, 1.0);                  // Y = I - V^T V
-        if (!st) st = nd_cuda_check(h, cudaMemcpyAsync(Vn, V, voff * 8, cudaMemcpyDeviceToDevice, s), "svd copy");
-        if (!st) st = block_gemm(h, blocks, 1, V, Y, Vn, 0.5, 1.0);         // Vn = V + V Y / 2
+      ExecCache cR, cW, cS, cV, cR64, cW64, cS64, cWE;
+      const int saved = h->ozaki_slices;
+      h->ozaki_slices = 6;
+      // One refinement step.  mode 0: split-GEMM step; 1: FP64 R, W X and S; 2: Newton-
+      // Schulz with an FP64 R.  Modes 1 and 2 keep W0 = W X current (W0 += W0 E).
+      // Leaves em[0] (largest rotation) and em[1] (largest |E_ij|) on the host.
+      double em[2] = {0.0, 0.0};
+      auto step = [&](int mode) -> nd_status {
+        const int pr = mode ? ND_PREC_FP64 : ND_PREC_OZAKI;
+        set_identity<<<gv, 256, 0, s>>>(dblk, Y);
+        ND_LAUNCHED(h);
+        nd_prof_begin(h, "svd_refine_gemm");
+        nd_status e = block_gemm(h, mode ? cR64 : cR, blocks, 0, V, V, Y, -1.0, 1.0, pr);             // R = I - X^T X
+        if (!e && mode < 2) e = block_gemm(h, mode ? cW64 : cW, blocks, 2, W, V, W0, 1.0, 0.0, pr);  // W0 = W X
+        if (!e && mode < 2) e = block_gemm(h, mode ? cS64 : cS, blocks, 3, W0, W0, S, 1.0, 0.0, pr); // S = W0^T W0
+        nd_prof_end(h);
+        if (e) return e;
+        if ((e = nd_cuda_check(h, cudaMemsetAsync(emax, 0, 16, s), "svd refine"))) return e;
+        nd_prof_begin(h, "svd_refine");
+        const double tau = mode == 0 ? OA_TAU : mode == 1 ? OA_TAU_FP64 : -1.0;
+        oa_correction<<<gv, 256, 0, s>>>(dblk, S, Y, tau, emax);                                      // Y <- E
+        ND_LAUNCHED(h);
+        e = nd_cuda_check(h, cudaMemcpyAsync(Vn, V, voff * 8, cudaMemcpyDeviceToDevice, s), "svd copy");
+        if (!e && mode) e = nd_cuda_check(h, cudaMemcpyAsync(W1, W0, woff * 8, cudaMemcpyDeviceToDevice, s), "svd copy");
+        nd_prof_end(h);
+        nd_prof_begin(h, "svd_refine_gemm");
+        if (!e) e = block_gemm(h, cV, blocks, 1, V, Y, Vn, 1.0, 1.0, ND_PREC_OZAKI);                 // X + X E
+        if (!e && mode) e = block_gemm(h, cWE, blocks, 2, W0, Y, W1, 1.0, 1.0, ND_PREC_OZAKI);       // W0 + W0 E
+        nd_prof_end(h);
+        if (e) return e;
         std::swap(V, Vn);
+        if (mode) std::swap(W0, W1);
+        unsigned long long eb[2] = {0, 0};
+        if ((e = nd_cuda_check(h, cudaMemcpyAsync(eb, emax, 16, cudaMemcpyDeviceToHost, s), "svd refine"))) return e;
+        if ((e = nd_cuda_check(h, cudaStreamSynchronize(s), "svd refine"))) return e;
+        em[0] = bits_to_double(eb[0]);
+        em[1] = bits_to_double(eb[1]);
+        ++nref;
+        ref_angles.push_back(mode == 2 ? em[1] : em[0]);
+        return ND_OK;
+      };
+      // split-GEMM steps while they still converge (their noise floor is ~1e-12 / gap)
+      double prev = INFINITY;
+      for (int it = 0; it < 6 && !st; ++it) {
+        st = step(0);
+        if (!st && (em[0] <= 1e-10 || em[0] > 0.5 * prev)) break;
+        prev = em[0];
       }
-      if (!st) st = block_gemm(h, blocks, 2, W, V, W0, 1.0, 0.0);           // W0 = W Q
-      if (!st) std::swap(W, W0);
+      if (!st && ND_SVD_EXACT_STEP) st = step(1);
+      // |E| <= 3e-8 leaves X orthogonal to 1e-15; otherwise Newton-Schulz (quadratic)
+      for (int it = 0; it < 3 && !st && em[1] > 3e-8; ++it) st = step(2);
+      if (!st && !ND_SVD_EXACT_STEP) st = block_gemm(h, cW64, blocks, 2, W, V, W0, 1.0, 0.0, ND_PREC_FP64);
+      if (!st) std::swap(W, W0);                                                                      // W <- W X
+      h->ozaki_slices = saved;
+      for (ExecCache* c : {&cR, &cW, &cS, &cV, &cR64, &cW64, &cS64, &cWE}) c->free_all(h);
     }
     cudaFreeAsync(W32, s); cudaFreeAsync(V32, s); cudaFreeAsync(Y, s); cudaFreeAsync(Vn, s);
-    cudaFreeAsync(W0, s); cudaFreeAsync(bmax, s);
+    cudaFreeAsync(S, s); cudaFreeAsync(W0, s); cudaFreeAsync(W1, s); cudaFreeAsync(bmax, s); cudaFreeAsync(emax, s);
   }
-  if (!st) st = run_sweeps<double>(h, dblk, nb, task0, maxr, soff, W, V, offmax, bar, 2.220446049250313e-16,
-                                   max_sweeps, converged, sweeps64);
+  if (!st) {
+    const double u64 = 2.220446049250313e-16;
+    if (panel_group<double>(maxmm))
+      st = run_panel_sweeps<double>(h, blocks, dblk, W, V, offmax, bar, u64, max_sweeps, converged, sweeps64, &act64,
+                                    &off64);
+    else
+      st = run_sweeps<double>(h, dblk, nb, task0, maxr, soff, W, V, offmax, bar, u64, max_sweeps, converged, sweeps64);
+  }
+  h->svd_info_i = {sweeps32, nref, sweeps64, panel_group<double>(maxmm) ? 1 : 0};
+  h->svd_info_i.insert(h->svd_info_i.end(), act64.begin(), act64.end());
+  h->svd_info_d = ref_angles;
+  h->svd_info_d.insert(h->svd_info_d.end(), off64.begin(), off64.end());
+  h->svd_info_d.insert(h->svd_info_d.end(), off32.begin(), off32.end());
   if (st) {
     cudaFreeAsync(W, s); cudaFreeAsync(V, s); cudaFreeAsync(sig, s); cudaFreeAsync(order, s);
     cudaFreeAsync(dblk, s); cudaFreeAsync(offmax, s); cudaFreeAsync(bar, s);

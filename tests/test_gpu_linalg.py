@@ -313,3 +313,35 @@ def test_uncombine_inverts_matricize(nd):
         j = back.blocks.index(tuple(b))
         n = int(np.prod(psi.blockdims(b)))
         np.testing.assert_array_equal(data[back.offsets[j]:back.offsets[j] + n], psi.data[psi.offsets[i]:psi.offsets[i] + n])
+
+
+@pytest.mark.parametrize("dims,panel", [
+    ([(2000, 320), (120, 90)], 1),     # tall block: FP32 panels of 2 x 8 columns, FP64 panels of 2 x 4
+    ([(7000, 20), (30, 30)], 0),       # taller than any shared-memory panel: scalar sweeps
+])
+def test_svd_panel_widths_and_scalar_fallback(nd, dims, panel):
+    """The sweep stage picks the widest column group whose panel fits shared memory and
+    falls back to the scalar sweep above that; every path meets the same bars.  The
+    convergence record (nd_svd_last_info) reports which one ran."""
+    import ctypes as C
+    rng = np.random.default_rng(41 + panel)
+    mats = [rng.standard_normal(d) for d in dims]
+    offs, o = [], 0
+    for m in mats:
+        offs.append(o)
+        o += m.size
+    A = obs.BlockSparseTensor([[d[0] for d in dims], [d[1] for d in dims]], [(i + 1, i + 1) for i in range(len(dims))],
+                              offs, np.concatenate([m.reshape(-1, order="F") for m in mats]))
+    U, S, V, spec, kept = nd.svd(_gpu(nd, A))
+    ints = (C.c_int32 * 16)()
+    dbls = (C.c_double * 16)()
+    nd.handle(0).call("nd_svd_last_info", ints, 16, dbls, 16)
+    assert ints[3] == panel and ints[2] >= 1                  # panel flag, FP64 sweeps
+    Ub, Vb = _blocks(nd, U), _blocks(nd, V)
+    for n, m in enumerate(mats):
+        s = S[n].cpu().numpy()
+        ref = np.linalg.svd(m, compute_uv=False)
+        np.testing.assert_allclose(s, ref, rtol=0, atol=1e-12 * ref[0])
+        assert odense.rel_frobenius_error(Ub[n] @ np.diag(s) @ Vb[n].T, m) <= 1e-12
+        np.testing.assert_allclose(Vb[n].T @ Vb[n], np.eye(len(s)), atol=1e-12)
+        np.testing.assert_allclose(Ub[n].T @ Ub[n], np.eye(len(s)), atol=1e-12)
