@@ -266,6 +266,31 @@ def tune_summary(h):
     return {"entries": len(out), "choices": out}
 
 
+def cta_schedule_skew(h, one_step):
+    """Run one step with per-CTA timestamps on the split-GEMM launches and summarise, per
+    launch, how evenly the longest-first schedule finishes: span = last end - first start,
+    skew = last end - first end, idle = mean over CTAs of (last end - own end) / span."""
+    import ctypes as C
+    import torch
+    h.call("nd_set_cta_timing", 1)
+    one_step()
+    torch.cuda.synchronize()
+    times = (C.c_uint64 * (8 * 2048))()
+    nctas = (C.c_int32 * 8)()
+    nl = C.c_int32()
+    h.call("nd_cta_times_read", times, nctas, C.byref(nl))
+    h.call("nd_set_cta_timing", 0)
+    out = []
+    for k in range(nl.value):
+        n = nctas[k]
+        t = np.frombuffer(times, dtype=np.uint64, count=2 * n, offset=8 * k * 2048).reshape(n, 2).astype(np.float64)
+        start, end = t[:, 0], t[:, 1]
+        span = end.max() - start.min()
+        out.append({"ctas": int(n), "span_us": round(span / 1e3, 1), "skew_us": round((end.max() - end.min()) / 1e3, 1),
+                    "idle_frac": round(float(np.mean(end.max() - end)) / span, 4)})
+    return out
+
+
 def run_ours(args):
     import torch
     rank, ws, local, dist = dist_init()
@@ -384,6 +409,10 @@ def run_ours(args):
                 "units": f"{npair_levels} BF16 slice-pair products x 2MNK per block pair",
                 "kernel_share_of_step": round(gemm_ms / max(1e-9, float(np.sum(ts))), 3),
                 "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()}}
+
+    # per-CTA finish skew of the longest-first tile schedule: one step with CTA timestamps
+    if roof is not None:
+        roof["cta_schedule"] = cta_schedule_skew(h, lambda: step(args.precision))
 
     # end to end through the public API with host buffers (plans rebuilt, as a fresh contract call does)
     pinned = {k: torch.from_numpy(np.ascontiguousarray(net[k].data)).pin_memory() for k in ("L", "psi", "W1", "W2", "R")}

@@ -85,6 +85,13 @@ nd_status nd_set_svd_max_sweeps(nd_handle h, int32_t sweeps);
  * each refinement step, then the largest relative off-diagonal |w_i . w_j| /
  * (|w_i| |w_j|) rotated in each FP64 sweep, then the same for each FP32 sweep. */
 nd_status nd_svd_last_info(nd_handle h, int32_t* ints, int32_t nints, double* dbls, int32_t ndbls);
+/* Per-CTA timing of the persistent split-GEMM launches (diagnostics for the
+ * longest-first tile schedule; no counterpart in the reference).  With timing on,
+ * each split-GEMM launch records, per CTA, its start and end (%globaltimer, ns).
+ * nd_cta_times_read synchronises and returns the last min(#launches, 8) launches in
+ * order: times[k * 2048 + 2 * c + {0, 1}] for CTA c < nctas[k] of launch k. */
+nd_status nd_set_cta_timing(nd_handle h, int32_t enable);
+nd_status nd_cta_times_read(nd_handle h, uint64_t* times, int32_t* nctas, int32_t* nlaunch);
 /* Output tile of the split-precision (Ozaki / 3xBF16) GEMM when the autotuner has no
  * entry for a contraction: 0 (default) = 128 x 64 tiles on single CTAs, 1 = 256 x 64
  * tiles on pairs of CTAs (tcgen05.mma.cta_group::2).  With tuning on, both are timed

@@ -59,6 +59,14 @@ nd_status nd_upload(nd_handle h, void* dst, const void* src, size_t bytes) {
   return ND_OK;
 }
 
+unsigned long long* nd_cta_slot(nd_handle h, int nctas) {
+  if (!h->cta_timing || !h->d_cta_times || nctas > ND_CTA_MAX || nd_capturing(h)) return nullptr;
+  const int slot = h->cta_nlaunch % ND_CTA_SLOTS;
+  h->cta_nctas[slot] = nctas;
+  ++h->cta_nlaunch;
+  return h->d_cta_times + (size_t)slot * 2 * ND_CTA_MAX;
+}
+
 nd_status nd_dalloc(nd_handle h, void** p, size_t bytes) {
   *p = nullptr;
   ND_CUDA(h, cudaMallocAsync(p, std::max<size_t>(bytes, 16), h->stream));
@@ -152,6 +160,7 @@ nd_status nd_destroy(nd_handle h) {
   if (h->d_plan_status) cudaFree(h->d_plan_status);
   if (h->d_status) cudaFree(h->d_status);
   for (auto& r : h->prof) { cudaEventDestroy(r.e0); cudaEventDestroy(r.e1); }
+  if (h->d_cta_times) cudaFree(h->d_cta_times);
   for (auto e : h->event_pool) cudaEventDestroy(e);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -232,6 +241,31 @@ nd_status nd_set_spin_limit(nd_handle h, uint32_t polls) {
 nd_status nd_set_svd_max_sweeps(nd_handle h, int32_t sweeps) {
   if (!h) return ND_ERR_ARG;
   h->svd_max_sweeps = sweeps < 0 ? -1 : sweeps;
+  return ND_OK;
+}
+
+nd_status nd_set_cta_timing(nd_handle h, int32_t enable) {
+  if (!h) return ND_ERR_ARG;
+  if (enable && !h->d_cta_times)
+    ND_CUDA(h, cudaMalloc(&h->d_cta_times, sizeof(unsigned long long) * 2 * ND_CTA_SLOTS * ND_CTA_MAX));
+  h->cta_timing = enable != 0;
+  h->cta_nlaunch = 0;
+  return ND_OK;
+}
+
+nd_status nd_cta_times_read(nd_handle h, uint64_t* times, int32_t* nctas, int32_t* nlaunch) {
+  if (!h || !times || !nctas || !nlaunch) return ND_ERR_ARG;
+  const int n = std::min(h->cta_nlaunch, ND_CTA_SLOTS);
+  *nlaunch = n;
+  if (!n) return ND_OK;
+  ND_CUDA(h, cudaStreamSynchronize(h->stream));
+  const int first = h->cta_nlaunch - n;
+  for (int k = 0; k < n; ++k) {
+    const int slot = (first + k) % ND_CTA_SLOTS;
+    nctas[k] = h->cta_nctas[slot];
+    ND_CUDA(h, cudaMemcpy(times + (size_t)k * 2 * ND_CTA_MAX, h->d_cta_times + (size_t)slot * 2 * ND_CTA_MAX,
+                          sizeof(uint64_t) * 2 * ND_CTA_MAX, cudaMemcpyDeviceToHost));
+  }
   return ND_OK;
 }
 

@@ -52,6 +52,11 @@ struct nd_context {
   int num_sms = 0;
   int ozaki_slices = 5;
   int svd_max_sweeps = -1;            // FP64 Jacobi sweep limit of the SVD (-1 = default 60)
+  // per-CTA start / end times of the last split-GEMM launches (nd_set_cta_timing)
+  int cta_timing = 0;
+  unsigned long long* d_cta_times = nullptr;   // ND_CTA_SLOTS x ND_CTA_MAX x {start, end}
+  int cta_nlaunch = 0;
+  int cta_nctas[8] = {0};
   // convergence record of the last SVD (nd_svd_last_info)
   std::vector<int32_t> svd_info_i;
   std::vector<double> svd_info_d;
@@ -123,6 +128,10 @@ nd_status nd_check_device_status(nd_handle h, const char* what);  // syncs
   } while (0)
 
 #define ND_LAUNCHED(h) do { (h)->launches++; } while (0)
+
+constexpr int ND_CTA_SLOTS = 8, ND_CTA_MAX = 1024;
+// Slot for the per-CTA timestamps of the next split-GEMM launch (nullptr when timing is off).
+unsigned long long* nd_cta_slot(nd_handle h, int nctas);
 
 // Bracket a launch with timing events when profiling is on (not inside capture).
 void nd_prof_begin(nd_handle h, const char* name);

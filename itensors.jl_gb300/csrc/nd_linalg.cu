@@ -133,7 +133,9 @@ struct SweepArgs {
   unsigned int* bar_count;
   unsigned int* bar_gen;
   DeviceStatus* st;
-  double tol;        // unit roundoff of T; rotations below mm * tol are skipped
+  double tol;        // rotations below min(tol * mm^tol_pow, tol_cap) are skipped
+  double tol_pow;
+  double tol_cap;
 };
 
 template <typename T>
@@ -229,7 +231,7 @@ __global__ void __launch_bounds__(512, 2) svd_sweep(SweepArgs<T> a) {
       const T al = __ldcg(a.nrm + b.s_off + p), be = __ldcg(a.nrm + b.s_off + q);
       const T nrm = sqrt(al) * sqrt(be);
       double rel = nrm > T(0) ? (double)(fabs(ga) / nrm) : 0.0;
-      const double tolb = a.tol * (double)b.mm;        // m * unit roundoff, as one-sided Jacobi codes use
+      const double tolb = fmin(a.tol_cap, a.tol * (a.tol_pow == 1.0 ? (double)b.mm : pow((double)b.mm, a.tol_pow)));
       if (rel > tolb && ga != T(0)) {
         const T zeta = (be - al) / (T(2) * ga);
         const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
@@ -569,8 +571,9 @@ struct BjArgs {
   unsigned int* bar_count;
   unsigned int* bar_gen;
   DeviceStatus* st;
-  double tol;        // pairs with |w_p . w_q| <= tol * mm^tol_pow |w_p||w_q| are left
+  double tol;        // pairs with |w_p . w_q| <= min(tol * mm^tol_pow, tol_cap) |w_p||w_q| are left
   double tol_pow;
+  double tol_cap;
 };
 
 // 16-byte vectors of the panel element type: a lane handles VW consecutive rows.
@@ -668,7 +671,7 @@ __global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
       const int mm = b.mm;
       constexpr int VW = PanVec<T>::W;
       const int mmv = (mm + VW - 1) / VW * VW;         // rows padded to whole vectors (zeros)
-      const double tolb = a.tol * (a.tol_pow == 1.0 ? (double)mm : pow((double)mm, a.tol_pow));
+      const double tolb = fmin(a.tol_cap, a.tol * (a.tol_pow == 1.0 ? (double)mm : pow((double)mm, a.tol_pow)));
       if (threadIdx.x < P2) {
         const int g = threadIdx.x < B ? gp : gq;
         const int col = g * B + (threadIdx.x < B ? threadIdx.x : threadIdx.x - B);
@@ -783,6 +786,19 @@ __global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
 #ifndef ND_SVD_TOL32_POW
 #define ND_SVD_TOL32_POW 0.5
 #endif
+// FP64 sweeps: mm * eps (eps = 2^-52), capped at 2e-13, so that the left vectors are
+// orthogonal to 2e-13 or better however tall the block (LAPACK's dgesvj uses sqrt(mm)
+// times the unit roundoff; the cap is the looser bound that this library's accuracy
+// targets, 1e-12 relative, allow, and it saves a sweep on the large blocks).
+#ifndef ND_SVD_TOL64
+#define ND_SVD_TOL64 2.220446049250313e-16
+#endif
+#ifndef ND_SVD_TOL64_POW
+#define ND_SVD_TOL64_POW 1.0
+#endif
+#ifndef ND_SVD_TOL64_CAP
+#define ND_SVD_TOL64_CAP 2e-13
+#endif
 constexpr double OA_TAU = 1e-2;                   // split-GEMM steps
 constexpr double OA_TAU_FP64 = ND_SVD_TAU_FP64;   // FP64 steps: only the small corrections left at that point
 
@@ -891,7 +907,7 @@ __global__ void eig_vectors(const SvdBlock* blocks, const double* Vw, const int3
 template <typename T>
 static nd_status run_sweeps(nd_handle h, const SvdBlock* dblk, int nb, int task0, int maxr, int soff, T* Wt, T* Vt,
                             unsigned long long* offmax, unsigned int* bar, double tol, int max_sweeps,
-                            bool& converged, int& sweeps) {
+                            bool& converged, int& sweeps, double tol_pow = 1.0, double tol_cap = INFINITY) {
   cudaStream_t s = h->stream;
   converged = maxr == 0;
   sweeps = 0;
@@ -916,7 +932,7 @@ static nd_status run_sweeps(nd_handle h, const SvdBlock* dblk, int nb, int task0
     svd_norms<T><<<std::max(1, std::min((soff + 7) / 8, 8 * h->num_sms)), 256, 0, s>>>(dblk, nb, dact, Wt, nrm, soff);
     nd_prof_end(h);
     ND_LAUNCHED(h);
-    SweepArgs<T> sa{dblk, nb, task0, maxr, Wt, Vt, nrm, dact, offmax, bar, bar + 1, h->d_status, tol};
+    SweepArgs<T> sa{dblk, nb, task0, maxr, Wt, Vt, nrm, dact, offmax, bar, bar + 1, h->d_status, tol, tol_pow, tol_cap};
     void* args[] = {&sa};
     nd_prof_begin(h, name);
     e = cudaLaunchCooperativeKernel((void*)svd_sweep<T>, grid, 512, args, 0, s);
@@ -979,7 +995,8 @@ template <typename T>
 static nd_status run_panel_sweeps(nd_handle h, const std::vector<SvdBlock>& blocks, const SvdBlock* dblk, T* Wt,
                                   T* Vt, unsigned long long* offmax, unsigned int* bar, double tol, int max_sweeps,
                                   bool& converged, int& sweeps, std::vector<int32_t>* act_hist = nullptr,
-                                  std::vector<double>* off_hist = nullptr, double tol_pow = 1.0) {
+                                  std::vector<double>* off_hist = nullptr, double tol_pow = 1.0,
+                                  double tol_cap = INFINITY) {
   cudaStream_t s = h->stream;
   const int nb = (int)blocks.size();
   sweeps = 0;
@@ -1018,7 +1035,8 @@ static nd_status run_panel_sweeps(nd_handle h, const std::vector<SvdBlock>& bloc
     if (act_hist) act_hist->push_back((int32_t)std::count(act.begin(), act.end(), 1));
     if ((st = nd_upload(h, dtasks, tasks.data(), tasks.size() * sizeof(BjTask)))) break;
     if ((st = nd_cuda_check(h, cudaMemsetAsync(offmax, 0, nb * 8, s), "svd sweep set-up"))) break;
-    BjArgs<T> a{dblk, dtasks, (int)tasks.size(), nrounds, ldp, Wt, Vt, offmax, bar, bar + 1, h->d_status, tol, tol_pow};
+    BjArgs<T> a{dblk, dtasks, (int)tasks.size(), nrounds, ldp, Wt, Vt, offmax, bar, bar + 1, h->d_status, tol, tol_pow,
+                tol_cap};
     nd_prof_begin(h, name);
     if constexpr (sizeof(T) == 4) {
       if (B == 16) st = launch_bj<T, 16>(h, a, smem);
@@ -1195,7 +1213,8 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
       st = run_panel_sweeps<float>(h, blocks, dblk, W32, V32, offmax, bar, u32, sweeps32_max, c32, sweeps32, &act32,
                                    &off32, ND_SVD_TOL32_POW);
     else
-      st = run_sweeps<float>(h, dblk, nb, task0, maxr, soff, W32, V32, offmax, bar, u32, sweeps32_max, c32, sweeps32);
+      st = run_sweeps<float>(h, dblk, nb, task0, maxr, soff, W32, V32, offmax, bar, u32, sweeps32_max, c32, sweeps32,
+                             ND_SVD_TOL32_POW);
     if (!st) {
       v_to_f64<<<gv, 256, 0, s>>>(dblk, V32, V);
       ND_LAUNCHED(h);
@@ -1259,12 +1278,13 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
     cudaFreeAsync(S, s); cudaFreeAsync(W0, s); cudaFreeAsync(W1, s); cudaFreeAsync(bmax, s); cudaFreeAsync(emax, s);
   }
   if (!st) {
-    const double u64 = 2.220446049250313e-16;
+    const double u64 = ND_SVD_TOL64;
     if (panel_group<double>(maxmm))
       st = run_panel_sweeps<double>(h, blocks, dblk, W, V, offmax, bar, u64, max_sweeps, converged, sweeps64, &act64,
-                                    &off64);
+                                    &off64, ND_SVD_TOL64_POW, ND_SVD_TOL64_CAP);
     else
-      st = run_sweeps<double>(h, dblk, nb, task0, maxr, soff, W, V, offmax, bar, u64, max_sweeps, converged, sweeps64);
+      st = run_sweeps<double>(h, dblk, nb, task0, maxr, soff, W, V, offmax, bar, u64, max_sweeps, converged, sweeps64,
+                              ND_SVD_TOL64_POW, ND_SVD_TOL64_CAP);
   }
   h->svd_info_i = {sweeps32, nref, sweeps64, panel_group<double>(maxmm) ? 1 : 0};
   h->svd_info_i.insert(h->svd_info_i.end(), act64.begin(), act64.end());

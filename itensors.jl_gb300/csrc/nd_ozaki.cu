@@ -349,7 +349,14 @@ struct GemmArgs {
   int32_t amode;      // 0: alpha == 1, 1: general alpha
   int32_t bmode;      // 0: beta == 0 (overwrite), 1: general beta
   DeviceStatus* st;
+  unsigned long long* cta_times;   // optional: {start, end} (%globaltimer, ns) per CTA
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
   // tcgen05 shared-memory matrix descriptor: K-major, 64-byte swizzle,
@@ -461,6 +468,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   __shared__ int64_t colR_s[BN];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t lim = nd_spin_limit(g.st);
+  if (g.cta_times && threadIdx.x == 0) g.cta_times[2 * blockIdx.x] = global_ns();
 
   if (tid == 0) {
     for (int s = 0; s < C::STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -700,6 +708,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   __syncthreads();
   fence_after();
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(C::TMEM_COLS));
+  if (g.cta_times && tid == 0) g.cta_times[2 * blockIdx.x + 1] = global_ns();
 }
 
 template <int S>
@@ -712,8 +721,10 @@ nd_status launch_gemm(nd_handle h, const GemmArgs& g) {
     attr = true;
   }
   int blocks = std::min(g.nitems, h->num_sms);
+  GemmArgs gt = g;
+  gt.cta_times = nd_cta_slot(h, blocks);
   nd_prof_begin(h, "split_gemm");
-  split_gemm<S><<<blocks, NTHREADS, C::SMEM, h->stream>>>(g);
+  split_gemm<S><<<blocks, NTHREADS, C::SMEM, h->stream>>>(gt);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "split_gemm");
@@ -822,6 +833,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1) split_g
   __shared__ int64_t colR_s[BN];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t lim = nd_spin_limit(g.st);
+  if (g.cta_times && threadIdx.x == 0) g.cta_times[2 * blockIdx.x] = global_ns();
   const uint32_t crank = cluster_ctarank();            // 0 issues the MMAs, 1 relays
   const int pair_id = blockIdx.x >> 1, npairs = gridDim.x >> 1;
 
@@ -1083,6 +1095,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1) split_g
   cluster_sync_all();                 // no MMA, copy or remote arrival of the pair is in flight
   fence_after();
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(C::TMEM_COLS));
+  if (g.cta_times && threadIdx.x == 0) g.cta_times[2 * blockIdx.x + 1] = global_ns();
 }
 
 // Shared-memory attribute of split_gemm2<S> (set once) and the number of CTA pairs that
@@ -1122,9 +1135,11 @@ int pair_slots(nd_handle h, int S) {
 template <int S>
 nd_status launch_gemm2(nd_handle h, const GemmArgs& g, int slots) {
   if (pair_slots_for<S>(h) <= 0) return nd_fail(h, ND_ERR_CUDA, "split_gemm2: no CTA pair can be resident");
+  GemmArgs gt = g;
+  gt.cta_times = nd_cta_slot(h, 2 * slots);
   nd_prof_begin(h, "split_gemm");
   using C = Cfg2<S>;
-  split_gemm2<S><<<2 * slots, NTHREADS, C::SMEM, h->stream>>>(g);
+  split_gemm2<S><<<2 * slots, NTHREADS, C::SMEM, h->stream>>>(gt);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "split_gemm2");
@@ -1318,7 +1333,7 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
   }
   GemmArgs g{c.d_split_pairs, c.d_split_items, c.nsplit_items, (const SplitOp*)c.d_operands,
              (const unsigned char*)c.d_pack, c.d_exp, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1,
-             h->d_status};
+             h->d_status, nullptr};
   if (c.nsplit_items == 0) return ND_OK;
   if (c.split_pair2) {
     switch (S) {

@@ -68,6 +68,8 @@ SIGNATURES = {
     "nd_set_spin_limit": [_P, C.c_uint32],
     "nd_set_svd_max_sweeps": [_P, _I32],
     "nd_svd_last_info": [_P, _P, _I32, _P, _I32],
+    "nd_set_cta_timing": [_P, _I32],
+    "nd_cta_times_read": [_P, _P, _P, _P],
     "nd_launch_count": [_P, _PI64],
     "nd_profile_enable": [_P, _I32],
     "nd_profile_read": [_P, _I32, C.c_char_p, _PI64, _PD, _PI32],
