@@ -253,6 +253,9 @@ struct PairDesc {
   Mixed rows;   // st0: A strides, st1: R strides
   Mixed cols;   // st0: B strides, st1: R strides
   Mixed ks;     // st0: A strides, st1: B strides
+  int32_t sym = 0;   // 1: R is symmetric (M == N); the FP64 tile kernel computes the tiles on
+                     // and above the diagonal only, the caller mirrors the rest
+  int32_t pad_[3] = {0, 0, 0};   // keeps the size a multiple of 16 bytes
 };
 
 // A split operand (one A block or one B block) for the split-precision GEMMs.

@@ -123,6 +123,7 @@ static void make_items(const std::vector<PairDesc>& pairs, int bm, int bn, Pick 
       int mt = (p.M + bm - 1) / bm, nt = (p.N + bn - 1) / bn;
       for (int a = 0; a < mt; ++a)
         for (int b = 0; b < nt; ++b) {
+          if (p.sym && bm == bn && a > b) continue;      // below the diagonal of a symmetric R
           int64_t mm = std::min(bm, p.M - a * bm), nn = std::min(bn, p.N - b * bn);
           tmp.push_back({mm * nn * std::max<int64_t>(ksum, 1), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
         }

@@ -230,8 +230,9 @@ __global__ void __launch_bounds__(512, 2) svd_sweep(SweepArgs<T> a) {
       ga = warp_sum(ga);
       const T al = __ldcg(a.nrm + b.s_off + p), be = __ldcg(a.nrm + b.s_off + q);
       const T nrm = sqrt(al) * sqrt(be);
-      double rel = nrm > T(0) ? (double)(fabs(ga) / nrm) : 0.0;
-      const double tolb = fmin(a.tol_cap, a.tol * (a.tol_pow == 1.0 ? (double)b.mm : pow((double)b.mm, a.tol_pow)));
+      T rel = nrm > T(0) ? fabs(ga) / nrm : T(0);
+      // tol_pow is 1 or 1/2; tolerance math in T (the FP64 pipe is narrow on this part)
+      const T tolb = min((T)a.tol_cap, (T)a.tol * (a.tol_pow != 1.0 ? sqrt((T)b.mm) : (T)b.mm));
       if (rel > tolb && ga != T(0)) {
         const T zeta = (be - al) / (T(2) * ga);
         const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
@@ -244,9 +245,9 @@ __global__ void __launch_bounds__(512, 2) svd_sweep(SweepArgs<T> a) {
           a.nrm[b.s_off + q] = be + tt * ga;
         }
       } else {
-        rel = 0.0;
+        rel = T(0);
       }
-      if (lane == 0 && rel > 0.0) atomicMax(&a.offmax[bi], (unsigned long long)__double_as_longlong(rel));
+      if (lane == 0 && rel > T(0)) atomicMax(&a.offmax[bi], (unsigned long long)__double_as_longlong((double)rel));
     }
     if (!grid_barrier(a.bar_count, a.bar_gen, gridDim.x, a.st)) return;
   }
@@ -602,7 +603,7 @@ __device__ __forceinline__ void vrot(double2& x, double2& y, double c, double s)
 // nv = rows / VW, the panel's rows padded with zeros to a whole vector.
 template <typename T, int P2>
 __device__ __forceinline__ void bj_pair(T* pan, int ldp, T* q, T* d, const int* cols, int p, int qq, int nv,
-                                        double tolb, int lane, int* any, unsigned long long* offmax) {
+                                        T tolb, int lane, int* any, unsigned long long* offmax) {
   using VT = typename PanVec<T>::type;
   if (cols[p] < 0 || cols[qq] < 0) return;
   VT* xp = reinterpret_cast<VT*>(pan + (size_t)p * ldp);
@@ -617,7 +618,7 @@ __device__ __forceinline__ void bj_pair(T* pan, int ldp, T* q, T* d, const int* 
   const T g = warp_sum((g0 + g2) + (g1 + g3));
   const T al = d[p], be = d[qq];
   const T nrm = sqrt(al) * sqrt(be);
-  const double rel = nrm > T(0) ? (double)(fabs(g) / nrm) : 0.0;
+  const T rel = nrm > T(0) ? fabs(g) / nrm : T(0);   // in T: the FP64 pipe is narrow on this part
   if (!(rel > tolb) || g == T(0)) return;
   const T zeta = (be - al) / (T(2) * g);
   const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
@@ -638,8 +639,81 @@ __device__ __forceinline__ void bj_pair(T* pan, int ldp, T* q, T* d, const int* 
     d[p] = al - tt * g;
     d[qq] = be + tt * g;
     *any = 1;
-    atomicMax(offmax, (unsigned long long)__double_as_longlong(rel));
+    atomicMax(offmax, (unsigned long long)__double_as_longlong((double)rel));
   }
+}
+
+// The cross rounds with column p of warp w (p = w, fixed through them) held in
+// registers, NV vectors per lane: each round reads its partner q into registers once
+// for both the dot product and the rotation and writes it back once, a third of the
+// shared-memory traffic of bj_pair (which the FP32 sweeps are bound by).  Column p,
+// its norm and column p of Q are touched by warp w alone during these rounds.
+template <typename T, int P2, int NV>
+__device__ __forceinline__ void bj_cross_regs(T* pan, int ldp, T* q, T* d, const int* cols, int B, int warp, int nv,
+                                              T tolb, int lane, int* any, unsigned long long* offmax) {
+  using VT = typename PanVec<T>::type;
+  const int p = warp;
+  const bool pv = cols[p] >= 0;
+  VT* xp = reinterpret_cast<VT*>(pan + (size_t)p * ldp);
+  VT rp[NV];
+#pragma unroll
+  for (int u = 0; u < NV; ++u) {
+    const int i = lane + 32 * u;
+    if (pv && i < nv) rp[u] = xp[i];
+    else memset(&rp[u], 0, sizeof(VT));
+  }
+  T dp = d[p];
+  for (int sr = 0; sr < B; ++sr) {
+    const int qq = B + (warp + sr) % B;
+    if (pv && cols[qq] >= 0) {
+      VT* xq = reinterpret_cast<VT*>(pan + (size_t)qq * ldp);
+      VT rq[NV];
+      T g0 = 0, g1 = 0;
+#pragma unroll
+      for (int u = 0; u < NV; ++u) {
+        const int i = lane + 32 * u;
+        if (i < nv) rq[u] = xq[i];
+        else memset(&rq[u], 0, sizeof(VT));
+        vdot(rp[u], rq[u], g0, g1);
+      }
+      const T g = warp_sum(g0 + g1);
+      const T al = dp, be = d[qq];
+      const T nrm = sqrt(al) * sqrt(be);
+      const T rel = nrm > T(0) ? fabs(g) / nrm : T(0);
+      if (rel > tolb && g != T(0)) {
+        const T zeta = (be - al) / (T(2) * g);
+        const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+        const T c = T(1) / sqrt(T(1) + tt * tt);
+        const T sn = c * tt;
+#pragma unroll
+        for (int u = 0; u < NV; ++u) {
+          vrot(rp[u], rq[u], c, sn);
+          const int i = lane + 32 * u;
+          if (i < nv) xq[i] = rq[u];
+        }
+        if (lane < P2) {
+          const T a = q[p * P2 + lane], b = q[qq * P2 + lane];
+          q[p * P2 + lane] = c * a - sn * b;
+          q[qq * P2 + lane] = sn * a + c * b;
+        }
+        dp = al - tt * g;
+        if (lane == 0) {
+          d[qq] = be + tt * g;
+          *any = 1;
+          atomicMax(offmax, (unsigned long long)__double_as_longlong((double)rel));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (pv) {
+#pragma unroll
+    for (int u = 0; u < NV; ++u) {
+      const int i = lane + 32 * u;
+      if (i < nv) xp[i] = rp[u];
+    }
+  }
+  if (lane == 0) d[p] = dp;
 }
 
 template <typename T, int B>
@@ -652,6 +726,8 @@ __global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
   __shared__ int s_cols[P2];                         // column index in the block, -1 if none
   __shared__ int s_any;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const T tol = (T)a.tol, tol_cap = (T)a.tol_cap;
+  const bool sqrt_pow = a.tol_pow != 1.0;          // tol_pow is 1 or 1/2
   for (int r = 0; r < a.nrounds; ++r) {
     // tasks are listed longest first; CTA i takes positions i, 2G-1-i, 2G+i, ... (a snake),
     // so the CTAs with the longest first task get the shortest second one
@@ -671,7 +747,7 @@ __global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
       const int mm = b.mm;
       constexpr int VW = PanVec<T>::W;
       const int mmv = (mm + VW - 1) / VW * VW;         // rows padded to whole vectors (zeros)
-      const double tolb = fmin(a.tol_cap, a.tol * (a.tol_pow == 1.0 ? (double)mm : pow((double)mm, a.tol_pow)));
+      const T tolb = min(tol_cap, tol * (sqrt_pow ? sqrt((T)mm) : (T)mm));
       if (threadIdx.x < P2) {
         const int g = threadIdx.x < B ? gp : gq;
         const int col = g * B + (threadIdx.x < B ? threadIdx.x : threadIdx.x - B);
@@ -709,10 +785,22 @@ __global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
         }
       }
       if (!lone) {
-        for (int sr = 0; sr < B; ++sr) {
-          bj_pair<T, P2>(pan, a.ldp, q, d, s_cols, warp, B + (warp + sr) % B, mmv / VW, tolb, lane, &s_any,
-                         &a.offmax[tk.block]);
-          __syncthreads();
+        // register path for the widest groups when a column fits NVR vectors per lane
+        constexpr int NVR = (sizeof(T) == 4 && B == 16) ? 9 : (sizeof(T) == 8 && B == 8) ? 17 : 0;
+        bool done = false;
+        if constexpr (NVR > 0) {
+          if (mmv / VW <= 32 * NVR) {
+            bj_cross_regs<T, P2, NVR>(pan, a.ldp, q, d, s_cols, B, warp, mmv / VW, tolb, lane, &s_any,
+                                      &a.offmax[tk.block]);
+            done = true;
+          }
+        }
+        if (!done) {
+          for (int sr = 0; sr < B; ++sr) {
+            bj_pair<T, P2>(pan, a.ldp, q, d, s_cols, warp, B + (warp + sr) % B, mmv / VW, tolb, lane, &s_any,
+                           &a.offmax[tk.block]);
+            __syncthreads();
+          }
         }
       }
       if (s_any) {
@@ -778,6 +866,15 @@ __global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
 #ifndef ND_SVD_EXACT_STEP
 #define ND_SVD_EXACT_STEP 1
 #endif
+// Split-GEMM refinement steps before the FP64 one (fewer when the rotations fall below
+// 1e-10; with ND_SVD_SPLIT_STALL also when a step does not halve them).  Four measured
+// best on the chi = 4096 sweep step (3 / 4 / 5 steps: 127 / 125 / 126 ms).
+#ifndef ND_SVD_SPLIT_STEPS
+#define ND_SVD_SPLIT_STEPS 4
+#endif
+#ifndef ND_SVD_SPLIT_STALL
+#define ND_SVD_SPLIT_STALL 0
+#endif
 // FP32 sweeps leave a pair when |w_p . w_q| <= ND_SVD_TOL32 * mm^ND_SVD_TOL32_POW |w_p||w_q|:
 // 4 u sqrt(mm) (u = 2^-24), about the rounding level of an FP32 dot product of mm terms.
 #ifndef ND_SVD_TOL32
@@ -837,6 +934,19 @@ __global__ void oa_correction(const SvdBlock* blocks, const double* S, double* R
   }
   if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(emax, (unsigned long long)__double_as_longlong(m));
   if ((threadIdx.x & 31) == 0 && ma > 0.0) atomicMax(emax + 1, (unsigned long long)__double_as_longlong(ma));
+}
+
+// Lower triangle of a symmetric nn x nn block from its upper triangle, for the elements
+// whose 64 x 64 tile lies below the diagonal (the tiles the FP64 GEMM skipped).
+__global__ void sym_mirror(const SvdBlock* blocks, double* R) {
+  const SvdBlock b = blocks[blockIdx.y];
+  const int n = b.nn;
+  double* Rb = R + b.v_off;
+  const int64_t tot = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    if ((i >> 6) > (j >> 6)) Rb[e] = Rb[(int64_t)i * n + j];
+  }
 }
 
 // FP32 -> FP64 copy of V, per block
@@ -991,6 +1101,7 @@ static int panel_group(int ldp) {
   return B >= bmin ? B : 0;
 }
 
+// tol_pow: 1 or 1/2 (the panel kernel evaluates mm^tol_pow as mm or sqrt(mm))
 template <typename T>
 static nd_status run_panel_sweeps(nd_handle h, const std::vector<SvdBlock>& blocks, const SvdBlock* dblk, T* Wt,
                                   T* Vt, unsigned long long* offmax, unsigned int* bar, double tol, int max_sweeps,
@@ -1088,8 +1199,9 @@ static Mixed mixed1(int64_t dim, int64_t st0, int64_t st1) {
 //   kind 1: Vn (nn x nn) = alpha * V Y   + beta * Vn
 //   kind 2: W0 (mm x nn) = alpha * W Q   + beta * W0
 //   kind 3: S  (nn x nn) = alpha * W^T W + beta * S
-static nd_status block_gemm(nd_handle h, ExecCache& c, const std::vector<SvdBlock>& blocks, int kind, const double* A,
-                            const double* B, double* R, double alpha, double beta, int precision) {
+static nd_status block_gemm(nd_handle h, ExecCache& c, const std::vector<SvdBlock>& blocks, const SvdBlock* dblk,
+                            int kind, const double* A, const double* B, double* R, double alpha, double beta,
+                            int precision) {
   std::vector<PairDesc> pairs(blocks.size());
   for (size_t i = 0; i < blocks.size(); ++i) {
     const SvdBlock& b = blocks[i];
@@ -1108,8 +1220,20 @@ static nd_status block_gemm(nd_handle h, ExecCache& c, const std::vector<SvdBloc
     pd.ks = mixed1(K, a_k, 1);                       // A k stride, B k stride
     pairs[i] = pd;
   }
+  // R = V^T V and S = W^T W are symmetric: the FP64 tile kernel computes the 64 x 64 tiles
+  // on and above the diagonal, sym_mirror copies the others
+  const bool sym = (kind == 0 || kind == 3) && precision == ND_PREC_FP64;
+  if (sym)
+    for (auto& pd : pairs) pd.sym = 1;
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
-  return nd_execute_cached(h, c, pairs, (int)blocks.size(), ptrs, alpha, beta, precision);
+  nd_status st = nd_execute_cached(h, c, pairs, (int)blocks.size(), ptrs, alpha, beta, precision);
+  if (st || !sym) return st;
+  int64_t maxv = 1;
+  for (auto& b : blocks) maxv = std::max(maxv, (int64_t)b.nn * b.nn);
+  const dim3 gv((unsigned)std::min<int64_t>((maxv + 255) / 256, 1024), (unsigned)blocks.size());
+  sym_mirror<<<gv, 256, 0, h->stream>>>(dblk, R);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "sym_mirror");
 }
 
 static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_t* cols, const int64_t* offsets,
@@ -1230,9 +1354,9 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
         set_identity<<<gv, 256, 0, s>>>(dblk, Y);
         ND_LAUNCHED(h);
         nd_prof_begin(h, "svd_refine_gemm");
-        nd_status e = block_gemm(h, mode ? cR64 : cR, blocks, 0, V, V, Y, -1.0, 1.0, pr);             // R = I - X^T X
-        if (!e && mode < 2) e = block_gemm(h, mode ? cW64 : cW, blocks, 2, W, V, W0, 1.0, 0.0, pr);  // W0 = W X
-        if (!e && mode < 2) e = block_gemm(h, mode ? cS64 : cS, blocks, 3, W0, W0, S, 1.0, 0.0, pr); // S = W0^T W0
+        nd_status e = block_gemm(h, mode ? cR64 : cR, blocks, dblk, 0, V, V, Y, -1.0, 1.0, pr);             // R = I - X^T X
+        if (!e && mode < 2) e = block_gemm(h, mode ? cW64 : cW, blocks, dblk, 2, W, V, W0, 1.0, 0.0, pr);  // W0 = W X
+        if (!e && mode < 2) e = block_gemm(h, mode ? cS64 : cS, blocks, dblk, 3, W0, W0, S, 1.0, 0.0, pr); // S = W0^T W0
         nd_prof_end(h);
         if (e) return e;
         if ((e = nd_cuda_check(h, cudaMemsetAsync(emax, 0, 16, s), "svd refine"))) return e;
@@ -1244,8 +1368,8 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
         if (!e && mode) e = nd_cuda_check(h, cudaMemcpyAsync(W1, W0, woff * 8, cudaMemcpyDeviceToDevice, s), "svd copy");
         nd_prof_end(h);
         nd_prof_begin(h, "svd_refine_gemm");
-        if (!e) e = block_gemm(h, cV, blocks, 1, V, Y, Vn, 1.0, 1.0, ND_PREC_OZAKI);                 // X + X E
-        if (!e && mode) e = block_gemm(h, cWE, blocks, 2, W0, Y, W1, 1.0, 1.0, ND_PREC_OZAKI);       // W0 + W0 E
+        if (!e) e = block_gemm(h, cV, blocks, dblk, 1, V, Y, Vn, 1.0, 1.0, ND_PREC_OZAKI);                 // X + X E
+        if (!e && mode) e = block_gemm(h, cWE, blocks, dblk, 2, W0, Y, W1, 1.0, 1.0, ND_PREC_OZAKI);       // W0 + W0 E
         nd_prof_end(h);
         if (e) return e;
         std::swap(V, Vn);
@@ -1261,15 +1385,15 @@ static nd_status svd_core(nd_handle h, int nb, const int64_t* rows, const int64_
       };
       // split-GEMM steps while they still converge (their noise floor is ~1e-12 / gap)
       double prev = INFINITY;
-      for (int it = 0; it < 6 && !st; ++it) {
+      for (int it = 0; it < ND_SVD_SPLIT_STEPS && !st; ++it) {
         st = step(0);
-        if (!st && (em[0] <= 1e-10 || em[0] > 0.5 * prev)) break;
+        if (!st && (em[0] <= 1e-10 || (ND_SVD_SPLIT_STALL && em[0] > 0.5 * prev))) break;
         prev = em[0];
       }
       if (!st && ND_SVD_EXACT_STEP) st = step(1);
       // |E| <= 3e-8 leaves X orthogonal to 1e-15; otherwise Newton-Schulz (quadratic)
       for (int it = 0; it < 3 && !st && em[1] > 3e-8; ++it) st = step(2);
-      if (!st && !ND_SVD_EXACT_STEP) st = block_gemm(h, cW64, blocks, 2, W, V, W0, 1.0, 0.0, ND_PREC_FP64);
+      if (!st && !ND_SVD_EXACT_STEP) st = block_gemm(h, cW64, blocks, dblk, 2, W, V, W0, 1.0, 0.0, ND_PREC_FP64);
       if (!st) std::swap(W, W0);                                                                      // W <- W X
       h->ozaki_slices = saved;
       for (ExecCache* c : {&cR, &cW, &cS, &cV, &cR64, &cW64, &cS64, &cWE}) c->free_all(h);
