@@ -15,6 +15,10 @@
 #   rrule(contract, T1, labels1, T2, labels2, labelsR) on block-sparse
 #   storage, and the pullback contract_pullback_gb300 that
 #   rrule(contract, ::ITensor, ::ITensor) hands GB300 storage to  (ext/ITensorsChainRulesCoreExt/itensor.jl:94-103)
+#   contract(::BlockSparseTensor, ::DiagBlockSparseTensor)         (NDTensors/src/blocksparse/diagblocksparse.jl:601-696)
+#   eigen(::Hermitian{<:BlockSparseMatrix})                       (NDTensors/src/blocksparse/linearalgebra.jl:221-348)
+#   dot / norm / rmul! / axpby! on the storage vector, as reached by
+#   inner / norm / scale! / add!                                  (ext/ITensorsVectorInterfaceExt/ITensorsVectorInterfaceExt.jl:5-84)
 #
 # Fermionic sign fixes of the reference's svd (right_arrow_sign / left_arrow_sign) are
 # not applied: auto-fermion is off by default and this backend is bosonic (real FP64).
@@ -130,7 +134,7 @@ struct BsDesc
   offsets::Ptr{Int64}
 end
 
-function desc_arrays(T::BlockSparseTensor)
+function desc_arrays(T::Union{BlockSparseTensor,DiagBlockSparseTensor})
   is = inds(T)
   nb = Int32[NDTensors.nblocks(i) for i in is]
   bd = Int64[NDTensors.blockdim(i, b) for i in is for b in 1:NDTensors.nblocks(i)]
@@ -324,5 +328,118 @@ function ChainRulesCore.rrule(::typeof(NDTensors.contract), T1::GB300BlockSparse
   end
   return R, contract_pullback
 end
+
+# ---- BlockSparse x DiagBlockSparse (NDTensors/src/blocksparse/diagblocksparse.jl:601-696) ----
+# D is passed as its diagonals; one launch writes R (no dense expansion of D, no GEMM).
+const GB300DiagBlockSparseTensor = DiagBlockSparseTensor{Float64,N,<:NDTensors.DiagBlockSparse{Float64,<:GB300Vector}} where {N}
+
+function NDTensors.contract(T1::GB300BlockSparseTensor, labels1, T2::GB300DiagBlockSparseTensor, labels2,
+                            labelsR=contract_labels(labels1, labels2))
+  plan = bs_plan(T1, labels1, T2, labels2, labelsR)
+  np, nr, nnz = Ref{Int32}(0), Ref{Int32}(0), Ref{Int64}(0)
+  check(ccall((:nd_bs_plan_sizes, LIB), Int32, (Ptr{Cvoid}, Ref{Int32}, Ref{Int32}, Ref{Int64}), plan, np, nr, nnz))
+  NR = length(labelsR)
+  blocksR = Vector{Int32}(undef, max(1, nr[] * NR))
+  offsR = Vector{Int64}(undef, max(1, nr[]))
+  check(ccall((:nd_bs_plan_get, LIB), Int32, (Ptr{Cvoid}, Ptr{Int32}, Ptr{Int64}, Ptr{Int32}), plan, blocksR, offsR, C_NULL))
+  indsR = NDTensors.contract_inds(inds(T1), labels1, inds(T2), labels2, labelsR)
+  boffsR = BlockOffsets{NR}()
+  for k in 1:nr[]
+    insert!(boffsR, Block(ntuple(i -> UInt(blocksR[(k - 1) * NR + i]), NR)), offsR[k])
+  end
+  R = BlockSparseTensor(NDTensors.BlockSparse(GB300Vector(undef, nnz[]), boffsR), indsR)
+  diag_offs = Int64[NDTensors.offset(T2, b) for b in nzblocks(T2)]
+  st = np[] > 0 ? ccall((:nd_bs_contract_diag_f64, LIB), Int32,
+                        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int64}, Float64),
+                        handle(), plan, data(R).ptr, data(T1).ptr, data(T2).ptr, diag_offs, 1.0) : Int32(0)
+  ccall((:nd_bs_plan_destroy, LIB), Int32, (Ptr{Cvoid},), plan)
+  check(st)
+  return R
+end
+NDTensors.contract(T1::GB300DiagBlockSparseTensor, labels1, T2::GB300BlockSparseTensor, labels2,
+                   labelsR=contract_labels(labels1, labels2)) = NDTensors.contract(T2, labels2, T1, labels1, labelsR)
+
+# ---- blockwise Hermitian eigen (NDTensors/src/blocksparse/linearalgebra.jl:221-348) ----
+# One device call: every block's eigendecomposition, the pooled |lambda| sort,
+# truncate! and the kept dimensions; this method builds the reference's output
+# structure (D on (l, r), V on (dag(i2), r), blocks (n, n) and (b, n)).
+function LinearAlgebra.eigen(X::Union{Hermitian{Float64,<:GB300BlockSparseMatrix},GB300BlockSparseMatrix};
+                             min_blockdim=nothing, mindim=nothing, maxdim=nothing, cutoff=nothing,
+                             use_absolute_cutoff=nothing, use_relative_cutoff=nothing)
+  T = X isa Hermitian ? parent(X) : X
+  nzb, rows, cols, offs = matrix_blocks(T)
+  all(b -> b[1] == b[2], nzb) || error("Eigen currently only supports block diagonal matrices.")
+  nb = length(nzb)
+  D = GB300Vector(undef, sum(rows))
+  V = GB300Vector(undef, sum(rows .* rows))
+  kept = zeros(Int32, max(nb, 1))
+  spec = Vector{Float64}(undef, max(sum(rows), 1))
+  slen, terr, dcut = Ref{Int32}(0), Ref{Float64}(0), Ref{Float64}(0)
+  check(ccall((:nd_bs_eigen_f64, LIB), Int32,
+              (Ptr{Cvoid}, Int32, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32, Int32,
+               Float64, Int32, Int32, Int32, Ptr{Int32}, Ptr{Float64}, Ref{Int32}, Ref{Float64}, Ref{Float64}),
+              handle(), nb, rows, offs, data(T).ptr, D.ptr, V.ptr,
+              Int32(something(mindim, 1)), Int32(something(maxdim, -1)), Float64(something(cutoff, -1.0)),
+              Int32(something(use_absolute_cutoff, false)), Int32(something(use_relative_cutoff, true)),
+              Int32(something(min_blockdim, 0)), kept, spec, slen, terr, dcut))
+  surv = [n for n in 1:nb if kept[n] > 0]
+  i1, i2 = inds(T)
+  l = sim(i1)
+  deleteat!(l, setdiff(1:NDTensors.nblocks(l), Int[nzb[m][1] for m in surv]))
+  for (n, m) in enumerate(surv)
+    NDTensors.setblockdim!(l, Int(kept[m]), n)
+  end
+  r = dag(sim(l))
+  indsD, indsV = (l, r), (dag(i2), r)
+  nzblocksD = [Block(UInt(n), UInt(n)) for n in 1:length(surv)]
+  nzblocksV = [Block(nzb[m][1], UInt(n)) for (n, m) in enumerate(surv)]
+  # the library wrote the kept blocks in this order (V blocks column-major dims x kept)
+  bV, _ = NDTensors.blockoffsets(nzblocksV, indsV)
+  bD = BlockOffsets{2}()
+  o = 0
+  for (n, m) in enumerate(surv)
+    insert!(bD, nzblocksD[n], o)
+    o += Int(kept[m])
+  end
+  Dt = DiagBlockSparseTensor(NDTensors.DiagBlockSparse(D, bD), indsD)
+  Vt = BlockSparseTensor(NDTensors.BlockSparse(V, bV), indsV)
+  return Dt, Vt, Spectrum(spec[1:slen[]], terr[])
+end
+
+# ---- vector space (ext/ITensorsVectorInterfaceExt/ITensorsVectorInterfaceExt.jl:5-84) ----
+# inner / norm / scale! / add! of ITensors reach the storage as LinearAlgebra.dot, norm,
+# rmul! and axpby! on the data vector; each is one library launch (deterministic
+# reduction order), the scalar results come back to the host.
+const GB300Data = Union{GB300Vector,GB300View}
+
+function LinearAlgebra.dot(x::GB300Data, y::GB300Data)
+  length(x) == length(y) || throw(DimensionMismatch("dot: lengths $(length(x)) and $(length(y))"))
+  out = GB300Vector(undef, 1)
+  check(ccall((:nd_vec_inner_f64, LIB), Int32, (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+              handle(), length(x), x.ptr, y.ptr, out.ptr))
+  return Array(out)[1]
+end
+
+function LinearAlgebra.norm(x::GB300Data)
+  out = GB300Vector(undef, 1)
+  check(ccall((:nd_vec_norm_f64, LIB), Int32, (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Float64}),
+              handle(), length(x), x.ptr, out.ptr))
+  return Array(out)[1]
+end
+
+function LinearAlgebra.rmul!(x::GB300Data, a::Real)
+  check(ccall((:nd_vec_scale_f64, LIB), Int32, (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Float64}, Float64, Ptr{Float64}, Int32),
+              handle(), length(x), x.ptr, x.ptr, Float64(a), C_NULL, Int32(0)))
+  return x
+end
+
+function LinearAlgebra.axpby!(a::Real, x::GB300Data, b::Real, y::GB300Data)
+  length(x) == length(y) || throw(DimensionMismatch("axpby!: lengths $(length(x)) and $(length(y))"))
+  check(ccall((:nd_vec_add_f64, LIB), Int32, (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Float64}, Float64, Float64),
+              handle(), length(x), x.ptr, y.ptr, Float64(a), Float64(b)))
+  return y
+end
+
+LinearAlgebra.axpy!(a::Real, x::GB300Data, y::GB300Data) = LinearAlgebra.axpby!(a, x, 1.0, y)
 
 end # module
