@@ -98,6 +98,7 @@ bool nd_make_pair(const Roles& ro, const int64_t* dA, const int64_t* dB, const i
 
 static nd_status upload(nd_handle h, void** dst, const void* src, size_t bytes) {
   if (*dst) { cudaFreeAsync(*dst, h->stream); *dst = nullptr; }
+  if (!bytes) return ND_OK;                     // an empty list stays NULL (its kernels are not launched)
   nd_status s = nd_dalloc(h, dst, bytes);
   if (s) return s;
   return nd_upload(h, *dst, src, bytes);
@@ -108,7 +109,10 @@ static nd_status upload(nd_handle h, void** dst, const void* src, size_t bytes) 
 template <class Pick>
 static void make_items(const std::vector<PairDesc>& pairs, int bm, int bn, Pick pick, std::vector<WorkItem>& items) {
   items.clear();
-  std::vector<std::pair<int64_t, WorkItem>> tmp;
+  // groups longest first (work of a full tile; ties in group order), each expanded into
+  // its tiles; the order only steers the schedule, every tile's result is the same
+  struct Grp { int64_t cost; size_t i, n; };
+  std::vector<Grp> grps;
   for (size_t i = 0; i < pairs.size();) {
     size_t j = i;
     int64_t ksum = 0;
@@ -120,18 +124,21 @@ static void make_items(const std::vector<PairDesc>& pairs, int bm, int bn, Pick 
     }
     if (all) {
       const PairDesc& p = pairs[i];
-      int mt = (p.M + bm - 1) / bm, nt = (p.N + bn - 1) / bn;
-      for (int a = 0; a < mt; ++a)
-        for (int b = 0; b < nt; ++b) {
-          if (p.sym && bm == bn && a > b) continue;      // below the diagonal of a symmetric R
-          int64_t mm = std::min(bm, p.M - a * bm), nn = std::min(bn, p.N - b * bn);
-          tmp.push_back({mm * nn * std::max<int64_t>(ksum, 1), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
-        }
+      const int64_t mm = std::min(bm, p.M), nn = std::min(bn, p.N);
+      grps.push_back({mm * nn * std::max<int64_t>(ksum, 1), i, j - i});
     }
     i = j;
   }
-  std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
-  for (auto& t : tmp) items.push_back(t.second);
+  std::stable_sort(grps.begin(), grps.end(), [](const Grp& x, const Grp& y) { return x.cost > y.cost; });
+  for (const Grp& g : grps) {
+    const PairDesc& p = pairs[g.i];
+    const int mt = (p.M + bm - 1) / bm, nt = (p.N + bn - 1) / bn;
+    for (int a = 0; a < mt; ++a)
+      for (int b = 0; b < nt; ++b) {
+        if (p.sym && bm == bn && a > b) continue;        // below the diagonal of a symmetric R
+        items.push_back(WorkItem{p.group, (int)g.i, (int)g.n, a, b});
+      }
+  }
 }
 
 // Split-K for the FP64 tile kernel.  The launch's work is measured in k-steps
@@ -198,16 +205,20 @@ static nd_status build_exec(nd_handle h, ExecCache& c, const std::vector<PairDes
   c.precision = precision;
   c.slices = slices;
   c.req_pair2 = h->split_pair2;
-  nd_status s = upload(h, (void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc));
-  if (s) return s;
   // which pairs sit in skinny groups (routed to the FP64 CUDA-core kernel)
   std::vector<char> sk(pairs.size(), 0);
+  bool any_sk = false;
   for (size_t i = 0; i < pairs.size();) {
     size_t j = i;
     const bool g = tc.skinny && group_skinny(pairs, i);
+    any_sk = any_sk || g;
     while (j < pairs.size() && pairs[j].group == pairs[i].group && pairs[j].job == pairs[i].job) sk[j++] = g;
     i = j;
   }
+  nd_status s = ND_OK;
+  // the FP64 kernels read the pair list; the split-precision path uploads its own copy
+  if (precision == ND_PREC_FP64 || any_sk)
+    if ((s = upload(h, (void**)&c.d_pairs, pairs.data(), pairs.size() * sizeof(PairDesc)))) return s;
   std::vector<WorkItem> items;
   make_items(pairs, nd_skinny_rows(), 1 << 30, [&](const PairDesc& p) { return sk[&p - pairs.data()] != 0; }, items);
   c.nsk_items = (int)items.size();

@@ -50,6 +50,7 @@
 #include <cuda_bf16.h>
 #include <algorithm>
 #include <map>
+#include <unordered_map>
 
 namespace {
 
@@ -1149,29 +1150,56 @@ nd_status launch_gemm2(nd_handle h, const GemmArgs& g, int slots) {
 // least-loaded of G = min(#items, SMs) CTAs, and laid out so that the kernels'
 // stride-G walk (item = blockIdx.x + r G) visits exactly each CTA's list; shorter
 // lists are padded with empty items (pair_count 0), which every role skips.
-std::vector<WorkItem> balance_items(std::vector<std::pair<int64_t, WorkItem>> tmp, int num_slots, int* slots_out) {
-  std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+// tmp must be sorted longest first (ties in list order).
+std::vector<WorkItem> balance_items(const std::vector<std::pair<int64_t, WorkItem>>& tmp, int num_slots, int* slots_out) {
   std::vector<WorkItem> items;
   if (slots_out) *slots_out = 0;
   if (tmp.empty()) return items;
   const int G = std::max(1, std::min((int)tmp.size(), num_slots));
   if (slots_out) *slots_out = G;
-  std::vector<std::vector<WorkItem>> lists(G);
-  std::vector<std::pair<int64_t, int>> heap;
-  for (int b = 0; b < G; ++b) heap.push_back({0, b});
+  // Longest processing time first: each tile to the least-loaded slot (ties: lowest
+  // index).  Tiles come in runs of equal cost c.  While every load lies within c of the
+  // smallest, LPT gives G consecutive tiles of a run to the slots in (load, index) order
+  // and keeps that order, so such a run is assigned in O(n) and the order repaired once
+  // (a merge); otherwise the run goes tile by tile through a heap.
+  std::vector<int> slot_of(tmp.size()), count(G, 0);
+  std::vector<std::pair<int64_t, int>> order(G);                 // (load, slot), ascending
+  for (int b = 0; b < G; ++b) order[b] = {0, b};
   auto later = [](const auto& x, const auto& y) { return x.first > y.first || (x.first == y.first && x.second > y.second); };
-  std::make_heap(heap.begin(), heap.end(), later);
-  for (auto& t : tmp) {
-    std::pop_heap(heap.begin(), heap.end(), later);
-    lists[heap.back().second].push_back(t.second);
-    heap.back().first += t.first;
-    std::push_heap(heap.begin(), heap.end(), later);
+  for (size_t t0 = 0; t0 < tmp.size();) {
+    size_t t1 = t0;
+    while (t1 < tmp.size() && tmp[t1].first == tmp[t0].first) ++t1;
+    const int64_t c = tmp[t0].first;
+    if (order.back().first - order.front().first < c) {
+      const size_t n = t1 - t0, q = n / G, r = n % G;
+      for (size_t t = t0; t < t1; ++t) {
+        const int b = order[(t - t0) % G].second;
+        slot_of[t] = b;
+        ++count[b];
+      }
+      for (int k = 0; k < G; ++k) order[k].first += (int64_t)q * c + ((size_t)k < r ? c : 0);
+      std::inplace_merge(order.begin(), order.begin() + r, order.end());
+    } else {
+      std::make_heap(order.begin(), order.end(), later);
+      for (size_t t = t0; t < t1; ++t) {
+        std::pop_heap(order.begin(), order.end(), later);
+        slot_of[t] = order.back().second;
+        ++count[order.back().second];
+        order.back().first += c;
+        std::push_heap(order.begin(), order.end(), later);
+      }
+      std::sort(order.begin(), order.end());
+    }
+    t0 = t1;
   }
-  size_t L = 0;
-  for (auto& l : lists) L = std::max(L, l.size());
+  const int L = *std::max_element(count.begin(), count.end());
   const WorkItem empty{tmp[0].second.group, tmp[0].second.pair_begin, 0, 0, 0};
-  for (size_t r = 0; r < L; ++r)
-    for (int b = 0; b < G; ++b) items.push_back(r < lists[b].size() ? lists[b][r] : empty);
+  items.assign((size_t)L * G, empty);
+  std::fill(count.begin(), count.end(), 0);
+  for (size_t t = 0; t < tmp.size(); ++t) {      // slot b's r-th item sits at r * G + b
+    const int b = slot_of[t];
+    items[(size_t)count[b]++ * G + b] = tmp[t].second;
+  }
   return items;
 }
 
@@ -1204,14 +1232,18 @@ static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int
   L = SplitLayout{};
   L.pair2 = pair2 ? 1 : 0;
   L.pairs = pairs_in;
-  std::map<std::pair<int, int64_t>, int> amap, bmap;   // (job, offset) -> op
+  // (job, offset) -> op, ids in first-appearance order
+  std::unordered_map<uint64_t, int> amap, bmap;
+  amap.reserve(pairs_in.size());
+  bmap.reserve(pairs_in.size());
   auto add_op = [&](bool is_b, const PairDesc& pd) -> int {
     auto& mp = is_b ? bmap : amap;
-    auto key = std::make_pair(pd.job, is_b ? pd.b_off : pd.a_off);
+    const int64_t off = is_b ? pd.b_off : pd.a_off;
+    const uint64_t key = ((uint64_t)off << 1) | (uint64_t)(pd.job & 1);   // offsets < 2^62, job 0 / 1
     auto f = mp.find(key);
     if (f != mp.end()) return f->second;
     SplitOp o{};
-    o.src_off = key.second;
+    o.src_off = off;
     o.is_b = is_b;
     o.job = pd.job;
     o.rows = is_b ? pd.N : pd.M;
@@ -1240,8 +1272,11 @@ static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int
   for (int i = 0; i < (int)L.ops.size(); ++i)
     for (int t = 0; t < L.ops[i].row_tiles; ++t)
       for (int kc = 0; kc * PACK_KC < L.ops[i].k_steps; ++kc) L.pitems.push_back({i, t, kc});
-  // work items: BM x BN output tiles, balanced over the persistent CTAs
-  std::vector<std::pair<int64_t, WorkItem>> tmp;
+  // work items: BM x BN output tiles, balanced over the persistent CTAs.  Every tile of
+  // a group costs the same, so the groups are sorted (longest first, ties in group
+  // order) and expanded into tiles: the order a stable sort of the tiles would give.
+  struct Grp { int64_t cost; size_t i, n; };
+  std::vector<Grp> grps;
   for (size_t i = 0; i < L.pairs.size();) {
     size_t j = i;
     int64_t ksteps = 0;
@@ -1249,14 +1284,18 @@ static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int
       ksteps += (L.pairs[j].K + BK - 1) / BK;
       ++j;
     }
-    const PairDesc& p = L.pairs[i];
+    grps.push_back({tile_cost(ksteps, (int)(j - i)), i, j - i});
+    i = j;
+  }
+  std::stable_sort(grps.begin(), grps.end(), [](const Grp& x, const Grp& y) { return x.cost > y.cost; });
+  std::vector<std::pair<int64_t, WorkItem>> tmp;
+  for (const Grp& g : grps) {
+    const PairDesc& p = L.pairs[g.i];
     int mt = (p.M + BM - 1) / BM;
     const int nt = (p.N + BN - 1) / BN;
     if (L.pair2) mt = (mt + 1) / 2;
     for (int a = 0; a < mt; ++a)
-      for (int b = 0; b < nt; ++b)
-        tmp.push_back({tile_cost(ksteps, (int)(j - i)), WorkItem{p.group, (int)i, (int)(j - i), a, b}});
-    i = j;
+      for (int b = 0; b < nt; ++b) tmp.push_back({g.cost, WorkItem{p.group, (int)g.i, (int)g.n, a, b}});
   }
   int nslots = h->num_sms;
   if (L.pair2) {
@@ -1267,7 +1306,7 @@ static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int
       return;
     }
   }
-  L.items = balance_items(std::move(tmp), nslots, &L.slots);
+  L.items = balance_items(tmp, nslots, &L.slots);
 }
 
 static void split_adopt(ExecCache& c, const SplitLayout& L, int S) {

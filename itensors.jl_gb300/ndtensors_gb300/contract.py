@@ -91,6 +91,7 @@ class ContractionPlan:
 
     def __init__(self, T1: BlockSparseTensor, l1, T2: BlockSparseTensor, l2, lr):
         self.l1, self.l2, self.lr = tuple(l1), tuple(l2), tuple(lr)
+        self._custom_offsets = None
         if len(self.l1) != T1.rank or len(self.l2) != T2.rank:
             raise ValueError("contract: number of labels does not match the tensor ranks")
         self.h = handle(T1.data.device.index or 0)
@@ -108,14 +109,23 @@ class ContractionPlan:
         P32, P64 = C.POINTER(C.c_int32), C.POINTER(C.c_int64)
         self.h._check(self.h.lib.nd_bs_plan_get(self.ptr, br.ctypes.data_as(P32), of.ctypes.data_as(P64),
                                                 self._pairs_raw.ctypes.data_as(P32)))
-        self.blocksR = list(map(tuple, br[:self.nblocksR * rank].reshape(self.nblocksR, rank).tolist()))
-        self.offsetsR = of[:self.nblocksR].tolist()
+        self._br = br[:self.nblocksR * rank].copy()         # kept as arrays: the output's descriptor
+        self._of = of[:self.nblocksR].copy()
+        self.blocksR = list(map(tuple, self._br.reshape(self.nblocksR, rank).tolist()))
+        self.offsetsR = self._of.tolist()
         self._pairs = None
         self.indsR = [tuple(T1.inds[self.l1.index(l)]) if l in self.l1 else tuple(T2.inds[self.l2.index(l)])
                       for l in self.lr]
-        self.T1_key, self.T2_key = T1.structure_key(), T2.structure_key()
         from ._lib import _live_plans
         _live_plans.add(self)
+
+    def output(self, data):
+        """The output tensor on `data` (a flat device vector of nnzR), with its C-ABI
+        descriptor built from the plan's arrays."""
+        R = BlockSparseTensor(list(self.indsR), list(self.blocksR), list(self.offsetsR), data)
+        if self._custom_offsets is None:
+            R.set_desc_arrays(self._br, self._of)
+        return R
 
     def pair_shapes(self, T1, T2):
         """(M, N, K, output block) of every block pair, in plan order."""
@@ -152,6 +162,7 @@ class ContractionPlan:
             raise ValueError("set_output_offsets: one offset per output block")
         self.h._check(self.h.lib.nd_bs_plan_set_output_offsets(self.ptr, i64arr(offs)))
         self.offsetsR = offs
+        self._custom_offsets = offs
 
     def flops(self, T1, T2):
         return sum(2 * m * n * k for (m, n, k, _) in self.pair_shapes(T1, T2))
@@ -192,7 +203,7 @@ def contract_blocksparse(T1, l1, T2, l2, lr=None, alpha=1.0, precision="fp64", p
     if R is None:
         import torch
         data = torch.empty(max(plan.nnzR, 1), dtype=torch.float64, device=T1.data.device)[:plan.nnzR]
-        R = BlockSparseTensor(list(plan.indsR), list(plan.blocksR), list(plan.offsetsR), data)
+        R = plan.output(data)
     if plan.npairs:
         handle(T1.data.device.index or 0)          # bind the handle to torch's current stream
         plan.h.call("nd_bs_contract_f64", plan.ptr, C.c_void_p(R.data.data_ptr()), C.c_void_p(T1.data.data_ptr()),

@@ -131,6 +131,21 @@ class BlockSparseTensor:
         n = _prod(d)
         return self.data[self.offsets[i]:self.offsets[i] + n]
 
+    def set_desc_arrays(self, blocks, offsets):
+        """Build the C-ABI descriptor from block and offset arrays the caller already has
+        (int32 rank-major block numbers, int64 offsets) instead of from the lists."""
+        import ctypes as C
+        from ._lib import BsDesc
+        nb = np.array([len(i) for i in self.inds], dtype=np.int32)
+        bd = np.array([d for i in self.inds for d in i], dtype=np.int64)
+        bl = np.ascontiguousarray(blocks, dtype=np.int32) if len(self.blocks) else np.zeros(1, np.int32)
+        of = np.ascontiguousarray(offsets, dtype=np.int64) if len(self.offsets) else np.zeros(1, np.int64)
+        P32, P64 = C.POINTER(C.c_int32), C.POINTER(C.c_int64)
+        d = BsDesc(self.rank, nb.ctypes.data_as(P32), bd.ctypes.data_as(P64), len(self.blocks),
+                   bl.ctypes.data_as(P32), of.ctypes.data_as(P64))
+        d._keep = (nb, bd, bl, of)
+        self._desc = d
+
     def desc(self):
         """nd_bs_desc for the C ABI (arrays built once per tensor and kept on it)."""
         import ctypes as C
