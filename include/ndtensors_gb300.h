@@ -239,6 +239,28 @@ nd_status nd_bs_svd_f64(nd_handle h, int32_t nblocks, const int64_t *rows, const
                         int32_t *kept, double *spectrum, int32_t *spectrum_len,
                         double *truncerr, double *docut);
 
+/* Blockwise SVD plan (no counterpart in the reference): the blockwise truncated SVD
+ * of nd_bs_svd_f64 for fixed block dimensions (block b is rows[b] x cols[b]), with
+ * every buffer and launch state built at creation (creation runs the SVD once on
+ * zeros and synchronises), fixed sweep and refinement counts, and convergence, kept
+ * dimensions, spectrum and truncation error left in DEVICE memory.  An execution only
+ * enqueues work on the handle's stream, so it can be captured into a CUDA graph (for
+ * example with the Krylov loop of a sweep step).  Outputs: U, S, V as nd_bs_svd_f64
+ * (kept prefixes concatenated in block order; size them for the untruncated case),
+ * kept[nblocks], spectrum[sum of min(rows, cols)] (the first *spectrum_len entries are
+ * the truncated pooled s^2, descending), truncerr[1], status[1] = ND_OK or
+ * ND_ERR_NOCONV (all device).  offsets: host, the blocks' offsets in A (a change is
+ * uploaded, which is refused during capture).  Blocks taller than a shared-memory
+ * panel (3200 rows in FP64) give ND_ERR_UNSUPPORTED at creation. */
+typedef struct nd_svd_plan_s *nd_svd_plan;
+nd_status nd_bs_svd_plan_create(nd_handle h, int32_t nblocks, const int64_t *rows, const int64_t *cols,
+                                nd_svd_plan *plan);
+nd_status nd_bs_svd_plan_exec(nd_svd_plan plan, const int64_t *offsets, const double *A, double *U, double *S,
+                              double *V, int32_t mindim, int32_t maxdim, double cutoff, int32_t use_absolute_cutoff,
+                              int32_t use_relative_cutoff, int32_t min_blockdim, int32_t *kept, double *spectrum,
+                              int32_t *spectrum_len, double *truncerr, int32_t *status);
+nd_status nd_bs_svd_plan_destroy(nd_svd_plan plan);
+
 /* Blockwise eigendecomposition of a real symmetric block-diagonal matrix with
  * truncation (eigen(::Hermitian{<:BlockSparseMatrix}), NDTensors/src/blocksparse/
  * linearalgebra.jl:221-348; per block the dense Hermitian eigen sorted by |lambda|

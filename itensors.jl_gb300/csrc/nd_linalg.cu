@@ -575,6 +575,7 @@ struct BjArgs {
   double tol;        // pairs with |w_p . w_q| <= min(tol * mm^tol_pow, tol_cap) |w_p||w_q| are left
   double tol_pow;
   double tol_cap;
+  const int32_t* active;   // optional: per block, 0 once converged (its tasks are skipped)
 };
 
 // 16-byte vectors of the panel element type: a lane handles VW consecutive rows.
@@ -735,6 +736,7 @@ __global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
       const int t = w * (int)gridDim.x + ((w & 1) ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x);
       if (t >= a.ntasks) break;
       const BjTask tk = a.tasks[t];
+      if (a.active && !a.active[tk.block]) continue;
       const SvdBlock b = a.blocks[tk.block];
       const int nblk = (b.nn + B - 1) / B, nbp = nblk + (nblk & 1);
       if (r >= nbp - 1) continue;
@@ -1074,13 +1076,22 @@ template <typename T, int B>
 static nd_status launch_bj(nd_handle h, const BjArgs<T>& a, size_t smem) {
   static size_t attr = 0;   // dynamic shared memory this instantiation is opted in to
   if (smem > attr) {
+    if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd panel sweep: run once before graph capture");
     nd_status st = nd_cuda_check(h, cudaFuncSetAttribute(bj_sweep<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                          (int)smem), "svd panel sweep shared memory");
     if (st) return st;
     attr = smem;
   }
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bj_sweep<T, B>, 32 * B, smem);
+  // resident CTAs per SM, queried once per shared-memory size (no query while capturing)
+  static size_t occ_smem = 0;
+  static int occ = 0;
+  if (smem != occ_smem) {
+    if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd panel sweep: run once before graph capture");
+    occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bj_sweep<T, B>, 32 * B, smem);
+    occ_smem = smem;
+  }
+  const int per_sm = occ;
   if (per_sm < 1) return nd_fail(h, ND_ERR_UNSUPPORTED, "svd panel sweep does not fit an SM");
   const int grid = std::max(1, std::min(a.ntasks, per_sm * h->num_sms));
   BjArgs<T> args = a;
@@ -1147,7 +1158,7 @@ static nd_status run_panel_sweeps(nd_handle h, const std::vector<SvdBlock>& bloc
     if ((st = nd_upload(h, dtasks, tasks.data(), tasks.size() * sizeof(BjTask)))) break;
     if ((st = nd_cuda_check(h, cudaMemsetAsync(offmax, 0, nb * 8, s), "svd sweep set-up"))) break;
     BjArgs<T> a{dblk, dtasks, (int)tasks.size(), nrounds, ldp, Wt, Vt, offmax, bar, bar + 1, h->d_status, tol, tol_pow,
-                tol_cap};
+                tol_cap, nullptr};
     nd_prof_begin(h, name);
     if constexpr (sizeof(T) == 4) {
       if (B == 16) st = launch_bj<T, 16>(h, a, smem);
@@ -1642,6 +1653,387 @@ extern "C" nd_status nd_bs_eigen_f64(nd_handle h, int32_t nb, const int64_t* dim
   if (e != cudaSuccess) return nd_cuda_check(h, e, "eigen outputs");
   ND_CUDA(h, cudaStreamSynchronize(s));
   return nd_check_device_status(h, "eigen");
+}
+
+// ---------------------------------------------------------------------------
+// Blockwise SVD plan: the same three stages for fixed block dimensions, with every
+// buffer, task table and GEMM launch state built once, fixed sweep and refinement
+// counts, convergence tracked per block on the device and the kept dimensions,
+// spectrum and truncation error left in device memory: an execution enqueues work
+// only, so it can be captured into a CUDA graph with the Krylov loop of a sweep step.
+// ---------------------------------------------------------------------------
+namespace {
+
+// after a sweep: a block whose sweep rotated nothing is done; reset the sweep maxima
+__global__ void svd_active_update(int nb, unsigned long long* offmax, int32_t* active) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  if (offmax[b] == 0ull) active[b] = 0;
+  offmax[b] = 0ull;
+}
+
+__global__ void svd_fill_i32(int n, int32_t* x, int32_t v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = v;
+}
+
+// status = ND_ERR_NOCONV when a block still rotated in the last FP64 sweep
+__global__ void svd_noconv_status(int nb, const int32_t* active, int32_t* status) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    if (active[b]) any = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) *status = any ? ND_ERR_NOCONV : ND_OK;
+}
+
+// kept prefixes of U (m x k), S (k) and V (n x k) of every block, concatenated in block
+// order (blocks with kept 0 take no space); one CTA row per block
+__global__ void svd_compact(const SvdBlock* blocks, int nb, const int32_t* kept, const double* Uf, const double* Vf,
+                            const int64_t* uo, const int64_t* vo, const double* sig, double* U, double* S, double* V) {
+  const int bi = blockIdx.y;
+  __shared__ int64_t off[3];
+  if (threadIdx.x == 0) {
+    int64_t cu = 0, cs = 0, cv = 0;
+    for (int j = 0; j < bi; ++j) {
+      const int k = kept[j];
+      cu += (int64_t)blocks[j].m * k;
+      cs += k;
+      cv += (int64_t)blocks[j].n * k;
+    }
+    off[0] = cu; off[1] = cs; off[2] = cv;
+  }
+  __syncthreads();
+  const SvdBlock b = blocks[bi];
+  const int k = kept[bi];
+  const int64_t nu = (int64_t)b.m * k, nv = (int64_t)b.n * k;
+  const int64_t str = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nu; e += str) U[off[0] + e] = Uf[uo[bi] + e];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nv; e += str) V[off[2] + e] = Vf[vo[bi] + e];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < k; e += str) S[off[1] + e] = sig[b.s_off + e];
+}
+
+}  // namespace
+
+struct nd_svd_plan_s {
+  nd_handle h = nullptr;
+  int nb = 0, total = 0, npow2 = 1, maxn = 1;
+  bool big = false;
+  int n32 = 0, n64 = 0;                       // fixed sweep counts
+  int64_t woff = 0, voff = 0, ut = 0, vt = 0;
+  std::vector<SvdBlock> blocks;
+  SvdBlock* dblk = nullptr;
+  // panel sweeps: group sizes, shared memory, task tables (all blocks, longest first)
+  int B32 = 0, B64 = 0, ldp = 0, nrounds32 = 0, nrounds64 = 0, ntasks32 = 0, ntasks64 = 0;
+  size_t smem32 = 0, smem64 = 0;
+  BjTask *tasks32 = nullptr, *tasks64 = nullptr;
+  // work buffers
+  double *W = nullptr, *V = nullptr, *sig = nullptr, *Y = nullptr, *Vn = nullptr, *W0 = nullptr, *W1 = nullptr,
+         *S = nullptr, *Uf = nullptr, *Vf = nullptr, *P = nullptr, *res = nullptr, *Wsrc = nullptr;
+  float *W32 = nullptr, *V32 = nullptr;
+  int32_t *order = nullptr, *active = nullptr, *dkept = nullptr;
+  int* dlen = nullptr;
+  unsigned long long *offmax = nullptr, *bmax = nullptr, *emax = nullptr;
+  unsigned int* bar = nullptr;
+  int64_t *duo = nullptr, *dvo = nullptr;
+  ExecCache cR, cW, cS, cV, cR64, cW64, cS64, cWE;
+  void release();
+};
+
+void nd_svd_plan_s::release() {
+  if (!h) return;
+  for (ExecCache* c : {&cR, &cW, &cS, &cV, &cR64, &cW64, &cS64, &cWE}) c->free_all(h);
+  for (void* q : {(void*)dblk, (void*)tasks32, (void*)tasks64, (void*)W, (void*)V, (void*)sig, (void*)Y, (void*)Vn,
+                  (void*)W0, (void*)W1, (void*)S, (void*)Uf, (void*)Vf, (void*)P, (void*)res, (void*)Wsrc, (void*)W32,
+                  (void*)V32, (void*)order, (void*)active, (void*)dkept, (void*)dlen, (void*)offmax, (void*)bmax,
+                  (void*)emax, (void*)bar, (void*)duo, (void*)dvo})
+    if (q) cudaFreeAsync(q, h->stream);
+}
+
+namespace {
+
+template <typename T>
+nd_status plan_sweeps(nd_svd_plan p, T* Wt, T* Vt, int nsweeps, double tol, double tol_pow, double tol_cap) {
+  nd_handle h = p->h;
+  const bool f32 = sizeof(T) == 4;
+  const int B = f32 ? p->B32 : p->B64;
+  BjArgs<T> a{p->dblk, f32 ? p->tasks32 : p->tasks64, f32 ? p->ntasks32 : p->ntasks64,
+              f32 ? p->nrounds32 : p->nrounds64, p->ldp, Wt, Vt, p->offmax, p->bar, p->bar + 1, h->d_status,
+              tol, tol_pow, tol_cap, p->active};
+  const size_t smem = f32 ? p->smem32 : p->smem64;
+  const int gb = (p->nb + 127) / 128;
+  ND_CUDA(h, cudaMemsetAsync(p->offmax, 0, p->nb * 8, h->stream));
+  svd_fill_i32<<<gb, 128, 0, h->stream>>>(p->nb, p->active, 1);
+  ND_LAUNCHED(h);
+  for (int sw = 0; sw < nsweeps; ++sw) {
+    nd_status st;
+    nd_prof_begin(h, f32 ? "svd_panel_sweep_f32" : "svd_panel_sweep");
+    if constexpr (sizeof(T) == 4) {
+      st = B == 16 ? launch_bj<T, 16>(h, a, smem) : B == 8 ? launch_bj<T, 8>(h, a, smem) : launch_bj<T, 4>(h, a, smem);
+    } else {
+      st = B == 8 ? launch_bj<T, 8>(h, a, smem) : B == 4 ? launch_bj<T, 4>(h, a, smem) : launch_bj<T, 2>(h, a, smem);
+    }
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    if (st) return st;
+    svd_active_update<<<gb, 128, 0, h->stream>>>(p->nb, p->offmax, p->active);
+    ND_LAUNCHED(h);
+  }
+  return nd_cuda_check(h, cudaGetLastError(), "svd plan sweeps");
+}
+
+// The whole SVD of A (blocks at the plan's offsets) into the plan's buffers; no host
+// synchronisation.  status (device) receives ND_OK or ND_ERR_NOCONV.
+nd_status plan_run(nd_svd_plan p, const double* A, const TruncParams& tp, int min_blockdim, bool trunc,
+                   int32_t* status) {
+  nd_handle h = p->h;
+  cudaStream_t s = h->stream;
+  const int nb = p->nb;
+  double *W = p->W, *V = p->V, *Vn = p->Vn, *W0 = p->W0, *W1 = p->W1;
+  int64_t maxe = 1, maxv = 1;
+  for (auto& b : p->blocks) { maxe = std::max(maxe, (int64_t)b.mm * b.nn); maxv = std::max(maxv, (int64_t)b.nn * b.nn); }
+  const dim3 ge((unsigned)std::min<int64_t>((maxe + 255) / 256, 1024), nb);
+  const dim3 gv((unsigned)std::min<int64_t>((maxv + 255) / 256, 1024), nb);
+  nd_prof_begin(h, "svd_init");
+  svd_init<<<ge, 256, 0, s>>>(p->dblk, nb, A, W, V);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  nd_status st = ND_OK;
+  if (p->big) {
+    ND_CUDA(h, cudaMemsetAsync(p->bmax, 0, nb * 8, s));
+    block_absmax<<<ge, 256, 0, s>>>(p->dblk, W, p->bmax);
+    to_f32_scaled<<<ge, 256, 0, s>>>(p->dblk, W, p->bmax, p->W32, p->V32);
+    ND_LAUNCHED(h);
+    ND_LAUNCHED(h);
+    if ((st = plan_sweeps<float>(p, p->W32, p->V32, p->n32, ND_SVD_TOL32, ND_SVD_TOL32_POW, INFINITY))) return st;
+    v_to_f64<<<gv, 256, 0, s>>>(p->dblk, p->V32, V);
+    ND_LAUNCHED(h);
+    const int saved = h->ozaki_slices;
+    h->ozaki_slices = 6;
+    // fixed refinement: ND_SVD_SPLIT_STEPS split-GEMM steps, one FP64 step, one Newton-Schulz step
+    for (int it = 0; it < ND_SVD_SPLIT_STEPS + 2 && !st; ++it) {
+      const int mode = it < ND_SVD_SPLIT_STEPS ? 0 : it == ND_SVD_SPLIT_STEPS ? 1 : 2;
+      const int pr = mode ? ND_PREC_FP64 : ND_PREC_OZAKI;
+      set_identity<<<gv, 256, 0, s>>>(p->dblk, p->Y);
+      ND_LAUNCHED(h);
+      nd_prof_begin(h, "svd_refine_gemm");
+      st = block_gemm(h, mode ? p->cR64 : p->cR, p->blocks, p->dblk, 0, V, V, p->Y, -1.0, 1.0, pr);
+      if (!st && mode < 2) st = block_gemm(h, mode ? p->cW64 : p->cW, p->blocks, p->dblk, 2, W, V, W0, 1.0, 0.0, pr);
+      if (!st && mode < 2) st = block_gemm(h, mode ? p->cS64 : p->cS, p->blocks, p->dblk, 3, W0, W0, p->S, 1.0, 0.0, pr);
+      nd_prof_end(h);
+      if (st) break;
+      const double tau = mode == 0 ? OA_TAU : mode == 1 ? OA_TAU_FP64 : -1.0;
+      nd_prof_begin(h, "svd_refine");
+      oa_correction<<<gv, 256, 0, s>>>(p->dblk, p->S, p->Y, tau, p->emax);
+      ND_LAUNCHED(h);
+      st = nd_cuda_check(h, cudaMemcpyAsync(Vn, V, p->voff * 8, cudaMemcpyDeviceToDevice, s), "svd copy");
+      if (!st && mode) st = nd_cuda_check(h, cudaMemcpyAsync(W1, W0, p->woff * 8, cudaMemcpyDeviceToDevice, s), "svd copy");
+      nd_prof_end(h);
+      nd_prof_begin(h, "svd_refine_gemm");
+      if (!st) st = block_gemm(h, p->cV, p->blocks, p->dblk, 1, V, p->Y, Vn, 1.0, 1.0, ND_PREC_OZAKI);
+      if (!st && mode) st = block_gemm(h, p->cWE, p->blocks, p->dblk, 2, W0, p->Y, W1, 1.0, 1.0, ND_PREC_OZAKI);
+      nd_prof_end(h);
+      if (st) break;
+      std::swap(V, Vn);
+      if (mode) std::swap(W0, W1);
+    }
+    h->ozaki_slices = saved;
+    if (st) return st;
+    W = W0;                                            // W X
+  }
+  if ((st = plan_sweeps<double>(p, W, V, p->n64, ND_SVD_TOL64, ND_SVD_TOL64_POW, ND_SVD_TOL64_CAP))) return st;
+  svd_noconv_status<<<1, 256, 0, s>>>(nb, p->active, status);
+  ND_LAUNCHED(h);
+  nd_prof_begin(h, "svd_finish");
+  svd_finish<<<nb, 256, p->maxn * 8, s>>>(p->dblk, W, p->sig, p->order);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  {
+    dim3 grid((unsigned)std::min<int64_t>((maxe + 255) / 256, 1024), nb);
+    nd_prof_begin(h, "svd_outputs");
+    svd_outputs<<<grid, 256, 0, s>>>(p->dblk, W, V, p->sig, p->order, p->Uf, p->Vf, p->duo, p->dvo);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+  }
+  nd_prof_begin(h, "sort_truncate");
+  sort_truncate<<<1, 1024, p->npow2 * 8, s>>>(p->sig, p->total, p->npow2, 1, 1, tp, p->P, p->dlen, p->res, p->res + 1);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  kept_dims<<<(nb + 127) / 128, 128, 0, s>>>(p->dblk, nb, p->sig, p->res + 1, min_blockdim < 0 ? 0 : min_blockdim,
+                                             trunc ? 1 : 0, p->dkept);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "svd plan");
+}
+
+}  // namespace
+
+extern "C" nd_status nd_bs_svd_plan_create(nd_handle h, int32_t nb, const int64_t* rows, const int64_t* cols,
+                                           nd_svd_plan* out) {
+  if (!h || !out) return ND_ERR_ARG;
+  *out = nullptr;
+  if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd plan: create it before graph capture");
+  if (nb <= 0 || !rows || !cols) return nd_fail(h, ND_ERR_ARG, "svd plan: need at least one block");
+  cudaStream_t s = h->stream;
+  auto p = new nd_svd_plan_s;
+  p->h = h;
+  p->nb = nb;
+  p->blocks.resize(nb);
+  int maxmm = 1;
+  double work = 0.0;
+  int task0 = 0;
+  for (int i = 0; i < nb; ++i) {
+    SvdBlock& b = p->blocks[i];
+    if (rows[i] <= 0 || cols[i] <= 0 || rows[i] > INT32_MAX || cols[i] > INT32_MAX) {
+      delete p;
+      return nd_fail(h, ND_ERR_ARG, "svd plan: block %d has invalid dims", i);
+    }
+    b.m = (int)rows[i]; b.n = (int)cols[i];
+    b.trans = b.m < b.n;
+    b.mm = b.trans ? b.n : b.m;
+    b.nn = b.trans ? b.m : b.n;
+    b.npad = b.nn + (b.nn & 1);
+    b.w_off = p->woff; p->woff += (int64_t)b.mm * b.nn;
+    b.v_off = p->voff; p->voff += (int64_t)b.nn * b.nn;
+    b.task0 = task0; b.ntask = b.npad / 2; task0 += b.ntask;
+    b.s_off = p->total; p->total += b.nn;
+    maxmm = std::max(maxmm, b.mm);
+    p->maxn = std::max(p->maxn, b.nn);
+    work += (double)b.mm * b.nn * b.nn;
+  }
+  p->big = work >= 2e8;
+  p->B32 = panel_group<float>(maxmm);
+  p->B64 = panel_group<double>(maxmm);
+  if (!p->B64 || (p->big && !p->B32)) {
+    delete p;
+    return nd_fail(h, ND_ERR_UNSUPPORTED, "svd plan: a block of %d rows is taller than a shared-memory panel "
+                                          "(use nd_bs_svd_f64)", maxmm);
+  }
+  p->ldp = (maxmm + 3) / 4 * 4;
+  p->smem32 = ((size_t)2 * p->B32 * p->ldp + (size_t)4 * p->B32 * p->B32 + 2 * p->B32) * sizeof(float);
+  p->smem64 = ((size_t)2 * p->B64 * p->ldp + (size_t)4 * p->B64 * p->B64 + 2 * p->B64) * sizeof(double);
+  while (p->npow2 < p->total) p->npow2 <<= 1;
+  if ((size_t)p->npow2 * 8 > 200 * 1024) {
+    delete p;
+    return nd_fail(h, ND_ERR_UNSUPPORTED, "svd plan: %d singular values exceed the on-chip sort", p->total);
+  }
+  const int ms = h->svd_max_sweeps;
+  p->n32 = std::min(24, ms < 0 ? 24 : ms);
+  p->n64 = ms < 0 ? (p->big ? 8 : 24) : ms;
+  // task tables: every block, longest first
+  std::vector<int> ord(nb);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+    return (int64_t)p->blocks[x].mm * p->blocks[x].nn > (int64_t)p->blocks[y].mm * p->blocks[y].nn;
+  });
+  auto table = [&](int B, std::vector<BjTask>& t, int& nrounds) {
+    nrounds = 0;
+    for (int bi : ord) {
+      const int g = (p->blocks[bi].nn + B - 1) / B, gp = g + (g & 1);
+      for (int k = 0; k < gp / 2; ++k) t.push_back(BjTask{bi, k});
+      nrounds = std::max(nrounds, gp - 1);
+    }
+  };
+  std::vector<BjTask> t32, t64;
+  if (p->big) table(p->B32, t32, p->nrounds32);
+  table(p->B64, t64, p->nrounds64);
+  p->ntasks32 = (int)t32.size();
+  p->ntasks64 = (int)t64.size();
+  std::vector<int64_t> uo(nb), vo(nb);
+  for (int i = 0; i < nb; ++i) {
+    uo[i] = p->ut; p->ut += (int64_t)p->blocks[i].m * p->blocks[i].nn;
+    vo[i] = p->vt; p->vt += (int64_t)p->blocks[i].n * p->blocks[i].nn;
+  }
+  nd_status st = ND_OK;
+  auto al = [&](void** q, size_t bytes) { if (!st) st = nd_dalloc(h, q, std::max<size_t>(bytes, 16)); };
+  al((void**)&p->dblk, nb * sizeof(SvdBlock));
+  al((void**)&p->tasks32, std::max<size_t>(t32.size(), 1) * sizeof(BjTask));
+  al((void**)&p->tasks64, std::max<size_t>(t64.size(), 1) * sizeof(BjTask));
+  al((void**)&p->W, p->woff * 8); al((void**)&p->V, p->voff * 8); al((void**)&p->sig, p->total * 8);
+  al((void**)&p->order, p->total * 4); al((void**)&p->active, nb * 4); al((void**)&p->dkept, nb * 4);
+  al((void**)&p->offmax, nb * 8); al((void**)&p->bar, 8); al((void**)&p->Uf, p->ut * 8); al((void**)&p->Vf, p->vt * 8);
+  al((void**)&p->duo, nb * 8); al((void**)&p->dvo, nb * 8); al((void**)&p->P, p->total * 8);
+  al((void**)&p->res, 32); al((void**)&p->dlen, 8);
+  if (p->big) {
+    al((void**)&p->W32, p->woff * 4); al((void**)&p->V32, p->voff * 4); al((void**)&p->bmax, nb * 8);
+    al((void**)&p->Y, p->voff * 8); al((void**)&p->Vn, p->voff * 8); al((void**)&p->S, p->voff * 8);
+    al((void**)&p->W0, p->woff * 8); al((void**)&p->W1, p->woff * 8); al((void**)&p->emax, 16);
+  }
+  al((void**)&p->Wsrc, std::max<int64_t>(p->woff, 1) * 8);
+  if (!st) st = nd_upload(h, p->dblk, p->blocks.data(), nb * sizeof(SvdBlock));
+  if (!st && !t32.empty()) st = nd_upload(h, p->tasks32, t32.data(), t32.size() * sizeof(BjTask));
+  if (!st) st = nd_upload(h, p->tasks64, t64.data(), t64.size() * sizeof(BjTask));
+  if (!st) st = nd_upload(h, p->duo, uo.data(), nb * 8);
+  if (!st) st = nd_upload(h, p->dvo, vo.data(), nb * 8);
+  if (!st) st = nd_cuda_check(h, cudaMemsetAsync(p->bar, 0, 8, s), "svd plan");
+  // one run on zeros builds every GEMM's launch state (the state a capture needs)
+  if (!st) {
+    // the plan's blocks sit back to back at the working offsets of a dummy zero matrix
+    st = nd_cuda_check(h, cudaMemsetAsync(p->Wsrc, 0, std::max<int64_t>(p->woff, 1) * 8, s), "svd plan");
+  }
+  if (!st) {
+    static bool attr = false;
+    if (!attr) { cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    std::vector<SvdBlock> zb = p->blocks;               // a_off: the dummy's block offsets
+    int64_t o = 0;
+    for (auto& b : zb) { b.a_off = o; o += (int64_t)b.m * b.n; }
+    p->blocks = zb;
+    st = nd_upload(h, p->dblk, p->blocks.data(), nb * sizeof(SvdBlock));
+    int32_t* dstat = nullptr;
+    if (!st) st = nd_dalloc(h, (void**)&dstat, 8);
+    TruncParams tp{1, -1, -1.0, 0, 0, 1};
+    if (!st) st = plan_run(p, p->Wsrc, tp, 0, false, dstat);
+    if (dstat) cudaFreeAsync(dstat, s);
+    if (!st) st = nd_cuda_check(h, cudaStreamSynchronize(s), "svd plan");
+    if (!st) st = nd_check_device_status(h, "svd plan");
+  }
+  if (st) {
+    p->release();
+    delete p;
+    return st;
+  }
+  *out = p;
+  return ND_OK;
+}
+
+extern "C" nd_status nd_bs_svd_plan_exec(nd_svd_plan p, const int64_t* offsets, const double* A, double* U, double* S,
+                                         double* V, int32_t mindim, int32_t maxdim, double cutoff,
+                                         int32_t use_absolute_cutoff, int32_t use_relative_cutoff, int32_t min_blockdim,
+                                         int32_t* kept, double* spectrum, int32_t* spectrum_len, double* truncerr,
+                                         int32_t* status) {
+  if (!p) return ND_ERR_ARG;
+  nd_handle h = p->h;
+  if (!offsets || !A || !U || !S || !V || !kept || !spectrum || !spectrum_len || !truncerr || !status)
+    return nd_fail(h, ND_ERR_ARG, "svd plan exec: NULL argument");
+  // block offsets in A: uploaded when they change (not allowed during capture)
+  bool same = true;
+  for (int i = 0; i < p->nb; ++i) same = same && p->blocks[i].a_off == offsets[i];
+  if (!same) {
+    if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd plan exec: new block offsets during capture (run once first)");
+    for (int i = 0; i < p->nb; ++i) p->blocks[i].a_off = offsets[i];
+    nd_status st = nd_upload(h, p->dblk, p->blocks.data(), p->nb * sizeof(SvdBlock));
+    if (st) return st;
+  }
+  TruncParams tp{mindim < 1 ? 1 : mindim, maxdim, cutoff, cutoff >= 0.0 ? 1 : 0, use_absolute_cutoff, use_relative_cutoff};
+  const bool trunc = maxdim >= 0 || cutoff >= 0.0;
+  nd_status st = plan_run(p, A, tp, min_blockdim, trunc, status);
+  if (st) return st;
+  cudaStream_t s = h->stream;
+  dim3 grid((unsigned)std::min<int64_t>((std::max<int64_t>(p->ut, p->vt) / p->nb + 255) / 256 + 1, 512), p->nb);
+  svd_compact<<<grid, 256, 0, s>>>(p->dblk, p->nb, p->dkept, p->Uf, p->Vf, p->duo, p->dvo, p->sig, U, S, V);
+  ND_LAUNCHED(h);
+  ND_CUDA(h, cudaMemcpyAsync(kept, p->dkept, p->nb * 4, cudaMemcpyDeviceToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(spectrum, p->P, (size_t)p->total * 8, cudaMemcpyDeviceToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(spectrum_len, p->dlen, 4, cudaMemcpyDeviceToDevice, s));
+  ND_CUDA(h, cudaMemcpyAsync(truncerr, p->res, 8, cudaMemcpyDeviceToDevice, s));
+  return nd_cuda_check(h, cudaGetLastError(), "svd plan exec");
+}
+
+extern "C" nd_status nd_bs_svd_plan_destroy(nd_svd_plan p) {
+  if (!p) return ND_OK;
+  p->release();
+  delete p;
+  return ND_OK;
 }
 
 extern "C" nd_status nd_truncate_f64(nd_handle h, const double* Pin, int32_t n, int32_t mindim, int32_t maxdim,

@@ -10,7 +10,7 @@ from . import workloads
 from . import linalg
 from . import autodiff
 from .autodiff import contract_autograd, contract_rrule, dense_structure
-from .linalg import Spectrum, eigen, matricize, qr, svd, truncate, uncombine
+from .linalg import Spectrum, SvdPlan, eigen, matricize, qr, svd, truncate, uncombine
 from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
 from . import krylov
@@ -21,7 +21,7 @@ __all__ = [
     "BlockSparseTensor", "DenseTensor", "DiagBlockSparseTensor", "blockoffsets",
     "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
     "permutedims", "permutedims_", "permutedims_blocksparse",
-    "linalg", "Spectrum", "eigen", "matricize", "qr", "svd", "truncate", "uncombine",
+    "linalg", "Spectrum", "SvdPlan", "eigen", "matricize", "qr", "svd", "truncate", "uncombine",
     "autodiff", "contract_autograd", "contract_rrule", "dense_structure",
     "krylov", "HeffOperator", "Lanczos", "lanczos",
 ]

@@ -18,7 +18,7 @@ import itertools
 
 import numpy as np
 
-from ._lib import BlockCopy, MAX_RANK, NoConvergence, handle, i32arr, i64arr
+from ._lib import ND_ERR_NOCONV, BlockCopy, MAX_RANK, NoConvergence, handle, i32arr, i64arr
 from .tensors import BlockSparseTensor, blockoffsets
 
 
@@ -89,6 +89,86 @@ def svd(T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absolut
         o += k
     sp = np.array(spec[:slen.value])          # sorted s^2, computed on the device
     return Ut, Sv, Vt, Spectrum(sp, terr.value), kept
+
+
+class SvdPlan:
+    """Blockwise truncated SVD for a fixed block structure whose run() only enqueues
+    work on the device, so it can be captured into a CUDA graph (for example with the
+    Lanczos loop of a sweep step).  nd_bs_svd_plan_* in the library; the result is the
+    one svd() returns (NDTensors/src/blocksparse/linearalgebra.jl:45-215), with kept
+    dimensions, spectrum, truncation error and convergence left on the device until
+    result() reads them.  Truncation parameters are fixed at construction."""
+
+    def __init__(self, T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absolute_cutoff=None,
+                 use_relative_cutoff=None, min_blockdim=None):
+        import torch
+        self.rows, self.cols = _matrix_blocks(T)
+        self.nb = len(T.blocks)
+        self.blocks = [tuple(b) for b in T.blocks]
+        self.inds = [tuple(i) for i in T.inds]
+        self.dev = T.data.device
+        self.h = handle(self.dev.index or 0)
+        self.ptr = C.c_void_p()
+        self.h.call("nd_bs_svd_plan_create", self.nb, i64arr(self.rows), i64arr(self.cols), C.byref(self.ptr))
+        ks = [min(r, c) for r, c in zip(self.rows, self.cols)]
+        f64 = dict(dtype=torch.float64, device=self.dev)
+        i32 = dict(dtype=torch.int32, device=self.dev)
+        self.U = torch.empty(max(1, sum(r * k for r, k in zip(self.rows, ks))), **f64)
+        self.S = torch.empty(max(1, sum(ks)), **f64)
+        self.V = torch.empty(max(1, sum(c * k for c, k in zip(self.cols, ks))), **f64)
+        self.kept = torch.zeros(max(1, self.nb), **i32)
+        self.spectrum = torch.zeros(max(1, sum(ks)), **f64)
+        self.slen = torch.zeros(1, **i32)
+        self.truncerr = torch.zeros(1, **f64)
+        self.status = torch.zeros(1, **i32)
+        self.params = (int(_opt(mindim, 1)), int(_opt(maxdim, -1)), float(_opt(cutoff, -1.0)),
+                       int(bool(use_absolute_cutoff)) if use_absolute_cutoff is not None else 0,
+                       int(bool(use_relative_cutoff)) if use_relative_cutoff is not None else 1,
+                       int(_opt(min_blockdim, 0)))
+
+    def run(self, T: BlockSparseTensor):
+        """Enqueue the SVD of T (the plan's block structure, any data)."""
+        if [tuple(b) for b in T.blocks] != self.blocks:
+            raise ValueError("SvdPlan.run: block structure differs from the plan's")
+        P = lambda t: C.c_void_p(t.data_ptr())
+        handle(self.dev.index or 0)          # bind the handle to torch's current stream
+        self.h._check(self.h.lib.nd_bs_svd_plan_exec(
+            self.ptr, i64arr(T.offsets), P(T.data), P(self.U), P(self.S), P(self.V), *self.params, P(self.kept),
+            P(self.spectrum), P(self.slen), P(self.truncerr), P(self.status)))
+
+    def result(self):
+        """(U, S, V, Spectrum, kept) as svd() returns them, or None if a block did not
+        converge (reads the device results: synchronises)."""
+        if int(self.status.item()) == ND_ERR_NOCONV:
+            return None
+        kept = self.kept.cpu().tolist()[:self.nb]
+        surv = [n for n in range(self.nb) if kept[n] > 0]
+        kdims = [kept[n] for n in surv]
+        u_ind = tuple(kdims)
+        Ublocks = [(self.blocks[n][0], i + 1) for i, n in enumerate(surv)]
+        Vblocks = [(self.blocks[n][1], i + 1) for i, n in enumerate(surv)]
+        Uo, nu = blockoffsets(Ublocks, [self.inds[0], u_ind])
+        Vo, nv = blockoffsets(Vblocks, [self.inds[1], u_ind])
+        Ut = BlockSparseTensor([self.inds[0], u_ind], Ublocks, Uo, self.U[:nu])
+        Vt = BlockSparseTensor([self.inds[1], u_ind], Vblocks, Vo, self.V[:nv])
+        Sv, o = [], 0
+        for k in kdims:
+            Sv.append(self.S[o:o + k])
+            o += k
+        n = int(self.slen.item())
+        sp = self.spectrum[:n].cpu().numpy()
+        return Ut, Sv, Vt, Spectrum(sp, float(self.truncerr.item())), kept
+
+    def destroy(self):
+        if self.ptr:
+            self.h.lib.nd_bs_svd_plan_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 def eigen(T: BlockSparseTensor, mindim=None, maxdim=None, cutoff=None, use_absolute_cutoff=None,
