@@ -302,6 +302,12 @@ typedef struct {
 } nd_block_copy;
 nd_status nd_block_copy_f64(nd_handle h, int32_t n, const nd_block_copy *list /* host */, const double *src,
                             double *dst);
+/* The same copies prepared once (the list converted and uploaded at creation), so that
+ * a run only launches the kernel and can be captured into a CUDA graph. */
+typedef struct nd_copy_plan_s *nd_copy_plan;
+nd_status nd_block_copy_plan_create(nd_handle h, int32_t n, const nd_block_copy *list /* host */, nd_copy_plan *plan);
+nd_status nd_block_copy_plan_run(nd_copy_plan plan, const double *src, double *dst);
+nd_status nd_block_copy_plan_destroy(nd_copy_plan plan);
 
 /* ---- vector-space operations (Krylov solvers) ---------------------------------
  * The VectorInterface methods the reference defines for ITensors
@@ -326,6 +332,13 @@ nd_status nd_vec_dots_f64(nd_handle h, int64_t n, int32_t k, const double *V, in
 /* y += sign * sum_j coef[j] * V_j, j < k (coef a device array) */
 nd_status nd_vec_update_f64(nd_handle h, int64_t n, int32_t k, const double *V, int64_t ldv, const double *coef,
                             double sign, double *y);
+/* Lowest eigenpair of the k x k symmetric tridiagonal matrix (diagonal alpha[k],
+ * off-diagonal beta[k - 1]; k <= 32), all device arrays: *value, and y[k] normalised
+ * with its largest component positive.  The Krylov solver's small eigenproblem on the
+ * device, so that a whole Lanczos solve can be one CUDA graph (the reference's solver,
+ * KrylovKit, solves it on the host). */
+nd_status nd_tridiag_lowest_f64(nd_handle h, int32_t k, const double *alpha, const double *beta, double *value,
+                                double *y);
 
 /* ---- autotuner -------------------------------------------------------------
  * Execution parameters of a contraction (today: the split-K target of the FP64

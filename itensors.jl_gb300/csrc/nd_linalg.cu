@@ -2104,12 +2104,11 @@ extern "C" nd_status nd_bs_qr_f64(nd_handle h, int32_t nb, const int64_t* rows, 
   return nd_cuda_check(h, cudaGetLastError(), "qr_blocks");
 }
 
-extern "C" nd_status nd_block_copy_f64(nd_handle h, int32_t n, const nd_block_copy* list, const double* src, double* dst) {
-  if (!h) return ND_ERR_ARG;
-  if (n < 0 || (n > 0 && (!list || !src || !dst))) return nd_fail(h, ND_ERR_ARG, "block_copy: NULL argument");
-  if (n == 0) return ND_OK;
-  std::vector<BlockCopyDev> dl(n);
-  int64_t maxc = 0;
+// host list -> device form (mixed-radix index per copy); maxc: the largest count
+static nd_status prepare_copies(nd_handle h, int32_t n, const nd_block_copy* list, std::vector<BlockCopyDev>& dl,
+                                int64_t& maxc) {
+  dl.assign(n, BlockCopyDev{});
+  maxc = 0;
   for (int i = 0; i < n; ++i) {
     const nd_block_copy& c = list[i];
     if (c.rank < 0 || c.rank > ND_MAX_RANK) return nd_fail(h, ND_ERR_ARG, "block_copy: rank out of range");
@@ -2126,6 +2125,64 @@ extern "C" nd_status nd_block_copy_f64(nd_handle h, int32_t n, const nd_block_co
     mixed_simplify(d.idx);
     maxc = std::max(maxc, d.count);
   }
+  return ND_OK;
+}
+
+struct nd_copy_plan_s {
+  nd_handle h = nullptr;
+  int n = 0;
+  int64_t maxc = 0;
+  BlockCopyDev* list = nullptr;
+};
+
+extern "C" nd_status nd_block_copy_plan_create(nd_handle h, int32_t n, const nd_block_copy* list, nd_copy_plan* out) {
+  if (!h || !out) return ND_ERR_ARG;
+  *out = nullptr;
+  if (n < 0 || (n > 0 && !list)) return nd_fail(h, ND_ERR_ARG, "block_copy_plan: NULL argument");
+  if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "block_copy_plan: create it before graph capture");
+  std::vector<BlockCopyDev> dl;
+  int64_t maxc = 0;
+  nd_status st = prepare_copies(h, n, list, dl, maxc);
+  if (st) return st;
+  auto p = new nd_copy_plan_s;
+  p->h = h; p->n = n; p->maxc = maxc;
+  if (n > 0) {
+    st = nd_dalloc(h, (void**)&p->list, n * sizeof(BlockCopyDev));
+    if (!st) st = nd_upload(h, p->list, dl.data(), n * sizeof(BlockCopyDev));
+    if (st) { if (p->list) cudaFreeAsync(p->list, h->stream); delete p; return st; }
+  }
+  *out = p;
+  return ND_OK;
+}
+
+extern "C" nd_status nd_block_copy_plan_run(nd_copy_plan p, const double* src, double* dst) {
+  if (!p) return ND_ERR_ARG;
+  nd_handle h = p->h;
+  if (p->n == 0 || p->maxc == 0) return ND_OK;
+  if (!src || !dst) return nd_fail(h, ND_ERR_ARG, "block_copy_plan: NULL argument");
+  dim3 grid((unsigned)std::min<int64_t>((p->maxc + 255) / 256, 512), (unsigned)std::min(p->n, 65535));
+  nd_prof_begin(h, "block_copy");
+  block_copy<<<grid, 256, 0, h->stream>>>(p->list, p->n, src, dst);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "block_copy");
+}
+
+extern "C" nd_status nd_block_copy_plan_destroy(nd_copy_plan p) {
+  if (!p) return ND_OK;
+  if (p->list) cudaFreeAsync(p->list, p->h->stream);
+  delete p;
+  return ND_OK;
+}
+
+extern "C" nd_status nd_block_copy_f64(nd_handle h, int32_t n, const nd_block_copy* list, const double* src, double* dst) {
+  if (!h) return ND_ERR_ARG;
+  if (n < 0 || (n > 0 && (!list || !src || !dst))) return nd_fail(h, ND_ERR_ARG, "block_copy: NULL argument");
+  if (n == 0) return ND_OK;
+  std::vector<BlockCopyDev> dl;
+  int64_t maxc = 0;
+  nd_status pst = prepare_copies(h, n, list, dl, maxc);
+  if (pst) return pst;
   if (maxc == 0) return ND_OK;
   cudaStream_t s = h->stream;
   BlockCopyDev* dd = nullptr;

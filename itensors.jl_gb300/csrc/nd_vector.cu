@@ -190,6 +190,81 @@ int grid_for(nd_handle h, int64_t n, int per_thread) {
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + per_cta - 1) / per_cta, (int64_t)h->num_sms * 8));
 }
 
+// Lowest eigenpair of the k x k symmetric tridiagonal matrix with diagonal a and
+// off-diagonal b (a Lanczos matrix), one thread: bisection on the Sturm count of
+// T - x I (Barth, Martin and Wilkinson, "Calculation of the eigenvalues of a symmetric
+// tridiagonal matrix by the method of bisection", Numer. Math. 9, 1967) to the
+// resolution of double precision, then three steps of inverse iteration with the
+// Thomas algorithm (near-zero pivots replaced by eps * ||T||, as inverse iteration
+// codes do).  The vector is normalised with its largest component positive; the value
+// is its Rayleigh quotient.
+__global__ void tridiag_lowest(int k, const double* __restrict__ a, const double* __restrict__ b, double* value,
+                               double* y) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double lo = 0.0, hi = 0.0, nrm = 0.0;
+  for (int i = 0; i < k; ++i) {
+    const double r = (i > 0 ? fabs(b[i - 1]) : 0.0) + (i < k - 1 ? fabs(b[i]) : 0.0);
+    lo = i ? fmin(lo, a[i] - r) : a[i] - r;
+    hi = i ? fmax(hi, a[i] + r) : a[i] + r;
+    nrm = fmax(nrm, fabs(a[i]) + r);
+  }
+  const double tiny = 2.2250738585072014e-308 / 2.220446049250313e-16;   // safe pivot floor
+  for (int it = 0; it < 2100; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    int count = 0;
+    double q = a[0] - mid;
+    if (q < 0.0) ++count;
+    for (int i = 1; i < k; ++i) {
+      if (fabs(q) < tiny) q = -tiny;
+      q = a[i] - mid - b[i - 1] * b[i - 1] / q;
+      if (q < 0.0) ++count;
+    }
+    if (count >= 1) hi = mid; else lo = mid;
+  }
+  const double lam = 0.5 * (lo + hi);
+  const double piv = 2.220446049250313e-16 * fmax(nrm, tiny);
+  double x[32], c[32], d[32];
+  for (int i = 0; i < k; ++i) x[i] = 1.0;
+  for (int step = 0; step < 3; ++step) {
+    // solve (T - lam I) z = x (Thomas), z into x
+    double den = a[0] - lam;
+    if (fabs(den) < piv) den = den < 0 ? -piv : piv;
+    c[0] = k > 1 ? b[0] / den : 0.0;
+    d[0] = x[0] / den;
+    for (int i = 1; i < k; ++i) {
+      den = a[i] - lam - b[i - 1] * c[i - 1];
+      if (fabs(den) < piv) den = den < 0 ? -piv : piv;
+      c[i] = i < k - 1 ? b[i] / den : 0.0;
+      d[i] = (x[i] - b[i - 1] * d[i - 1]) / den;
+    }
+    x[k - 1] = d[k - 1];
+    for (int i = k - 2; i >= 0; --i) x[i] = d[i] - c[i] * x[i + 1];
+    double s = 0.0;
+    for (int i = 0; i < k; ++i) s = fmax(s, fabs(x[i]));
+    for (int i = 0; i < k; ++i) x[i] /= s;
+  }
+  double n2 = 0.0, big = 0.0;
+  int ib = 0;
+  for (int i = 0; i < k; ++i) {
+    n2 += x[i] * x[i];
+    if (fabs(x[i]) > big) { big = fabs(x[i]); ib = i; }
+  }
+  const double sc = (x[ib] < 0 ? -1.0 : 1.0) / sqrt(n2);
+  double rq = 0.0;
+  for (int i = 0; i < k; ++i) {
+    x[i] *= sc;
+    y[i] = x[i];
+  }
+  for (int i = 0; i < k; ++i) {
+    double tx = a[i] * x[i];
+    if (i > 0) tx += b[i - 1] * x[i - 1];
+    if (i < k - 1) tx += b[i] * x[i + 1];
+    rq += x[i] * tx;
+  }
+  *value = rq;
+}
+
 }  // namespace
 
 extern "C" nd_status nd_vec_inner_f64(nd_handle h, int64_t n, const double* x, const double* y, double* out) {
@@ -242,4 +317,16 @@ extern "C" nd_status nd_vec_add_f64(nd_handle h, int64_t n, const double* x, dou
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "vec_add");
+}
+
+extern "C" nd_status nd_tridiag_lowest_f64(nd_handle h, int32_t k, const double* alpha, const double* beta,
+                                          double* value, double* y) {
+  if (!h) return ND_ERR_ARG;
+  if (k < 1 || k > 32 || !alpha || !value || !y || (k > 1 && !beta))
+    return nd_fail(h, ND_ERR_ARG, "tridiag_lowest: need 1 <= k <= 32 and device arrays");
+  nd_prof_begin(h, "tridiag_lowest");
+  tridiag_lowest<<<1, 32, 0, h->stream>>>(k, alpha, beta, value, y);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  return nd_cuda_check(h, cudaGetLastError(), "tridiag_lowest");
 }

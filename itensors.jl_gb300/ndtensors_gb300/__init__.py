@@ -10,18 +10,18 @@ from . import workloads
 from . import linalg
 from . import autodiff
 from .autodiff import contract_autograd, contract_rrule, dense_structure
-from .linalg import Spectrum, SvdPlan, eigen, matricize, qr, svd, truncate, uncombine
+from .linalg import MatricizePlan, Spectrum, SvdPlan, eigen, matricize, qr, svd, truncate, uncombine
 from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
 from . import krylov
-from .krylov import HeffOperator, Lanczos, lanczos
+from .krylov import HeffOperator, Lanczos, SweepStep, lanczos
 
 __all__ = [
     "workloads", "NDError", "NoConvergence", "PRECISIONS", "handle", "load", "LIB_PATH",
     "BlockSparseTensor", "DenseTensor", "DiagBlockSparseTensor", "blockoffsets",
     "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
     "permutedims", "permutedims_", "permutedims_blocksparse",
-    "linalg", "Spectrum", "SvdPlan", "eigen", "matricize", "qr", "svd", "truncate", "uncombine",
+    "linalg", "MatricizePlan", "Spectrum", "SvdPlan", "eigen", "matricize", "qr", "svd", "truncate", "uncombine",
     "autodiff", "contract_autograd", "contract_rrule", "dense_structure",
-    "krylov", "HeffOperator", "Lanczos", "lanczos",
+    "krylov", "HeffOperator", "Lanczos", "SweepStep", "lanczos",
 ]

@@ -68,6 +68,10 @@ SIGNATURES = {
     "nd_set_spin_limit": [_P, C.c_uint32],
     "nd_set_svd_max_sweeps": [_P, _I32],
     "nd_svd_last_info": [_P, _P, _I32, _P, _I32],
+    "nd_block_copy_plan_create": [_P, _I32, _P, _P],
+    "nd_block_copy_plan_run": [_P, _P, _P],
+    "nd_block_copy_plan_destroy": [_P],
+    "nd_tridiag_lowest_f64": [_P, _I32, _P, _P, _P, _P],
     "nd_bs_svd_plan_create": [_P, _I32, _P, _P, _P],
     "nd_bs_svd_plan_exec": [_P, _P, _P, _P, _P, _P, _I32, _I32, _D, _I32, _I32, _I32, _P, _P, _P, _P, _P],
     "nd_bs_svd_plan_destroy": [_P],

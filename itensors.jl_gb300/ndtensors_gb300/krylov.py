@@ -131,11 +131,15 @@ class LanczosResult:
 
 class Lanczos:
     """Krylov basis construction for one operator and vector length, reusable (and
-    capturable) across calls: `run(v0)` returns the lowest Ritz pair ("SR")."""
+    capturable) across calls: `run(v0)` returns the lowest Ritz pair ("SR").  With
+    device_solve the krylovdim x krylovdim tridiagonal problem and the Ritz vector are
+    computed on the device too (nd_tridiag_lowest_f64), so `enqueue()` is a whole solve
+    with no host synchronisation."""
 
-    def __init__(self, apply, n, krylovdim=10, device=0, graph=False):
+    def __init__(self, apply, n, krylovdim=10, device=0, graph=False, device_solve=False):
         import torch
         self.apply, self.n, self.k, self.graph = apply, n, int(krylovdim), graph
+        self.device_solve = device_solve
         if self.k + 1 > 32:
             raise ValueError("krylovdim must be at most 31 (the library's basis operations take 32 vectors)")
         dev = torch.device("cuda", device)
@@ -147,6 +151,9 @@ class Lanczos:
         self.beta = torch.zeros(self.k, **f64)
         self.s = torch.empty(1, **f64)
         self.start = torch.empty(n, **f64)
+        self.value = torch.zeros(1, **f64)                    # device solve: lowest Ritz value
+        self.y = torch.zeros(self.k, **f64)                   # and its coefficients in the basis
+        self.x = torch.empty(n, **f64)                        # the Ritz vector
         self.device = device
         self._graph = None
 
@@ -167,10 +174,40 @@ class Lanczos:
             h.call("nd_vec_norm_f64", n, _p(w), _p(self.beta, j))                          # beta_j = |w|
             h.call("nd_vec_scale_f64", n, _p(w), _p(V, (j + 1) * n), 1.0, _p(self.beta, j), 1)   # V_{j+1} = w / beta_j
 
+    def _solve_device(self):
+        h = handle(self.device)
+        h.call("nd_tridiag_lowest_f64", self.k, _p(self.alpha), _p(self.beta), _p(self.value), _p(self.y))
+        h.call("nd_vec_scale_f64", self.n, _p(self.V), _p(self.x), 0.0, None, 0)                   # x = 0
+        h.call("nd_vec_update_f64", self.n, self.k, _p(self.V), self.n, _p(self.y), 1.0, _p(self.x))  # x = V^T y
+
+    def enqueue(self):
+        """The whole solve from self.start (basis, tridiagonal eigenpair, Ritz vector into
+        self.x, value into self.value): library launches only, no synchronisation."""
+        self._body()
+        self._solve_device()
+
     def run(self, v0):
         import torch
         h = handle(self.device)
         h.call("nd_vec_scale_f64", self.n, _p(v0), _p(self.start), 1.0, None, 0)
+        if self.device_solve:
+            if not self.graph:
+                self.enqueue()
+            else:
+                if self._graph is None:
+                    s = torch.cuda.Stream()
+                    s.wait_stream(torch.cuda.current_stream())
+                    with torch.cuda.stream(s):
+                        self.enqueue()                  # warm-up outside capture: builds every cache
+                    torch.cuda.current_stream().wait_stream(s)
+                    self._graph = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(self._graph):
+                        self.enqueue()
+                self._graph.replay()
+            b = self.beta.cpu().numpy()
+            y = self.y.cpu().numpy()
+            return LanczosResult(float(self.value.item()), self.x, float(abs(b[-1] * y[-1])),
+                                 self.alpha.cpu().numpy(), b, self.k)
         if not self.graph:
             self._body()
         else:
@@ -199,3 +236,55 @@ class Lanczos:
 def lanczos(apply, v0, krylovdim=10, graph=False):
     """Lowest Ritz pair of the operator `apply(x, out)` from a Krylov basis built on v0."""
     return Lanczos(apply, v0.numel(), krylovdim, v0.device.index or 0, graph).run(v0)
+
+
+class SweepStep:
+    """One two-site update of a DMRG sweep on the device: the lowest eigenpair of H_eff
+    by Lanczos (cached contraction plans, the small tridiagonal problem on the device),
+    the Ritz vector matricized to (row dims) x (column dims) and its truncated blockwise
+    SVD (SvdPlan).  Every step is library launches with no host synchronisation, so with
+    graph=True the whole update is captured once into one CUDA graph and replayed; the
+    energy, the factors and the kept dimensions are read after the replay (result()).
+    The reference performs this update in ITensorMPS (outside the repository) on
+    NDTensors' contract, svd and truncate! (NDTensors/src/blocksparse/linearalgebra.jl:45-215)."""
+
+    def __init__(self, L, W1, W2, R, psi: BlockSparseTensor, steps, qinds, row_dims, col_dims, krylovdim=10,
+                 precision="ozaki", graph=True, **svd_kwargs):
+        from .linalg import MatricizePlan, SvdPlan
+        self.op = HeffOperator(L, W1, W2, R, psi, steps, precision=precision)
+        dev = psi.data.device.index or 0
+        self.lz = Lanczos(self.op.apply, self.op.n, krylovdim, dev, device_solve=True)
+        self.psi_struct = (list(psi.inds), list(psi.blocks), list(psi.offsets))
+        self.mat = MatricizePlan(psi, qinds, row_dims, col_dims)
+        self.svd = SvdPlan(self.mat.M, **svd_kwargs)
+        self.graph = graph
+        self._graph = None
+        self.device = dev
+
+    def _enqueue(self):
+        self.lz.enqueue()
+        M = self.mat.run(self.lz.x)
+        self.svd.run(M)
+
+    def run(self, v0):
+        """Enqueue (or replay) one update from the start vector v0 (psi-ordered data)."""
+        import torch
+        handle(self.device).call("nd_vec_scale_f64", self.lz.n, _p(v0), _p(self.lz.start), 1.0, None, 0)
+        if not self.graph:
+            self._enqueue()
+            return
+        if self._graph is None:
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                self._enqueue()                         # warm-up outside capture: builds every cache
+            torch.cuda.current_stream().wait_stream(s)
+            torch.cuda.synchronize()
+            self._graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self._graph):
+                self._enqueue()
+        self._graph.replay()
+
+    def result(self):
+        """(energy, Ritz vector, svd result as svd() returns it or None) after run()."""
+        return float(self.lz.value.item()), self.lz.x, self.svd.result()

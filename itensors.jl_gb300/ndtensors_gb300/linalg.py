@@ -294,11 +294,10 @@ def _group_place(group):
     return merged, place
 
 
-def matricize(T: BlockSparseTensor, qinds, row_dims, col_dims):
-    """Fuse T's dimensions into (row group, column group) as ITensor's svd / qr do
-    with two combiners (src/tensor_operations/matrix_decomposition.jl:153-160).
-    qinds: per dimension (sectors, arrow).  Returns (matrix, row_info, col_info)."""
-    import torch
+def _matricize_layout(T: BlockSparseTensor, qinds, row_dims, col_dims):
+    """Structure of T fused into (row group, column group) as ITensor's svd / qr do with
+    two combiners (src/tensor_operations/matrix_decomposition.jl:153-160), and the block
+    copies that fill it: (inds, blocks, offsets, nnz, copies, row_info, col_info)."""
     rows_g = [qinds[d] for d in row_dims]
     cols_g = [qinds[d] for d in col_dims]
     rsec, rplace = _group_place(rows_g)
@@ -321,8 +320,6 @@ def matricize(T: BlockSparseTensor, qinds, row_dims, col_dims):
     mblocks = sorted(entries, key=lambda x: (x[1], x[0]))       # isblockless: column block most significant
     minds = [tuple(d for _, d in rsec), tuple(d for _, d in csec)]
     offs, nnz = blockoffsets(mblocks, minds)
-    data = torch.zeros(max(nnz, 1), dtype=torch.float64, device=T.data.device)[:nnz]
-    M = BlockSparseTensor(minds, mblocks, offs, data)
     copies = []
     for j, mb in enumerate(mblocks):
         ld = minds[0][mb[0] - 1]
@@ -349,11 +346,60 @@ def matricize(T: BlockSparseTensor, qinds, row_dims, col_dims):
                 c.src_strides[k] = st[k]
                 c.dst_strides[k] = dst[k]
             copies.append(c)
+    return minds, mblocks, offs, nnz, copies, (rsec, rplace), (csec, cplace)
+
+
+def matricize(T: BlockSparseTensor, qinds, row_dims, col_dims):
+    """Fuse T's dimensions into (row group, column group) as ITensor's svd / qr do
+    with two combiners (src/tensor_operations/matrix_decomposition.jl:153-160).
+    qinds: per dimension (sectors, arrow).  Returns (matrix, row_info, col_info)."""
+    import torch
+    minds, mblocks, offs, nnz, copies, rinfo, cinfo = _matricize_layout(T, qinds, row_dims, col_dims)
+    data = torch.zeros(max(nnz, 1), dtype=torch.float64, device=T.data.device)[:nnz]
+    M = BlockSparseTensor(minds, mblocks, offs, data)
     if copies:
         arr = (BlockCopy * len(copies))(*copies)
         handle(T.data.device.index or 0).call("nd_block_copy_f64", len(copies), arr, C.c_void_p(T.data.data_ptr()),
                                               C.c_void_p(data.data_ptr()))
-    return M, (rsec, rplace), (csec, cplace)
+    return M, rinfo, cinfo
+
+
+class MatricizePlan:
+    """matricize() for a fixed block structure, prepared once (nd_block_copy_plan_*): run()
+    zeroes the matrix and launches the copies, nothing else, so it can be captured into
+    a CUDA graph.  The matrix is self.M (its data buffer is reused by every run)."""
+
+    def __init__(self, T: BlockSparseTensor, qinds, row_dims, col_dims):
+        import torch
+        minds, mblocks, offs, nnz, copies, self.row_info, self.col_info = _matricize_layout(T, qinds, row_dims,
+                                                                                           col_dims)
+        self.dev = T.data.device
+        self.h = handle(self.dev.index or 0)
+        self.nnz = nnz
+        self.M = BlockSparseTensor(minds, mblocks, offs,
+                                   torch.empty(max(nnz, 1), dtype=torch.float64, device=self.dev)[:nnz])
+        self.ptr = C.c_void_p()
+        arr = (BlockCopy * max(1, len(copies)))(*copies)
+        self.h.call("nd_block_copy_plan_create", len(copies), arr, C.byref(self.ptr))
+
+    def run(self, data):
+        """self.M <- the matricisation of T's structure on `data` (a flat device vector)."""
+        handle(self.dev.index or 0)
+        self.h.call("nd_memset0", C.c_void_p(self.M.data.data_ptr()), 8 * self.nnz)
+        self.h._check(self.h.lib.nd_block_copy_plan_run(self.ptr, C.c_void_p(data.data_ptr()),
+                                                        C.c_void_p(self.M.data.data_ptr())))
+        return self.M
+
+    def destroy(self):
+        if self.ptr:
+            self.h.lib.nd_block_copy_plan_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 def uncombine(T: BlockSparseTensor, combdim, group, info):
