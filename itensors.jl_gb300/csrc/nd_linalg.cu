@@ -576,6 +576,7 @@ struct BjArgs {
   double tol_pow;
   double tol_cap;
   const int32_t* active;   // optional: per block, 0 once converged (its tasks are skipped)
+  const int32_t* any_active;   // optional: 0 when no block is active (the sweep returns at once)
 };
 
 // 16-byte vectors of the panel element type: a lane handles VW consecutive rows.
@@ -729,6 +730,7 @@ __global__ void __launch_bounds__(32 * B, 1) bj_sweep(BjArgs<T> a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const T tol = (T)a.tol, tol_cap = (T)a.tol_cap;
   const bool sqrt_pow = a.tol_pow != 1.0;          // tol_pow is 1 or 1/2
+  if (a.any_active && !*a.any_active) return;      // every block converged: nothing to sweep (uniform)
   for (int r = 0; r < a.nrounds; ++r) {
     // tasks are listed longest first; CTA i takes positions i, 2G-1-i, 2G+i, ... (a snake),
     // so the CTAs with the longest first task get the shortest second one
@@ -1158,7 +1160,7 @@ static nd_status run_panel_sweeps(nd_handle h, const std::vector<SvdBlock>& bloc
     if ((st = nd_upload(h, dtasks, tasks.data(), tasks.size() * sizeof(BjTask)))) break;
     if ((st = nd_cuda_check(h, cudaMemsetAsync(offmax, 0, nb * 8, s), "svd sweep set-up"))) break;
     BjArgs<T> a{dblk, dtasks, (int)tasks.size(), nrounds, ldp, Wt, Vt, offmax, bar, bar + 1, h->d_status, tol, tol_pow,
-                tol_cap, nullptr};
+                tol_cap, nullptr, nullptr};
     nd_prof_begin(h, name);
     if constexpr (sizeof(T) == 4) {
       if (B == 16) st = launch_bj<T, 16>(h, a, smem);
@@ -1664,12 +1666,19 @@ extern "C" nd_status nd_bs_eigen_f64(nd_handle h, int32_t nb, const int64_t* dim
 // ---------------------------------------------------------------------------
 namespace {
 
-// after a sweep: a block whose sweep rotated nothing is done; reset the sweep maxima
-__global__ void svd_active_update(int nb, unsigned long long* offmax, int32_t* active) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  if (offmax[b] == 0ull) active[b] = 0;
-  offmax[b] = 0ull;
+// after a sweep (one CTA): a block whose sweep rotated nothing is done; reset the sweep
+// maxima; any = whether a block is still active
+__global__ void svd_active_update(int nb, unsigned long long* offmax, int32_t* active, int32_t* any) {
+  __shared__ int a;
+  if (threadIdx.x == 0) a = 0;
+  __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    if (offmax[b] == 0ull) active[b] = 0;
+    offmax[b] = 0ull;
+    if (active[b]) a = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *any = a;
 }
 
 __global__ void svd_fill_i32(int n, int32_t* x, int32_t v) {
@@ -1732,7 +1741,7 @@ struct nd_svd_plan_s {
   double *W = nullptr, *V = nullptr, *sig = nullptr, *Y = nullptr, *Vn = nullptr, *W0 = nullptr, *W1 = nullptr,
          *S = nullptr, *Uf = nullptr, *Vf = nullptr, *P = nullptr, *res = nullptr, *Wsrc = nullptr;
   float *W32 = nullptr, *V32 = nullptr;
-  int32_t *order = nullptr, *active = nullptr, *dkept = nullptr;
+  int32_t *order = nullptr, *active = nullptr, *any_active = nullptr, *dkept = nullptr;
   int* dlen = nullptr;
   unsigned long long *offmax = nullptr, *bmax = nullptr, *emax = nullptr;
   unsigned int* bar = nullptr;
@@ -1746,7 +1755,7 @@ void nd_svd_plan_s::release() {
   for (ExecCache* c : {&cR, &cW, &cS, &cV, &cR64, &cW64, &cS64, &cWE}) c->free_all(h);
   for (void* q : {(void*)dblk, (void*)tasks32, (void*)tasks64, (void*)W, (void*)V, (void*)sig, (void*)Y, (void*)Vn,
                   (void*)W0, (void*)W1, (void*)S, (void*)Uf, (void*)Vf, (void*)P, (void*)res, (void*)Wsrc, (void*)W32,
-                  (void*)V32, (void*)order, (void*)active, (void*)dkept, (void*)dlen, (void*)offmax, (void*)bmax,
+                  (void*)V32, (void*)order, (void*)active, (void*)any_active, (void*)dkept, (void*)dlen, (void*)offmax, (void*)bmax,
                   (void*)emax, (void*)bar, (void*)duo, (void*)dvo})
     if (q) cudaFreeAsync(q, h->stream);
 }
@@ -1760,11 +1769,13 @@ nd_status plan_sweeps(nd_svd_plan p, T* Wt, T* Vt, int nsweeps, double tol, doub
   const int B = f32 ? p->B32 : p->B64;
   BjArgs<T> a{p->dblk, f32 ? p->tasks32 : p->tasks64, f32 ? p->ntasks32 : p->ntasks64,
               f32 ? p->nrounds32 : p->nrounds64, p->ldp, Wt, Vt, p->offmax, p->bar, p->bar + 1, h->d_status,
-              tol, tol_pow, tol_cap, p->active};
+              tol, tol_pow, tol_cap, p->active, p->any_active};
   const size_t smem = f32 ? p->smem32 : p->smem64;
   const int gb = (p->nb + 127) / 128;
   ND_CUDA(h, cudaMemsetAsync(p->offmax, 0, p->nb * 8, h->stream));
   svd_fill_i32<<<gb, 128, 0, h->stream>>>(p->nb, p->active, 1);
+  svd_fill_i32<<<1, 32, 0, h->stream>>>(1, p->any_active, 1);
+  ND_LAUNCHED(h);
   ND_LAUNCHED(h);
   for (int sw = 0; sw < nsweeps; ++sw) {
     nd_status st;
@@ -1777,7 +1788,7 @@ nd_status plan_sweeps(nd_svd_plan p, T* Wt, T* Vt, int nsweeps, double tol, doub
     nd_prof_end(h);
     ND_LAUNCHED(h);
     if (st) return st;
-    svd_active_update<<<gb, 128, 0, h->stream>>>(p->nb, p->offmax, p->active);
+    svd_active_update<<<1, 256, 0, h->stream>>>(p->nb, p->offmax, p->active, p->any_active);
     ND_LAUNCHED(h);
   }
   return nd_cuda_check(h, cudaGetLastError(), "svd plan sweeps");
@@ -1951,6 +1962,7 @@ extern "C" nd_status nd_bs_svd_plan_create(nd_handle h, int32_t nb, const int64_
   al((void**)&p->tasks64, std::max<size_t>(t64.size(), 1) * sizeof(BjTask));
   al((void**)&p->W, p->woff * 8); al((void**)&p->V, p->voff * 8); al((void**)&p->sig, p->total * 8);
   al((void**)&p->order, p->total * 4); al((void**)&p->active, nb * 4); al((void**)&p->dkept, nb * 4);
+  al((void**)&p->any_active, 16);
   al((void**)&p->offmax, nb * 8); al((void**)&p->bar, 8); al((void**)&p->Uf, p->ut * 8); al((void**)&p->Vf, p->vt * 8);
   al((void**)&p->duo, nb * 8); al((void**)&p->dvo, nb * 8); al((void**)&p->P, p->total * 8);
   al((void**)&p->res, 32); al((void**)&p->dlen, 8);

@@ -110,6 +110,8 @@ class SvdPlan:
         self.h = handle(self.dev.index or 0)
         self.ptr = C.c_void_p()
         self.h.call("nd_bs_svd_plan_create", self.nb, i64arr(self.rows), i64arr(self.cols), C.byref(self.ptr))
+        from ._lib import _live_plans
+        _live_plans.add(self)                   # destroyed before the handle at exit
         ks = [min(r, c) for r, c in zip(self.rows, self.cols)]
         f64 = dict(dtype=torch.float64, device=self.dev)
         i32 = dict(dtype=torch.int32, device=self.dev)
@@ -160,9 +162,9 @@ class SvdPlan:
         return Ut, Sv, Vt, Spectrum(sp, float(self.truncerr.item())), kept
 
     def destroy(self):
-        if self.ptr:
+        if self.ptr and self.h.ptr:             # the handle owns the plan's stream and pool
             self.h.lib.nd_bs_svd_plan_destroy(self.ptr)
-            self.ptr = C.c_void_p()
+        self.ptr = C.c_void_p()
 
     def __del__(self):
         try:
@@ -381,6 +383,8 @@ class MatricizePlan:
         self.ptr = C.c_void_p()
         arr = (BlockCopy * max(1, len(copies)))(*copies)
         self.h.call("nd_block_copy_plan_create", len(copies), arr, C.byref(self.ptr))
+        from ._lib import _live_plans
+        _live_plans.add(self)                   # destroyed before the handle at exit
 
     def run(self, data):
         """self.M <- the matricisation of T's structure on `data` (a flat device vector)."""
@@ -391,9 +395,9 @@ class MatricizePlan:
         return self.M
 
     def destroy(self):
-        if self.ptr:
+        if self.ptr and self.h.ptr:
             self.h.lib.nd_block_copy_plan_destroy(self.ptr)
-            self.ptr = C.c_void_p()
+        self.ptr = C.c_void_p()
 
     def __del__(self):
         try:
