@@ -1000,6 +1000,55 @@ __global__ void eig_finish(const SvdBlock* blocks, const double* sig, const int3
   }
 }
 
+// Unshifted path: the Jacobi SVD of a symmetric block gives w_j = A v_j = sigma_j u_j with
+// u_j = +-v_j when the eigenvalue +-sigma_j is not paired with one of opposite sign;
+// lambda_j = v_j . w_j then carries the sign.  A column whose |v_j . w_j| falls short of
+// sigma_j by more than 1e-6 (near +-lambda pairs mix v_j) marks its block ambiguous
+// (*flag = 1); columns below 1e-12 of the block's largest are left as they are
+// (their sign does not matter at that size).  One warp per column.
+__global__ void eig_sign(const SvdBlock* blocks, const double* W, const double* Vw, const double* sig, double* lamJ,
+                         int32_t* flag) {
+  const SvdBlock b = blocks[blockIdx.x];
+  const int n = b.nn, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const double smax = sig[b.s_off];                 // sorted descending by svd_finish
+  for (int j = warp; j < n; j += nw) {
+    const double* w = W + b.w_off + (int64_t)j * b.mm;
+    const double* v = Vw + b.v_off + (int64_t)j * n;
+    double ww = 0.0, wv = 0.0;
+    for (int i = lane; i < n; i += 32) {
+      ww = fma(w[i], w[i], ww);
+      wv = fma(w[i], v[i], wv);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      ww += __shfl_xor_sync(0xffffffffu, ww, o);
+      wv += __shfl_xor_sync(0xffffffffu, wv, o);
+    }
+    if (lane == 0) {
+      const double sj = sqrt(ww);
+      lamJ[b.s_off + j] = wv;
+      if (sj > 1e-12 * smax && fabs(wv) < (1.0 - 1e-6) * sj) atomicExch(flag, 1);
+    }
+  }
+}
+
+// per block: the signed eigenvalues of the unshifted path, ordered by |lambda| descending
+// (ties by the sigma order), as eig_finish does for the shifted one
+__global__ void eig_finish_signed(const SvdBlock* blocks, const int32_t* order, const double* lamJ, double* lam,
+                                  double* absl, int32_t* vcol) {
+  const SvdBlock b = blocks[blockIdx.x];
+  for (int j = threadIdx.x; j < b.nn; j += blockDim.x) {
+    const double v = lamJ[b.s_off + order[b.s_off + j]], av = fabs(v);
+    int rank = 0;
+    for (int k = 0; k < b.nn; ++k) {
+      const double u = fabs(lamJ[b.s_off + order[b.s_off + k]]);
+      rank += (u > av) || (u == av && k < j);
+    }
+    lam[b.s_off + rank] = v;
+    absl[b.s_off + rank] = av;
+    vcol[b.s_off + rank] = order[b.s_off + j];
+  }
+}
+
 // eigenvectors (n x n per block, columns in |lambda| order) from the Jacobi V
 __global__ void eig_vectors(const SvdBlock* blocks, const double* Vw, const int32_t* vcol, double* Vfull,
                             const int64_t* v_off) {
@@ -1557,28 +1606,61 @@ extern "C" nd_status nd_bs_eigen_f64(nd_handle h, int32_t nb, const int64_t* dim
     if (dims[i] <= 0) return nd_fail(h, ND_ERR_ARG, "eigen: block %d has dimension %lld", i, (long long)dims[i]);
     span = std::max(span, offsets[i] + dims[i] * dims[i]);
   }
-  // shifted copy (same layout as A), then the batched Jacobi SVD of every block
-  std::vector<SvdBlock> hb(nb);
-  for (int i = 0; i < nb; ++i) { hb[i] = SvdBlock{}; hb[i].a_off = offsets[i]; hb[i].n = (int)dims[i]; }
-  double *As = nullptr, *shift = nullptr;
-  SvdBlock* dpre = nullptr;
-  ND_CUDA(h, cudaMallocAsync(&As, std::max<int64_t>(span, 1) * 8, s));
-  ND_CUDA(h, cudaMallocAsync(&shift, nb * 8, s));
-  ND_CUDA(h, cudaMallocAsync(&dpre, nb * sizeof(SvdBlock), s));
-  ND_CUDA(h, cudaMemcpyAsync(dpre, hb.data(), nb * sizeof(SvdBlock), cudaMemcpyHostToDevice, s));
-  nd_prof_begin(h, "eig_shift");
-  eig_shift<<<nb, 256, 0, s>>>(dpre, A, As, shift);
-  nd_prof_end(h);
-  ND_LAUNCHED(h);
+  // First the batched Jacobi SVD of the blocks themselves: when every singular vector
+  // pair shows a clean sign (u_j = +-v_j), that is the eigendecomposition, with the full
+  // relative gaps of the spectrum (positive semidefinite blocks, such as density
+  // matrices, always take this path).  Otherwise every block is shifted to
+  // A + c I with c = 1.01 ||A||_F (positive definite) and decomposed again.
   std::vector<SvdBlock> blocks;
-  double *sig = nullptr, *W = nullptr, *Vw = nullptr;
+  double *sig = nullptr, *W = nullptr, *Vw = nullptr, *shift = nullptr, *lamJ = nullptr;
   int32_t* order = nullptr;
   SvdBlock* dblk = nullptr;
   int total = 0;
-  nd_status st = svd_core(h, nb, dims, dims, offsets, As, blocks, &sig, &order, &W, &Vw, &dblk, total);
-  cudaFreeAsync(As, s);
-  cudaFreeAsync(dpre, s);
-  if (st) { cudaFreeAsync(shift, s); return st; }
+  bool shifted = false;
+  nd_status st = svd_core(h, nb, dims, dims, offsets, A, blocks, &sig, &order, &W, &Vw, &dblk, total);
+  if (st == ND_ERR_NOCONV) {
+    shifted = true;                                    // the shifted problem may still converge
+  } else if (st) {
+    return st;
+  } else {
+    int32_t* dflag = nullptr;
+    int32_t hflag = 0;
+    ND_CUDA(h, cudaMallocAsync(&lamJ, std::max(total, 1) * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&dflag, 8, s));
+    ND_CUDA(h, cudaMemsetAsync(dflag, 0, 4, s));
+    nd_prof_begin(h, "eig_sign");
+    eig_sign<<<nb, 256, 0, s>>>(dblk, W, Vw, sig, lamJ, dflag);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    ND_CUDA(h, cudaMemcpyAsync(&hflag, dflag, 4, cudaMemcpyDeviceToHost, s));
+    ND_CUDA(h, cudaStreamSynchronize(s));
+    cudaFreeAsync(dflag, s);
+    if (hflag) {
+      shifted = true;
+      for (void* q : {(void*)sig, (void*)order, (void*)W, (void*)Vw, (void*)dblk, (void*)lamJ}) cudaFreeAsync(q, s);
+      sig = W = Vw = lamJ = nullptr; order = nullptr; dblk = nullptr;
+    }
+  }
+  if (shifted) {
+    h->last_error.clear();
+    std::vector<SvdBlock> hb(nb);
+    for (int i = 0; i < nb; ++i) { hb[i] = SvdBlock{}; hb[i].a_off = offsets[i]; hb[i].n = (int)dims[i]; }
+    double* As = nullptr;
+    SvdBlock* dpre = nullptr;
+    ND_CUDA(h, cudaMallocAsync(&As, std::max<int64_t>(span, 1) * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&shift, nb * 8, s));
+    ND_CUDA(h, cudaMallocAsync(&dpre, nb * sizeof(SvdBlock), s));
+    ND_CUDA(h, cudaMemcpyAsync(dpre, hb.data(), nb * sizeof(SvdBlock), cudaMemcpyHostToDevice, s));
+    nd_prof_begin(h, "eig_shift");
+    eig_shift<<<nb, 256, 0, s>>>(dpre, A, As, shift);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    blocks.clear();
+    st = svd_core(h, nb, dims, dims, offsets, As, blocks, &sig, &order, &W, &Vw, &dblk, total);
+    cudaFreeAsync(As, s);
+    cudaFreeAsync(dpre, s);
+    if (st) { cudaFreeAsync(shift, s); return st; }
+  }
   std::vector<int64_t> vo(nb);
   int64_t vt = 0;
   for (int i = 0; i < nb; ++i) { vo[i] = vt; vt += dims[i] * dims[i]; }
@@ -1590,7 +1672,7 @@ extern "C" nd_status nd_bs_eigen_f64(nd_handle h, int32_t nb, const int64_t* dim
   int* dlen = nullptr;
   auto cleanup = [&]() {
     for (void* p : {(void*)lam, (void*)absl, (void*)Vf, (void*)P, (void*)res, (void*)vcol, (void*)dkept, (void*)dvo,
-                    (void*)dlen, (void*)sig, (void*)order, (void*)W, (void*)Vw, (void*)dblk, (void*)shift})
+                    (void*)dlen, (void*)sig, (void*)order, (void*)W, (void*)Vw, (void*)dblk, (void*)shift, (void*)lamJ})
       if (p) cudaFreeAsync(p, s);
   };
   if ((size_t)npow2 * 8 > 200 * 1024) { cleanup(); return nd_fail(h, ND_ERR_UNSUPPORTED, "eigen: %d eigenvalues exceed the on-chip sort", total); }
@@ -1604,7 +1686,8 @@ extern "C" nd_status nd_bs_eigen_f64(nd_handle h, int32_t nb, const int64_t* dim
   if (e == cudaSuccess) e = cudaMemcpyAsync(dvo, vo.data(), nb * 8, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) { cleanup(); return nd_cuda_check(h, e, "eigen buffers"); }
   nd_prof_begin(h, "eig_finish");
-  eig_finish<<<nb, 256, 0, s>>>(dblk, sig, order, shift, lam, absl, vcol);
+  if (shifted) eig_finish<<<nb, 256, 0, s>>>(dblk, sig, order, shift, lam, absl, vcol);
+  else eig_finish_signed<<<nb, 256, 0, s>>>(dblk, order, lamJ, lam, absl, vcol);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   {

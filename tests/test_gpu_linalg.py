@@ -259,6 +259,44 @@ def test_eigen_blockwise_matches_oracle(nd, case):
         np.testing.assert_allclose(m @ vec, vec * lam, rtol=0, atol=1e-11 * scale)   # eigenpairs
 
 
+@pytest.mark.parametrize("kind", ["psd", "plus_minus_pairs"])
+def test_eigen_unshifted_and_fallback_paths(nd, kind):
+    """Positive semidefinite blocks (density matrices) take the unshifted path: the SVD of
+    the block is its eigendecomposition.  Blocks with exact +-lambda pairs make the
+    singular vectors of a pair mix, which the sign check catches, and the shifted path
+    decomposes them instead.  Both vs the oracle (numpy eigh)."""
+    rng = np.random.default_rng(64 if kind == "psd" else 65)
+    mats = []
+    for n in (90, 250, 12):
+        q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        if kind == "psd":
+            lam = np.exp(rng.uniform(-18, 0, n))
+        else:
+            half = np.exp(rng.uniform(-6, 0, n // 2))
+            lam = np.concatenate([half, -half, [0.5]][: 3 if n % 2 else 2])[:n]
+        mats.append((q * lam) @ q.T)
+    dims = [m.shape[0] for m in mats]
+    offs, o = [], 0
+    for m in mats:
+        offs.append(o)
+        o += m.size
+    A = obs.BlockSparseTensor([dims, dims], [(i + 1, i + 1) for i in range(len(dims))], offs,
+                              np.concatenate([m.reshape(-1, order="F") for m in mats]))
+    kw = {"maxdim": 200, "cutoff": 1e-12}
+    ref = olin.eigen_blocks(mats, **kw)
+    D, V, spec, kept = nd.eigen(_gpu(nd, A), **kw)
+    assert kept == ref["kept"]
+    Vb = _blocks(nd, V)
+    surv = [n for n in range(len(mats)) if kept[n] > 0]
+    for i, n in enumerate(surv):
+        m, lam, vec = mats[n], D[i].cpu().numpy(), Vb[i]
+        scale = np.linalg.norm(m)
+        np.testing.assert_allclose(np.sort(np.abs(lam))[::-1], np.sort(np.abs(ref["D"][i]))[::-1], rtol=0,
+                                   atol=1e-12 * scale)
+        np.testing.assert_allclose(vec.T @ vec, np.eye(len(lam)), atol=1e-12)
+        np.testing.assert_allclose(m @ vec, vec * lam, rtol=0, atol=1e-11 * scale)
+
+
 def test_diag_blocksparse_contraction_rebuilds_svd(nd):
     """BlockSparse x DiagBlockSparse (blocksparse/diagblocksparse.jl:601-696): U * S * V^T
     rebuilt from the blockwise SVD equals the input; the output structure is the plan's
