@@ -150,7 +150,19 @@ __global__ void __launch_bounds__(VEC_THREADS) vec_add(int64_t n, const double* 
   }
 }
 
-int vec_ctas(nd_handle h) { return 4 * h->num_sms; }
+int vec_ctas(nd_handle h) { return 4 * h->num_sms; }   // upper bound of the reduction grid (partials buffer)
+
+// Reduction grid of one instantiation: the CTAs that are resident at once (at most
+// vec_ctas), so the fixed grid runs in one wave.  Queried once per instantiation.
+template <int KT>
+int dots_ctas(nd_handle h) {
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vec_dots_part<KT>, VEC_THREADS, 0);
+    per_sm = std::max(1, std::min(per_sm, 4));
+  }
+  return per_sm * h->num_sms;
+}
 
 nd_status vec_partials(nd_handle h, double** part) {
   // fixed per-handle buffer: the reductions must not allocate (they are captured in graphs)
@@ -169,7 +181,7 @@ nd_status dots(nd_handle h, int64_t n, int32_t k, const double* V, int64_t ldv, 
   double* part = nullptr;
   nd_status s = vec_partials(h, &part);
   if (s) return s;
-  const int ctas = vec_ctas(h);
+  const int ctas = k <= 1 ? dots_ctas<1>(h) : k <= 8 ? dots_ctas<8>(h) : k <= 16 ? dots_ctas<16>(h) : dots_ctas<32>(h);
   // chunk: a multiple of VEC_THREADS * 8 (every unroll factor divides it)
   constexpr int64_t q = VEC_THREADS * 8;
   int64_t chunk = (n + ctas - 1) / ctas;
