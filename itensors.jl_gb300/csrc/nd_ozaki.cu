@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(256) pack_rowmax(PackArgs2 a) {
       uint32_t mx = 0u;
       if (rv) {
         const unsigned int* rowp = (const unsigned int*)(src + rowoff[r]) + 1;   // high 32 bits of each double
+#pragma unroll 4
         for (int ks = 0; ks < ks1 - ks0; ++ks) {
 #pragma unroll
           for (int e = 0; e < 8; ++e) {
@@ -315,6 +316,7 @@ __global__ void __launch_bounds__(256) pack_digits(PackArgs2 a) {
         if (pi.kc == 0 && c == 0) a.exps[op.exp_off + pi.rt * ROWS + r] = E;
       }
       const double* rowp = src + rowoff[r];
+#pragma unroll 2
       for (int ks = ks0; ks < ks1; ++ks) {
         unsigned char* tile = a.pack + op.pack_off + ((int64_t)(pi.rt * op.k_steps + ks) * S) * (ROWS * 64);
         uint32_t w[S][4];
