@@ -909,16 +909,20 @@ def cfg_sweep_ops(args):
     out["vec_update_k10"] = gbs(8 * n * (k + 2), lambda: h.call("nd_vec_update_f64", n, k, P(V), n, P(coef), -1.0, P(w)))
     out["vec_norm"] = gbs(8 * n, lambda: h.call("nd_vec_norm_f64", n, P(w), P(coef)))
     out["vec_scale"] = gbs(16 * n, lambda: h.call("nd_vec_scale_f64", n, P(w), P(V), 1.0, P(coef), 1))
-    # block plans of the four H_eff contractions (device planner; oracle: the sequential loop)
-    x, pl_ms, pl_cpu = G["L"], [], []
+    # block plans of the four H_eff contractions (each placement of the planner, wall time
+    # of ContractionPlan per plan with the GPU idle; oracle: the sequential loop)
+    x, pl_ms, pl_cpu = G["L"], {"host": [], "device": []}, []
     for (a, b, c), key in zip(st, ("psi", "W1", "W2", "R")):
         T = G[key]
-        nd.ContractionPlan(x, a, T, b, c).destroy()
-        t0 = time.perf_counter()
-        for _ in range(10):
-            pl = nd.ContractionPlan(x, a, T, b, c)
-            pl.destroy()
-        pl_ms.append(round((time.perf_counter() - t0) * 100, 4))
+        for where, name in ((2, "host"), (1, "device")):
+            h.call("nd_set_plan_placement", where)
+            nd.ContractionPlan(x, a, T, b, c).destroy()
+            t0 = time.perf_counter()
+            for _ in range(10):
+                pl = nd.ContractionPlan(x, a, T, b, c)
+                pl.destroy()
+            pl_ms[name].append(round((time.perf_counter() - t0) * 100, 4))
+        h.call("nd_set_plan_placement", 0)
         ox = obs.BlockSparseTensor([tuple(i) for i in x.inds], [tuple(bb) for bb in x.blocks], list(x.offsets),
                                    np.zeros(1))
         oT = obs.BlockSparseTensor([tuple(i) for i in T.inds], [tuple(bb) for bb in T.blocks], list(T.offsets),
@@ -927,7 +931,8 @@ def cfg_sweep_ops(args):
         obs.contract_blockoffsets(ox, a, oT, b, c)
         pl_cpu.append(round((time.perf_counter() - t0) * 1e3, 4))
         x = nd.contract(x, a, T, b, c, precision="ozaki")
-    out["block_plan_ms"] = {"device_planner_wall_ms": pl_ms, "oracle_sequential_ms": pl_cpu}
+    out["block_plan_ms"] = {"host_planner_wall_ms": pl_ms["host"], "device_planner_wall_ms": pl_ms["device"],
+                            "oracle_sequential_ms": pl_cpu}
     # truncated SVD of psi's matricisation, then U * S (diagonal contraction) and uncombine
     sec = net["sectors"]
     qinds = [(sec, 1), (wl.SPIN_SECTORS, 1), (wl.SPIN_SECTORS, 1), (sec, -1)]

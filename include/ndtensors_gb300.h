@@ -97,6 +97,11 @@ nd_status nd_cta_times_read(nd_handle h, uint64_t* times, int32_t* nctas, int32_
  * tiles on pairs of CTAs (tcgen05.mma.cta_group::2).  With tuning on, both are timed
  * and the faster is cached.  No counterpart in the reference. */
 nd_status nd_set_split_tile(nd_handle h, int32_t shape);
+/* Where nd_bs_plan_create builds plans: 0 (default) = on the host up to 4096 pairs,
+ * else on the device; 1 = always on the device; 2 = on the host whenever the
+ * contracted block numbers fit a 64-bit key.  Every placement gives the same plan.
+ * No counterpart in the reference (its plan is host code). */
+nd_status nd_set_plan_placement(nd_handle h, int32_t where);
 /* Number of slice digits used by ND_PREC_OZAKI (3..6, default 5). */
 nd_status nd_set_ozaki_slices(nd_handle h, int32_t slices);
 /* Count of kernel launches this handle enqueued so far (diagnostics). */
@@ -165,12 +170,13 @@ typedef struct {
   const int64_t *offsets;    /* [nnzblocks] 0-based element offsets                      */
 } nd_bs_desc;
 
-/* Build the contraction plan ON THE DEVICE: the list of contracted block pairs
- * in the reference's sequential order (A-block major, B-block minor), the
- * output block list in first-appearance order and its offsets.  Bit-exact with
+/* Build the contraction plan: the list of contracted block pairs in the
+ * reference's sequential order (A-block major, B-block minor), the output block
+ * list in first-appearance order and its offsets.  Bit-exact with
  * contract_blockoffsets(::Algorithm"sequential", ...)
  * (NDTensors/src/blocksparse/contract_sequential.jl:1-41,
- *  contract_utilities.jl:45-91, contract.jl:20-55). */
+ *  contract_utilities.jl:45-91, contract.jl:20-55).  Plans of up to 4096 pairs are
+ * built on the host, larger ones by the device planner (see nd_set_plan_placement). */
 nd_status nd_bs_plan_create(nd_handle h, const nd_bs_desc *A, const int32_t *labelsA,
                             const nd_bs_desc *B, const int32_t *labelsB,
                             int32_t rankR, const int32_t *labelsR, nd_plan *plan);

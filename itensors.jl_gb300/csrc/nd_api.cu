@@ -283,6 +283,13 @@ nd_status nd_set_split_tile(nd_handle h, int32_t shape) {
   return ND_OK;
 }
 
+nd_status nd_set_plan_placement(nd_handle h, int32_t where) {
+  if (!h) return ND_ERR_ARG;
+  if (where < 0 || where > 2) return nd_fail(h, ND_ERR_ARG, "plan placement must be 0 (by size), 1 (device) or 2 (host)");
+  h->plan_where = where;
+  return ND_OK;
+}
+
 nd_status nd_set_ozaki_slices(nd_handle h, int32_t s) {
   if (!h) return ND_ERR_ARG;
   if (s < 3 || s > 6) return nd_fail(h, ND_ERR_ARG, "ozaki slices must be in 3..6 (got %d)", s);

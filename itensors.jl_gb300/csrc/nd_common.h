@@ -75,6 +75,7 @@ struct nd_context {
   // plan waits only for the planner, not for contractions queued on the handle's stream
   cudaStream_t plan_stream = nullptr;
   DeviceStatus* d_plan_status = nullptr;
+  int plan_where = 0;                 // nd_set_plan_placement: 0 by size, 1 device, 2 host
   // pinned ring for descriptor uploads (nd_upload): region [begin, end) may be reused
   // once its copy's event has completed
   unsigned char* up_ring = nullptr;

@@ -229,9 +229,14 @@ static nd_status build_exec(nd_handle h, ExecCache& c, const std::vector<PairDes
     c.nitems = (int)items.size();
     if ((s = upload(h, (void**)&c.d_items, items.data(), items.size() * sizeof(WorkItem)))) return s;
   } else {
-    std::vector<PairDesc> regular;
-    for (size_t i = 0; i < pairs.size(); ++i) if (!sk[i]) regular.push_back(pairs[i]);
-    if (!regular.empty() && (s = nd_split_build(h, c, regular, ngroups, precision, tc.pair2))) return s;
+    if (!any_sk) {
+      if ((s = nd_split_build(h, c, pairs, ngroups, precision, tc.pair2))) return s;
+    } else {
+      std::vector<PairDesc> regular;
+      regular.reserve(pairs.size());
+      for (size_t i = 0; i < pairs.size(); ++i) if (!sk[i]) regular.push_back(pairs[i]);
+      if (!regular.empty() && (s = nd_split_build(h, c, regular, ngroups, precision, tc.pair2))) return s;
+    }
   }
   c.built = true;
   return ND_OK;
@@ -501,7 +506,7 @@ extern "C" nd_status nd_bs_plan_create(nd_handle h, const nd_bs_desc* A, const i
     p->r_nblocks[ro.r_bfree[t]] = p->B.nblocks[ro.b_free[t]];
     p->r_blockdims[ro.r_bfree[t]] = p->B.blockdims[ro.b_free[t]];
   }
-  s = nd_device_plan(h, ro, p->A, p->B, p->r_nblocks, p->r_blockdims, p->res);
+  s = nd_block_plan(h, ro, p->A, p->B, p->r_nblocks, p->r_blockdims, p->res);
   if (s) { delete p; return s; }
   *plan = p;
   return ND_OK;
@@ -558,6 +563,7 @@ static nd_status build_forward_descs(nd_plan p) {
   std::vector<std::vector<int>> by_group(r.nR);
   for (int q = 0; q < r.npairs; ++q) by_group[r.pairs[3 * q + 2]].push_back(q);
   std::string why;
+  p->descs.reserve(r.npairs);
   for (int g = 0; g < r.nR; ++g) {
     int64_t dR[ND_MAX_RANK];
     for (int k = 0; k < rankR; ++k) dR[k] = p->r_blockdims[k][r.blocksR[(size_t)g * rankR + k] - 1];

@@ -1163,16 +1163,21 @@ std::vector<WorkItem> balance_items(const std::vector<std::pair<int64_t, WorkIte
   // index).  Tiles come in runs of equal cost c.  While every load lies within c of the
   // smallest, LPT gives G consecutive tiles of a run to the slots in (load, index) order
   // and keeps that order, so such a run is assigned in O(n) and the order repaired once
-  // (a merge); otherwise the run goes tile by tile through a heap.
+  // (a merge); otherwise the run goes tile by tile through a heap.  `order` is kept
+  // either sorted or as that heap (the sorted array is a valid heap), and sorted again
+  // only when a dealt run follows heap runs.
   std::vector<int> slot_of(tmp.size()), count(G, 0);
-  std::vector<std::pair<int64_t, int>> order(G);                 // (load, slot), ascending
+  std::vector<std::pair<int64_t, int>> order(G);                 // (load, slot)
   for (int b = 0; b < G; ++b) order[b] = {0, b};
   auto later = [](const auto& x, const auto& y) { return x.first > y.first || (x.first == y.first && x.second > y.second); };
+  bool sorted = true;
+  int64_t maxload = 0;
   for (size_t t0 = 0; t0 < tmp.size();) {
     size_t t1 = t0;
     while (t1 < tmp.size() && tmp[t1].first == tmp[t0].first) ++t1;
     const int64_t c = tmp[t0].first;
-    if (order.back().first - order.front().first < c) {
+    if (maxload - order.front().first < c) {      // front: the smallest load, sorted or heap
+      if (!sorted) { std::sort(order.begin(), order.end()); sorted = true; }
       const size_t n = t1 - t0, q = n / G, r = n % G;
       for (size_t t = t0; t < t1; ++t) {
         const int b = order[(t - t0) % G].second;
@@ -1181,16 +1186,17 @@ std::vector<WorkItem> balance_items(const std::vector<std::pair<int64_t, WorkIte
       }
       for (int k = 0; k < G; ++k) order[k].first += (int64_t)q * c + ((size_t)k < r ? c : 0);
       std::inplace_merge(order.begin(), order.begin() + r, order.end());
+      maxload = order.back().first;
     } else {
-      std::make_heap(order.begin(), order.end(), later);
+      if (sorted) { std::make_heap(order.begin(), order.end(), later); sorted = false; }
       for (size_t t = t0; t < t1; ++t) {
         std::pop_heap(order.begin(), order.end(), later);
         slot_of[t] = order.back().second;
         ++count[order.back().second];
         order.back().first += c;
+        maxload = std::max(maxload, order.back().first);
         std::push_heap(order.begin(), order.end(), later);
       }
-      std::sort(order.begin(), order.end());
     }
     t0 = t1;
   }
@@ -1291,6 +1297,15 @@ static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int
   }
   std::stable_sort(grps.begin(), grps.end(), [](const Grp& x, const Grp& y) { return x.cost > y.cost; });
   std::vector<std::pair<int64_t, WorkItem>> tmp;
+  {
+    size_t ntiles = 0;
+    for (const Grp& g : grps) {
+      const PairDesc& p = L.pairs[g.i];
+      const size_t mt = (p.M + BM - 1) / BM;
+      ntiles += (L.pair2 ? (mt + 1) / 2 : mt) * ((p.N + BN - 1) / BN);
+    }
+    tmp.reserve(ntiles);
+  }
   for (const Grp& g : grps) {
     const PairDesc& p = L.pairs[g.i];
     int mt = (p.M + BM - 1) / BM;

@@ -31,9 +31,11 @@ struct PlanResult {
 };
 
 nd_status nd_device_exclusive_scan(nd_handle h, int64_t* data, int64_t n, int64_t* total_dev);
-nd_status nd_device_plan(nd_handle h, const Roles& ro, const BsDesc& A, const BsDesc& B,
-                         const std::vector<int64_t>& r_nblocks,
-                         const std::vector<std::vector<int64_t>>& r_blockdims, PlanResult& out);
+// The block plan of A x B: on the host up to a few thousand pairs, else on the device
+// (nd_set_plan_placement overrides the choice); both give the same plan.
+nd_status nd_block_plan(nd_handle h, const Roles& ro, const BsDesc& A, const BsDesc& B,
+                        const std::vector<int64_t>& r_nblocks,
+                        const std::vector<std::vector<int64_t>>& r_blockdims, PlanResult& out);
 
 // Device-resident execution state of one contraction (built once, reused by
 // every call and by captured graphs).

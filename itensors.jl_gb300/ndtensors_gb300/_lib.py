@@ -65,6 +65,7 @@ SIGNATURES = {
     "nd_memset0": [_P, _P, C.c_size_t],
     "nd_set_ozaki_slices": [_P, _I32],
     "nd_set_split_tile": [_P, _I32],
+    "nd_set_plan_placement": [_P, _I32],
     "nd_set_spin_limit": [_P, C.c_uint32],
     "nd_set_svd_max_sweeps": [_P, _I32],
     "nd_svd_last_info": [_P, _P, _I32, _P, _I32],

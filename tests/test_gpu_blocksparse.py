@@ -127,6 +127,59 @@ def test_adjoint(nd, precision):
     assert odense.rel_frobenius_error(Bb, gB) <= TOL[precision]
 
 
+def _plan_structure(nd, GA, la, GB, lb, lr):
+    p = nd.ContractionPlan(GA, la, GB, lb, lr)
+    s = (p.pairs, p.blocksR, p.offsetsR, p.nnzR)
+    p.destroy()
+    return s
+
+
+def _placement_cases():
+    """(A, labels A, B, labels B, labels R) covering several shapes of plan."""
+    rng = np.random.default_rng(410)
+    out = []
+    A, B, _ = networks.qn_pair(2048)
+    out.append((A, (1, 2, -1), B, (-1, 3, 4), (1, 2, 3, 4)))
+    for seed in range(3):
+        r = np.random.default_rng(420 + seed)
+        nq = 3
+        def idx(tag):
+            return _q([[q, int(r.integers(1, 6))] for q in range(-nq, nq + 1)], 1, tag)
+        i, j, k, m = idx("i"), idx("j"), idx("k"), idx("m")
+        A_inds, B_inds = [i, k.dag(), j], [m, k, j.dag()]
+        A = obs.random_blocksparse(r, [x.dims for x in A_inds], qn.nzblocks(0, A_inds))
+        B = obs.random_blocksparse(r, [x.dims for x in B_inds], qn.nzblocks(0, B_inds))
+        out.append((A, (1, -1, -2), B, (2, -1, -2), (2, 1) if seed % 2 else (1, 2)))
+    # no contracted index (outer product): every pair matches, 90 x 70 = 6300 pairs, more
+    # than the host placement takes by default
+    A = obs.random_blocksparse(rng, [(1,) * 90, (2,)], [(a, 1) for a in range(1, 91)])
+    B = obs.random_blocksparse(rng, [(1,) * 70], [(b,) for b in range(1, 71)])
+    out.append((A, (1, 2), B, (3,), (3, 1, 2)))
+    # two contracted indices, B blocks listed out of order, output order swapped
+    A = obs.random_blocksparse(rng, [(3, 4), (2, 2, 5), (1, 2)], [(1, 1, 2), (2, 2, 1), (1, 3, 1), (2, 3, 2)])
+    B = obs.random_blocksparse(rng, [(2, 2, 5), (1, 2), (6, 2)], [(3, 1, 1), (2, 1, 2), (3, 2, 2), (1, 2, 1)])
+    out.append((A, (1, -1, -2), B, (-1, -2, 2), (2, 1)))
+    return out
+
+
+def test_plan_placements_agree(nd):
+    """Host planner, device planner and the size-based choice give the reference's plan:
+    pairs, output blocks and offsets bit-exact with the oracle in every placement."""
+    h = nd.handle(0)
+    try:
+        for A, la, B, lb, lr in _placement_cases():
+            ref, plan = obs.contract(A, la, B, lb, lr)
+            want = ([tuple(x) for x in plan], [tuple(b) for b in ref.blocks], list(ref.offsets), ref.nnz)
+            GA, GB = nd.BlockSparseTensor.from_oracle(A), nd.BlockSparseTensor.from_oracle(B)
+            for where in (2, 1, 0):
+                h.call("nd_set_plan_placement", where)
+                assert _plan_structure(nd, GA, la, GB, lb, lr) == want, f"placement {where}"
+        with pytest.raises(nd.NDError):
+            h.call("nd_set_plan_placement", 3)
+    finally:
+        h.call("nd_set_plan_placement", 0)
+
+
 def test_plan_rejects_mismatched_blocks(nd):
     A = obs.random_blocksparse(np.random.default_rng(0), [[2, 3], [4, 5]], [(1, 1)])
     B = obs.random_blocksparse(np.random.default_rng(0), [[4, 6], [2]], [(1, 1)])
