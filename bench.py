@@ -590,6 +590,7 @@ def cfg_permute_sweep(args):
     import torch
     import ndtensors_gb300 as nd
     pk = peaks()
+    h = nd.handle(0)
     cases = [((1024, 1024, 128), (3, 2, 1)), ((1024, 1024, 128), (2, 1, 3)), ((1024, 1024, 128), (1, 3, 2)),
              ((128, 128, 64, 128), (4, 3, 2, 1)), ((128, 128, 64, 128), (2, 3, 4, 1)),
              ((32, 64, 32, 64, 32), (5, 4, 3, 2, 1)), ((32, 64, 32, 64, 32), (2, 1, 4, 3, 5)),
@@ -599,15 +600,21 @@ def cfg_permute_sweep(args):
         n = int(np.prod(dims))
         T = nd.DenseTensor(tuple(dims), torch.randn(n, dtype=torch.float64, device="cuda"))
         R = nd.DenseTensor.empty(tuple(dims[p - 1] for p in perm))
-        for _ in range(3):
-            nd.permutedims_(R, T, perm)
-        ts = _events_ms(lambda: nd.permutedims_(R, T, perm), max(5, min(args.steps, 10)))
-        ms = float(np.median(ts))
-        gbs = 2 * n * 8 / (ms * 1e-3) / 1e9
-        ok = bool(torch.equal(R.data.view(*reversed(R.dims)),
-                              T.data.view(*reversed(dims)).permute(*[len(dims) - p for p in reversed(perm)])))
+        want = T.data.view(*reversed(dims)).permute(*[len(dims) - p for p in reversed(perm)])
+        res = {}
+        for path in (1, 0):          # TMA tiles (where they apply), then the default group tiles
+            h.call("nd_set_permute_path", path)
+            for _ in range(3):
+                nd.permutedims_(R, T, perm)
+            ts = _events_ms(lambda: nd.permutedims_(R, T, perm), max(5, min(args.steps, 10)))
+            ms = float(np.median(ts))
+            res[path] = (ms, 2 * n * 8 / (ms * 1e-3) / 1e9, bool(torch.equal(R.data.view(*reversed(R.dims)), want)))
+        h.call("nd_set_permute_path", 0)
+        ms, gbs, ok = res[0]
         out.append({"dims": list(dims), "perm": list(perm), "ms": round(ms, 4), "GB/s": round(gbs, 1),
-                    "frac": round(gbs / pk["hbm_gbs"], 3), "exact": ok})
+                    "frac": round(gbs / pk["hbm_gbs"], 3), "exact": ok and res[1][2],
+                    "tma_path_GB/s": round(res[1][1], 1)})
+        del want
         del T, R
         torch.cuda.empty_cache()
     best = max(o["GB/s"] for o in out)

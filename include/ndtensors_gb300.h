@@ -97,6 +97,11 @@ nd_status nd_cta_times_read(nd_handle h, uint64_t* times, int32_t* nctas, int32_
  * tiles on pairs of CTAs (tcgen05.mma.cta_group::2).  With tuning on, both are timed
  * and the faster is cached.  No counterpart in the reference. */
 nd_status nd_set_split_tile(nd_handle h, int32_t shape);
+/* Transposing permutes: 0 (default) = shared-memory tiles over dimension groups with
+ * plain loads; 1 = TMA-staged tiles (cp.async.bulk.tensor) for shapes a 5-D tensor
+ * map describes, the group tiles otherwise.  Both are bit-exact.  No counterpart in
+ * the reference. */
+nd_status nd_set_permute_path(nd_handle h, int32_t path);
 /* Where nd_bs_plan_create builds plans: 0 (default) = on the host up to 4096 pairs,
  * else on the device; 1 = always on the device; 2 = on the host whenever the
  * contracted block numbers fit a 64-bit key.  Every placement gives the same plan.

@@ -290,6 +290,13 @@ nd_status nd_set_plan_placement(nd_handle h, int32_t where) {
   return ND_OK;
 }
 
+nd_status nd_set_permute_path(nd_handle h, int32_t path) {
+  if (!h) return ND_ERR_ARG;
+  if (path != 0 && path != 1) return nd_fail(h, ND_ERR_ARG, "permute path must be 0 (dimension-group tiles) or 1 (TMA tiles)");
+  h->permute_tma = path;
+  return ND_OK;
+}
+
 nd_status nd_set_ozaki_slices(nd_handle h, int32_t s) {
   if (!h) return ND_ERR_ARG;
   if (s < 3 || s > 6) return nd_fail(h, ND_ERR_ARG, "ozaki slices must be in 3..6 (got %d)", s);

@@ -76,6 +76,7 @@ struct nd_context {
   cudaStream_t plan_stream = nullptr;
   DeviceStatus* d_plan_status = nullptr;
   int plan_where = 0;                 // nd_set_plan_placement: 0 by size, 1 device, 2 host
+  int permute_tma = 0;                // nd_set_permute_path: 1 = TMA tiles where they apply
   // pinned ring for descriptor uploads (nd_upload): region [begin, end) may be reused
   // once its copy's event has completed
   unsigned char* up_ring = nullptr;

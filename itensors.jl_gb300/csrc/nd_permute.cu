@@ -9,13 +9,17 @@
 // layouts are fused.  Then:
 //   * perm[0] == 0: both tensors share their contiguous dimension, rows are
 //     copied with 128-bit accesses (kernel permute_rows);
-//   * otherwise a tiled transpose between T's contiguous dimension (i) and the
-//     T dimension that becomes R's contiguous one (j).  Tiles of 32(i) x 64(j)
-//     FP64 are staged in shared memory by TMA (cp.async.bulk.tensor, 128-byte
-//     swizzle, 4-stage mbarrier ring in a persistent grid) and written to R
-//     with 128-bit stores along j (kernel permute_tma).  Shapes TMA cannot
-//     describe (rank > 5 after fusion, odd leading extent, unaligned base) use
-//     the same tiling with plain loads (kernel permute_tiles).
+//   * otherwise a tiled transpose through shared memory, 32(i) x 64(j) FP64 tiles
+//     with i flattened over several T dims (T's contiguous one first) and j over
+//     several R dims (R's contiguous one first), so tiles stay full however small
+//     each extent is (kernel permute_groups, plain loads);
+//   * on request (nd_set_permute_path), a TMA variant tiles T's contiguous dim (i)
+//     against the T dim that becomes R's contiguous one (j): tiles staged by
+//     cp.async.bulk.tensor (128-byte swizzle, 4-stage mbarrier ring, persistent
+//     grid), 128-bit stores along j (kernel permute_tma).  It was the default until
+//     the group tiling measured faster on every shape of the 1 GiB rank-3..6 sweep
+//     (0.86-0.96 of HBM against 0.83-0.89 for the shapes TMA takes; 0.46 / 0.30
+//     for TMA and the one-dimension plain tiling on rank-5 / rank-6 reversals).
 #include "nd_common.h"
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -45,6 +49,12 @@ struct PermParams {
   int32_t fast;
   uint32_t mul_j, shr_j, mul_i, shr_i;
   uint32_t bmul[ND_MAX_RANK], bshr[ND_MAX_RANK];
+  // permute_groups: i runs over the dims of group I (T's dim 0 first), j over the dims
+  // of group J (R's dim 0 first); both flattened, with their T and R strides
+  int32_t ni, nj;
+  int64_t iext[ND_MAX_RANK], its[ND_MAX_RANK], irs[ND_MAX_RANK];
+  int64_t jext[ND_MAX_RANK], jts[ND_MAX_RANK], jrs[ND_MAX_RANK];
+  uint32_t imul[ND_MAX_RANK], ishr[ND_MAX_RANK], jmul[ND_MAX_RANK], jshr[ND_MAX_RANK];
 };
 
 // q = x / d for 0 <= x < 2^31 with the divisor's precomputed (mul, shr), else plain division
@@ -234,11 +244,33 @@ __global__ void __launch_bounds__(256) permute_tma(const __grid_constant__ CUten
   }
 }
 
-// Same tiling, plain loads: T[i, j, batch] -> smem (padded) -> R.
+// T and R offsets of flattened index x over extents ext[0..n) (ext[0] fastest).
+__device__ __forceinline__ void group_offsets(const PermParams& p, int64_t x, int n, const int64_t* ext,
+                                              const int64_t* st, const int64_t* sr, const uint32_t* mul,
+                                              const uint32_t* shr, int64_t& ot, int64_t& orr) {
+  ot = 0;
+  orr = 0;
+  for (int k = 0; k < n; ++k) {
+    const int64_t q = k + 1 < n ? pdiv(p, x, ext[k], mul[k], shr[k]) : 0;
+    const int64_t r = x - q * ext[k];
+    ot += r * st[k];
+    orr += r * sr[k];
+    x = q;
+  }
+}
+
+// Tiled transpose over dimension groups, plain loads: T -> smem (padded) -> R.  The
+// tile's i axis is flattened over the dims of group I (T's dim 0 first, so a warp's 32
+// loads along i are contiguous over that dim) and its j axis over group J (R's dim 0
+// first, so a warp's stores along j are contiguous over that dim); the groups are
+// filled up to 32 and 64 elements, so tiles stay full however small each extent is.
+// Per tile the T and R offsets of its i's and j's are decoded once into shared
+// memory; each thread issues its eight loads before storing any of them.
 template <bool COPY>
-__global__ void __launch_bounds__(256) permute_tiles(const double* __restrict__ T, double* R,
-                                                     const double* Rin, PermParams p) {
+__global__ void __launch_bounds__(256) permute_groups(const double* __restrict__ T, double* R,
+                                                      const double* Rin, PermParams p) {
   __shared__ double tile[TJ][TI + 1];
+  __shared__ int64_t jt[TJ], jr[TJ], it[TI], ir[TI];
   const double a = eff_alpha(p);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int64_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
@@ -249,20 +281,47 @@ __global__ void __launch_bounds__(256) permute_tiles(const double* __restrict__ 
     int64_t to, ro;
     batch_offsets(p, b, to, ro, nullptr);
     const int64_t i0 = ti * TI, j0 = tj * TJ;
-    // load: lanes along i (T-contiguous)
-    for (int jj = warp; jj < TJ; jj += 8) {
-      int64_t j = j0 + jj, i = i0 + lane;
-      tile[jj][lane] = (j < p.dq && i < p.d0) ? __ldg(T + to + j * p.ts_j + i) : 0.0;
+    if (tid < TJ) {
+      const int64_t j = j0 + tid;
+      int64_t ot = 0, orr = 0;
+      if (j < p.dq) group_offsets(p, j, p.nj, p.jext, p.jts, p.jrs, p.jmul, p.jshr, ot, orr);
+      jt[tid] = to + ot;
+      jr[tid] = ro + orr;
+    } else if (tid < TJ + TI) {
+      const int64_t i = i0 + tid - TJ;
+      int64_t ot = 0, orr = 0;
+      if (i < p.d0) group_offsets(p, i, p.ni, p.iext, p.its, p.irs, p.imul, p.ishr, ot, orr);
+      it[tid - TJ] = ot;
+      ir[tid - TJ] = orr;
     }
     __syncthreads();
-    for (int ii = warp; ii < TI; ii += 8) {
-      int64_t i = i0 + ii;
-      if (i >= p.d0) break;
-      for (int jj = lane; jj < TJ; jj += 32) {
-        int64_t j = j0 + jj;
-        if (j < p.dq) {
-          int64_t roff = ro + i * p.rs_i + j;
-          R[roff] = combine<COPY>(p, a, tile[jj][ii], Rin + roff);
+    // load: lanes along i
+    {
+      const bool iok = i0 + lane < p.d0;
+      const int64_t oi = it[lane];
+      double v[TJ / 8];
+#pragma unroll
+      for (int k = 0; k < TJ / 8; ++k) {
+        const int jj = warp + 8 * k;
+        v[k] = (iok && j0 + jj < p.dq) ? __ldg(T + jt[jj] + oi) : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < TJ / 8; ++k) tile[warp + 8 * k][lane] = v[k];
+    }
+    __syncthreads();
+    // store: lanes along j
+#pragma unroll
+    for (int k = 0; k < TI / 8; ++k) {
+      const int ii = warp + 8 * k;
+      if (i0 + ii < p.d0) {
+        const int64_t ri = ir[ii];
+#pragma unroll
+        for (int h = 0; h < TJ / 32; ++h) {
+          const int jj = lane + 32 * h;
+          if (j0 + jj < p.dq) {
+            const int64_t roff = ri + jr[jj];
+            R[roff] = combine<COPY>(p, a, tile[jj][ii], Rin + roff);
+          }
         }
       }
     }
@@ -396,32 +455,33 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
   }
   // transpose: i = T group 0, j = T group gperm[0]
   int q = gperm[0];
-  p.d0 = gd[0];
-  p.dq = gd[q];
-  p.rs_i = rs[0];
-  p.ts_j = ts[q];
-  p.q = q;
-  p.nb = 0;
-  for (int g = 1; g < ng; ++g) {
-    if (g == q) continue;
-    p.bdim[p.nb] = gd[g]; p.bts[p.nb] = ts[g]; p.brs[p.nb] = rs[g]; p.bcoord[p.nb] = g; p.nb++;
-  }
-  p.ntile_i = (p.d0 + TI - 1) / TI;
-  p.ntile_j = (p.dq + TJ - 1) / TJ;
-  int64_t nbatch = total / (p.d0 * p.dq);
-  p.ntiles = p.ntile_i * p.ntile_j * nbatch;
-  p.fast = p.ntiles < (int64_t)0x7fffffff;
-  fast_divisor(p.ntile_j, p.mul_j, p.shr_j);
-  fast_divisor(p.ntile_i, p.mul_i, p.shr_i);
-  for (int b = 0; b < p.nb; ++b) fast_divisor(p.bdim[b], p.bmul[b], p.bshr[b]);
-  bool rvec = ((uintptr_t)R % 16 == 0) && (p.rs_i % 2 == 0);
-  for (int b = 0; b < p.nb; ++b) if (p.brs[b] % 2) rvec = false;
-  p.vec = rvec ? 1 : 0;
-
+  bool rvec = ((uintptr_t)R % 16 == 0) && (rs[0] % 2 == 0);
+  for (int g = 1; g < ng; ++g) if (g != q && rs[g] % 2) rvec = false;
   auto enc = encode_fn();
-  bool tma_ok = enc && ng <= 5 && (p.d0 % 2 == 0) && ((uintptr_t)T % 16 == 0);
+  // the TMA tiling (one dimension on each side of the tile) runs when the handle asks
+  // for it and TMA can describe the shape; the dimension-group tiling is the default
+  bool tma_ok = h->permute_tma && enc && ng <= 5 && (gd[0] % 2 == 0) && ((uintptr_t)T % 16 == 0);
   for (int g = 0; g < ng && tma_ok; ++g) if (gd[g] > (int64_t)0x7fffffff) tma_ok = false;
   if (tma_ok) {
+    p.d0 = gd[0];
+    p.dq = gd[q];
+    p.rs_i = rs[0];
+    p.ts_j = ts[q];
+    p.q = q;
+    p.nb = 0;
+    for (int g = 1; g < ng; ++g) {
+      if (g == q) continue;
+      p.bdim[p.nb] = gd[g]; p.bts[p.nb] = ts[g]; p.brs[p.nb] = rs[g]; p.bcoord[p.nb] = g; p.nb++;
+    }
+    p.ntile_i = (p.d0 + TI - 1) / TI;
+    p.ntile_j = (p.dq + TJ - 1) / TJ;
+    int64_t nbatch = total / (p.d0 * p.dq);
+    p.ntiles = p.ntile_i * p.ntile_j * nbatch;
+    p.fast = p.ntiles < (int64_t)0x7fffffff;
+    fast_divisor(p.ntile_j, p.mul_j, p.shr_j);
+    fast_divisor(p.ntile_i, p.mul_i, p.shr_i);
+    for (int b = 0; b < p.nb; ++b) fast_divisor(p.bdim[b], p.bmul[b], p.bshr[b]);
+    p.vec = rvec ? 1 : 0;
     CUtensorMap tmap;
     cuuint64_t gdim[5] = {1, 1, 1, 1, 1};
     cuuint64_t gstride[4] = {0, 0, 0, 0};
@@ -454,13 +514,49 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
       return nd_cuda_check(h, cudaGetLastError(), "permute_tma");
     }
   }
+  // plain-load tiling over dimension groups: J = R's dims in R order (skipping T's dim
+  // 0) until their product reaches TJ, then I = T's dims in T order (skipping J's)
+  // until theirs reaches TI; the remaining dims are the batch
+  bool inJ[ND_MAX_RANK] = {false}, inI[ND_MAX_RANK] = {false};
+  int64_t DJ = 1, DI = 1;
+  p.nj = 0;
+  for (int r = 0; r < ngp && DJ < TJ; ++r) {
+    const int g = gperm[r];
+    if (g == 0) continue;
+    inJ[g] = true;
+    p.jext[p.nj] = gd[g]; p.jts[p.nj] = ts[g]; p.jrs[p.nj] = rs[g]; p.nj++;
+    DJ *= gd[g];
+  }
+  p.ni = 0;
+  for (int g = 0; g < ng && DI < TI; ++g) {
+    if (inJ[g]) continue;
+    inI[g] = true;
+    p.iext[p.ni] = gd[g]; p.its[p.ni] = ts[g]; p.irs[p.ni] = rs[g]; p.ni++;
+    DI *= gd[g];
+  }
+  p.nb = 0;
+  for (int g = 0; g < ng; ++g) {
+    if (inI[g] || inJ[g]) continue;
+    p.bdim[p.nb] = gd[g]; p.bts[p.nb] = ts[g]; p.brs[p.nb] = rs[g]; p.bcoord[p.nb] = g; p.nb++;
+  }
+  p.d0 = DI;
+  p.dq = DJ;
+  p.ntile_i = (DI + TI - 1) / TI;
+  p.ntile_j = (DJ + TJ - 1) / TJ;
+  p.ntiles = p.ntile_i * p.ntile_j * (total / (DI * DJ));
+  p.fast = p.ntiles < (int64_t)0x7fffffff && DI < (int64_t)0x7fffffff && DJ < (int64_t)0x7fffffff;
+  fast_divisor(p.ntile_j, p.mul_j, p.shr_j);
+  fast_divisor(p.ntile_i, p.mul_i, p.shr_i);
+  for (int b = 0; b < p.nb; ++b) fast_divisor(p.bdim[b], p.bmul[b], p.bshr[b]);
+  for (int k = 0; k < p.ni; ++k) fast_divisor(p.iext[k], p.imul[k], p.ishr[k]);
+  for (int k = 0; k < p.nj; ++k) fast_divisor(p.jext[k], p.jmul[k], p.jshr[k]);
   int64_t blocks = std::min<int64_t>(p.ntiles, (int64_t)h->num_sms * 8);
-  nd_prof_begin(h, "permute_tiles");
-  if (p.mode == 0) permute_tiles<true><<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
-  else permute_tiles<false><<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
+  nd_prof_begin(h, "permute_groups");
+  if (p.mode == 0) permute_groups<true><<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
+  else permute_groups<false><<<(unsigned)blocks, threads, 0, h->stream>>>(T, R, Rin, p);
   nd_prof_end(h);
   ND_LAUNCHED(h);
-  return nd_cuda_check(h, cudaGetLastError(), "permute_tiles");
+  return nd_cuda_check(h, cudaGetLastError(), "permute_groups");
 }
 
 extern "C" nd_status nd_permutedims_f64(nd_handle h, double* R, const double* T, int32_t rank,

@@ -66,6 +66,7 @@ SIGNATURES = {
     "nd_set_ozaki_slices": [_P, _I32],
     "nd_set_split_tile": [_P, _I32],
     "nd_set_plan_placement": [_P, _I32],
+    "nd_set_permute_path": [_P, _I32],
     "nd_set_spin_limit": [_P, C.c_uint32],
     "nd_set_svd_max_sweeps": [_P, _I32],
     "nd_svd_last_info": [_P, _P, _I32, _P, _I32],

@@ -1,7 +1,7 @@
 """Failure paths that the library reports instead of hanging or aborting (GPU).
 
 - A device-side wait that runs past the handle's spin limit makes the call report
-  ND_ERR_TIMEOUT: the TMA pipeline of permutedims (mbarrier waits) and the grid
+  ND_ERR_TIMEOUT: the TMA pipeline of permutedims (nd_set_permute_path 1; mbarrier waits) and the grid
   barriers of the blockwise SVD.  The limit is set to one or two polls, far below the
   time a copy or a neighbouring CTA needs, so the waits run out; each kernel still
   waits for its own copies in flight before it exits.  The same handle then runs a
@@ -36,15 +36,19 @@ def test_permute_wait_timeout_then_recovers(nd):
     T = nd.DenseTensor(dims, torch.randn(int(np.prod(dims)), dtype=torch.float64, device="cuda"))
     R = nd.DenseTensor.empty(tuple(dims[p - 1] for p in perm))
     h = nd.handle(0)
+    h.call("nd_set_permute_path", 1)
     try:
-        h.call("nd_set_spin_limit", 1)
-        with pytest.raises(nd.NDError) as e:
-            nd.permutedims_(R, T, perm)
-            h.sync()
-        assert e.value.status == ND_ERR_TIMEOUT
+        try:
+            h.call("nd_set_spin_limit", 1)
+            with pytest.raises(nd.NDError) as e:
+                nd.permutedims_(R, T, perm)
+                h.sync()
+            assert e.value.status == ND_ERR_TIMEOUT
+        finally:
+            h.call("nd_set_spin_limit", 0)
+        nd.permutedims_(R, T, perm)
     finally:
-        h.call("nd_set_spin_limit", 0)
-    nd.permutedims_(R, T, perm)
+        h.call("nd_set_permute_path", 0)
     h.sync()
     want = T.data.view(*reversed(dims)).permute(0, 2, 1)        # row-major view of the column-major perm
     assert torch.equal(R.data.view(*reversed(R.dims)), want.contiguous())

@@ -21,15 +21,29 @@ CASES = [
     ((2, 2, 2, 2, 2, 2, 2, 2), (8, 1, 7, 2, 6, 3, 5, 4)),
     ((130, 66, 3), (1, 3, 2)),
     ((4, 1, 1), (2, 3, 1)),
+    # small extents: tiles over dimension groups (i over T's leading dims, j over R's)
+    ((4, 8, 4, 8, 4, 8), (6, 5, 4, 3, 2, 1)),
+    ((4, 8, 4, 8, 4, 8), (2, 1, 4, 3, 6, 5)),
+    ((32, 8, 32, 8, 32), (5, 4, 3, 2, 1)),
+    ((16, 8, 16, 8, 16), (3, 5, 1, 4, 2)),
+    ((3, 5, 7, 11), (4, 2, 3, 1)),
+    ((2, 3, 4, 5, 6, 7), (5, 6, 1, 2, 3, 4)),
 ]
 
 
+@pytest.mark.parametrize("path", [0, 1])
 @pytest.mark.parametrize("dims,perm", CASES)
-def test_permutedims_exact(nd, dims, perm):
+def test_permutedims_exact(nd, dims, perm, path):
+    """Both transposing paths (0: dimension-group tiles, 1: TMA tiles where they apply)."""
     rng = np.random.default_rng(hash((dims, perm)) % 2**32)
     a = rng.standard_normal(dims)
     T = nd.DenseTensor.from_numpy(a)
-    R = nd.permutedims(T, perm)
+    h = nd.handle(0)
+    h.call("nd_set_permute_path", path)
+    try:
+        R = nd.permutedims(T, perm)
+    finally:
+        h.call("nd_set_permute_path", 0)
     ref = odense.permutedims(a, perm)
     np.testing.assert_array_equal(R.to_numpy(), ref)
 
@@ -64,6 +78,19 @@ def test_permutedims_large_exact(nd):
     R = nd.permutedims(T, (3, 1, 2))
     a = data.cpu().numpy().reshape(dims, order="F")
     np.testing.assert_array_equal(R.to_numpy(), odense.permutedims(a, (3, 1, 2)))
+
+
+def test_permutedims_small_extents_large_exact(nd):
+    # larger than L2 (134 MB), every extent <= 64: the dimension-group tiling, rank-5 reversal
+    import torch
+    dims = (16, 32, 16, 32, 64)
+    g = torch.Generator(device="cuda").manual_seed(4)
+    data = torch.randn(int(np.prod(dims)), dtype=torch.float64, device="cuda", generator=g)
+    T = nd.DenseTensor(dims, data)
+    for perm in ((5, 4, 3, 2, 1), (2, 4, 1, 5, 3)):
+        R = nd.permutedims(T, perm)
+        a = data.cpu().numpy().reshape(dims, order="F")
+        np.testing.assert_array_equal(R.to_numpy(), odense.permutedims(a, perm))
 
 
 def test_bad_perm_rejected(nd):
