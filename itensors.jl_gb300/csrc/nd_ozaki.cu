@@ -150,7 +150,9 @@ __device__ __forceinline__ double i64_scaled_to_f64(long long v, int e) {
 
 // ---- pack kernels ----------------------------------------------------------
 // Two launches over fine-grained items (operand, row tile, chunk of PACK_KC
-// k-steps), so every SM has work: pack_rowmax folds |x| maxima of its chunk
+// k-steps), one CTA per item, so the block scheduler balances them over the SMs
+// (4 k-steps per item measured best: 8 left a partial last wave, 2 paid more per-item
+// set-up): pack_rowmax folds |x| maxima of its chunk
 // into a per-row global maximum (IEEE bit patterns are monotonic for finite
 // x, so an integer atomicMax suffices); pack_digits turns each element into S
 // digit slices written straight to global memory in the tcgen05 canonical
@@ -161,7 +163,7 @@ __device__ __forceinline__ double i64_scaled_to_f64(long long v, int e) {
 // (row, 512-wide chunk), digitised in a single pack pass that reads its chunk
 // twice, was measured too: the second, L2-resident read made pack_digits 1.5-1.8x
 // slower, more than the row-maximum pass it removes.)
-constexpr int PACK_KC = 8;                 // k-steps (of 32) per pack item
+constexpr int PACK_KC = 4;                 // k-steps (of 32) per pack item
 
 struct PackItem2 {
   int32_t op, rt, kc;
@@ -1366,7 +1368,10 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
   const int S = c.slices;
   PackArgs2 pa{(const SplitOp*)c.d_operands, (const PackItem2*)c.d_pack_items, c.npack_items, ptrs,
                (unsigned char*)c.d_pack, c.d_exp, (unsigned long long*)c.d_rowmax, S, h->d_status};
-  int pblocks = std::min(c.npack_items, h->num_sms * 8);
+  // one CTA per pack item: the block scheduler hands items to SMs as they free up, so
+  // the launch ends within about one item of the ideal (a fixed per-CTA item list left
+  // a second partial wave)
+  int pblocks = c.npack_items;
   if (pblocks > 0) {
     if (S > 2) {
       ND_CUDA(h, cudaMemsetAsync(c.d_rowmax, 0, c.exp_count * 8, h->stream));
