@@ -400,6 +400,97 @@ __device__ __forceinline__ void mma(uint32_t dt, uint64_t ad, uint64_t bd, uint3
                  :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc) : "memory");
 }
 
+// The same MMA issued by the lane whose `leader` is non-zero (elected once per warp
+// instead of once per instruction).
+template <int CU>
+__device__ __forceinline__ void mmaL(uint32_t leader, uint32_t dt, uint64_t ad, uint64_t bd, uint32_t id, uint32_t acc) {
+  if constexpr (CU == 1)
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.b32 p, %4, 0;\n setp.ne.b32 q, %5, 0;\n"
+                 " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc), "r"(leader) : "memory");
+  else if constexpr (CU == 2)
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.b32 p, %4, 0;\n setp.ne.b32 q, %5, 0;\n"
+                 " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc), "r"(leader) : "memory");
+  else if constexpr (CU == 3)
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.b32 p, %4, 0;\n setp.ne.b32 q, %5, 0;\n"
+                 " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc), "r"(leader) : "memory");
+  else
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.b32 p, %4, 0;\n setp.ne.b32 q, %5, 0;\n"
+                 " @q tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(acc), "r"(leader) : "memory");
+}
+
+// Accumulating MMA (enable-input-d true) issued by the `leader` lane: one predicate
+// serves as both the issue guard and the accumulate flag.
+template <int CU>
+__device__ __forceinline__ void mmaA(uint32_t leader, uint32_t dt, uint64_t ad, uint64_t bd, uint32_t id) {
+  if constexpr (CU == 1)
+    asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
+                 " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, q;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(leader) : "memory");
+  else if constexpr (CU == 2)
+    asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
+                 " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, q;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(leader) : "memory");
+  else if constexpr (CU == 3)
+    asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
+                 " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, q;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(leader) : "memory");
+  else
+    asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %4, 0;\n"
+                 " @q tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n}"
+                 :: "r"(dt), "l"(ad), "l"(bd), "r"(id), "r"(leader) : "memory");
+}
+
+// One 16-wide k step of the S = 5 schedule, its nine MMAs in one asm block: the slice
+// descriptors are formed from the stage's descriptors by 32-bit adds on their low words
+// (the start-address field never carries: every stage lies below 2^18 bytes), and
+// one predicate is both the issue guard and the accumulate flag.  A slot is
+// [L2 | L3 | T4 | T5+] (columns X, X+64, X+128, X+192):
+//   A1 x [B1..B4] N=256 -> X (starts the chunk when accx == 0), A1 x B5 -> T5+,
+//   A2 x [B1..B3] N=192 -> X+64, A2 x B4 -> T5+, A3 x [B1 B2] N=128 -> X+128,
+//   A3 x B3 -> T5+, A4 x B1 -> T5+, A4 x B2 -> T5+, A5 x B1 -> T5+,
+// consecutive MMAs of one A slice reading it once through the A collector.
+__device__ __forceinline__ void mma_s5_k16(uint32_t leader, uint32_t accx, uint32_t X, uint32_t alo, uint32_t ahi,
+                                           uint32_t blo, uint32_t bhi, uint32_t i256, uint32_t i192,
+                                           uint32_t i128, uint32_t i64) {
+  asm volatile(
+      "{\n"
+      " .reg .pred q, p;\n"
+      " .reg .b32 t<10>, d<3>;\n"
+      " .reg .b64 a<5>, b<5>;\n"
+      " setp.ne.b32 q, %0, 0;\n"
+      " setp.ne.b32 p, %1, 0;\n"
+      " add.u32 t1, %3, 512;\n add.u32 t2, %3, 1024;\n add.u32 t3, %3, 1536;\n add.u32 t4, %3, 2048;\n"
+      " add.u32 t6, %5, 256;\n add.u32 t7, %5, 512;\n add.u32 t8, %5, 768;\n add.u32 t9, %5, 1024;\n"
+      " mov.b64 a0, {%3, %4};\n mov.b64 a1, {t1, %4};\n mov.b64 a2, {t2, %4};\n"
+      " mov.b64 a3, {t3, %4};\n mov.b64 a4, {t4, %4};\n"
+      " mov.b64 b0, {%5, %6};\n mov.b64 b1, {t6, %6};\n mov.b64 b2, {t7, %6};\n"
+      " mov.b64 b3, {t8, %6};\n mov.b64 b4, {t9, %6};\n"
+      " add.u32 d0, %2, 64;\n add.u32 d1, %2, 128;\n add.u32 d2, %2, 192;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%2], a0, b0, %7, p;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [d2], a0, b4, %10, q;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [d0], a1, b0, %8, q;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [d2], a1, b3, %10, q;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [d1], a2, b0, %9, q;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [d2], a2, b2, %10, q;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [d2], a3, b0, %10, q;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [d2], a3, b1, %10, q;\n"
+      " @q tcgen05.mma.cta_group::1.kind::f16 [d2], a4, b0, %10, q;\n"
+      "}\n"
+      :: "r"(leader), "r"(accx), "r"(X), "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(i256), "r"(i192),
+         "r"(i128), "r"(i64)
+      : "memory");
+}
+
+__device__ __forceinline__ void commitL(uint32_t leader, uint64_t* bar) {
+  asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %1, 0;\n"
+               " @q tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}"
+               :: "r"(smem_u32(bar)), "r"(leader) : "memory");
+}
+
 __device__ __forceinline__ void commit(uint64_t* bar) {
   asm volatile("{\n" ND_ELECT "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}"
                :: "r"(smem_u32(bar)) : "memory");
@@ -534,6 +625,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
       const uint32_t smem_base = smem_u32(smem);
       const uint32_t i64 = idesc(BN);
       constexpr int NBLK = 2 + C::TBLK;     // accumulator blocks of a slot: L2 L3 [T4 [T5+]]
+      uint32_t leader;
+      asm volatile("{\n .reg .pred e;\n elect.sync _|e, 0xffffffff;\n selp.u32 %0, 1, 0, e;\n}" : "=r"(leader));
       for (int it = blockIdx.x; it < g.nitems && ok; it += gridDim.x) {
         const WorkItem wi = g.items[it];
         for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
@@ -560,6 +653,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
             for (int kk = 0; kk < 2; ++kk) {
               const uint32_t accx = (cstart && kk == 0) ? 0u : 1u;
               const uint32_t ko = kk * 32;
+              if constexpr (S == 5 && NBLK == 4) {
+                mma_s5_k16(leader, accx, X, (uint32_t)adesc0 + (ko >> 4), (uint32_t)(adesc0 >> 32),
+                           (uint32_t)bdesc0 + (ko >> 4), (uint32_t)(bdesc0 >> 32), idesc(4 * BN), idesc(3 * BN),
+                           idesc(2 * BN), i64);
+                continue;
+              }
               auto A = [&](int p) { return adesc0 + (uint64_t)((((p - 1) * A_SLICE) + ko) >> 4); };
               auto B = [&](int q) { return bdesc0 + (uint64_t)((((q - 1) * B_SLICE) + ko) >> 4); };
               // A slot is [L2 | L3 | T4 | T5+], 64 columns each, and level t = p + q sits in
@@ -574,28 +673,33 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
                 const int nm = (r0 > 0 ? 1 : 0) + (S + 1 - p - r0);    // MMAs sharing A_p
                 int m = 0;
                 if (r0 > 0) {
-                  const uint32_t d = X + (p - 1) * BN, id = idesc(r0 * BN), ac = p == 1 ? accx : 1u;
-                  if (nm > 1) mma<1>(d, A(p), B(1), id, ac);
-                  else mma<0>(d, A(p), B(1), id, ac);
+                  const uint32_t d = X + (p - 1) * BN, id = idesc(r0 * BN);
+                  if (p == 1) {          // the chunk's first MMA may start the accumulation
+                    if (nm > 1) mmaL<1>(leader, d, A(p), B(1), id, accx);
+                    else mmaL<0>(leader, d, A(p), B(1), id, accx);
+                  } else {
+                    if (nm > 1) mmaA<1>(leader, d, A(p), B(1), id);
+                    else mmaA<0>(leader, d, A(p), B(1), id);
+                  }
                   ++m;
                 }
 #pragma unroll
                 for (int q = r0 + 1; q <= S + 1 - p; ++q, ++m) {
                   const uint32_t d = X + (NBLK - 1) * BN;
-                  if (nm == 1) mma<0>(d, A(p), B(q), i64, 1u);
-                  else if (m == 0) mma<1>(d, A(p), B(q), i64, 1u);
-                  else if (m == nm - 1) mma<3>(d, A(p), B(q), i64, 1u);
-                  else mma<2>(d, A(p), B(q), i64, 1u);
+                  if (nm == 1) mmaA<0>(leader, d, A(p), B(q), i64);
+                  else if (m == 0) mmaA<1>(leader, d, A(p), B(q), i64);
+                  else if (m == nm - 1) mmaA<3>(leader, d, A(p), B(q), i64);
+                  else mmaA<2>(leader, d, A(p), B(q), i64);
                 }
               }
             }
-            commit(&empty[s]);
-            if (cend) { commit(&xfull[chunk & 1]); ++chunk; }
+            commitL(leader, &empty[s]);
+            if (cend) { commitL(leader, &xfull[chunk & 1]); ++chunk; }
           }
           if (!ok) break;
         }
       }
-      commit(&done_bar);
+      commitL(leader, &done_bar);
       mbar_wait(smem_u32(&done_bar), 0, g.st, 413, nullptr);
     }
   } else {
