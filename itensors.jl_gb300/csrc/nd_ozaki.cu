@@ -246,46 +246,71 @@ __device__ __forceinline__ void pack_setup(const SplitOp& op, const PackItem2& p
   }
 }
 
+// Row maxima: only the exponent of each row's max |x| is used, so the kernel reads the
+// high 32-bit word of every double.  A maximum does not care which lane reads which
+// element, so lanes follow the operand's contiguous direction: along k when k is
+// unit-stride (a warp takes whole rows, 32 consecutive k per load, then a shuffle
+// reduction), else along the rows (a warp takes 32 rows, the item's k split over the
+// warps that share them).
 __global__ void __launch_bounds__(256) pack_rowmax(PackArgs2 a) {
   __shared__ int64_t rowoff[BM];
   __shared__ int64_t koff[PACK_KC * BK];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, c = lane & 3;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
     const PackItem2 pi = a.items[it];
     const SplitOp& op = a.ops[pi.op];
     const int ROWS = op.is_b ? BN : BM;
-    const int units = ROWS / 64;
     const double* src = (op.is_b ? job_B(a.ptrs, op.job) : job_A(a.ptrs, op.job)) + op.src_off;
     int ks0, ks1;
     __syncthreads();
     pack_setup(op, pi, ROWS, rowoff, koff, ks0, ks1);
     __syncthreads();
+    const int nrows = min(ROWS, op.rows - pi.rt * ROWS);
+    const int nk = min((ks1 - ks0) * BK, op.kdim - ks0 * BK);
+    unsigned long long* rmx = a.rowmax + op.exp_off + pi.rt * ROWS;
     bool bad = false;
+    if (nk >= 2 && koff[1] == koff[0] + 1) {
+      // four rows per pass, all their loads issued before any is used
+      constexpr int RB = 4, KB = PACK_KC * BK / 32;
+      for (int r0 = warp * RB; r0 < nrows; r0 += 8 * RB) {
+        uint32_t hw[RB][KB];
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      if (j >= units) continue;
-      const int r = (lane >> 2) + 8 * warp + 64 * j;
-      const bool rv = pi.rt * ROWS + r < op.rows;
-      // only the exponent of the row maximum is used: max of the high words' exponent field
-      uint32_t mx = 0u;
-      if (rv) {
-        const unsigned int* rowp = (const unsigned int*)(src + rowoff[r]) + 1;   // high 32 bits of each double
-#pragma unroll 4
-        for (int ks = 0; ks < ks1 - ks0; ++ks) {
+        for (int i = 0; i < RB; ++i) {
+          const int r = r0 + i;
+          const unsigned int* rowp = (const unsigned int*)(src + rowoff[r < nrows ? r : 0]) + 1;   // high words
 #pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            const int64_t ko = koff[ks * BK + c * 8 + e];
-            if (ko >= 0) {
-              const uint32_t hw = __ldg(rowp + 2 * ko) & 0x7ff00000u;
-              if (hw == 0x7ff00000u) bad = true;
-              else mx = max(mx, hw);
-            }
+          for (int j = 0; j < KB; ++j) {
+            const int k = lane + 32 * j;
+            hw[i][j] = (r < nrows && k < nk) ? __ldg(rowp + 2 * koff[k]) & 0x7ff00000u : 0u;
           }
         }
+#pragma unroll
+        for (int i = 0; i < RB; ++i) {
+          uint32_t mx = 0u;
+#pragma unroll
+          for (int j = 0; j < KB; ++j) {
+            if (hw[i][j] == 0x7ff00000u) bad = true;
+            else mx = max(mx, hw[i][j]);
+          }
+#pragma unroll
+          for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+          if (lane == 0 && mx && r0 + i < nrows) atomicMax(&rmx[r0 + i], (unsigned long long)mx << 32);
+        }
       }
-      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
-      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
-      if (c == 0 && rv && mx) atomicMax(&a.rowmax[op.exp_off + pi.rt * ROWS + r], (unsigned long long)mx << 32);
+    } else {
+      const int rgroups = ROWS / 32, kgroups = 8 / rgroups;
+      const int r = lane + 32 * (warp % rgroups), kg = warp / rgroups;
+      if (r < nrows) {
+        const unsigned int* rowp = (const unsigned int*)(src + rowoff[r]) + 1;
+        uint32_t mx = 0u;
+#pragma unroll 16
+        for (int k = kg; k < nk; k += kgroups) {
+          const uint32_t hw = __ldg(rowp + 2 * koff[k]) & 0x7ff00000u;
+          if (hw == 0x7ff00000u) bad = true;
+          else mx = max(mx, hw);
+        }
+        if (mx) atomicMax(&rmx[r], (unsigned long long)mx << 32);
+      }
     }
     if (bad && atomicCAS(&a.st->code, 0, ND_ERR_NONFINITE) == 0) a.st->where = 300;
   }
