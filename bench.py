@@ -229,8 +229,8 @@ def run_oracle_sample(args):
 
 
 # DRAM traffic of split_gemm per launch from one ncu capture of this workload at S = 5
-# (dram__bytes_read.sum + dram__bytes_write.sum: L*psi 361.6 MB, *R 642.4 MB; mean of the two)
-NCU_SPLIT_GEMM_TRAFFIC = {4096: 502.0e6}
+# (dram__bytes_read.sum + dram__bytes_write.sum: L*psi 347.5 MB, *R 579.6 MB; mean of the two)
+NCU_SPLIT_GEMM_TRAFFIC = {4096: 463.6e6}
 
 
 def split_routed_flops(shapes):
