@@ -15,6 +15,8 @@ from .contract import (ContractionPlan, contract, contract_, contract_blockspars
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
 from . import krylov
 from .krylov import HeffOperator, Lanczos, SweepStep, lanczos
+from . import hdf5io
+from .hdf5io import H5Reader, load_blocksparse, read_blocksparse, save_blocksparse, write_blocksparse
 
 __all__ = [
     "workloads", "NDError", "NoConvergence", "PRECISIONS", "handle", "load", "LIB_PATH",
@@ -24,4 +26,5 @@ __all__ = [
     "linalg", "MatricizePlan", "Spectrum", "SvdPlan", "eigen", "matricize", "qr", "svd", "truncate", "uncombine",
     "autodiff", "contract_autograd", "contract_rrule", "dense_structure",
     "krylov", "HeffOperator", "Lanczos", "SweepStep", "lanczos",
+    "hdf5io", "H5Reader", "load_blocksparse", "read_blocksparse", "save_blocksparse", "write_blocksparse",
 ]

@@ -1,4 +1,4 @@
-"""Write tests/golden/reference_kats.json.
+"""Write tests/golden/reference_kats.json (and copy the reference's HDF5 test file).
 
 The reference (ITensors.jl / NDTensors.jl, Julia) cannot run here (there is no
 Julia toolchain), and its test suite stores no numeric golden vectors for the
@@ -75,7 +75,18 @@ KATS = {
     },
 }
 
+# HDF5 file written by the reference through libhdf5 (an ITensor with Dense{Float64}
+# storage), the fixture of its test/base/test_readwrite.jl:182-190; it pins the HDF5
+# reader of the package's BlockSparse storage I/O.
+HDF5_FIXTURE = ("test/base/utils/testfilev0.1.41.h5", "itensor_v0.1.41_dense.h5")
+
 if __name__ == "__main__":
     out = Path(__file__).with_name("reference_kats.json")
     out.write_text(json.dumps(KATS, indent=1) + "\n")
     print(out)
+    import shutil
+    src = Path("/root/reference") / HDF5_FIXTURE[0]
+    if src.exists():
+        dst = Path(__file__).with_name(HDF5_FIXTURE[1])
+        shutil.copyfile(src, dst)
+        print(dst)
