@@ -410,7 +410,7 @@ static bool host_plan(const Roles& ro, const BsDesc& A, const BsDesc& B, const s
     if (ok) kb.push_back({k, i2});
   }
   std::sort(kb.begin(), kb.end());
-  std::vector<std::pair<int32_t, int32_t>> range(nA, {0, 0});  // each A block's bucket in kb
+  std::vector<std::pair<int32_t, int32_t>> bucket(nA, {0, 0});  // each A block's matching range of kb
   int64_t npairs = 0;
   for (int i1 = 0; i1 < nA; ++i1) {
     const int32_t* bA = A.blocks + (size_t)i1 * ro.rankA;
@@ -419,7 +419,7 @@ static bool host_plan(const Roles& ro, const BsDesc& A, const BsDesc& B, const s
     auto lo = std::lower_bound(kb.begin(), kb.end(), std::make_pair(k, (int32_t)INT32_MIN));
     auto hi = lo;
     while (hi != kb.end() && hi->first == k) ++hi;
-    range[i1] = {(int32_t)(lo - kb.begin()), (int32_t)(hi - kb.begin())};
+    bucket[i1] = {(int32_t)(lo - kb.begin()), (int32_t)(hi - kb.begin())};
     npairs += hi - lo;
     if (npairs > max_pairs) return false;
   }
@@ -431,7 +431,7 @@ static bool host_plan(const Roles& ro, const BsDesc& A, const BsDesc& B, const s
   int64_t q = 0;
   for (int i1 = 0; i1 < nA; ++i1) {
     const int32_t* bA = A.blocks + (size_t)i1 * ro.rankA;
-    for (int32_t j = range[i1].first; j < range[i1].second; ++j) {
+    for (int32_t j = bucket[i1].first; j < bucket[i1].second; ++j) {
       const int32_t i2 = kb[j].second;
       const int32_t* bB = B.blocks + (size_t)i2 * ro.rankB;
       int32_t c[ND_MAX_RANK];
