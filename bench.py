@@ -940,11 +940,23 @@ def cfg_sweep_ops(args):
     P = lambda t: C.c_void_p(t.data_ptr())
 
     def gbs(nbytes, fn):
+        # kernel time from the library's own per-kernel CUDA events (events recorded around
+        # a host call would also count the call's launch latency, tens of microseconds)
         for _ in range(3):
             fn()
-        ms = float(np.median(_events_ms(fn, reps, flush)))
+        torch.cuda.synchronize()
+        h.profile(True)
+        for _ in range(reps):
+            flush.fill_(1.0)
+            fn()
+        prof = h.profile_read()
+        h.profile(False)
+        ms = sum(v[1] for v in prof.values()) / reps
+        if ms <= 0.0:                                   # no library region: events around the call
+            ms = float(np.median(_events_ms(fn, reps, flush)))
         return {"ms": round(ms, 4), "GB/s": round(nbytes / (ms * 1e-3) / 1e9, 1),
-                "frac_of_hbm": round(nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], 3)}
+                "frac_of_hbm": round(nbytes / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], 3),
+                "kernels": sorted(prof)}
 
     out["vec_dots_k10"] = gbs(8 * n * (k + 1), lambda: h.call("nd_vec_dots_f64", n, k, P(V), n, P(w), P(coef)))
     out["vec_update_k10"] = gbs(8 * n * (k + 2), lambda: h.call("nd_vec_update_f64", n, k, P(V), n, P(coef), -1.0, P(w)))

@@ -7,8 +7,9 @@
 // All of them only launch kernels: scalars that feed later steps (norms, Gram-Schmidt
 // coefficients, Lanczos alpha / beta) stay in device memory, so a whole Krylov
 // iteration can be captured into one CUDA graph.  Reductions are deterministic: a
-// fixed grid of VEC_CTAS CTAs writes per-CTA partial sums in a fixed order and one
-// CTA adds them in that order, so a replay reproduces an eager run bit for bit.
+// fixed grid of CTAs writes per-CTA partial sums and a second kernel adds them in a
+// fixed order (strided sums, then a fixed-shape tree), so a replay reproduces an eager
+// run bit for bit.
 //
 // Every kernel streams its vectors once from HBM (the basis forms read k vectors and
 // one or two more); the bound is HBM bandwidth, 8 bytes per element read or written.
@@ -75,13 +76,26 @@ __global__ void __launch_bounds__(VEC_THREADS) vec_dots_part(int64_t n, int k, c
   }
 }
 
-// out[j] = sum_b part[b * k + j] in b order (optionally the square root: a norm)
-__global__ void vec_dots_final(int k, int nparts, const double* __restrict__ part, double* out, int root) {
-  const int j = threadIdx.x;
-  if (j >= k) return;
+// out[j] = sum_b part[b * k + j] (optionally the square root: a norm), one CTA per j:
+// thread t adds the partials t, t + 256, ... in that order, then a fixed-shape tree adds
+// the threads' sums, so the result does not depend on thread timing.  (One thread adding
+// all partials in sequence was a chain of dependent FP64 adds and loads that took tens of
+// microseconds.)
+constexpr int FINAL_THREADS = 256;
+__global__ void __launch_bounds__(FINAL_THREADS) vec_dots_final(int k, int nparts, const double* __restrict__ part,
+                                                                double* out, int root) {
+  __shared__ double red[FINAL_THREADS];
+  const int j = blockIdx.x, t = threadIdx.x;
   double s = 0.0;
-  for (int b = 0; b < nparts; ++b) s += part[(int64_t)b * k + j];
-  out[j] = root ? sqrt(s) : s;
+  for (int b = t; b < nparts; b += FINAL_THREADS) s += part[(int64_t)b * k + j];
+  red[t] = s;
+  __syncthreads();
+#pragma unroll
+  for (int w = FINAL_THREADS / 2; w > 0; w >>= 1) {
+    if (t < w) red[t] += red[t + w];
+    __syncthreads();
+  }
+  if (t == 0) out[j] = root ? sqrt(red[0]) : red[0];
 }
 
 // Elementwise kernels: each thread handles VEC_U elements VEC_THREADS apart per
@@ -191,7 +205,7 @@ nd_status dots(nd_handle h, int64_t n, int32_t k, const double* V, int64_t ldv, 
   else if (k <= 8) vec_dots_part<8><<<ctas, VEC_THREADS, 0, h->stream>>>(n, k, V, ldv, x, chunk, part);
   else if (k <= 16) vec_dots_part<16><<<ctas, VEC_THREADS, 0, h->stream>>>(n, k, V, ldv, x, chunk, part);
   else vec_dots_part<32><<<ctas, VEC_THREADS, 0, h->stream>>>(n, k, V, ldv, x, chunk, part);
-  vec_dots_final<<<1, VEC_KMAX, 0, h->stream>>>(k, ctas, part, out, root);
+  vec_dots_final<<<k, FINAL_THREADS, 0, h->stream>>>(k, ctas, part, out, root);
   nd_prof_end(h);
   h->launches += 2;
   return nd_cuda_check(h, cudaGetLastError(), name);
