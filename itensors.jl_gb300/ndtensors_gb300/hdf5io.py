@@ -218,7 +218,9 @@ class _Reader:
         a = np.frombuffer(raw, dtype=dt, count=n).copy()
         if not dims:
             return a[0].item()
-        return a.reshape(tuple(reversed(dims))).transpose() if len(dims) > 1 else a
+        # HDF5 stores row-major with the file's dims (a column-major writer such as Julia
+        # lists its dims reversed); returned in the file's order, as h5py does
+        return a.reshape(tuple(int(d) for d in dims))
 
     def attributes(self, addr):
         out = {}

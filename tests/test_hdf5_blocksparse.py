@@ -119,6 +119,19 @@ def test_blocksparse_round_trip(tmp_path):
     assert h.read_blocksparse(tmp_path / "e.h5", "E")[0] == []
 
 
+def test_multidimensional_dataset(tmp_path):
+    """Row-major data with the file's dims (a column-major writer lists them reversed)."""
+    h = _h5()
+    a = np.arange(24, dtype=np.float64).reshape(2, 3, 4) * 0.5
+    w = h._Writer()
+    root = w.group({"a": w.dataset(a), "s": w.dataset("text"), "i": w.dataset(np.int64(-7))})
+    p = tmp_path / "nd.h5"
+    p.write_bytes(w.finish(root))
+    f = h.H5Reader(p)
+    np.testing.assert_array_equal(f.read("a"), a)
+    assert f.read("s") == "text" and f.read("i") == -7
+
+
 def test_read_rejects_other_storage(tmp_path):
     h = _h5()
     with pytest.raises(h.HDF5FormatError):
