@@ -380,6 +380,7 @@ struct GemmArgs {
   int32_t bmode;      // 0: beta == 0 (overwrite), 1: general beta
   DeviceStatus* st;
   unsigned long long* cta_times;   // optional: {start, end} (%globaltimer, ns) per CTA
+  long long* ws;                   // split-K: int64 fixed-point tiles, BM x BN per slot (row-major)
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -516,11 +517,6 @@ __device__ __forceinline__ void commitL(uint32_t leader, uint64_t* bar) {
                :: "r"(smem_u32(bar)), "r"(leader) : "memory");
 }
 
-__device__ __forceinline__ void commit(uint64_t* bar) {
-  asm volatile("{\n" ND_ELECT "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n}"
-               :: "r"(smem_u32(bar)) : "memory");
-}
-
 #define TMEM_LD8(taddr, r)                                                                                    \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"                           \
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])  \
@@ -620,7 +616,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
           const SplitOp& ob = g.ops[pd.b_op];
           const unsigned char* srcA = g.pack + oa.pack_off + (int64_t)wi.mt * oa.k_steps * S * A_SLICE;
           const unsigned char* srcB = g.pack + ob.pack_off + (int64_t)wi.nt * ob.k_steps * S * B_SLICE;
-          for (int ks = 0; ks < oa.k_steps; ++ks, ++n) {
+          const int k0 = wi.slot >= 0 ? wi.kbeg : 0, k1 = wi.slot >= 0 ? wi.kend : oa.k_steps;
+          for (int ks = k0; ks < k1; ++ks, ++n) {
             const uint32_t s = n % C::STAGES, u = n / C::STAGES;
             if (u >= 1 && !mbar_wait(smem_u32(&empty[s]), (u - 1) & 1, g.st, 400, &abort_flag, lim)) { ok = false; break; }
             unsigned char* dA = smem + s * C::STAGE;
@@ -656,7 +653,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
         const WorkItem wi = g.items[it];
         for (int pi = 0; pi < wi.pair_count && ok; ++pi) {
           const PairDesc& pd = g.pairs[wi.pair_begin + pi];
-          const int nks = g.ops[pd.a_op].k_steps;
+          // k steps of this item: the pair's whole K, or a split-K range [kbeg, kend)
+          const int nks = wi.slot >= 0 ? wi.kend - wi.kbeg : g.ops[pd.a_op].k_steps;
           const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
           uint32_t X = tmem;
           for (int ks = 0; ks < nks; ++ks, ++n) {
@@ -757,7 +755,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
         const PairDesc& pd = g.pairs[wi.pair_begin + pi];
         const SplitOp& oa = g.ops[pd.a_op];
         const SplitOp& ob = g.ops[pd.b_op];
-        const int nks = oa.k_steps;
+        const int nks = wi.slot >= 0 ? wi.kend - wi.kbeg : oa.k_steps;
         const int chunk_steps = S > 2 ? CHUNK_STEPS : nks;
         const int nchunks = (nks + chunk_steps - 1) / chunk_steps;
         long long acc[EPI_COLS];
@@ -810,6 +808,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
           if (lane == 0) mbar_arrive(&xempty[xs]);
         }
         if (!ok) break;
+        if (wi.slot >= 0) {
+          // split-K: this K range's exact fixed-point tile, added to the others by split_reduce
+          long long* wsl = g.ws + (int64_t)wi.slot * (BM * BN) + (int64_t)row * BN + cg * EPI_COLS;
+#pragma unroll
+          for (int c = 0; c < EPI_COLS; ++c) wsl[c] = acc[c];
+          continue;
+        }
         // finalize this pair into R
         if (row_ok && ncols > 0) {
           const int Ei = S > 2 ? g.exps[oa.exp_off + gm] : 0;
@@ -843,6 +848,45 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_gemm(GemmArgs g) {
   fence_after();
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(C::TMEM_COLS));
   if (g.cta_times && tid == 0) g.cta_times[2 * blockIdx.x + 1] = global_ns();
+}
+
+// Split-K reduction: the K ranges of one output tile were computed by different CTAs as
+// exact int64 fixed-point tiles (split_gemm, `ws`).  They begin at the same 512-K chunk
+// boundaries the unsplit kernel drains at, so their integer sum is the unsplit kernel's
+// accumulator bit for bit; it is converted with the pair's row and column exponents and
+// stored with the pair's alpha / beta (split tiles belong to single-pair output blocks).
+__global__ void __launch_bounds__(256) split_reduce(const PairDesc* pairs, const ReduceItem* red, int nred,
+                                                    const SplitOp* ops, const int32_t* exps, const long long* ws,
+                                                    JobPtrs ptrs, double alpha, double beta, int amode, int bmode) {
+  __shared__ int64_t colR[BN];
+  for (int r = blockIdx.x; r < nred; r += gridDim.x) {
+    const ReduceItem ri = red[r];
+    const PairDesc& pd = pairs[ri.pair];
+    const SplitOp& oa = ops[pd.a_op];
+    const SplitOp& ob = ops[pd.b_op];
+    __syncthreads();
+    if (threadIdx.x < BN) {
+      const int gn = ri.nt * BN + threadIdx.x;
+      int64_t co = 0, d;
+      if (gn < pd.N) mixed_offsets32(pd.cols, (uint32_t)gn, d, co);
+      colR[threadIdx.x] = co;
+    }
+    __syncthreads();
+    double* Rb = job_R(ptrs, pd.job) + pd.r_off;
+    for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
+      const int row = e / BN, col = e - row * BN;
+      const int gm = ri.mt * BM + row, gn = ri.nt * BN + col;
+      if (gm >= pd.M || gn >= pd.N) continue;
+      long long s = 0;
+      for (int q = 0; q < ri.nslots; ++q) s += ws[(int64_t)(ri.slot0 + q) * (BM * BN) + e];
+      const double v = i64_scaled_to_f64(s, exps[oa.exp_off + gm] + exps[ob.exp_off + gn] - 38);
+      int64_t ro, d;
+      mixed_offsets32(pd.rows, (uint32_t)gm, d, ro);
+      double* dst = Rb + ro + colR[col];
+      if (pd.first) *dst = bmode == 0 ? (amode ? alpha * v : v) : alpha * v + beta * *dst;
+      else *dst = amode ? *dst + alpha * v : *dst + v;
+    }
+  }
 }
 
 template <int S>
@@ -1362,12 +1406,15 @@ struct SplitLayout {
   int nops_a = 0, nops_b = 0;
   int pair2 = 0;     // 1: 256 x 64 tiles on CTA pairs (split_gemm2); 0: 128 x 64 tiles (split_gemm)
   int slots = 0;     // persistent CTAs (1-CTA tiles) or CTA pairs (2-CTA tiles)
+  std::vector<ReduceItem> red;   // split-K tiles and their workspace slots
+  int nws = 0;                   // workspace slots (BM x BN int64 each)
 };
 
 // pair2: tiles for CTA pairs.  A operands then hold an even number of 128-row tiles
 // (the odd CTA of a pair whose rows run past M stages zero digits, and the epilogue
 // stores nothing for those rows); work item mt is the index of a pair of row tiles.
-static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int S, int pair2, SplitLayout& L) {
+static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int S, int pair2, SplitLayout& L,
+                         bool splitk = false) {
   L = SplitLayout{};
   L.pair2 = pair2 ? 1 : 0;
   L.pairs = pairs_in;
@@ -1428,23 +1475,57 @@ static void split_layout(nd_handle h, const std::vector<PairDesc>& pairs_in, int
   }
   std::stable_sort(grps.begin(), grps.end(), [](const Grp& x, const Grp& y) { return x.cost > y.cost; });
   std::vector<std::pair<int64_t, WorkItem>> tmp;
+  int64_t total_ksteps = 0;
   {
     size_t ntiles = 0;
     for (const Grp& g : grps) {
       const PairDesc& p = L.pairs[g.i];
       const size_t mt = (p.M + BM - 1) / BM;
-      ntiles += (L.pair2 ? (mt + 1) / 2 : mt) * ((p.N + BN - 1) / BN);
+      const size_t tiles = (L.pair2 ? (mt + 1) / 2 : mt) * ((p.N + BN - 1) / BN);
+      ntiles += tiles;
+      for (size_t q = g.i; q < g.i + g.n; ++q) total_ksteps += (int64_t)tiles * ((L.pairs[q].K + BK - 1) / BK);
     }
     tmp.reserve(ntiles);
   }
+  // Split-K (1-CTA tiles, S > 2): a tile of a single-pair output block whose K is long
+  // against the launch's fair share (twice the k steps per CTA) is cut into K ranges that
+  // start at 512-K chunk boundaries; each range's CTA writes its exact int64 tile to a
+  // workspace slot and split_reduce adds them.  A 10 x 10 output with K = 5e5 (a cotangent
+  // of an MPO tensor) otherwise runs on one CTA.
+  int64_t share = INT64_MAX;
+  if (splitk && !L.pair2 && S > 2) {
+    const int64_t fair = (total_ksteps + h->num_sms - 1) / h->num_sms;
+    share = std::max<int64_t>(2 * CHUNK_STEPS, (2 * fair + CHUNK_STEPS - 1) / CHUNK_STEPS * CHUNK_STEPS);
+  }
+  bool any_split = false;
   for (const Grp& g : grps) {
     const PairDesc& p = L.pairs[g.i];
     int mt = (p.M + BM - 1) / BM;
     const int nt = (p.N + BN - 1) / BN;
     if (L.pair2) mt = (mt + 1) / 2;
+    const int64_t kst = (p.K + BK - 1) / BK;
     for (int a = 0; a < mt; ++a)
-      for (int b = 0; b < nt; ++b) tmp.push_back({g.cost, WorkItem{p.group, (int)g.i, (int)g.n, a, b}});
+      for (int b = 0; b < nt; ++b) {
+        if (g.n == 1 && kst > share) {
+          const int64_t nch = (kst + share - 1) / share;
+          const int64_t kc = ((kst + nch - 1) / nch + CHUNK_STEPS - 1) / CHUNK_STEPS * CHUNK_STEPS;
+          const int slot0 = L.nws;
+          for (int64_t k0 = 0; k0 < kst; k0 += kc) {
+            WorkItem w{p.group, (int)g.i, 1, a, b};
+            w.kbeg = (int32_t)k0;
+            w.kend = (int32_t)std::min(kst, k0 + kc);
+            w.slot = L.nws++;
+            tmp.push_back({tile_cost(w.kend - w.kbeg, 1), w});
+          }
+          L.red.push_back(ReduceItem{(int32_t)g.i, a, b, slot0, L.nws - slot0});
+          any_split = true;
+        } else {
+          tmp.push_back({g.cost, WorkItem{p.group, (int)g.i, (int)g.n, a, b}});
+        }
+      }
   }
+  if (any_split)      // balance_items takes the items longest first
+    std::stable_sort(tmp.begin(), tmp.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
   int nslots = h->num_sms;
   if (L.pair2) {
     nslots = pair_slots(h, S);
@@ -1475,7 +1556,7 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
   (void)ngroups;
   const int S = precision == ND_PREC_OZAKI ? h->ozaki_slices : 2;
   SplitLayout L;
-  split_layout(h, pairs_in, S, pair2, L);
+  split_layout(h, pairs_in, S, pair2, L, true);
   auto up = [&](void** dst, const void* src, size_t bytes) -> nd_status {
     nd_status e = nd_dalloc(h, dst, bytes);
     if (e) return e;
@@ -1489,6 +1570,11 @@ nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>&
   if ((s = nd_dalloc(h, &c.d_rowmax, std::max<int64_t>(L.exp_count, 1) * 8))) return s;
   if ((s = nd_dalloc(h, &c.d_pack, std::max<int64_t>(L.pack_bytes, 16)))) return s;
   if ((s = nd_dalloc(h, (void**)&c.d_exp, std::max<int64_t>(L.exp_count, 4) * 4))) return s;
+  if (!L.red.empty()) {
+    if ((s = up((void**)&c.d_red, L.red.data(), L.red.size() * sizeof(ReduceItem)))) return s;
+    if ((s = nd_dalloc(h, (void**)&c.d_ws, (size_t)L.nws * BM * BN * sizeof(long long)))) return s;
+  }
+  c.nred = (int)L.red.size();
   split_adopt(c, L, S);
   return ND_OK;
 }
@@ -1523,7 +1609,7 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
   }
   GemmArgs g{c.d_split_pairs, c.d_split_items, c.nsplit_items, (const SplitOp*)c.d_operands,
              (const unsigned char*)c.d_pack, c.d_exp, ptrs, alpha, beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1,
-             h->d_status, nullptr};
+             h->d_status, nullptr, (long long*)c.d_ws};
   if (c.nsplit_items == 0) return ND_OK;
   if (c.split_pair2) {
     switch (S) {
@@ -1534,13 +1620,23 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
       case 6: return launch_gemm2<6>(h, g, c.split_slots);
     }
   } else {
+    nd_status s = ND_OK;
     switch (S) {
-      case 2: return launch_gemm<2>(h, g);
-      case 3: return launch_gemm<3>(h, g);
-      case 4: return launch_gemm<4>(h, g);
-      case 5: return launch_gemm<5>(h, g);
-      case 6: return launch_gemm<6>(h, g);
+      case 2: s = launch_gemm<2>(h, g); break;
+      case 3: s = launch_gemm<3>(h, g); break;
+      case 4: s = launch_gemm<4>(h, g); break;
+      case 5: s = launch_gemm<5>(h, g); break;
+      case 6: s = launch_gemm<6>(h, g); break;
+      default: return nd_fail(h, ND_ERR_ARG, "unsupported slice count %d", S);
     }
+    if (s || c.nred == 0) return s;
+    nd_prof_begin(h, "split_reduce");
+    split_reduce<<<std::min(c.nred, 4 * h->num_sms), 256, 0, h->stream>>>(
+        c.d_split_pairs, c.d_red, c.nred, (const SplitOp*)c.d_operands, c.d_exp, (const long long*)c.d_ws, ptrs, alpha,
+        beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    return nd_cuda_check(h, cudaGetLastError(), "split_reduce");
   }
   return nd_fail(h, ND_ERR_ARG, "unsupported slice count %d", S);
 }
