@@ -102,6 +102,17 @@ nd_status nd_set_split_tile(nd_handle h, int32_t shape);
  * map describes, the group tiles otherwise.  Both are bit-exact.  No counterpart in
  * the reference. */
 nd_status nd_set_permute_path(nd_handle h, int32_t path);
+/* Verify mode.  With on != 0, every contraction in a split precision (ND_PREC_OZAKI,
+ * ND_PREC_BF16X3) through nd_contract_dense_f64, nd_bs_contract_f64 and
+ * nd_bs_contract_adjoint_f64 is computed a second time with the FP64 kernels into
+ * scratch memory, and the relative Frobenius distance of the two results,
+ * ||R - R_fp64||_F / ||R_fp64||_F over every element the call writes (both cotangents
+ * for the adjoint), is recorded; FP64 calls record 0.  A verified call synchronises the
+ * stream and is refused (ND_ERR_ARG) during graph capture.  Switching the mode resets
+ * the record.  No counterpart in the reference (its BLAS path has one precision). */
+nd_status nd_set_verify(nd_handle h, int32_t on);
+/* The relative error recorded by the last verified contraction, -1 when none. */
+nd_status nd_verify_last(nd_handle h, double* rel_err);
 /* Where nd_bs_plan_create builds plans: 0 (default) = on the host up to 4096 pairs,
  * else on the device; 1 = always on the device; 2 = on the host whenever the
  * contracted block numbers fit a 64-bit key.  Every placement gives the same plan.

@@ -297,6 +297,19 @@ nd_status nd_set_permute_path(nd_handle h, int32_t path) {
   return ND_OK;
 }
 
+nd_status nd_set_verify(nd_handle h, int32_t on) {
+  if (!h) return ND_ERR_ARG;
+  h->verify = on ? 1 : 0;
+  h->verify_err = -1.0;
+  return ND_OK;
+}
+
+nd_status nd_verify_last(nd_handle h, double* rel_err) {
+  if (!h || !rel_err) return ND_ERR_ARG;
+  *rel_err = h->verify_err;
+  return ND_OK;
+}
+
 nd_status nd_set_ozaki_slices(nd_handle h, int32_t s) {
   if (!h) return ND_ERR_ARG;
   if (s < 3 || s > 6) return nd_fail(h, ND_ERR_ARG, "ozaki slices must be in 3..6 (got %d)", s);

@@ -77,6 +77,8 @@ struct nd_context {
   DeviceStatus* d_plan_status = nullptr;
   int plan_where = 0;                 // nd_set_plan_placement: 0 by size, 1 device, 2 host
   int permute_tma = 0;                // nd_set_permute_path: 1 = TMA tiles where they apply
+  int verify = 0;                     // nd_set_verify: rerun split-precision contractions in FP64
+  double verify_err = -1.0;           // nd_verify_last: last recorded relative Frobenius distance
   // pinned ring for descriptor uploads (nd_upload): region [begin, end) may be reused
   // once its copy's event has completed
   unsigned char* up_ring = nullptr;

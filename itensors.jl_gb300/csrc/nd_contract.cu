@@ -17,6 +17,7 @@
 #include <string>
 #include <new>
 #include <climits>
+#include <cmath>
 
 nd_status nd_split_build(nd_handle h, ExecCache& c, const std::vector<PairDesc>& pairs, int ngroups, int precision,
                          int pair2);
@@ -345,6 +346,94 @@ nd_status nd_execute_cached(nd_handle h, ExecCache& c, const std::vector<PairDes
 }
 
 // ---------------------------------------------------------------------------
+// Verify mode (nd_set_verify): a split-precision contraction is run a second time
+// with the FP64 kernels into scratch memory and the relative Frobenius distance of the
+// two results is recorded.
+// ---------------------------------------------------------------------------
+constexpr int kVerifyCtas = 256;
+
+// Per-CTA sums of (x - y)^2 and y^2 over element ranges [start[r], start[r] + len) of
+// two buffers; flat index t lies in range r when prefix[r] <= t < prefix[r + 1].
+__global__ void __launch_bounds__(256) verify_partial(const double* x, const double* y, const int64_t* start,
+                                                      const int64_t* prefix, int nranges, double* part) {
+  __shared__ double s0[256], s1[256];
+  const int64_t total = prefix[nranges];
+  double a = 0.0, b = 0.0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nranges - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (prefix[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const int64_t i = start[lo] + (t - prefix[lo]);
+    const double yv = y[i], d = x[i] - yv;
+    a += d * d;
+    b += yv * yv;
+  }
+  s0[threadIdx.x] = a;
+  s1[threadIdx.x] = b;
+  __syncthreads();
+  for (int o = 128; o; o >>= 1) {
+    if ((int)threadIdx.x < o) { s0[threadIdx.x] += s0[threadIdx.x + o]; s1[threadIdx.x] += s1[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = s0[0]; part[2 * blockIdx.x + 1] = s1[0]; }
+}
+
+// One output of a verified call: the split-precision result x, the FP64 result y and
+// the element ranges (offset, length) the call wrote.
+struct VerifyOut {
+  const double* x;
+  const double* y;
+  std::vector<std::pair<int64_t, int64_t>> ranges;
+};
+
+// Records sqrt(sum |x - y|^2 / sum |y|^2) over every output; synchronises the stream.
+static nd_status verify_record(nd_handle h, const std::vector<VerifyOut>& outs) {
+  double num = 0.0, den = 0.0;
+  std::vector<double> part(2 * kVerifyCtas);
+  for (const VerifyOut& o : outs) {
+    std::vector<std::pair<int64_t, int64_t>> r = o.ranges;
+    std::sort(r.begin(), r.end());
+    std::vector<int64_t> start, prefix{0};
+    for (const auto& q : r) {
+      if (q.second <= 0) continue;
+      if (!start.empty() && start.back() + (prefix.back() - prefix[prefix.size() - 2]) == q.first) {
+        prefix.back() += q.second;                      // adjacent to the previous range: merge
+      } else {
+        start.push_back(q.first);
+        prefix.push_back(prefix.back() + q.second);
+      }
+    }
+    if (start.empty()) continue;
+    const int n = (int)start.size();
+    std::vector<int64_t> hostbuf(start);
+    hostbuf.insert(hostbuf.end(), prefix.begin(), prefix.end());
+    int64_t* d = nullptr;
+    ND_CUDA(h, cudaMallocAsync(&d, hostbuf.size() * 8 + part.size() * 8, h->stream));
+    double* dpart = (double*)(d + hostbuf.size());
+    nd_status s = nd_upload(h, d, hostbuf.data(), hostbuf.size() * 8);
+    if (s == ND_OK) {
+      nd_prof_begin(h, "verify_partial");
+      verify_partial<<<kVerifyCtas, 256, 0, h->stream>>>(o.x, o.y, d, d + n, n, dpart);
+      nd_prof_end(h);
+      ND_LAUNCHED(h);
+      s = nd_cuda_check(h, cudaGetLastError(), "verify_partial");
+    }
+    cudaError_t e = s == ND_OK ? cudaMemcpyAsync(part.data(), dpart, part.size() * 8, cudaMemcpyDeviceToHost, h->stream)
+                               : cudaSuccess;
+    cudaFreeAsync(d, h->stream);
+    if (s != ND_OK) return s;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return nd_cuda_check(h, e, "verify");
+    for (int b = 0; b < kVerifyCtas; ++b) { num += part[2 * b]; den += part[2 * b + 1]; }
+  }
+  h->verify_err = den > 0.0 ? std::sqrt(num / den) : std::sqrt(num);
+  return ND_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Dense contract!
 // ---------------------------------------------------------------------------
 constexpr size_t kDenseCacheEntries = 64;
@@ -460,8 +549,34 @@ extern "C" nd_status nd_contract_dense_f64(nd_handle h, double* R, int32_t rankR
   if (!c && nd_capturing(h))
     return nd_fail(h, ND_ERR_ARG, "contract: run this shape once before graph capture (its state is built then)");
   if (!c) return nd_fail(h, ND_ERR_OOM, "contract: host allocation failed");
+  const bool verify = h->verify && precision != ND_PREC_FP64;
+  if (h->verify && nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "contract: verify mode cannot be graph-captured");
+  double* saved = nullptr;   // verify with beta != 0: R before the call, the FP64 run's input
+  if (verify && beta != 0.0) {
+    ND_CUDA(h, cudaMallocAsync(&saved, nR * 8, h->stream));
+    ND_CUDA(h, cudaMemcpyAsync(saved, R, nR * 8, cudaMemcpyDeviceToDevice, h->stream));
+  }
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
   nd_status s = nd_execute_cached(h, *c, pairs, 1, ptrs, alpha, beta, precision);
+  if (s == ND_OK && verify) {
+    ExecCache* c64 = dense_exec(h, pd, ND_PREC_FP64);
+    if (!c64) s = nd_fail(h, ND_ERR_OOM, "contract: host allocation failed");
+    double* F = saved;
+    if (s == ND_OK && !F) {
+      cudaError_t e = cudaMallocAsync(&F, nR * 8, h->stream);
+      if (e != cudaSuccess) s = nd_cuda_check(h, e, "verify scratch");
+    }
+    if (s == ND_OK) {
+      JobPtrs p64{{A, nullptr}, {B, nullptr}, {F, nullptr}};
+      s = nd_execute_cached(h, *c64, pairs, 1, p64, alpha, beta, ND_PREC_FP64);
+    }
+    if (s == ND_OK) s = verify_record(h, {VerifyOut{R, F, {{0, nR}}}});
+    if (F) cudaFreeAsync(F, h->stream);
+    saved = nullptr;
+  } else if (s == ND_OK && h->verify) {
+    h->verify_err = 0.0;
+  }
+  if (saved) cudaFreeAsync(saved, h->stream);
   if (s != ND_OK) return s;
   if (nd_capturing(h)) return ND_OK;
   return nd_check_device_status(h, "contract");   // synchronises the stream
@@ -599,8 +714,32 @@ extern "C" nd_status nd_bs_contract_f64(nd_handle h, nd_plan p, double* R, const
   if (precision < 0 || precision > 2) return nd_fail(h, ND_ERR_ARG, "bs_contract: unknown precision %d", precision);
   nd_status s = build_forward_descs(p);
   if (s) return s;
+  if (h->verify && nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "bs_contract: verify mode cannot be graph-captured");
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
-  return nd_execute_cached(h, p->cache[precision], p->descs, p->ngroups, ptrs, alpha, 0.0, precision);
+  s = nd_execute_cached(h, p->cache[precision], p->descs, p->ngroups, ptrs, alpha, 0.0, precision);
+  if (s || !h->verify) return s;
+  if (precision == ND_PREC_FP64) {
+    h->verify_err = 0.0;
+    return ND_OK;
+  }
+  // every output block is written whole (its first pair overwrites), so only those
+  // ranges are compared; the scratch spans the highest one
+  VerifyOut vo{R, nullptr, {}};
+  int64_t extent = 0;
+  for (int32_t g = 0; g < p->res.nR; ++g) {
+    int64_t n = 1;
+    for (int k = 0; k < p->rankR; ++k) n *= p->r_blockdims[k][p->res.blocksR[(size_t)g * p->rankR + k] - 1];
+    vo.ranges.push_back({p->res.offsetsR[g], n});
+    extent = std::max(extent, p->res.offsetsR[g] + n);
+  }
+  double* F = nullptr;
+  ND_CUDA(h, cudaMallocAsync(&F, std::max<int64_t>(extent, 1) * 8, h->stream));
+  vo.y = F;
+  JobPtrs p64{{A, nullptr}, {B, nullptr}, {F, nullptr}};
+  s = nd_execute_cached(h, p->cache[ND_PREC_FP64], p->descs, p->ngroups, p64, alpha, 0.0, ND_PREC_FP64);
+  if (s == ND_OK) s = verify_record(h, {vo});
+  cudaFreeAsync(F, h->stream);
+  return s;
 }
 
 // Pullback: job 0: Abar = Rbar * B grouped by A block; job 1: Bbar = A * Rbar grouped by B block.
@@ -669,6 +808,7 @@ extern "C" nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan p, const do
   if (!h || !p) return ND_ERR_ARG;
   if (!Abar || !Bbar) return nd_fail(h, ND_ERR_ARG, "adjoint: NULL output");
   if (precision < 0 || precision > 2) return nd_fail(h, ND_ERR_ARG, "adjoint: unknown precision %d", precision);
+  if (h->verify && nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "adjoint: verify mode cannot be graph-captured");
   nd_status s = build_adjoint_descs(p);
   if (s) return s;
   // blocks of A / B that no pair touches have a zero cotangent
@@ -691,9 +831,40 @@ extern "C" nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan p, const do
     ND_LAUNCHED(h);
     ND_CUDA(h, cudaFreeAsync(d, h->stream));
   }
-  if (p->adj_descs.empty()) return ND_OK;
+  if (p->adj_descs.empty()) {
+    if (h->verify) h->verify_err = 0.0;
+    return ND_OK;
+  }
   JobPtrs ptrs{{Rbar, A}, {B, Rbar}, {Abar, Bbar}};
-  return nd_execute_cached(h, p->adj_cache[precision], p->adj_descs, p->adj_ngroups, ptrs, 1.0, 0.0, precision);
+  s = nd_execute_cached(h, p->adj_cache[precision], p->adj_descs, p->adj_ngroups, ptrs, 1.0, 0.0, precision);
+  if (s || !h->verify) return s;
+  if (precision == ND_PREC_FP64) {
+    h->verify_err = 0.0;
+    return ND_OK;
+  }
+  // both cotangents over every block of A and B (untouched blocks are zero in both runs)
+  VerifyOut va{Abar, nullptr, {}}, vb{Bbar, nullptr, {}};
+  int64_t ea = 0, eb = 0;
+  for (int a = 0; a < p->A.nnzblocks; ++a) {
+    va.ranges.push_back({p->A.offsets[a], p->A.block_elems(a)});
+    ea = std::max(ea, p->A.offsets[a] + p->A.block_elems(a));
+  }
+  for (int b = 0; b < p->B.nnzblocks; ++b) {
+    vb.ranges.push_back({p->B.offsets[b], p->B.block_elems(b)});
+    eb = std::max(eb, p->B.offsets[b] + p->B.block_elems(b));
+  }
+  double* F = nullptr;
+  ND_CUDA(h, cudaMallocAsync(&F, std::max<int64_t>(ea + eb, 1) * 8, h->stream));
+  nd_status s2 = nd_cuda_check(h, cudaMemsetAsync(F, 0, (ea + eb) * 8, h->stream), "verify scratch");
+  va.y = F;
+  vb.y = F + ea;
+  if (s2 == ND_OK) {
+    JobPtrs p64{{Rbar, A}, {B, Rbar}, {F, F + ea}};
+    s2 = nd_execute_cached(h, p->adj_cache[ND_PREC_FP64], p->adj_descs, p->adj_ngroups, p64, 1.0, 0.0, ND_PREC_FP64);
+  }
+  if (s2 == ND_OK) s2 = verify_record(h, {va, vb});
+  cudaFreeAsync(F, h->stream);
+  return s2;
 }
 
 // ---------------------------------------------------------------------------

@@ -319,7 +319,10 @@ nd_status nd_device_exclusive_scan(nd_handle h, int64_t* data, int64_t n, int64_
     nd_prof_end(h);
     ND_LAUNCHED(h);
     nd_status s = nd_device_exclusive_scan(h, sums, nb, sums + nb + 1);
-    if (s != ND_OK) return s;
+    if (s != ND_OK) {
+      cudaFreeAsync(sums, h->stream);
+      return s;
+    }
     nd_prof_begin(h, "scan_apply");
     scan_apply<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(data, sums, n);
     nd_prof_end(h);

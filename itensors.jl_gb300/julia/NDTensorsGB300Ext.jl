@@ -62,6 +62,15 @@ end
 check(st) = st == 0 ? nothing :
   throw(NDError(st, unsafe_string(ccall((:nd_last_error, LIB), Cstring, (Ptr{Cvoid},), handle()))))
 
+# Verify mode: split-precision contractions are recomputed in FP64 and the relative
+# Frobenius distance of the last one is kept (0 for FP64 calls, -1 before any).
+set_verify!(on::Bool) = check(ccall((:nd_set_verify, LIB), Int32, (Ptr{Cvoid}, Int32), handle(), on ? 1 : 0))
+function verify_last()
+  e = Ref{Float64}(-1.0)
+  check(ccall((:nd_verify_last, LIB), Int32, (Ptr{Cvoid}, Ref{Float64}), handle(), e))
+  return e[]
+end
+
 # ---- device vector --------------------------------------------------------
 mutable struct GB300Vector <: AbstractVector{Float64}
   ptr::Ptr{Float64}

@@ -67,6 +67,8 @@ SIGNATURES = {
     "nd_set_split_tile": [_P, _I32],
     "nd_set_plan_placement": [_P, _I32],
     "nd_set_permute_path": [_P, _I32],
+    "nd_set_verify": [_P, _I32],
+    "nd_verify_last": [_P, _PD],
     "nd_set_spin_limit": [_P, C.c_uint32],
     "nd_set_svd_max_sweeps": [_P, _I32],
     "nd_svd_last_info": [_P, _P, _I32, _P, _I32],
@@ -223,6 +225,17 @@ class Handle:
 
     def tune_load(self, path):
         self._check(self.lib.nd_tune_load(self.ptr, os.fsencode(str(path))))
+
+    def verify(self, enable=True):
+        """Verify mode: split-precision contractions are recomputed in FP64 and the relative
+        Frobenius distance of the two results is recorded (read it with verify_last)."""
+        self._check(self.lib.nd_set_verify(self.ptr, 1 if enable else 0))
+
+    def verify_last(self):
+        """The relative error of the last verified contraction (0 for FP64, -1 if none)."""
+        v = C.c_double()
+        self._check(self.lib.nd_verify_last(self.ptr, C.byref(v)))
+        return v.value
 
     def launches(self):
         c = C.c_int64()
