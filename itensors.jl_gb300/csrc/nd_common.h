@@ -125,6 +125,24 @@ nd_status nd_upload(nd_handle h, void* dst, const void* src, size_t bytes);
 nd_status nd_dalloc(nd_handle h, void** p, size_t bytes);
 nd_status nd_check_device_status(nd_handle h, const char* what);  // syncs
 
+// One-time set-up of a launch site (a kernel's shared-memory opt-in, an occupancy
+// query) per device, since kernel attributes apply per device: thread-safe, so that
+// handles driven from different host threads may launch concurrently, and retried
+// after a failure.
+struct NdOnce {
+  std::mutex m;
+  uint64_t done = 0;   // bit d: device d is set up
+};
+template <typename F>
+cudaError_t nd_once(NdOnce& o, int device, F&& f) {
+  std::lock_guard<std::mutex> lk(o.m);
+  const uint64_t bit = 1ull << (device & 63);
+  if (o.done & bit) return cudaSuccess;
+  const cudaError_t e = f();
+  if (e == cudaSuccess) o.done |= bit;
+  return e;
+}
+
 #define ND_CUDA(h, call)                                              \
   do {                                                                \
     cudaError_t _e = (call);                                          \

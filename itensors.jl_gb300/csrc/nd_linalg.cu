@@ -1125,24 +1125,31 @@ static nd_status run_sweeps(nd_handle h, const SvdBlock* dblk, int nb, int task0
 // panel in shared memory (the caller then uses the scalar sweeps).
 template <typename T, int B>
 static nd_status launch_bj(nd_handle h, const BjArgs<T>& a, size_t smem) {
-  static size_t attr = 0;   // dynamic shared memory this instantiation is opted in to
-  if (smem > attr) {
-    if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd panel sweep: run once before graph capture");
-    nd_status st = nd_cuda_check(h, cudaFuncSetAttribute(bj_sweep<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         (int)smem), "svd panel sweep shared memory");
-    if (st) return st;
-    attr = smem;
+  // per device: the dynamic shared memory this instantiation is opted in to, and the
+  // resident CTAs per SM for each size (neither set up while capturing)
+  static std::mutex mu;
+  static std::map<int, size_t> attr;
+  static std::map<std::pair<int, size_t>, int> occ_of;
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& opted = attr[h->device];
+    if (smem > opted) {
+      if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd panel sweep: run once before graph capture");
+      nd_status st = nd_cuda_check(h, cudaFuncSetAttribute(bj_sweep<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                           (int)smem), "svd panel sweep shared memory");
+      if (st) return st;
+      opted = smem;
+    }
+    auto it = occ_of.find({h->device, smem});
+    if (it == occ_of.end()) {
+      if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd panel sweep: run once before graph capture");
+      int occ = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bj_sweep<T, B>, 32 * B, smem);
+      it = occ_of.emplace(std::make_pair(h->device, smem), occ).first;
+    }
+    per_sm = it->second;
   }
-  // resident CTAs per SM, queried once per shared-memory size (no query while capturing)
-  static size_t occ_smem = 0;
-  static int occ = 0;
-  if (smem != occ_smem) {
-    if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd panel sweep: run once before graph capture");
-    occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bj_sweep<T, B>, 32 * B, smem);
-    occ_smem = smem;
-  }
-  const int per_sm = occ;
   if (per_sm < 1) return nd_fail(h, ND_ERR_UNSUPPORTED, "svd panel sweep does not fit an SM");
   const int grid = std::max(1, std::min(a.ntasks, per_sm * h->num_sms));
   BjArgs<T> args = a;
@@ -1553,8 +1560,8 @@ extern "C" nd_status nd_bs_svd_f64(nd_handle h, int32_t nb, const int64_t* rows,
   if ((size_t)npow2 * 8 > 200 * 1024) return nd_fail(h, ND_ERR_UNSUPPORTED, "svd: %d singular values exceed the on-chip sort", total);
   TruncParams tp{mindim < 1 ? 1 : mindim, maxdim, cutoff, cutoff >= 0.0 ? 1 : 0, use_absolute_cutoff, use_relative_cutoff};
   const bool trunc = maxdim >= 0 || cutoff >= 0.0;
-  static bool attr = false;
-  if (!attr) { cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+  static NdOnce sort_attr;
+  nd_once(sort_attr, h->device, [] { return cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
   nd_prof_begin(h, "sort_truncate");
   sort_truncate<<<1, 1024, npow2 * 8, s>>>(sig, total, npow2, 1, 1, tp, P, dlen, res, res + 1);
   nd_prof_end(h);
@@ -1702,8 +1709,8 @@ extern "C" nd_status nd_bs_eigen_f64(nd_handle h, int32_t nb, const int64_t* dim
   // pooled |lambda|: sort + truncate! on the device, then the kept dims per block
   TruncParams tp{mindim < 1 ? 1 : mindim, maxdim, cutoff, cutoff >= 0.0 ? 1 : 0, use_absolute_cutoff, use_relative_cutoff};
   const bool trunc = maxdim >= 0 || cutoff >= 0.0;
-  static bool attr = false;
-  if (!attr) { cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+  static NdOnce sort_attr;
+  nd_once(sort_attr, h->device, [] { return cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
   nd_prof_begin(h, "sort_truncate");
   sort_truncate<<<1, 1024, npow2 * 8, s>>>(absl, total, npow2, 0, 1, tp, P, dlen, res, res + 1);
   nd_prof_end(h);
@@ -2067,8 +2074,8 @@ extern "C" nd_status nd_bs_svd_plan_create(nd_handle h, int32_t nb, const int64_
     st = nd_cuda_check(h, cudaMemsetAsync(p->Wsrc, 0, std::max<int64_t>(p->woff, 1) * 8, s), "svd plan");
   }
   if (!st) {
-    static bool attr = false;
-    if (!attr) { cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+    static NdOnce sort_attr;
+    nd_once(sort_attr, h->device, [] { return cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
     std::vector<SvdBlock> zb = p->blocks;               // a_off: the dummy's block offsets
     int64_t o = 0;
     for (auto& b : zb) { b.a_off = o; o += (int64_t)b.m * b.n; }
@@ -2146,8 +2153,8 @@ extern "C" nd_status nd_truncate_f64(nd_handle h, const double* Pin, int32_t n, 
   ND_CUDA(h, cudaMallocAsync(&res, 16, s));
   ND_CUDA(h, cudaMallocAsync(&len, 8, s));
   TruncParams tp{mindim < 1 ? 1 : mindim, maxdim, cutoff, cutoff >= 0.0 ? 1 : 0, use_absolute_cutoff, use_relative_cutoff};
-  static bool attr = false;
-  if (!attr) { cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); attr = true; }
+  static NdOnce sort_attr;
+  nd_once(sort_attr, h->device, [] { return cudaFuncSetAttribute(sort_truncate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); });
   // the caller's order is kept (truncate! takes a descending spectrum; a negative
   // spectrum is descending in magnitude, which a value sort would reverse)
   nd_prof_begin(h, "sort_truncate");

@@ -892,12 +892,11 @@ __global__ void __launch_bounds__(256) split_reduce(const PairDesc* pairs, const
 template <int S>
 nd_status launch_gemm(nd_handle h, const GemmArgs& g) {
   using C = Cfg<S>;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(split_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
-    if (e != cudaSuccess) return nd_cuda_check(h, e, "split_gemm smem attribute");
-    attr = true;
-  }
+  static NdOnce attr;
+  cudaError_t e = nd_once(attr, h->device, [] {
+    return cudaFuncSetAttribute(split_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+  });
+  if (e != cudaSuccess) return nd_cuda_check(h, e, "split_gemm smem attribute");
   int blocks = std::min(g.nitems, h->num_sms);
   GemmArgs gt = g;
   gt.cta_times = nd_cta_slot(h, blocks);
@@ -1282,9 +1281,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1) split_g
 template <int S>
 int pair_slots_for(nd_handle h) {
   using C = Cfg2<S>;
-  static int slots = -1;
-  if (slots < 0) {
-    slots = 0;
+  static std::mutex mu;
+  static std::map<int, int> slots_of;   // per device
+  std::lock_guard<std::mutex> lk(mu);
+  auto known = slots_of.find(h->device);
+  if (known != slots_of.end()) return known->second;
+  int slots = 0;
+  {
     if (cudaFuncSetAttribute(split_gemm2<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) == cudaSuccess) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(2 * std::max(1, h->num_sms / 2));
@@ -1297,6 +1300,7 @@ int pair_slots_for(nd_handle h) {
       cudaGetLastError();
     }
   }
+  slots_of[h->device] = slots;
   return slots;
 }
 

@@ -366,16 +366,15 @@ __global__ void permute_scalar(const double* T, double* R, PermParams p) {
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  // looked up once (a function-local static is initialised once, thread-safely)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     cudaDriverEntryPointQueryResult q;
     void* f = nullptr;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000)f;
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   return fn;
 }
 
@@ -499,12 +498,12 @@ nd_status nd_launch_permute(nd_handle h, double* R, const double* T, int rank, c
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r == CUDA_SUCCESS) {
       size_t smem = STAGES * TILE_BYTES + 1024;
-      static bool attr_set = false;
-      if (!attr_set) {
-        cudaFuncSetAttribute(permute_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(permute_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
-      }
+      static NdOnce attr;
+      nd_once(attr, h->device, [smem] {
+        cudaError_t e = cudaFuncSetAttribute(permute_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        return e == cudaSuccess ? cudaFuncSetAttribute(permute_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                : e;
+      });
       int64_t blocks = std::min<int64_t>(p.ntiles, (int64_t)h->num_sms * 3);
       nd_prof_begin(h, "permute_tma");
       if (p.mode == 0) permute_tma<true><<<(unsigned)blocks, threads, smem, h->stream>>>(tmap, R, Rin, p, h->d_status);

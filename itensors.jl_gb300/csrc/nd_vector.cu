@@ -170,11 +170,11 @@ int vec_ctas(nd_handle h) { return 4 * h->num_sms; }   // upper bound of the red
 // vec_ctas), so the fixed grid runs in one wave.  Queried once per instantiation.
 template <int KT>
 int dots_ctas(nd_handle h) {
-  static int per_sm = 0;
-  if (!per_sm) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vec_dots_part<KT>, VEC_THREADS, 0);
-    per_sm = std::max(1, std::min(per_sm, 4));
-  }
+  static const int per_sm = [] {    // initialised once, thread-safely
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, vec_dots_part<KT>, VEC_THREADS, 0);
+    return std::max(1, std::min(n, 4));
+  }();
   return per_sm * h->num_sms;
 }
 
