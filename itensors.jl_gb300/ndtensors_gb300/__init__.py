@@ -10,7 +10,8 @@ from . import workloads
 from . import linalg
 from . import autodiff
 from .autodiff import contract_autograd, contract_rrule, dense_structure
-from .linalg import MatricizePlan, Spectrum, SvdPlan, eigen, matricize, qr, svd, truncate, uncombine
+from .linalg import (CombinerTensor, MatricizePlan, Spectrum, SvdPlan, combine, contract_combiner, eigen,
+                     matricize, qr, svd, truncate, uncombine)
 from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
 from . import krylov
@@ -23,7 +24,8 @@ __all__ = [
     "BlockSparseTensor", "DenseTensor", "DiagBlockSparseTensor", "blockoffsets",
     "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
     "permutedims", "permutedims_", "permutedims_blocksparse",
-    "linalg", "MatricizePlan", "Spectrum", "SvdPlan", "eigen", "matricize", "qr", "svd", "truncate", "uncombine",
+    "linalg", "CombinerTensor", "MatricizePlan", "Spectrum", "SvdPlan", "combine", "contract_combiner", "eigen",
+    "matricize", "qr", "svd", "truncate", "uncombine",
     "autodiff", "contract_autograd", "contract_rrule", "dense_structure",
     "krylov", "HeffOperator", "Lanczos", "SweepStep", "lanczos",
     "hdf5io", "H5Reader", "load_blocksparse", "read_blocksparse", "save_blocksparse", "write_blocksparse",

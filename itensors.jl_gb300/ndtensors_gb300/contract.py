@@ -235,14 +235,24 @@ def contract_diag(T1: BlockSparseTensor, l1, D, l2, lr=None, alpha=1.0):
 
 def contract(T1, labels1, T2, labels2, labelsR=None, precision="fp64"):
     """contract(T1, labelsT1, T2, labelsT2[, labelsR]) for Dense, BlockSparse or
-    BlockSparse x DiagBlockSparse storage.
+    BlockSparse x DiagBlockSparse storage, or a tensor with a CombinerTensor
+    (linalg.contract_combiner; NDTensors/src/blocksparse/combiner.jl:25-143,
+    NDTensors/src/combiner/contract.jl:14-77).
 
     A block-diagonal DiagBlockSparse operand runs on the library's diagonal kernel
     (contract_diag; NDTensors/src/blocksparse/diagblocksparse.jl:601-696) with the block
     plan and output structure of contraction_output; the result is exact (no
     precision choice applies: each output element is one product or a short sum)."""
+    from .linalg import CombinerTensor, contract_combiner
     from .tensors import DiagBlockSparseTensor
     l1, l2 = tuple(labels1), tuple(labels2)
+    first = isinstance(T1, CombinerTensor)
+    if first:
+        T1, l1, T2, l2 = T2, l2, T1, l1
+    if isinstance(T2, CombinerTensor):
+        if not isinstance(T1, (BlockSparseTensor, DenseTensor)):
+            raise TypeError("contract: a combiner needs a Dense or BlockSparse partner")
+        return contract_combiner(T1, l1, T2, l2, labelsR, combiner_first=first)[0]
     if isinstance(T1, DiagBlockSparseTensor):
         return contract(T2, l2, T1, l1, contract_labels(l2, l1) if labelsR is None else labelsR, precision)
     if isinstance(T2, DiagBlockSparseTensor):

@@ -8,6 +8,7 @@ Mirrors:
   combiner matricization (permutedims_combine)  NDTensors/src/blocksparse/blocksparsetensor.jl:537-638,
                                                 src/qn/qnindex.jl:359-426
   uncombine                                     NDTensors/src/blocksparse/blocksparsetensor.jl:664-791
+  contract(::BlockSparseTensor, ::CombinerTensor) NDTensors/src/blocksparse/combiner.jl:25-143
 The factorizations, the spectrum sort and truncate! run on the device; only
 the block structure (which blocks survive, their new dims) is host logic.
 """
@@ -406,7 +407,7 @@ class MatricizePlan:
             pass
 
 
-def uncombine(T: BlockSparseTensor, combdim, group, info):
+def uncombine(T: BlockSparseTensor, combdim, group, info, front=False):
     """Split the fused dimension ``combdim`` of T back into the indices of ``group``
     (NDTensors/src/blocksparse/blocksparsetensor.jl:693-791: uncombine_output +
     uncombine, with uncombine_blocks :664-678).
@@ -416,7 +417,11 @@ def uncombine(T: BlockSparseTensor, combdim, group, info):
     block of T, in T's order, yields one block per uncombined sector of its combined
     sector, in the combined index's sorted order (the reference's block order); the
     sub-block is the slice [off, off + dim) of T's block along ``combdim``, copied on
-    the device (nd_block_copy_f64) into its own column-major block.
+    the device (nd_block_copy_f64) into its own column-major block.  With ``front``
+    the uncombined indices come first and the others follow in T's order, as in the
+    uncombining contraction with a combiner (NDTensors/src/blocksparse/combiner.jl:90-140,
+    which moves the combined index to the front before splitting it; block order is
+    unchanged by that move).
     """
     import torch
     _, place = info
@@ -437,11 +442,15 @@ def uncombine(T: BlockSparseTensor, combdim, group, info):
             lin0 //= n
         return tuple(out)
 
-    inds = list(T.inds[:combdim]) + gdims + list(T.inds[combdim + 1:])
+    others = list(T.inds[:combdim]) + list(T.inds[combdim + 1:])
+    inds = gdims + others if front else list(T.inds[:combdim]) + gdims + list(T.inds[combdim + 1:])
     blocks, pieces = [], []
     for i, b in enumerate(T.blocks):
         for off, orig in subs[b[combdim]]:
-            blocks.append(tuple(b[:combdim]) + split(orig) + tuple(b[combdim + 1:]))
+            if front:
+                blocks.append(split(orig) + tuple(b[:combdim]) + tuple(b[combdim + 1:]))
+            else:
+                blocks.append(tuple(b[:combdim]) + split(orig) + tuple(b[combdim + 1:]))
             pieces.append((i, off))
     offs, nnz = blockoffsets(blocks, inds)
     data = torch.empty(max(nnz, 1), dtype=torch.float64, device=T.data.device)[:nnz]
@@ -458,12 +467,14 @@ def uncombine(T: BlockSparseTensor, combdim, group, info):
         c.src_off = T.offsets[i] + off * tst[combdim]
         c.dst_off = offs[j]
         c.rank = len(rb)
-        src = list(tst[:combdim])
+        gpos = 0 if front else combdim           # where the group's dims sit in the result
+        gsrc = []
         g = tst[combdim]
         for k in range(ng):                      # the fused dimension splits first index fastest
-            src.append(g)
-            g *= rb[combdim + k]
-        src += tst[combdim + 1:]
+            gsrc.append(g)
+            g *= rb[gpos + k]
+        rest = list(tst[:combdim]) + list(tst[combdim + 1:])
+        src = gsrc + rest if front else list(tst[:combdim]) + gsrc + list(tst[combdim + 1:])
         dst = 1
         for k in range(len(rb)):
             c.dims[k] = rb[k]
@@ -476,3 +487,188 @@ def uncombine(T: BlockSparseTensor, combdim, group, info):
         handle(T.data.device.index or 0).call("nd_block_copy_f64", len(copies), arr, C.c_void_p(T.data.data_ptr()),
                                               C.c_void_p(data.data_ptr()))
     return R
+
+
+# ---------------------------------------------------------------------------
+# Contraction with a combiner (NDTensors/src/blocksparse/combiner.jl:25-143)
+# ---------------------------------------------------------------------------
+
+class CombinerTensor:
+    """combiner(inds...): fuses QN indices into one combined index whose sectors are
+    the fused products (first index fastest), stably sorted by charge and merged
+    (src/qn/qnindex.jl:359-426; blockperm / blockcomb of NDTensors' Combiner).
+
+    ``group``: the uncombined indices as (sectors, arrow), in the combiner's order; by
+    the reference's convention the combined index is the combiner's first label."""
+
+    def __init__(self, group):
+        self.group = [(tuple((int(q), int(d)) for q, d in sec), int(a)) for sec, a in group]
+        if not self.group:
+            raise ValueError("combiner: no indices to combine")
+        merged, self.place = _group_place(self.group)
+        self.csec = tuple(tuple(m) for m in merged)
+        self.arrow = fused_sectors(self.group)[1]
+
+    @property
+    def info(self):
+        """(combined sectors, place) as matricize returns it for a group."""
+        return (self.csec, self.place)
+
+    @property
+    def combined_dims(self):
+        return tuple(d for _, d in self.csec)
+
+
+def _combine_layout(T, fuse_dims, cmb):
+    """Host structure of the combining contraction: (inds, blocks, offsets, nnz, copies)
+    with one block copy per block of T (see ``combine``)."""
+    fuse_dims = [int(d) for d in fuse_dims]
+    if len(fuse_dims) != len(cmb.group) or len(set(fuse_dims)) != len(fuse_dims):
+        raise ValueError("combine: one distinct tensor dimension per combiner index")
+    for d, (sec, _) in zip(fuse_dims, cmb.group):
+        if not 0 <= d < T.rank or tuple(T.inds[d]) != tuple(x for _, x in sec):
+            raise ValueError(f"combine: dimension {d} does not match the combiner's index")
+    rest = [d for d in range(T.rank) if d not in fuse_dims]
+    nbs = [len(sec) for sec, _ in cmb.group]
+    entries = {}
+    for i, b in enumerate(T.blocks):
+        lin, mul = 0, 1
+        for d, n in zip(fuse_dims, nbs):
+            lin += (b[d] - 1) * mul
+            mul *= n
+        cb, off = cmb.place[lin]
+        entries.setdefault((cb,) + tuple(b[d] for d in rest), []).append((i, off))
+    cblocks = sorted(entries, key=lambda x: tuple(reversed(x)))    # isblockless
+    inds = [cmb.combined_dims] + [tuple(T.inds[d]) for d in rest]
+    offs, nnz = blockoffsets(cblocks, inds)
+    copies = []
+    for j, kb in enumerate(cblocks):
+        ld = inds[0][kb[0] - 1]
+        for (i, off) in entries[kb]:
+            bd = T.blockdims(T.blocks[i])
+            c = BlockCopy()
+            c.src_off = T.offsets[i]
+            c.dst_off = offs[j] + off
+            c.rank = len(bd)
+            st, dst = 1, [0] * len(bd)
+            for d in fuse_dims:                  # inside the combined dimension, combiner order
+                dst[d] = st
+                st *= bd[d]
+            st = ld
+            for d in rest:
+                dst[d] = st
+                st *= bd[d]
+            s = 1
+            for k in range(len(bd)):
+                c.dims[k] = bd[k]
+                c.src_strides[k] = s
+                c.dst_strides[k] = dst[k]
+                s *= bd[k]
+            copies.append(c)
+    return inds, cblocks, offs, nnz, copies
+
+
+def combine(T: BlockSparseTensor, fuse_dims, cmb: CombinerTensor):
+    """The combining contraction: T's dimensions ``fuse_dims`` (0-based, in the
+    combiner's order) become the combined index, placed first, the other dimensions
+    follow in T's order (NDTensors/src/blocksparse/combiner.jl:25-89 with
+    permutedims_combine_output / permutedims_combine, blocksparsetensor.jl:537-638).
+
+    Output blocks are the combined coordinates ordered by isblockless (last dimension
+    most significant) without repeats, offsets in that order; every block of T is
+    permuted into its place inside its combined block by one device block copy.
+    (Sorting the combined coordinates equals the reference's sort of the sorted-position
+    coordinates followed by the merge, since the merge map is non-decreasing.)"""
+    import torch
+    inds, cblocks, offs, nnz, copies = _combine_layout(T, fuse_dims, cmb)
+    data = torch.empty(max(nnz, 1), dtype=torch.float64, device=T.data.device)[:nnz]
+    R = BlockSparseTensor(inds, cblocks, offs, data)
+    if copies:
+        arr = (BlockCopy * len(copies))(*copies)
+        handle(T.data.device.index or 0).call("nd_block_copy_f64", len(copies), arr, C.c_void_p(T.data.data_ptr()),
+                                              C.c_void_p(data.data_ptr()))
+    return R
+
+
+def contract_combiner(T: BlockSparseTensor, labelsT, Cmb: CombinerTensor, labelsC, labelsR=None,
+                      combiner_first=False):
+    """contract(T, labelsT, combiner, labelsC) (NDTensors/src/blocksparse/combiner.jl:25-143).
+
+    Combining when the combined label (``labelsC[0]``) is not among T's labels: the
+    combiner's other labels must all be T's, and the result is (combined index, T's
+    other indices in order).  Uncombining when it is: the result is (the combiner's
+    uncombined indices, T's other indices in order).  ``labelsR``, when given, permutes
+    that result (block-sparse permutedims).  Dense storage follows the dense rules
+    (``_contract_combiner_dense``; ``combiner_first``: the combiner was the call's first
+    operand).  Returns (tensor, its labels)."""
+    from .contract import permutedims_blocksparse
+    from .tensors import DenseTensor
+    lt, lc = tuple(labelsT), tuple(labelsC)
+    if len(lc) != len(Cmb.group) + 1 or len(lt) != T.rank:
+        raise ValueError("combiner contraction: label counts do not match the tensors")
+    clabel, uc = lc[0], lc[1:]
+    if isinstance(T, DenseTensor):
+        return _contract_combiner_dense(T, lt, Cmb, clabel, uc, labelsR, combiner_first)
+    if clabel not in lt:
+        if any(l not in lt for l in uc):
+            raise ValueError("combiner contraction: every uncombined label must be one of the tensor's")
+        R = combine(T, [lt.index(l) for l in uc], Cmb)
+        out = (clabel,) + tuple(l for l in lt if l not in uc)
+    else:
+        if any(l in lt for l in uc):
+            raise ValueError("combiner contraction: uncombined labels already present on the tensor")
+        cpos = lt.index(clabel)
+        if tuple(T.inds[cpos]) != Cmb.combined_dims:
+            raise ValueError("combiner contraction: the tensor's combined dimension does not match the combiner")
+        R = uncombine(T, cpos, Cmb.group, Cmb.info, front=True)
+        out = tuple(uc) + tuple(l for l in lt if l != clabel)
+    if labelsR is not None and tuple(labelsR) != out:
+        lr = tuple(labelsR)
+        if sorted(lr) != sorted(out):
+            raise ValueError("combiner contraction: output labels do not match")
+        R = permutedims_blocksparse(R, [out.index(l) + 1 for l in lr])
+        out = lr
+    return R, out
+
+
+def _contract_combiner_dense(T, lt, Cmb, clabel, uc, labelsR, combiner_first):
+    """Dense storage (NDTensors/src/combiner/contract.jl:14-77): the output labels follow
+    contract_labels of the call (the tensor's free labels, then the combiner's) unless
+    ``labelsR`` is given.  Combining permutes the uncombined dimensions together, in the
+    combiner's order, to the combined label's place (one device permute) and reshapes;
+    uncombining is a reshape of a copy, the uncombined labels taking the combined
+    label's place, then a permute if ``labelsR`` asks for another order."""
+    from .contract import permutedims
+    from .tensors import DenseTensor
+    gd = [sum(d for _, d in sec) for sec, _ in Cmb.group]
+    if clabel not in lt:
+        if any(l not in lt for l in uc):
+            raise ValueError("combiner contraction: every uncombined label must be one of the tensor's")
+        for l, d in zip(uc, gd):
+            if T.dims[lt.index(l)] != d:
+                raise ValueError("combiner contraction: a dimension does not match the combiner's index")
+        free = tuple(l for l in lt if l not in uc)
+        natural = (clabel,) + free if combiner_first else free + (clabel,)
+        out = natural if labelsR is None else tuple(labelsR)
+        if sorted(out) != sorted(natural):
+            raise ValueError("combiner contraction: output labels do not match")
+        expanded = []
+        for l in out:
+            expanded.extend(uc if l == clabel else (l,))
+        P = permutedims(T, [lt.index(l) + 1 for l in expanded])
+        dims = tuple(int(np.prod(gd)) if l == clabel else T.dims[lt.index(l)] for l in out)
+        return DenseTensor(dims, P.data), out
+    cpos = lt.index(clabel)
+    if any(l in lt for l in uc):
+        raise ValueError("combiner contraction: uncombined labels already present on the tensor")
+    if T.dims[cpos] != int(np.prod(gd)):
+        raise ValueError("combiner contraction: the tensor's combined dimension does not match the combiner")
+    natural = lt[:cpos] + tuple(uc) + lt[cpos + 1:]
+    dims = tuple(T.dims[:cpos]) + tuple(gd) + tuple(T.dims[cpos + 1:])
+    R = DenseTensor(dims, T.data.clone())
+    if labelsR is None or tuple(labelsR) == natural:
+        return R, natural
+    lr = tuple(labelsR)
+    if sorted(lr) != sorted(natural):
+        raise ValueError("combiner contraction: output labels do not match")
+    return permutedims(R, [natural.index(l) + 1 for l in lr]), lr

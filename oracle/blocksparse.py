@@ -13,6 +13,8 @@ Follows:
   NDTensors/src/blocksparse/blockoffsets.jl:103-111       permutedims of block offsets
   NDTensors/src/blocksparse/blocksparsetensor.jl:834-881  permutedims! per block
   NDTensors/src/blocksparse/blocksparsetensor.jl:537-638  permutedims_combine (matricization)
+  NDTensors/src/blocksparse/combiner.jl:25-143            contraction with a combiner
+  NDTensors/src/blocksparse/blocksparsetensor.jl:664-791  uncombine
 """
 from __future__ import annotations
 
@@ -208,6 +210,26 @@ def _isblockless_key(b):
     return tuple(reversed(b))
 
 
+def combiner_group(idx):
+    """The combined index of combiner(idx...) (src/qn/qnindex.jl:359-426): the fused
+    index (first index fastest), its sectors stably sorted by charge and merged
+    (combineblocks), and for every fused product block (1-based) its (combined block,
+    offset inside it), sub-blocks placed in sorted order.  Returns (fused, csec, place)."""
+    from .qn import combineblocks, fuse
+    fused = fuse(list(idx))
+    csec, perm, comb = combineblocks(fused.sectors)
+    place = {}
+    for pos, orig in enumerate(perm):             # pos: sorted position (0-based), orig: 1-based
+        cb = comb[pos]
+        off = 0
+        q = pos - 1
+        while q >= 0 and comb[q] == cb:
+            off += fused.sectors[perm[q] - 1][1]
+            q -= 1
+        place[orig] = (cb, off)
+    return fused, csec, place
+
+
 def matricize(t, qinds, row_dims, col_dims):
     """Fuse a QN block-sparse tensor into a 2-index block matrix.
 
@@ -223,26 +245,8 @@ def matricize(t, qinds, row_dims, col_dims):
     combined sectors (charge, dim) plus, for every original block-combination of
     the group, its (combined block, offset inside it).
     """
-    from .qn import combineblocks, fuse
-
-    def group_info(dims):
-        idx = [qinds[d] for d in dims]
-        fused = fuse(idx)
-        csec, perm, comb = combineblocks(fused.sectors)
-        # position of each uncombined product block: combined block + offset
-        place = {}
-        for pos, orig in enumerate(perm):         # pos: sorted position (0-based), orig: 1-based
-            cb = comb[pos]
-            off = 0
-            q = pos - 1
-            while q >= 0 and comb[q] == cb:
-                off += fused.sectors[perm[q] - 1][1]
-                q -= 1
-            place[orig] = (cb, off)
-        return fused, csec, place
-
-    rfused, rsec, rplace = group_info(row_dims)
-    cfused, csec, cplace = group_info(col_dims)
+    rfused, rsec, rplace = combiner_group([qinds[d] for d in row_dims])
+    cfused, csec, cplace = combiner_group([qinds[d] for d in col_dims])
     nb_rows = [qinds[d].nblocks for d in row_dims]
     nb_cols = [qinds[d].nblocks for d in col_dims]
     entries = {}
@@ -318,3 +322,72 @@ def uncombine(t, combdim, group_dims, group_info):
         sl[combdim] = slice(off, off + gsize)
         dst[...] = src[tuple(sl)].reshape(dst.shape, order="F")
     return r
+
+
+# --------------------------------------------------------------------------
+# Contraction with a combiner (NDTensors/src/blocksparse/combiner.jl:25-143)
+# --------------------------------------------------------------------------
+
+def combine(t, qinds, fuse_dims):
+    """contract(T, labels, combiner, labels) in the combining case
+    (NDTensors/src/blocksparse/combiner.jl:25-89): the indices ``fuse_dims`` of ``t``
+    (0-based, in the combiner's order) become one combined index, placed first, and the
+    other indices follow in ``t``'s order.  Restates permutedims_combine_output /
+    permutedims_combine (blocksparsetensor.jl:537-638) step by step: permute the block
+    coordinates, combine the fused coordinates column-major (combine_dims :487-507),
+    map them to sorted positions (perm_blocks :510-517), sort by isblockless, map to
+    combined blocks and drop repeats in order (combine_blocks :526-535); then place each
+    permuted block at its offset inside the combined block.
+
+    ``qinds``: oracle.qn.QNIndex of every dimension of ``t``.  Returns (tensor, (csec, place)).
+    """
+    from .qn import combineblocks
+    fuse_dims = list(fuse_dims)
+    nc = len(fuse_dims)
+    rest = [d for d in range(t.rank) if d not in fuse_dims]
+    perm = fuse_dims + rest                        # getperm(output_tensor_labels_uc, tensor_labels)
+    fused, csec, place = combiner_group([qinds[d] for d in fuse_dims])
+    _, blockperm, blockcomb = combineblocks(fused.sectors)
+    iperm = [0] * len(blockperm)
+    for pos, orig in enumerate(blockperm):
+        iperm[orig - 1] = pos + 1
+    nbl = [qinds[d].nblocks for d in fuse_dims]
+
+    def perm_comb(b):
+        bp = [b[p] for p in perm]
+        return (_colmajor_linear(bp[:nc], nbl),) + tuple(bp[nc:])
+
+    blocks = [perm_comb(b) for b in t.blocks]
+    blocks = [(iperm[x[0] - 1],) + x[1:] for x in blocks]
+    blocks = sorted(blocks, key=_isblockless_key)
+    blocks = [(blockcomb[x[0] - 1],) + x[1:] for x in blocks]
+    blocks = list(dict.fromkeys(blocks))           # unique!, first occurrences in order
+    inds = [tuple(d for _, d in csec)] + [t.inds[d] for d in rest]
+    offs, nnz = blockoffsets(blocks, inds)
+    r = BlockSparseTensor(inds, blocks, offs, np.zeros(nnz))
+    sorted_dims = [fused.sectors[o - 1][1] for o in blockperm]   # permuteblocks(ind_comb, blockperm)
+    for i, b in enumerate(t.blocks):
+        bpc = perm_comb(b)
+        bic = iperm[bpc[0] - 1]                    # b_in_combined_dim (sorted position, 1-based)
+        new = blockcomb[bic - 1]
+        offset, pos = 0, 1
+        while bic - pos > 0 and blockcomb[bic - pos - 1] == new:
+            offset += sorted_dims[bic - pos - 1]
+            pos += 1
+        j = blocks.index((new,) + bpc[1:])
+        blk = np.transpose(t.blockview(i), perm)
+        dc = sorted_dims[bic - 1]
+        sub = blk.reshape((dc,) + blk.shape[nc:], order="F")
+        r.blockview(j)[offset:offset + dc, ...] = sub
+    return r, (csec, place)
+
+
+def uncombine_front(t, combdim, group_dims, group_info):
+    """contract(T, labels, combiner, labels) in the uncombining case
+    (NDTensors/src/blocksparse/combiner.jl:90-140): the combined index (dimension
+    ``combdim``) is first moved to the front by a block-sparse permutedims (block order
+    kept), then split into the combiner's indices there (``uncombine``), so the result
+    is (uncombined indices..., the other indices of ``t`` in order)."""
+    perm1 = [combdim + 1] + [d + 1 for d in range(t.rank) if d != combdim]
+    tp = permutedims(t, perm1) if combdim != 0 else t
+    return uncombine(tp, 0, group_dims, group_info)
