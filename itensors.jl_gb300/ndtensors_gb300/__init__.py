@@ -10,8 +10,8 @@ from . import workloads
 from . import linalg
 from . import autodiff
 from .autodiff import contract_autograd, contract_rrule, dense_structure
-from .linalg import (CombinerTensor, MatricizePlan, Spectrum, SvdPlan, combine, contract_combiner, eigen,
-                     matricize, qr, svd, truncate, uncombine)
+from .linalg import (CombinerTensor, MatricizePlan, Spectrum, SvdPlan, combine, contract_combiner, eigen, eigs,
+                     entropy, matricize, qr, svd, truncate, truncerror, uncombine)
 from .contract import (ContractionPlan, contract, contract_, contract_blocksparse, contract_labels,
                        get_plan, permutedims, permutedims_, permutedims_blocksparse)
 from . import krylov
@@ -25,7 +25,7 @@ __all__ = [
     "ContractionPlan", "contract", "contract_", "contract_blocksparse", "contract_labels", "get_plan",
     "permutedims", "permutedims_", "permutedims_blocksparse",
     "linalg", "CombinerTensor", "MatricizePlan", "Spectrum", "SvdPlan", "combine", "contract_combiner", "eigen",
-    "matricize", "qr", "svd", "truncate", "uncombine",
+    "eigs", "entropy", "matricize", "qr", "svd", "truncate", "truncerror", "uncombine",
     "autodiff", "contract_autograd", "contract_rrule", "dense_structure",
     "krylov", "HeffOperator", "Lanczos", "SweepStep", "lanczos",
     "hdf5io", "H5Reader", "load_blocksparse", "read_blocksparse", "save_blocksparse", "write_blocksparse",

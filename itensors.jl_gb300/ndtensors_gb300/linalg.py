@@ -28,11 +28,35 @@ def _opt(x, none=-1):
 
 
 class Spectrum:
-    """Spectrum(eigs, truncerr) (NDTensors/src/lib/RankFactorization/src/spectrum.jl:6-9)."""
+    """Spectrum(eigs, truncerr) (NDTensors/src/lib/RankFactorization/src/spectrum.jl): the
+    kept density-matrix eigenvalues of a decomposition (or None) and its truncation error."""
 
     def __init__(self, eigs, truncerr):
-        self.eigs = np.asarray(eigs)
+        self.eigs = None if eigs is None else np.asarray(eigs)
         self.truncerr = float(truncerr)
+
+
+def eigs(spec: Spectrum):
+    """eigs(::Spectrum)."""
+    return spec.eigs
+
+
+def truncerror(spec: Spectrum):
+    """truncerror(::Spectrum)."""
+    return spec.truncerr
+
+
+def entropy(spec: Spectrum):
+    """entropy(::Spectrum): -sum p log p over the eigenvalues above 1e-13; an error when
+    the spectrum holds no eigenvalues (spectrum.jl:14-23)."""
+    if spec.eigs is None:
+        raise RuntimeError("Spectrum does not contain any eigenvalues, cannot compute the entropy")
+    S = 0.0
+    for p in spec.eigs:
+        p = float(p)
+        if p > 1.0e-13:
+            S -= p * np.log(p)
+    return S
 
 
 def _matrix_blocks(T: BlockSparseTensor):

@@ -71,6 +71,33 @@ def test_alpha_beta(nd, precision, alpha, beta):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("shape", [(4, 4, 4), (70, 90, 50)])
+def test_gemm_alpha_beta_transpose_matrix(nd, precision, shape):
+    """The reference's _gemm! matrix (NDTensors/test/test_dense.jl:216-235): alpha, beta in
+    {0, 1, 2} and either operand transposed (expressed here by the label order), against
+    numpy; 4 x 4 as in the reference and a larger rectangular case."""
+    m, k, n = shape
+    rng = np.random.default_rng(21)
+    for alpha in (0.0, 1.0, 2.0):
+        for beta in (0.0, 1.0, 2.0):
+            for ta in "NT":
+                for tb in "NT":
+                    a = rng.standard_normal((m, k) if ta == "N" else (k, m))
+                    b = rng.standard_normal((k, n) if tb == "N" else (n, k))
+                    r0 = rng.standard_normal((m, n))
+                    la = (1, -1) if ta == "N" else (-1, 1)
+                    lb = (-1, 2) if tb == "N" else (2, -1)
+                    out, _ = _run(nd, a, la, b, lb, (1, 2), precision, alpha, beta, r0)
+                    opa = a if ta == "N" else a.T
+                    opb = b if tb == "N" else b.T
+                    expect = alpha * (opa @ opb) + beta * r0
+                    if alpha == 0.0 and beta == 0.0:
+                        assert not np.any(out), (ta, tb)          # R overwritten with zeros
+                    else:
+                        assert odense.rel_frobenius_error(out, expect) <= TOL[precision], (alpha, beta, ta, tb)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
 @pytest.mark.parametrize("alpha,beta", [(1.0, 0.0), (-0.5, 2.0)])
 def test_long_k_small_output(nd, precision, alpha, beta):
     """Tiny M x N with K = 3e5 (the W-cotangent shape of the H_eff gradient): the FP64

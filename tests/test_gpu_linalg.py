@@ -383,3 +383,49 @@ def test_svd_panel_widths_and_scalar_fallback(nd, dims, panel):
         assert odense.rel_frobenius_error(Ub[n] @ np.diag(s) @ Vb[n].T, m) <= 1e-12
         np.testing.assert_allclose(Vb[n].T @ Vb[n], np.eye(len(s)), atol=1e-12)
         np.testing.assert_allclose(Ub[n].T @ Ub[n], np.eye(len(s)), atol=1e-12)
+
+
+def test_svd_spectrum_kat(nd):
+    """test/base/test_decomp.jl:433-446: the spectrum of A = U diag(S) V' with |S| = 1
+    holds S.^2 with no truncation error, and maxdim = length(S) - 3 discards exactly
+    the three smallest (truncerror = their sum of squares)."""
+    rng = np.random.default_rng(17)
+    u, s, vt = np.linalg.svd(rng.random((100, 100)))
+    s = s / np.linalg.norm(s)
+    a = u @ np.diag(s) @ vt
+    A = obs.random_blocksparse(rng, [(100,), (100,)], [(1, 1)])
+    A.data[:] = a.reshape(-1, order="F")
+    _, _, _, spec, _ = nd.svd(_gpu(nd, A))
+    np.testing.assert_allclose(nd.eigs(spec), s ** 2, rtol=1e-10, atol=1e-15)
+    assert nd.truncerror(spec) == 0.0
+    _, _, _, spec, kept = nd.svd(_gpu(nd, A), maxdim=len(s) - 3)
+    assert list(kept) == [len(s) - 3]
+    np.testing.assert_allclose(nd.truncerror(spec), np.sum(s[-3:] ** 2), rtol=1e-8)
+
+
+def test_qn_svd_truncation_invariants(nd):
+    """test/base/test_qnitensor.jl:1272-1318 (svd truncation example 1): A(i, j, i', j')
+    with i = j = [QN(0) => 2, QN(1) => 3], flux 0, raised to the 16th power as a matrix
+    (i, j) x (i', j') and normalised; svd with cutoff 1e-5 must keep fewer than dim(i)
+    dim(j) values, one per spectrum entry, with truncerr <= cutoff, and the
+    reconstruction's relative error 1 - |Ap|^2 / |A|^2 within rtol 1e-6 of truncerr."""
+    rng = np.random.default_rng(23)
+    i = qn.QNIndex(((0, 2), (1, 3)), 1, "i")
+    j = qn.QNIndex(((0, 2), (1, 3)), 1, "j")
+    inds = [i, j, i.dag().primed(), j.dag().primed()]
+    t = obs.random_blocksparse(rng, [x.dims for x in inds], qn.nzblocks(0, inds))
+    M, _, _ = obs.matricize(t, inds, (0, 1), (2, 3))
+    for _ in range(4):                                    # A = mapprime(A * A', 2, 1), four times
+        for n in range(len(M.blocks)):
+            v = M.blockview(n)
+            v[...] = v @ v
+    M.data /= np.linalg.norm(M.data)
+    cutoff = 1e-5
+    U, S, V, spec, kept = nd.svd(_gpu(nd, M), cutoff=cutoff)
+    assert sum(kept) == len(spec.eigs) < i.dim * j.dim
+    assert spec.truncerr <= cutoff
+    ub, vb = _blocks(nd, U), _blocks(nd, V)
+    ap2 = sum(float(np.sum((ub[n] @ np.diag(S[n].cpu().numpy()) @ vb[n].T) ** 2)) for n in range(len(ub)))
+    err = 1.0 - ap2 / float(np.sum(M.data ** 2))
+    assert err <= cutoff
+    np.testing.assert_allclose(err, spec.truncerr, rtol=1e-6)

@@ -1,4 +1,4 @@
-"""The C-ABI library builds, loads and exports every symbol the header declares (CPU only)."""
+"""The C-ABI library builds, loads and exports every symbol the header declares; host logic of the mirror (CPU only)."""
 import re
 import subprocess
 import sys
@@ -58,3 +58,16 @@ def test_host_mirror_labels_and_offsets():
     assert nd.contract_labels((1, -1, 2), (-1, 3)) == (1, 2, 3)
     offs, nnz = nd.blockoffsets([(1, 2), (2, 1)], [(2, 3), (4, 5)])
     assert offs == [0, 10] and nnz == 22
+
+
+def test_spectrum_kats():
+    """Spectrum identities of test/base/test_decomp.jl:448-455 (host logic)."""
+    import math
+    import ndtensors_gb300 as nd
+    assert nd.entropy(nd.Spectrum([0.5, 0.5], 0.0)) == math.log(2)
+    assert nd.entropy(nd.Spectrum([1.0], 0.0)) == 0.0
+    assert nd.entropy(nd.Spectrum([0.0], 0.0)) == 0.0
+    assert nd.eigs(nd.Spectrum(None, 1.0)) is None
+    with pytest.raises(RuntimeError):
+        nd.entropy(nd.Spectrum(None, 1.0))
+    assert nd.truncerror(nd.Spectrum(None, 1.0)) == 1.0
