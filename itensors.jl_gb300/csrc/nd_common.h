@@ -297,10 +297,11 @@ struct WorkItem {
   int32_t pair_begin;   // first pair (pairs sorted by group)
   int32_t pair_count;
   int32_t mt, nt;       // tile coordinates
-  // split-K (FP64 tile kernel only): the item covers [kbeg, kend) of the group's
-  // k axis (the pairs' K ranges concatenated in plan order) and writes its
-  // partial tile to workspace slot `slot`; slot < 0 means the whole k axis,
-  // written to R.
+  // split-K: the item covers [kbeg, kend) of the group's k axis and writes its
+  // partial tile to workspace slot `slot`; slot < 0 means the whole k axis, written
+  // to R.  FP64 tile kernel: the k axis is the pairs' K ranges concatenated in plan
+  // order, in elements; split GEMM (single-pair groups only): 32-wide k steps, ranges
+  // starting on 512-K chunk boundaries.
   int32_t kbeg = 0, kend = 0, slot = -1;
 };
 

@@ -46,7 +46,7 @@ struct ExecCache {
   PairDesc* d_pairs = nullptr;
   WorkItem* d_items = nullptr;     // FP64 tensor-core tiles of the regular groups
   int nitems = 0;
-  double* d_ws = nullptr;          // FP64 split-K partial tiles
+  double* d_ws = nullptr;          // split-K partial tiles: FP64 (DMMA path) or int64 fixed point (split GEMM)
   ReduceItem* d_red = nullptr;     // output tiles summed from the partials
   int nred = 0;
   WorkItem* d_sk_items = nullptr;  // skinny groups (FP64 CUDA-core kernel, every precision)
