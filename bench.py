@@ -917,7 +917,7 @@ def cfg_sweep_ops(args):
     events (median of repetitions, L2 flushed between them): the Krylov vector kernels on the
     psi-sized vectors (6.0 M doubles, a 11-vector basis), the block plan of each H_eff
     contraction, the diagonal contraction U * S and the uncombine of U after the truncated
-    SVD, and blockwise eigen on the 19 square blocks of psi's matricisation."""
+    SVD, blockwise qr and eigen on the 19 square blocks of psi's matricisation."""
     import ctypes as C
     import torch
     import ndtensors_gb300 as nd
@@ -995,6 +995,21 @@ def cfg_sweep_ops(args):
     nd.contract(U, (1, -1), D, (-1, 2))
     out["diag_contract_US"] = gbs(16 * U.nnz, lambda: nd.contract(U, (1, -1), D, (-1, 2)))
     out["uncombine_U"] = gbs(16 * U.nnz, lambda: nd.uncombine(U, 0, qinds[:2], rinfo))
+    # blockwise qr of the same 19 blocks (Householder, FP64): algorithmic flops 2 m n^2 - 2 n^3 / 3
+    # per m x n block (n <= m) for R, the same again to form the thin Q
+    from oracle import linalg as olin
+    host_m = M.data_numpy()
+    mblocks = []
+    for i, b in enumerate(M.blocks):
+        r_, c_ = M.inds[0][b[0] - 1], M.inds[1][b[1] - 1]
+        mblocks.append(host_m[M.offsets[i]:M.offsets[i] + r_ * c_].reshape((r_, c_), order="F"))
+    nd.qr(M)
+    q_ms = float(np.median(_events_ms(lambda: nd.qr(M), 3)))
+    qr_flops = sum(2 * (2 * max(x.shape) * min(x.shape) ** 2 - 2 * min(x.shape) ** 3 / 3) for x in mblocks)
+    t0 = time.perf_counter()
+    olin.qr_blocks(mblocks)
+    out["qr_19_blocks"] = {"ms": round(q_ms, 2), "GFLOP/s": round(qr_flops / (q_ms * 1e-3) / 1e9, 1),
+                           "cpu_oracle_ms": round((time.perf_counter() - t0) * 1e3, 1)}
     # blockwise eigen of the 19 symmetric blocks M_b M_b^T (square, up to 1036)
     rows = [M.inds[0][b[0] - 1] for b in M.blocks]
     blocks, offs, o, mats = [], [], 0, []
@@ -1010,7 +1025,6 @@ def cfg_sweep_ops(args):
                              torch.from_numpy(np.concatenate([q.reshape(-1, order="F") for q in mats])).to(dev))
     nd.eigen(H, maxdim=4096, cutoff=1e-10)
     e_ms = float(np.median(_events_ms(lambda: nd.eigen(H, maxdim=4096, cutoff=1e-10), 3)))
-    from oracle import linalg as olin
     t0 = time.perf_counter()
     olin.eigen_blocks(mats, maxdim=4096, cutoff=1e-10)
     out["eigen_19_blocks"] = {"ms": round(e_ms, 2), "cpu_oracle_ms": round((time.perf_counter() - t0) * 1e3, 1),

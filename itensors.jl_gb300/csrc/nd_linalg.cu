@@ -443,30 +443,60 @@ __global__ void block_copy(const BlockCopyDev* list, int n, const double* src, d
   }
 }
 
-// ---- Householder QR, one CTA per block -----------------------------------
+// ---- blocked Householder QR ----------------------------------------------
+// Panels of QR_NB columns: one CTA per block computes the panel's reflectors (LAPACK
+// dlarfg convention, as geqrf) and its compact WY factor T, Q_p = H_1 ... H_w =
+// I - V T V^T (dlarft, forward columnwise); the trailing columns are then updated as
+// C <- Q_p^T C = C - V (T^T (V^T C)) by CTAs that each own QR_SW columns of one block, so
+// the large blocks' O(n^3) updates spread over the SMs.  The thin Q is accumulated
+// backward from [I; 0]: X <- Q_p X = X - V (T (V^T X)), p from the last panel down,
+// with the same strip kernel.  Everything is FP64 on the CUDA cores (GB300's FP64 pipe
+// is narrow; the strip kernel keeps it busy from shared memory).
+constexpr int QR_NB = 32, QR_SW = 16, QR_RC = 64;   // panel width, strip width, rows per chunk
+constexpr int QR_THREADS = 256;
+static_assert(QR_NB * QR_SW == 2 * QR_THREADS, "two V^T X outputs per thread");
+
 struct QrBlock {
-  int64_t a_off, w_off, q_off, r_off;
+  int64_t a_off, w_off, q_off, r_off, t_off;   // t_off: one QR_NB x QR_NB factor per panel
   int32_t m, n, k;
-  int32_t pad;
+  int32_t tau_off;
 };
 
-__global__ void __launch_bounds__(256) qr_blocks(const QrBlock* blocks, const double* A, double* Wk, double* tau_all,
-                                                 int64_t* tau_off, double* Q, double* R, int positive) {
-  const QrBlock b = blocks[blockIdx.x];
+struct QrTask {
+  int32_t block, col0, ncols, pad;
+};
+
+// W <- A (working copy), Q <- [I_k; 0]
+__global__ void qr_init(const QrBlock* blocks, const double* A, double* Wk, double* Q) {
+  const QrBlock b = blocks[blockIdx.y];
+  const int64_t mn = (int64_t)b.m * b.n, mk = (int64_t)b.m * b.k;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < mn; e += (int64_t)gridDim.x * blockDim.x)
+    Wk[b.w_off + e] = A[b.a_off + e];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < mk; e += (int64_t)gridDim.x * blockDim.x)
+    Q[b.q_off + e] = (e % b.m) == (e / b.m) ? 1.0 : 0.0;
+}
+
+// Panel p of block ids[blockIdx.x]: reflectors of columns c0 .. c0 + w - 1 (applied
+// within the panel only), then T.
+__global__ void __launch_bounds__(QR_THREADS) qr_panel(const QrBlock* blocks, const int32_t* ids, int p, double* Wk,
+                                                       double* tau_all, double* Tall) {
+  const QrBlock b = blocks[ids[blockIdx.x]];
+  const int c0 = p * QR_NB, w = min(QR_NB, b.k - c0);
   __shared__ double red[8];
   __shared__ double sh[4];
-  double* W = Wk + b.w_off;                      // m x n working copy
-  double* tau = tau_all + tau_off[blockIdx.x];
-  for (int64_t e = threadIdx.x; e < (int64_t)b.m * b.n; e += blockDim.x) W[e] = A[b.a_off + e];
-  __syncthreads();
+  __shared__ double G[QR_NB][QR_NB + 1];
+  __shared__ double Ts[QR_NB][QR_NB + 1];
+  double* W = Wk + b.w_off;
+  double* tau = tau_all + b.tau_off;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int j = 0; j < b.k; ++j) {
+  for (int jj = 0; jj < w; ++jj) {
+    const int j = c0 + jj;
     double* x = W + (int64_t)j * b.m;
     double ss = 0.0;
     for (int i = j + 1 + threadIdx.x; i < b.m; i += blockDim.x) ss = fma(x[i], x[i], ss);
     ss = block_reduce_sum(ss, red);
     if (threadIdx.x == 0) {
-      // LAPACK dlarfg convention: beta = -sign(alpha) * |x|, v(0) = 1, tau = (beta - alpha) / beta
+      // dlarfg: beta = -sign(alpha) * |x|, v(0) = 1, tau = (beta - alpha) / beta
       const double alpha = x[j];
       double t = 0.0, beta = alpha, scal = 0.0;
       if (ss != 0.0) {
@@ -485,9 +515,9 @@ __global__ void __launch_bounds__(256) qr_blocks(const QrBlock* blocks, const do
     __syncthreads();
     if (threadIdx.x == 0) x[j] = beta;
     __syncthreads();
-    // apply H = I - tau v v^T to columns j+1..n-1, one warp per column
+    // H_j = I - tau v v^T on the panel's later columns, one warp per column
     if (t != 0.0) {
-      for (int c = j + 1 + warp; c < b.n; c += nw) {
+      for (int c = j + 1 + warp; c < c0 + w; c += nw) {
         double* y = W + (int64_t)c * b.m;
         double d = lane == 0 ? y[j] : 0.0;
         for (int i = j + 1 + lane; i < b.m; i += 32) d = fma(x[i], y[i], d);
@@ -499,41 +529,130 @@ __global__ void __launch_bounds__(256) qr_blocks(const QrBlock* blocks, const do
     }
     __syncthreads();
   }
-  // R (k x n): upper triangle of W
-  for (int64_t e = threadIdx.x; e < (int64_t)b.k * b.n; e += blockDim.x) {
-    const int i = (int)(e % b.k), c = (int)(e / b.k);
-    R[b.r_off + e] = (i <= c) ? W[(int64_t)c * b.m + i] : 0.0;
+  // G[a][c] = v_a . v_c (a < c); v_a = e_(c0+a) + W[c0+a+1 .., c0+a], zero above row c0+a
+  for (int pr = warp; pr < w * w; pr += nw) {
+    const int a = pr / w, c = pr % w;
+    if (a >= c) continue;
+    const double* va = W + (int64_t)(c0 + a) * b.m;
+    const double* vc = W + (int64_t)(c0 + c) * b.m;
+    double d = lane == 0 ? va[c0 + c] : 0.0;                 // row c0+c, where v_c is 1
+    for (int i = c0 + c + 1 + lane; i < b.m; i += 32) d = fma(va[i], vc[i], d);
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) G[a][c] = d;
   }
-  // Q (m x k) = H_0 ... H_{k-1} [I_k; 0], applied backward
-  double* Qb = Q + b.q_off;
-  for (int64_t e = threadIdx.x; e < (int64_t)b.m * b.k; e += blockDim.x) Qb[e] = ((e % b.m) == (e / b.m)) ? 1.0 : 0.0;
   __syncthreads();
-  for (int j = b.k - 1; j >= 0; --j) {
-    const double t = tau[j];
-    if (t == 0.0) continue;
-    const double* v = W + (int64_t)j * b.m;       // v(j) = 1 implicitly, v(j+1..) stored
-    for (int c = j + warp; c < b.k; c += nw) {
-      double* y = Qb + (int64_t)c * b.m;
-      double d = lane == 0 ? y[j] : 0.0;
-      for (int i = j + 1 + lane; i < b.m; i += 32) d = fma(v[i], y[i], d);
-      for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-      d *= t;
-      if (lane == 0) y[j] -= d;
-      for (int i = j + 1 + lane; i < b.m; i += 32) y[i] = fma(-d, v[i], y[i]);
+  // T(0:jj, jj) = -tau_jj T(0:jj, 0:jj) G(0:jj, jj), T(jj, jj) = tau_jj: lane a owns row a
+  if (warp == 0) {
+    for (int c = 0; c < QR_NB; ++c) Ts[lane][c] = 0.0;
+    __syncwarp();
+    for (int jj = 0; jj < w; ++jj) {
+      const double tj = tau[c0 + jj];
+      if (lane < jj) {
+        double acc = 0.0;
+        for (int c = lane; c < jj; ++c) acc = fma(Ts[lane][c], G[c][jj], acc);
+        Ts[lane][jj] = -tj * acc;
+      } else if (lane == jj) {
+        Ts[lane][jj] = tj;
+      }
+      __syncwarp();
+    }
+    double* T = Tall + b.t_off + (int64_t)p * QR_NB * QR_NB;   // column-major, ld QR_NB
+    for (int c = 0; c < QR_NB; ++c) T[lane + c * QR_NB] = Ts[lane][c];
+  }
+}
+
+// One strip of columns [col0, col0 + ncols) of the block's W (trailing update, op(T) =
+// T^T) or Q (accumulation, op(T) = T): X[c0:, strip] -= V op(T) (V^T X[c0:, strip]).
+__global__ void __launch_bounds__(QR_THREADS) qr_apply(const QrBlock* blocks, const QrTask* tasks, int p,
+                                                       const double* Wk, const double* Tall, double* Xk, int is_q) {
+  const QrTask tk = tasks[blockIdx.x];
+  const QrBlock b = blocks[tk.block];
+  const int c0 = p * QR_NB, w = min(QR_NB, b.k - c0);
+  const int L = b.m - c0;
+  const double* W = Wk + b.w_off;
+  double* X = Xk + (is_q ? b.q_off : b.w_off);
+  const double* T = Tall + b.t_off + (int64_t)p * QR_NB * QR_NB;
+  __shared__ double Vs[QR_RC][QR_NB + 1];
+  __shared__ double Xs[QR_RC][QR_SW + 1];
+  __shared__ double Ys[QR_NB][QR_SW + 1];
+  __shared__ double Ts[QR_NB][QR_NB + 1];
+  const int tid = threadIdx.x;
+  const int a0 = tid / QR_SW, cc = tid % QR_SW;          // outputs (a0, cc) and (a0 + 16, cc)
+  auto load_v = [&](int r0) {
+    for (int e = tid; e < QR_RC * QR_NB; e += QR_THREADS) {
+      const int i = e % QR_RC, a = e / QR_RC, ri = r0 + i;
+      double v = 0.0;
+      if (ri < L && a < w) v = ri < a ? 0.0 : (ri == a ? 1.0 : W[(int64_t)(c0 + a) * b.m + c0 + ri]);
+      Vs[i][a] = v;
+    }
+  };
+  double y0 = 0.0, y1 = 0.0;
+  for (int r0 = 0; r0 < L; r0 += QR_RC) {
+    __syncthreads();
+    load_v(r0);
+    for (int e = tid; e < QR_RC * QR_SW; e += QR_THREADS) {
+      const int i = e % QR_RC, c = e / QR_RC;
+      Xs[i][c] = (r0 + i < L && c < tk.ncols) ? X[(int64_t)(tk.col0 + c) * b.m + c0 + r0 + i] : 0.0;
     }
     __syncthreads();
-  }
-  if (positive) {
-    // flip signs so that diag(R) >= 0 (qr_positive, linearalgebra.jl:374-381)
-    for (int c = 0; c < b.k; ++c) {
-      const double d = R[b.r_off + (int64_t)c * b.k + c];
-      if (d < 0.0) {
-        for (int64_t i = threadIdx.x; i < b.m; i += blockDim.x) Qb[(int64_t)c * b.m + i] = -Qb[(int64_t)c * b.m + i];
-        for (int64_t cc = threadIdx.x; cc < b.n; cc += blockDim.x) R[b.r_off + cc * b.k + c] = -R[b.r_off + cc * b.k + c];
-      }
-      __syncthreads();
+#pragma unroll 16
+    for (int i = 0; i < QR_RC; ++i) {
+      const double xv = Xs[i][cc];
+      y0 = fma(Vs[i][a0], xv, y0);
+      y1 = fma(Vs[i][a0 + QR_THREADS / QR_SW], xv, y1);
     }
   }
+  for (int e = tid; e < QR_NB * QR_NB; e += QR_THREADS) {
+    const int r = e % QR_NB, c = e / QR_NB;
+    const double t = T[r + c * QR_NB];
+    if (is_q) Ts[r][c] = t;
+    else Ts[c][r] = t;
+  }
+  Ys[a0][cc] = y0;
+  Ys[a0 + QR_THREADS / QR_SW][cc] = y1;
+  __syncthreads();
+  double z0 = 0.0, z1 = 0.0;
+#pragma unroll 8
+  for (int q = 0; q < QR_NB; ++q) {
+    z0 = fma(Ts[a0][q], Ys[q][cc], z0);
+    z1 = fma(Ts[a0 + QR_THREADS / QR_SW][q], Ys[q][cc], z1);
+  }
+  __syncthreads();
+  Ys[a0][cc] = z0;
+  Ys[a0 + QR_THREADS / QR_SW][cc] = z1;
+  for (int r0 = 0; r0 < L; r0 += QR_RC) {
+    __syncthreads();
+    load_v(r0);
+    __syncthreads();
+    for (int e = tid; e < QR_RC * QR_SW; e += QR_THREADS) {
+      const int i = e % QR_RC, c = e / QR_RC;
+      if (r0 + i < L && c < tk.ncols) {
+        double acc = 0.0;
+#pragma unroll 8
+        for (int a = 0; a < QR_NB; ++a) acc = fma(Vs[i][a], Ys[a][c], acc);
+        X[(int64_t)(tk.col0 + c) * b.m + c0 + r0 + i] -= acc;
+      }
+    }
+  }
+}
+
+// R = upper triangle of W (k x n); positive: rows of R and columns of Q with a negative
+// diagonal entry change sign (qr_positive, NDTensors/src/linearalgebra/linearalgebra.jl:374-381)
+__global__ void qr_finish(const QrBlock* blocks, const double* Wk, double* Q, double* R, int positive) {
+  const QrBlock b = blocks[blockIdx.y];
+  const double* W = Wk + b.w_off;
+  const int64_t kn = (int64_t)b.k * b.n, mk = (int64_t)b.m * b.k;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < kn; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % b.k), c = (int)(e / b.k);
+    double v = i <= c ? W[(int64_t)c * b.m + i] : 0.0;
+    if (positive && W[(int64_t)i * b.m + i] < 0.0) v = -v;
+    R[b.r_off + e] = v;
+  }
+  if (positive)
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < mk; e += (int64_t)gridDim.x * blockDim.x) {
+      const int c = (int)(e / b.m);
+      if (W[(int64_t)c * b.m + c] < 0.0) Q[b.q_off + e] = -Q[b.q_off + e];
+    }
 }
 
 __global__ void set_identity(const SvdBlock* blocks, double* Y) {
@@ -2178,32 +2297,99 @@ extern "C" nd_status nd_bs_qr_f64(nd_handle h, int32_t nb, const int64_t* rows, 
   if (nb == 0) return ND_OK;
   cudaStream_t s = h->stream;
   std::vector<QrBlock> blocks(nb);
-  std::vector<int64_t> toff(nb);
   int64_t w = 0, q = 0, r = 0, t = 0;
+  int32_t tau = 0;
+  int npanels = 0, maxm = 0, maxk = 0;
   for (int i = 0; i < nb; ++i) {
     QrBlock& b = blocks[i];
-    if (rows[i] <= 0 || cols[i] <= 0) return nd_fail(h, ND_ERR_ARG, "qr: block %d has invalid dims", i);
+    if (rows[i] <= 0 || cols[i] <= 0 || rows[i] >= INT32_MAX || cols[i] >= INT32_MAX)
+      return nd_fail(h, ND_ERR_ARG, "qr: block %d has invalid dims", i);
     b.a_off = offsets[i]; b.m = (int)rows[i]; b.n = (int)cols[i]; b.k = std::min(b.m, b.n);
     b.w_off = w; w += (int64_t)b.m * b.n;
     b.q_off = q; q += (int64_t)b.m * b.k;
     b.r_off = r; r += (int64_t)b.k * b.n;
-    toff[i] = t; t += b.k;
+    const int pb = (b.k + QR_NB - 1) / QR_NB;
+    b.t_off = t; t += (int64_t)pb * QR_NB * QR_NB;
+    b.tau_off = tau; tau += b.k;
+    npanels = std::max(npanels, pb);
+    maxm = std::max(maxm, b.m);
+    maxk = std::max(maxk, b.k);
   }
-  QrBlock* dblk = nullptr;
-  double *Wk = nullptr, *tau = nullptr;
-  int64_t* dto = nullptr;
-  ND_CUDA(h, cudaMallocAsync(&dblk, nb * sizeof(QrBlock), s));
-  ND_CUDA(h, cudaMallocAsync(&Wk, std::max<int64_t>(w, 1) * 8, s));
-  ND_CUDA(h, cudaMallocAsync(&tau, std::max<int64_t>(t, 1) * 8, s));
-  ND_CUDA(h, cudaMallocAsync(&dto, nb * 8, s));
-  ND_CUDA(h, cudaMemcpyAsync(dblk, blocks.data(), nb * sizeof(QrBlock), cudaMemcpyHostToDevice, s));
-  ND_CUDA(h, cudaMemcpyAsync(dto, toff.data(), nb * 8, cudaMemcpyHostToDevice, s));
-  nd_prof_begin(h, "qr_blocks");
-  qr_blocks<<<nb, 256, 0, s>>>(dblk, A, Wk, tau, dto, Q, Rf, positive);
+  // per panel: the blocks that have it, their trailing strips and their Q strips
+  std::vector<int32_t> ids;
+  std::vector<QrTask> ttask, qtask;
+  std::vector<int64_t> id_off(npanels + 1), tt_off(npanels + 1), qt_off(npanels + 1);
+  for (int p = 0; p < npanels; ++p) {
+    id_off[p] = (int64_t)ids.size(); tt_off[p] = (int64_t)ttask.size(); qt_off[p] = (int64_t)qtask.size();
+    for (int i = 0; i < nb; ++i) {
+      const QrBlock& b = blocks[i];
+      const int c0 = p * QR_NB;
+      if (c0 >= b.k) continue;
+      const int wp = std::min(QR_NB, b.k - c0);
+      ids.push_back(i);
+      for (int c = c0 + wp; c < b.n; c += QR_SW) ttask.push_back(QrTask{i, c, std::min(QR_SW, b.n - c), 0});
+      for (int c = c0; c < b.k; c += QR_SW) qtask.push_back(QrTask{i, c, std::min(QR_SW, b.k - c), 0});
+    }
+  }
+  id_off[npanels] = (int64_t)ids.size(); tt_off[npanels] = (int64_t)ttask.size(); qt_off[npanels] = (int64_t)qtask.size();
+  if (ttask.size() > INT32_MAX / 2 || qtask.size() > INT32_MAX / 2) return nd_fail(h, ND_ERR_ARG, "qr: too many blocks");
+  const size_t bytes_blk = nb * sizeof(QrBlock), bytes_ids = std::max<size_t>(ids.size(), 1) * 4,
+               bytes_tt = std::max<size_t>(ttask.size(), 1) * sizeof(QrTask), bytes_qt = std::max<size_t>(qtask.size(), 1) * sizeof(QrTask);
+  unsigned char* meta = nullptr;
+  double *Wk = nullptr, *taus = nullptr, *Tm = nullptr;
+  ND_CUDA(h, cudaMallocAsync(&meta, bytes_blk + bytes_ids + bytes_tt + bytes_qt, s));
+  QrBlock* dblk = (QrBlock*)meta;
+  int32_t* dids = (int32_t*)(meta + bytes_blk);
+  QrTask* dtt = (QrTask*)(meta + bytes_blk + bytes_ids);
+  QrTask* dqt = (QrTask*)(meta + bytes_blk + bytes_ids + bytes_tt);
+  nd_status st = ND_OK;
+  auto fail_free = [&](nd_status e) {
+    cudaFreeAsync(meta, s);
+    if (Wk) cudaFreeAsync(Wk, s);
+    if (taus) cudaFreeAsync(taus, s);
+    if (Tm) cudaFreeAsync(Tm, s);
+    return e;
+  };
+  cudaError_t ce = cudaMallocAsync(&Wk, std::max<int64_t>(w, 1) * 8, s);
+  if (ce == cudaSuccess) ce = cudaMallocAsync(&taus, std::max<int64_t>(tau, 1) * 8, s);
+  if (ce == cudaSuccess) ce = cudaMallocAsync(&Tm, std::max<int64_t>(t, 1) * 8, s);
+  if (ce != cudaSuccess) return fail_free(nd_cuda_check(h, ce, "qr scratch"));
+  if ((st = nd_upload(h, dblk, blocks.data(), bytes_blk)) || (st = nd_upload(h, dids, ids.data(), ids.size() * 4)) ||
+      (st = nd_upload(h, dtt, ttask.data(), ttask.size() * sizeof(QrTask))) ||
+      (st = nd_upload(h, dqt, qtask.data(), qtask.size() * sizeof(QrTask))))
+    return fail_free(st);
+  const int gx = (int)std::min<int64_t>(((int64_t)maxm * std::max(maxk, 1) + 255) / 256, 64);
+  nd_prof_begin(h, "qr_init");
+  qr_init<<<dim3(std::max(gx, 1), nb), 256, 0, s>>>(dblk, A, Wk, Q);
   nd_prof_end(h);
   ND_LAUNCHED(h);
-  cudaFreeAsync(dblk, s); cudaFreeAsync(Wk, s); cudaFreeAsync(tau, s); cudaFreeAsync(dto, s);
-  return nd_cuda_check(h, cudaGetLastError(), "qr_blocks");
+  for (int p = 0; p < npanels; ++p) {
+    const int np_ = (int)(id_off[p + 1] - id_off[p]), nt = (int)(tt_off[p + 1] - tt_off[p]);
+    nd_prof_begin(h, "qr_panel");
+    qr_panel<<<np_, QR_THREADS, 0, s>>>(dblk, dids + id_off[p], p, Wk, taus, Tm);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+    if (nt) {
+      nd_prof_begin(h, "qr_apply");
+      qr_apply<<<nt, QR_THREADS, 0, s>>>(dblk, dtt + tt_off[p], p, Wk, Tm, Wk, 0);
+      nd_prof_end(h);
+      ND_LAUNCHED(h);
+    }
+  }
+  for (int p = npanels - 1; p >= 0; --p) {
+    const int nq = (int)(qt_off[p + 1] - qt_off[p]);
+    if (!nq) continue;
+    nd_prof_begin(h, "qr_apply");
+    qr_apply<<<nq, QR_THREADS, 0, s>>>(dblk, dqt + qt_off[p], p, Wk, Tm, Q, 1);
+    nd_prof_end(h);
+    ND_LAUNCHED(h);
+  }
+  nd_prof_begin(h, "qr_finish");
+  qr_finish<<<dim3(std::max(gx, 1), nb), 256, 0, s>>>(dblk, Wk, Q, Rf, positive);
+  nd_prof_end(h);
+  ND_LAUNCHED(h);
+  st = nd_cuda_check(h, cudaGetLastError(), "qr");
+  return fail_free(st);
 }
 
 // host list -> device form (mixed-radix index per copy); maxc: the largest count

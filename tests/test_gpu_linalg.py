@@ -182,6 +182,32 @@ def test_qr_blocks(nd, shape, positive):
         np.testing.assert_allclose(r, orr[n], rtol=1e-10, atol=1e-10)
 
 
+@pytest.mark.parametrize("positive", [False, True])
+def test_qr_blocked_panels(nd, positive):
+    """Blocks spanning several 32-column panels and partial 16-column strips (tall, wide,
+    square, a 1036 x 1036 block as in the chi = 4096 matricisation): Q R = A, Q
+    orthonormal, R upper triangular, LAPACK's geqrf signs."""
+    rng = np.random.default_rng(91)
+    shapes = [(300, 200), (130, 300), (257, 257), (64, 33), (1036, 1036), (5, 1)]
+    mats = [rng.standard_normal(sh) for sh in shapes]
+    inds = [[sh[0] for sh in shapes], [sh[1] for sh in shapes]]
+    blocks = [(i + 1, i + 1) for i in range(len(shapes))]
+    offs, nnz = obs.blockoffsets(blocks, inds)
+    A = obs.BlockSparseTensor(inds, blocks, offs, np.concatenate([m.reshape(-1, order="F") for m in mats]))
+    Q, R = nd.qr(_gpu(nd, A), positive=positive)
+    oq, orr = olin.qr_blocks(mats, positive=positive)
+    qb, rb = _blocks(nd, Q), _blocks(nd, R)
+    for n, m in enumerate(mats):
+        q, r = qb[n], rb[n]
+        np.testing.assert_allclose(q @ r, m, rtol=1e-12, atol=1e-12 * max(1.0, np.abs(m).max()) * max(m.shape))
+        np.testing.assert_allclose(q.T @ q, np.eye(q.shape[1]), atol=1e-12 * max(m.shape))
+        assert np.allclose(np.tril(r, -1), 0)
+        if positive:
+            assert (np.diag(r) >= 0).all()
+        np.testing.assert_allclose(q, oq[n], rtol=1e-9, atol=1e-9)
+        np.testing.assert_allclose(r, orr[n], rtol=1e-9, atol=1e-9 * max(1.0, np.abs(orr[n]).max()))
+
+
 def test_matricize_matches_oracle(nd):
     net = networks.qn_heff(chi=256, seed=11)
     psi = net["psi"]
