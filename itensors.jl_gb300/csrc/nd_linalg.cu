@@ -452,9 +452,11 @@ __global__ void block_copy(const BlockCopyDev* list, int n, const double* src, d
 // backward from [I; 0]: X <- Q_p X = X - V (T (V^T X)), p from the last panel down,
 // with the same strip kernel.  Everything is FP64 on the CUDA cores (GB300's FP64 pipe
 // is narrow; the strip kernel keeps it busy from shared memory).
-constexpr int QR_NB = 32, QR_SW = 16, QR_RC = 64;   // panel width, strip width, rows per chunk
-constexpr int QR_THREADS = 256;
-static_assert(QR_NB * QR_SW == 2 * QR_THREADS, "two V^T X outputs per thread");
+constexpr int QR_NB = 16, QR_SW = 8, QR_RC = 64;    // panel width, strip width, rows per chunk
+constexpr int QR_THREADS = 256;                        // panel kernel
+constexpr int QR_ATHREADS = 128;                       // strip kernel
+constexpr int QR_OPT = QR_NB * QR_SW / QR_ATHREADS;   // V^T X outputs per thread
+static_assert(QR_OPT >= 1 && QR_OPT * QR_ATHREADS == QR_NB * QR_SW, "whole V^T X outputs per thread");
 
 struct QrBlock {
   int64_t a_off, w_off, q_off, r_off, t_off;   // t_off: one QR_NB x QR_NB factor per panel
@@ -543,7 +545,9 @@ __global__ void __launch_bounds__(QR_THREADS) qr_panel(const QrBlock* blocks, co
   __syncthreads();
   // T(0:jj, jj) = -tau_jj T(0:jj, 0:jj) G(0:jj, jj), T(jj, jj) = tau_jj: lane a owns row a
   if (warp == 0) {
-    for (int c = 0; c < QR_NB; ++c) Ts[lane][c] = 0.0;
+    const bool row = lane < QR_NB;
+    if (row)
+      for (int c = 0; c < QR_NB; ++c) Ts[lane][c] = 0.0;
     __syncwarp();
     for (int jj = 0; jj < w; ++jj) {
       const double tj = tau[c0 + jj];
@@ -557,13 +561,14 @@ __global__ void __launch_bounds__(QR_THREADS) qr_panel(const QrBlock* blocks, co
       __syncwarp();
     }
     double* T = Tall + b.t_off + (int64_t)p * QR_NB * QR_NB;   // column-major, ld QR_NB
-    for (int c = 0; c < QR_NB; ++c) T[lane + c * QR_NB] = Ts[lane][c];
+    if (row)
+      for (int c = 0; c < QR_NB; ++c) T[lane + c * QR_NB] = Ts[lane][c];
   }
 }
 
 // One strip of columns [col0, col0 + ncols) of the block's W (trailing update, op(T) =
 // T^T) or Q (accumulation, op(T) = T): X[c0:, strip] -= V op(T) (V^T X[c0:, strip]).
-__global__ void __launch_bounds__(QR_THREADS) qr_apply(const QrBlock* blocks, const QrTask* tasks, int p,
+__global__ void __launch_bounds__(QR_ATHREADS) qr_apply(const QrBlock* blocks, const QrTask* tasks, int p,
                                                        const double* Wk, const double* Tall, double* Xk, int is_q) {
   const QrTask tk = tasks[blockIdx.x];
   const QrBlock b = blocks[tk.block];
@@ -577,20 +582,23 @@ __global__ void __launch_bounds__(QR_THREADS) qr_apply(const QrBlock* blocks, co
   __shared__ double Ys[QR_NB][QR_SW + 1];
   __shared__ double Ts[QR_NB][QR_NB + 1];
   const int tid = threadIdx.x;
-  const int a0 = tid / QR_SW, cc = tid % QR_SW;          // outputs (a0, cc) and (a0 + 16, cc)
+  const int a0 = tid / QR_SW, cc = tid % QR_SW;          // outputs (a0 + o * QR_ATHREADS / QR_SW, cc)
+  constexpr int AS = QR_ATHREADS / QR_SW;
   auto load_v = [&](int r0) {
-    for (int e = tid; e < QR_RC * QR_NB; e += QR_THREADS) {
+    for (int e = tid; e < QR_RC * QR_NB; e += QR_ATHREADS) {
       const int i = e % QR_RC, a = e / QR_RC, ri = r0 + i;
       double v = 0.0;
       if (ri < L && a < w) v = ri < a ? 0.0 : (ri == a ? 1.0 : W[(int64_t)(c0 + a) * b.m + c0 + ri]);
       Vs[i][a] = v;
     }
   };
-  double y0 = 0.0, y1 = 0.0;
+  double y[QR_OPT];
+#pragma unroll
+  for (int o = 0; o < QR_OPT; ++o) y[o] = 0.0;
   for (int r0 = 0; r0 < L; r0 += QR_RC) {
     __syncthreads();
     load_v(r0);
-    for (int e = tid; e < QR_RC * QR_SW; e += QR_THREADS) {
+    for (int e = tid; e < QR_RC * QR_SW; e += QR_ATHREADS) {
       const int i = e % QR_RC, c = e / QR_RC;
       Xs[i][c] = (r0 + i < L && c < tk.ncols) ? X[(int64_t)(tk.col0 + c) * b.m + c0 + r0 + i] : 0.0;
     }
@@ -598,33 +606,34 @@ __global__ void __launch_bounds__(QR_THREADS) qr_apply(const QrBlock* blocks, co
 #pragma unroll 16
     for (int i = 0; i < QR_RC; ++i) {
       const double xv = Xs[i][cc];
-      y0 = fma(Vs[i][a0], xv, y0);
-      y1 = fma(Vs[i][a0 + QR_THREADS / QR_SW], xv, y1);
+#pragma unroll
+      for (int o = 0; o < QR_OPT; ++o) y[o] = fma(Vs[i][a0 + o * AS], xv, y[o]);
     }
   }
-  for (int e = tid; e < QR_NB * QR_NB; e += QR_THREADS) {
+  for (int e = tid; e < QR_NB * QR_NB; e += QR_ATHREADS) {
     const int r = e % QR_NB, c = e / QR_NB;
     const double t = T[r + c * QR_NB];
     if (is_q) Ts[r][c] = t;
     else Ts[c][r] = t;
   }
-  Ys[a0][cc] = y0;
-  Ys[a0 + QR_THREADS / QR_SW][cc] = y1;
+#pragma unroll
+  for (int o = 0; o < QR_OPT; ++o) Ys[a0 + o * AS][cc] = y[o];
   __syncthreads();
-  double z0 = 0.0, z1 = 0.0;
+  double z[QR_OPT];
+#pragma unroll
+  for (int o = 0; o < QR_OPT; ++o) z[o] = 0.0;
 #pragma unroll 8
-  for (int q = 0; q < QR_NB; ++q) {
-    z0 = fma(Ts[a0][q], Ys[q][cc], z0);
-    z1 = fma(Ts[a0 + QR_THREADS / QR_SW][q], Ys[q][cc], z1);
-  }
+  for (int q = 0; q < QR_NB; ++q)
+#pragma unroll
+    for (int o = 0; o < QR_OPT; ++o) z[o] = fma(Ts[a0 + o * AS][q], Ys[q][cc], z[o]);
   __syncthreads();
-  Ys[a0][cc] = z0;
-  Ys[a0 + QR_THREADS / QR_SW][cc] = z1;
+#pragma unroll
+  for (int o = 0; o < QR_OPT; ++o) Ys[a0 + o * AS][cc] = z[o];
   for (int r0 = 0; r0 < L; r0 += QR_RC) {
     __syncthreads();
     load_v(r0);
     __syncthreads();
-    for (int e = tid; e < QR_RC * QR_SW; e += QR_THREADS) {
+    for (int e = tid; e < QR_RC * QR_SW; e += QR_ATHREADS) {
       const int i = e % QR_RC, c = e / QR_RC;
       if (r0 + i < L && c < tk.ncols) {
         double acc = 0.0;
@@ -2371,7 +2380,7 @@ extern "C" nd_status nd_bs_qr_f64(nd_handle h, int32_t nb, const int64_t* rows, 
     ND_LAUNCHED(h);
     if (nt) {
       nd_prof_begin(h, "qr_apply");
-      qr_apply<<<nt, QR_THREADS, 0, s>>>(dblk, dtt + tt_off[p], p, Wk, Tm, Wk, 0);
+      qr_apply<<<nt, QR_ATHREADS, 0, s>>>(dblk, dtt + tt_off[p], p, Wk, Tm, Wk, 0);
       nd_prof_end(h);
       ND_LAUNCHED(h);
     }
@@ -2380,7 +2389,7 @@ extern "C" nd_status nd_bs_qr_f64(nd_handle h, int32_t nb, const int64_t* rows, 
     const int nq = (int)(qt_off[p + 1] - qt_off[p]);
     if (!nq) continue;
     nd_prof_begin(h, "qr_apply");
-    qr_apply<<<nq, QR_THREADS, 0, s>>>(dblk, dqt + qt_off[p], p, Wk, Tm, Q, 1);
+    qr_apply<<<nq, QR_ATHREADS, 0, s>>>(dblk, dqt + qt_off[p], p, Wk, Tm, Q, 1);
     nd_prof_end(h);
     ND_LAUNCHED(h);
   }
