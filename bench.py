@@ -744,6 +744,89 @@ def cfg_qn_pair(args):
           k, 3)
 
 
+# Published numbers of the reference's block-sparse benchmark (docs/src/Multithreading.md:129-149,
+# a laptop with 6 CPU threads, BLAS and Strided at one thread): serial and 5 Julia threads.
+MULTITHREADING_DOC_MS = {"serial": 21.558, "threaded_5": 5.934}
+
+
+def cfg_multithreading_doc(args):
+    """The reference's published block-sparse benchmark (docs/src/Multithreading.md:95-149):
+    C = A' * B for order-4 QN tensors A, B with indices (i1', i2', dag(i1), dag(i2)), every
+    index [QN(0) => 20, QN(1) => 20], flux 0: six 20^4 blocks per tensor, ten 400 x 400 x 400
+    block pairs, 1.28 GFLOP.  Device time per contraction (CUDA events, L2 flushed between
+    repetitions), the same through contract() with host buffers (copies in the timed
+    region), and the CPU oracle on this machine."""
+    import torch
+    import ndtensors_gb300 as nd
+    from oracle import blocksparse as obs
+    from oracle import qn
+    d = 20
+    rng = np.random.default_rng(0)
+    i1 = qn.QNIndex(((0, d), (1, d)), 1, "i1")
+    i2 = qn.QNIndex(((0, d), (1, d)), 1, "i2")
+    inds = [i1.primed(), i2.primed(), i1.dag(), i2.dag()]
+    A = obs.random_blocksparse(rng, [x.dims for x in inds], qn.nzblocks(0, inds))
+    B = obs.random_blocksparse(rng, [x.dims for x in inds], qn.nzblocks(0, inds))
+    la, lb, lc = (1, 2, -1, -2), (-1, -2, 3, 4), (1, 2, 3, 4)     # A' * B: A's primed-dagger pair meets B's
+    cpu = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        ref, plan_ref = obs.contract(A, la, B, lb, lc)
+        cpu.append((time.perf_counter() - t0) * 1e3)
+    dA, dB = nd.BlockSparseTensor.from_oracle(A), nd.BlockSparseTensor.from_oracle(B)
+    plan = nd.ContractionPlan(dA, la, dB, lb, lc)
+    exact = (list(plan.blocksR) == [tuple(b) for b in ref.blocks] and list(plan.offsetsR) == list(ref.offsets)
+             and [tuple(p) for p in plan.pairs] == [tuple(p) for p in plan_ref])
+    flops = plan.flops(dA, dB)
+    flush = _flush_buffer()
+    k = max(10, args.steps)
+    res = {}
+    for prec in ("fp64", "ozaki"):
+        out = nd.contract_blocksparse(dA, la, dB, lb, lc, precision=prec, plan=plan)
+        for _ in range(3):
+            nd.contract_blocksparse(dA, la, dB, lb, lc, precision=prec, plan=plan, out=out)
+        err = _rel(out.data_numpy(), ref.data)
+        ts = _events_ms(lambda: nd.contract_blocksparse(dA, la, dB, lb, lc, precision=prec, plan=plan, out=out),
+                        k, flush)
+        ms = float(np.median(ts))
+        res[prec] = {"ms": round(ms, 4), "GFLOP/s": round(flops / (ms * 1e-3) / 1e9, 1), "rel_err_vs_oracle": err}
+    # end to end: pinned host inputs in, the public contract() (plan cache), result out
+    dev = torch.device("cuda")
+    pa = torch.from_numpy(np.ascontiguousarray(A.data)).pin_memory()
+    pb = torch.from_numpy(np.ascontiguousarray(B.data)).pin_memory()
+    out_host = torch.empty(ref.nnz, dtype=torch.float64).pin_memory()
+    e2e = {}
+    for prec in ("fp64", "ozaki"):
+        def step():
+            xa = nd.BlockSparseTensor(list(dA.inds), list(dA.blocks), list(dA.offsets), pa.to(dev, non_blocking=True))
+            xb = nd.BlockSparseTensor(list(dB.inds), list(dB.blocks), list(dB.offsets), pb.to(dev, non_blocking=True))
+            r = nd.contract(xa, la, xb, lb, lc, precision=prec)
+            out_host.copy_(r.data, non_blocking=True)
+            torch.cuda.synchronize()
+        step()
+        wall = []
+        for _ in range(k):
+            t0 = time.perf_counter()
+            step()
+            wall.append((time.perf_counter() - t0) * 1e3)
+        e2e[prec] = {"ms": round(float(np.median(wall)), 4),
+                     "rel_err_vs_oracle": _rel(out_host.numpy(), ref.data)}
+    msoz = res["ozaki"]["ms"]
+    _line("QN block-sparse contraction A'*B time, Ozaki (the reference's Multithreading.md benchmark, d = 20, "
+          "order 4)", msoz, "ms", False, "multithreading_doc_d20_order4",
+          {"precision": "ozaki-5slices", "vs_baseline": round(msoz / MULTITHREADING_DOC_MS["serial"], 5),
+           "vs_baseline_note": "value / the published serial time (21.558 ms, a laptop CPU, BLAS at 1 thread); "
+                               "lower is better; the FP64 drop-in's ratio is precisions.fp64.ms / 21.558",
+           "published_ms": MULTITHREADING_DOC_MS, "precisions": res,
+           "e2e": {"fp64": e2e["fp64"], "ozaki": e2e["ozaki"], "h2d_bytes_per_step": 8 * (A.nnz + B.nnz),
+                   "d2h_bytes_per_step": 8 * ref.nnz},
+           "block_pairs": plan.npairs, "output_blocks": len(plan.blocksR), "flops": flops,
+           "structure_bit_exact": exact, "l2": "flushed between repetitions (device timing)",
+           "cpu_baseline": {"value": round(float(np.median(cpu)), 2), "unit": "ms", "cores": cpu_threads(),
+                            "kind": "port", "sample": "1 contraction (oracle plan + per-pair OpenBLAS dgemm), median of 3"}},
+          k, 3)
+
+
 def cfg_gradient(args):
     """Gradient of E = <psi|H_eff|psi>/<psi|psi> wrt psi and W1, dense chi = 512: time and FD error."""
     import torch
@@ -1040,7 +1123,8 @@ def cfg_sweep_ops(args):
 
 
 CONFIGS = {"dense_pair": cfg_dense_pair, "permute_sweep": cfg_permute_sweep, "dense_heff": cfg_dense_heff,
-           "qn_pair": cfg_qn_pair, "gradient": cfg_gradient, "sweep_step": cfg_sweep_step, "sweep_ops": cfg_sweep_ops}
+           "qn_pair": cfg_qn_pair, "multithreading_doc": cfg_multithreading_doc, "gradient": cfg_gradient,
+           "sweep_step": cfg_sweep_step, "sweep_ops": cfg_sweep_ops}
 
 
 def run_configs(args):
