@@ -111,7 +111,8 @@ nd_status nd_set_permute_path(nd_handle h, int32_t path);
  * stream and is refused (ND_ERR_ARG) during graph capture.  Switching the mode resets
  * the record.  No counterpart in the reference (its BLAS path has one precision). */
 nd_status nd_set_verify(nd_handle h, int32_t on);
-/* The relative error recorded by the last verified contraction, -1 when none. */
+/* The relative error recorded by the last verified contraction; -1 before any, and when
+ * the last verified call failed before its comparison. */
 nd_status nd_verify_last(nd_handle h, double* rel_err);
 /* Where nd_bs_plan_create builds plans: 0 (default) = on the host up to 4096 pairs,
  * else on the device; 1 = always on the device; 2 = on the host whenever the

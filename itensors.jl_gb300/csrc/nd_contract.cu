@@ -491,6 +491,7 @@ extern "C" nd_status nd_contract_dense_f64(nd_handle h, double* R, int32_t rankR
                                            int32_t rankB, const int64_t* dimsB, const int32_t* labelsB,
                                            double alpha, double beta, int32_t precision) {
   if (!h) return ND_ERR_ARG;
+  if (h->verify) h->verify_err = 0.0;              // exact branches (scalar, empty K) record 0
   if (rankA < 0 || rankB < 0 || rankR < 0 || rankA > ND_MAX_RANK || rankB > ND_MAX_RANK || rankR > ND_MAX_RANK)
     return nd_fail(h, ND_ERR_ARG, "contract: rank out of range (max %d)", ND_MAX_RANK);
   int64_t nA = 1, nB = 1, nR = 1;
@@ -551,6 +552,7 @@ extern "C" nd_status nd_contract_dense_f64(nd_handle h, double* R, int32_t rankR
   if (!c) return nd_fail(h, ND_ERR_OOM, "contract: host allocation failed");
   const bool verify = h->verify && precision != ND_PREC_FP64;
   if (h->verify && nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "contract: verify mode cannot be graph-captured");
+  if (h->verify) h->verify_err = -1.0;             // until this call's figure is known
   double* saved = nullptr;   // verify with beta != 0: R before the call, the FP64 run's input
   if (verify && beta != 0.0) {
     ND_CUDA(h, cudaMallocAsync(&saved, nR * 8, h->stream));
@@ -715,6 +717,7 @@ extern "C" nd_status nd_bs_contract_f64(nd_handle h, nd_plan p, double* R, const
   nd_status s = build_forward_descs(p);
   if (s) return s;
   if (h->verify && nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "bs_contract: verify mode cannot be graph-captured");
+  if (h->verify) h->verify_err = -1.0;
   JobPtrs ptrs{{A, nullptr}, {B, nullptr}, {R, nullptr}};
   s = nd_execute_cached(h, p->cache[precision], p->descs, p->ngroups, ptrs, alpha, 0.0, precision);
   if (s || !h->verify) return s;
@@ -809,6 +812,7 @@ extern "C" nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan p, const do
   if (!Abar || !Bbar) return nd_fail(h, ND_ERR_ARG, "adjoint: NULL output");
   if (precision < 0 || precision > 2) return nd_fail(h, ND_ERR_ARG, "adjoint: unknown precision %d", precision);
   if (h->verify && nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "adjoint: verify mode cannot be graph-captured");
+  if (h->verify) h->verify_err = -1.0;
   nd_status s = build_adjoint_descs(p);
   if (s) return s;
   // blocks of A / B that no pair touches have a zero cotangent
