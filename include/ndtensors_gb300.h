@@ -300,7 +300,10 @@ nd_status nd_bs_eigen_f64(nd_handle h, int32_t nblocks, const int64_t *dims, con
 
 /* Blockwise QR (NDTensors/src/blocksparse/linearalgebra.jl:351-415, dense qr /
  * qr_positive NDTensors/src/linearalgebra/linearalgebra.jl:321-381).  Q blocks
- * m_b x k_b, R blocks k_b x n_b, k_b = min(m_b, n_b), concatenated in order. */
+ * m_b x k_b, R blocks k_b x n_b, k_b = min(m_b, n_b), concatenated in order.
+ * Householder reflectors with LAPACK geqrf's signs (positive != 0: diag(R) >= 0), in
+ * 16-column panels whose trailing updates and Q accumulation run on many CTAs per
+ * block; FP64 throughout.  Stream-ordered: returns once the work is enqueued. */
 nd_status nd_bs_qr_f64(nd_handle h, int32_t nblocks, const int64_t *rows, const int64_t *cols,
                        const int64_t *offsets, const double *A, double *Q, double *Rf,
                        int32_t positive);
