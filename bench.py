@@ -45,7 +45,9 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks/throttle reasons sampled every 100 ms around the timed region
+    (`load_until` keeps the GPU busy with untimed steps until a sample has landed, so the
+    samples before and after the timed steps are taken under the same load)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -53,24 +55,43 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
+        self.lines = []
+        self.reader = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            import threading
+            self.reader = threading.Thread(target=lambda: [self.lines.append(l) for l in self.proc.stdout],
+                                           daemon=True)
+            self.reader.start()
         except Exception:
             self.proc = None
         return self
 
+    def count(self):
+        return len(self.lines)
+
+    def load_until(self, fn, n, timeout_s=3.0):
+        """Run fn (an untimed step, synchronised) until n samples exist or the timeout."""
+        import torch
+        t0 = time.perf_counter()
+        while self.proc and self.count() < n and time.perf_counter() - t0 < timeout_s:
+            fn()
+            torch.cuda.synchronize()
+
     def __exit__(self, *a):
-        self.out = ""
         if self.proc:
             self.proc.terminate()
             try:
-                self.out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            if self.reader:
+                self.reader.join(timeout=5)
+        self.out = "\n".join(self.lines)
 
     def summary(self):
         rows = []
@@ -373,10 +394,15 @@ def run_ours(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    launches0 = h.launches()
     with ClockSampler(local) as cs:
+        cs.load_until(lambda: step(args.precision), 1)          # untimed load until a sample lands
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        launches0 = h.launches()
         ts = timed(args.precision, args.steps)
-    launches = h.launches() - launches0
+        launches = h.launches() - launches0
+        cs.load_until(lambda: step(args.precision), cs.count() + 1)   # and one more after
     torch.cuda.synchronize()
     ms = max_over_ranks(float(np.sum(ts)) / args.steps, dist, dev)
     value = whole_job_rate(flops, ms, ws)
