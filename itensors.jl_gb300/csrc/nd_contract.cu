@@ -145,8 +145,8 @@ static void make_items(const std::vector<PairDesc>& pairs, int bm, int bn, Pick 
 // Split-K for the FP64 tile kernel.  The launch's work is measured in k-steps
 // of 16 summed over its tiles (each tile's k axis is its group's pairs' K
 // concatenated in plan order); `ctas` resident CTAs share it.  Any tile longer
-// than twice the fair share per CTA (and at least 4 k-steps) is cut into chunks
-// of about that share, so one long-K tile cannot serialise the launch; the
+// than the chunk share below is cut into chunks of about that share, so one
+// long-K tile cannot serialise the launch and a small launch still fills the SMs; the
 // partial tiles go to a workspace and splitk_reduce sums them in chunk order
 // (deterministic) before applying alpha / beta.
 static nd_status plan_split_k(nd_handle h, const std::vector<PairDesc>& pairs, std::vector<WorkItem>& items,
@@ -160,7 +160,12 @@ static nd_status plan_split_k(nd_handle h, const std::vector<PairDesc>& pairs, s
     ksum[i] = k;
     total += (k + 15) / 16;
   }
-  const int64_t share = std::max<int64_t>(4, 2 * ((total + ctas - 1) / ctas));   // k-steps per chunk
+  // k-steps per chunk.  A launch of fewer tiles than half the SMs (a small contraction such
+  // as a 256 x 256 x 128 pair: 16 tiles) is cut until about one chunk per SM, down to
+  // single k-steps; otherwise chunks hold at least 4 k-steps to bound the reduction.
+  const bool few = items.size() * 2 < (size_t)h->num_sms;
+  const int64_t share = few ? std::max<int64_t>(1, (total + h->num_sms - 1) / h->num_sms)
+                            : std::max<int64_t>(4, 2 * ((total + ctas - 1) / ctas));
   std::vector<WorkItem> out;
   std::vector<ReduceItem> red;
   int slot = 0;

@@ -196,7 +196,10 @@ __global__ void __launch_bounds__(256) splitk_reduce(const PairDesc* pairs, cons
   }
   __syncthreads();
   double* R = job_R(ptrs, pd.job) + pd.r_off;
-  for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
+  // gridDim.y CTAs share a tile (a few tiles still fill the SMs)
+  const int per = (BM * BN + (int)gridDim.y - 1) / (int)gridDim.y;
+  const int e1 = min(BM * BN, ((int)blockIdx.y + 1) * per);
+  for (int e = (int)blockIdx.y * per + threadIdx.x; e < e1; e += blockDim.x) {
     const int m = e % BM, n = e / BM;
     if (m0 + m >= pd.M || n0 + n >= pd.N) continue;
     double sum = 0.0;
@@ -224,7 +227,8 @@ nd_status nd_launch_gemm_f64(nd_handle h, const PairDesc* d_pairs, const WorkIte
   nd_status s = nd_cuda_check(h, cudaGetLastError(), "gemm_f64_grouped");
   if (s || nred == 0) return s;
   nd_prof_begin(h, "splitk_reduce");
-  splitk_reduce<<<nred, 256, 0, h->stream>>>(d_pairs, d_red, ws, ptrs, alpha, beta, g.amode, g.bmode);
+  const int parts = std::max(1, std::min(16, (2 * h->num_sms + nred - 1) / nred));
+  splitk_reduce<<<dim3(nred, parts), 256, 0, h->stream>>>(d_pairs, d_red, ws, ptrs, alpha, beta, g.amode, g.bmode);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "splitk_reduce");

@@ -873,7 +873,9 @@ __global__ void __launch_bounds__(256) split_reduce(const PairDesc* pairs, const
     }
     __syncthreads();
     double* Rb = job_R(ptrs, pd.job) + pd.r_off;
-    for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
+    const int per = (BM * BN + (int)gridDim.y - 1) / (int)gridDim.y;   // gridDim.y CTAs share a tile
+    const int e1 = min(BM * BN, ((int)blockIdx.y + 1) * per);
+    for (int e = (int)blockIdx.y * per + threadIdx.x; e < e1; e += blockDim.x) {
       const int row = e / BN, col = e - row * BN;
       const int gm = ri.mt * BM + row, gn = ri.nt * BN + col;
       if (gm >= pd.M || gn >= pd.N) continue;
@@ -1635,7 +1637,8 @@ nd_status nd_split_run(nd_handle h, ExecCache& c, const JobPtrs& ptrs, double al
     }
     if (s || c.nred == 0) return s;
     nd_prof_begin(h, "split_reduce");
-    split_reduce<<<std::min(c.nred, 4 * h->num_sms), 256, 0, h->stream>>>(
+    const int parts = std::max(1, std::min(16, (2 * h->num_sms + c.nred - 1) / c.nred));
+    split_reduce<<<dim3(std::min(c.nred, 4 * h->num_sms), parts), 256, 0, h->stream>>>(
         c.d_split_pairs, c.d_red, c.nred, (const SplitOp*)c.d_operands, c.d_exp, (const long long*)c.d_ws, ptrs, alpha,
         beta, alpha == 1.0 ? 0 : 1, beta == 0.0 ? 0 : 1);
     nd_prof_end(h);
