@@ -443,6 +443,10 @@ __global__ void block_copy(const BlockCopyDev* list, int n, const double* src, d
   }
 }
 
+// Per-block kernels index their block by blockIdx.y (at most 65535): a factorisation
+// call takes at most that many blocks (a QN block matrix has one per charge sector).
+constexpr int kMaxBlocksPerCall = 65535;
+
 // ---- blocked Householder QR ----------------------------------------------
 // Panels of QR_NB columns: one CTA per block computes the panel's reflectors (LAPACK
 // dlarfg convention, as geqrf) and its compact WY factor T, Q_p = H_1 ... H_w =
@@ -1646,6 +1650,7 @@ extern "C" nd_status nd_bs_svd_f64(nd_handle h, int32_t nb, const int64_t* rows,
   if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd returns kept dimensions to the host and cannot be captured");
   if (nb < 0 || (nb > 0 && (!rows || !cols || !offsets || !A || !U || !S || !V || !kept)))
     return nd_fail(h, ND_ERR_ARG, "svd: NULL argument");
+  if (nb > kMaxBlocksPerCall) return nd_fail(h, ND_ERR_UNSUPPORTED, "svd: at most %d blocks per call", kMaxBlocksPerCall);
   if (nb == 0) { if (spectrum_len) *spectrum_len = 0; if (truncerr) *truncerr = 0; if (docut) *docut = 0; return ND_OK; }
   cudaStream_t s = h->stream;
   std::vector<SvdBlock> blocks;
@@ -1734,6 +1739,7 @@ extern "C" nd_status nd_bs_eigen_f64(nd_handle h, int32_t nb, const int64_t* dim
   if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "eigen returns kept dimensions to the host and cannot be captured");
   if (nb < 0 || (nb > 0 && (!dims || !offsets || !A || !D || !V || !kept)))
     return nd_fail(h, ND_ERR_ARG, "eigen: NULL argument");
+  if (nb > kMaxBlocksPerCall) return nd_fail(h, ND_ERR_UNSUPPORTED, "eigen: at most %d blocks per call", kMaxBlocksPerCall);
   if (nb == 0) { if (spectrum_len) *spectrum_len = 0; if (truncerr) *truncerr = 0; if (docut) *docut = 0; return ND_OK; }
   cudaStream_t s = h->stream;
   int64_t span = 0;
@@ -2103,6 +2109,7 @@ extern "C" nd_status nd_bs_svd_plan_create(nd_handle h, int32_t nb, const int64_
   *out = nullptr;
   if (nd_capturing(h)) return nd_fail(h, ND_ERR_ARG, "svd plan: create it before graph capture");
   if (nb <= 0 || !rows || !cols) return nd_fail(h, ND_ERR_ARG, "svd plan: need at least one block");
+  if (nb > kMaxBlocksPerCall) return nd_fail(h, ND_ERR_UNSUPPORTED, "svd plan: at most %d blocks per call", kMaxBlocksPerCall);
   cudaStream_t s = h->stream;
   auto p = new nd_svd_plan_s;
   p->h = h;
@@ -2303,6 +2310,7 @@ extern "C" nd_status nd_bs_qr_f64(nd_handle h, int32_t nb, const int64_t* rows, 
                                   const int64_t* offsets, const double* A, double* Q, double* Rf, int32_t positive) {
   if (!h) return ND_ERR_ARG;
   if (nb < 0 || (nb > 0 && (!rows || !cols || !offsets || !A || !Q || !Rf))) return nd_fail(h, ND_ERR_ARG, "qr: NULL argument");
+  if (nb > kMaxBlocksPerCall) return nd_fail(h, ND_ERR_UNSUPPORTED, "qr: at most %d blocks per call", kMaxBlocksPerCall);
   if (nb == 0) return ND_OK;
   cudaStream_t s = h->stream;
   std::vector<QrBlock> blocks(nb);
