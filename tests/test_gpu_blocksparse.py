@@ -217,3 +217,28 @@ def test_bs_permutedims_matches_oracle(nd, rank, seed):
     assert R.offsets == list(ref.offsets)
     assert [tuple(i) for i in R.inds] == [tuple(i) for i in ref.inds]
     np.testing.assert_array_equal(R.data_numpy(), ref.data)
+
+
+def test_ozaki_split_k_bit_identical(nd):
+    """The split GEMM cuts a long-K tile into K ranges only when the launch's other work is
+    small: a 10 x 12 output with K = 30000 is split when contracted alone and not when it
+    shares the launch with a 4000^3 block pair.  The ranges start on 512-K chunk
+    boundaries and their exact int64 partials are summed before the one conversion, so
+    both results must be equal bit for bit (and within 1e-10 of FP64)."""
+    rng = np.random.default_rng(77)
+    a1, b1 = rng.standard_normal((10, 30000)), rng.standard_normal((30000, 12))
+    a2, b2 = rng.standard_normal((4000, 4000)), rng.standard_normal((4000, 4000))
+    A = obs.BlockSparseTensor([(10, 4000), (30000, 4000)], [(1, 1), (2, 2)], [0, a1.size],
+                              np.concatenate([a1.reshape(-1, order="F"), a2.reshape(-1, order="F")]))
+    B = obs.BlockSparseTensor([(30000, 4000), (12, 4000)], [(1, 1), (2, 2)], [0, b1.size],
+                              np.concatenate([b1.reshape(-1, order="F"), b2.reshape(-1, order="F")]))
+    R = nd.contract(nd.BlockSparseTensor.from_oracle(A), (1, -1), nd.BlockSparseTensor.from_oracle(B), (-1, 2),
+                    precision="ozaki")
+    i = list(R.blocks).index((1, 1))
+    shared = R.data_numpy()[R.offsets[i]:R.offsets[i] + 120]
+    alone = nd.DenseTensor.empty((10, 12))
+    nd.contract_(alone, (1, 2), nd.DenseTensor.from_numpy(a1), (1, -1), nd.DenseTensor.from_numpy(b1), (-1, 2),
+                 1.0, 0.0, "ozaki")
+    alone = alone.to_numpy().reshape(-1, order="F")
+    np.testing.assert_array_equal(shared, alone)
+    assert odense.rel_frobenius_error(alone, (a1 @ b1).reshape(-1, order="F")) <= 1e-10
