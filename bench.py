@@ -1104,6 +1104,32 @@ def cfg_sweep_ops(args):
     nd.contract(U, (1, -1), D, (-1, 2))
     out["diag_contract_US"] = gbs(16 * U.nnz, lambda: nd.contract(U, (1, -1), D, (-1, 2)))
     out["uncombine_U"] = gbs(16 * U.nnz, lambda: nd.uncombine(U, 0, qinds[:2], rinfo))
+    # block-sparse permutedims of psi (l, s1, s2, r) -> (r, s2, s1, l) and the combining
+    # contraction of (l, s1) into one index, against the oracle's host versions
+    psi = G["psi"]
+    out["bs_permutedims_psi"] = gbs(16 * psi.nnz, lambda: nd.permutedims_blocksparse(psi, (4, 3, 2, 1)))
+    cmb = nd.CombinerTensor(qinds[:2])
+    out["combine_psi"] = gbs(16 * psi.nnz, lambda: nd.contract(psi, (1, 2, 3, 4), cmb, (9, 1, 2)))
+    hpsi = obs.BlockSparseTensor([tuple(i) for i in net["psi"].inds], [tuple(b) for b in net["psi"].blocks],
+                                 list(net["psi"].offsets), net["psi"].data)
+    t0 = time.perf_counter()
+    obs.permutedims(hpsi, (4, 3, 2, 1))
+    out["bs_permutedims_psi"]["cpu_oracle_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+    # HDF5 BlockSparse storage of psi (host-side file I/O, the device data crossing once)
+    import tempfile, os
+    with tempfile.TemporaryDirectory() as td:
+        f = os.path.join(td, "psi.h5")
+        t0 = time.perf_counter()
+        nd.save_blocksparse(f, "psi", psi)
+        t_save = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        back = nd.load_blocksparse(f, "psi", psi.inds)
+        torch.cuda.synchronize()
+        t_load = time.perf_counter() - t0
+        same = bool(torch.equal(back.data, psi.data))
+    out["hdf5_psi"] = {"bytes": 8 * psi.nnz, "save_ms": round(t_save * 1e3, 1), "load_ms": round(t_load * 1e3, 1),
+                       "save_MB/s": round(8 * psi.nnz / t_save / 1e6, 1),
+                       "load_MB/s": round(8 * psi.nnz / t_load / 1e6, 1), "round_trip_bit_exact": same}
     # blockwise qr of the same 19 blocks (Householder, FP64): algorithmic flops 2 m n^2 - 2 n^3 / 3
     # per m x n block (n <= m) for R, the same again to form the thin Q
     from oracle import linalg as olin

@@ -1044,11 +1044,33 @@ extern "C" nd_status nd_bs_permutedims_f64(nd_handle h, const nd_bs_desc* T, con
     seen[v] = true;
     p0[k] = v;
   }
+  // Blocks of 2^22 elements or more go through the tiled transposer, one launch each; all
+  // smaller blocks are permuted by one batched gather launch (per block: source strides
+  // column-major, destination strides those of the permuted block), since a QN tensor
+  // holds hundreds of small blocks and one launch per block would be launch-bound.
+  constexpr int64_t kTiledBlock = int64_t(1) << 22;
+  std::vector<nd_block_copy> small;
   for (int b = 0; b < d.nnzblocks; ++b) {
     int64_t dims[ND_MAX_RANK];
-    for (int k = 0; k < d.rank; ++k) dims[k] = d.bdim(b, k);
-    s = nd_launch_permute(h, Rdata + offsetsR[b], Tdata + d.offsets[b], d.rank, dims, p0, 1.0, 0.0, nullptr);
-    if (s) return s;
+    int64_t n = 1;
+    for (int k = 0; k < d.rank; ++k) { dims[k] = d.bdim(b, k); n *= dims[k]; }
+    if (n == 0) continue;
+    if (n >= kTiledBlock) {
+      s = nd_launch_permute(h, Rdata + offsetsR[b], Tdata + d.offsets[b], d.rank, dims, p0, 1.0, 0.0, nullptr);
+      if (s) return s;
+      continue;
+    }
+    nd_block_copy c{};
+    c.src_off = d.offsets[b];
+    c.dst_off = offsetsR[b];
+    c.rank = d.rank;
+    int64_t st = 1;
+    for (int k = 0; k < d.rank; ++k) { c.dims[k] = dims[k]; c.src_strides[k] = st; st *= dims[k]; }
+    st = 1;
+    for (int j = 0; j < d.rank; ++j) { c.dst_strides[p0[j]] = st; st *= dims[p0[j]]; }   // R dim j is T dim p0[j]
+    small.push_back(c);
   }
-  return ND_OK;
+  if (small.empty()) return ND_OK;
+  if (small.size() > (size_t)INT32_MAX) return nd_fail(h, ND_ERR_ARG, "bs_permutedims: too many blocks");
+  return nd_block_copy_f64(h, (int32_t)small.size(), small.data(), Tdata, Rdata);
 }

@@ -242,3 +242,17 @@ def test_ozaki_split_k_bit_identical(nd):
     alone = alone.to_numpy().reshape(-1, order="F")
     np.testing.assert_array_equal(shared, alone)
     assert odense.rel_frobenius_error(alone, (a1 @ b1).reshape(-1, order="F")) <= 1e-10
+
+
+def test_blocksparse_permutedims_large_and_small_blocks(nd):
+    """Blocks of 2^22 elements or more take the tiled transposer, smaller ones the batched
+    gather: a tensor with one large block (2048 x 2100) among small ones, permuted, is
+    bit-exact with the oracle (structure and data)."""
+    rng = np.random.default_rng(404)
+    inds = [(2048, 3, 5), (2100, 4, 6)]
+    blocks = [(1, 1), (2, 2), (3, 3), (2, 3), (3, 1)]
+    T = obs.random_blocksparse(rng, inds, blocks)
+    ref = obs.permutedims(T, (2, 1))
+    R = nd.permutedims_blocksparse(nd.BlockSparseTensor.from_oracle(T), (2, 1))
+    assert R.blocks == [tuple(b) for b in ref.blocks] and R.offsets == list(ref.offsets)
+    np.testing.assert_array_equal(R.data_numpy(), ref.data)
