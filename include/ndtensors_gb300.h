@@ -237,7 +237,9 @@ nd_status nd_bs_contract_adjoint_f64(nd_handle h, nd_plan plan, const double *Rb
 
 /* Block-sparse permutedims: every block permuted; output block order = input
  * order, offsets recomputed by the caller's layout (offsetsR, host).
- * (NDTensors/src/blocksparse/blocksparsetensor.jl:834-881, blockoffsets.jl:103-111) */
+ * (NDTensors/src/blocksparse/blocksparsetensor.jl:834-881, blockoffsets.jl:103-111)
+ * Blocks of 2^22 elements or more run through the tiled transposer one by one; all
+ * smaller blocks in one batched launch.  Bit-exact; stream-ordered. */
 nd_status nd_bs_permutedims_f64(nd_handle h, const nd_bs_desc *T, const double *Tdata,
                                 const int32_t *perm, const int64_t *offsetsR, double *Rdata);
 
