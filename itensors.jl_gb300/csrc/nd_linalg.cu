@@ -427,20 +427,44 @@ __global__ void kept_dims(const SvdBlock* blocks, int nb, const double* sig, con
 // ---- block copy (combiner gather / uncombine scatter) ----------------------
 struct BlockCopyDev {
   int64_t src_off, dst_off, count;
+  int64_t start;      // first index of this copy in the flat element space of the list
   Mixed idx;          // st0: source strides, st1: destination strides
 };
 
-__global__ void block_copy(const BlockCopyDev* list, int n, const double* src, double* dst) {
-  for (int r = blockIdx.y; r < n; r += gridDim.y) {
-    const BlockCopyDev& c = list[r];
-    const bool small = c.count < (1ll << 31);   // multiply-high division of 32-bit indices
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < c.count; e += (int64_t)gridDim.x * blockDim.x) {
-      int64_t so, d;
-      if (small) mixed_offsets32(c.idx, (uint32_t)e, so, d);
-      else mixed_offsets(c.idx, e, so, d);
-      dst[c.dst_off + d] = src[c.src_off + so];
-    }
+// All copies of a list as one flat element space (copy r covers [start_r, start_r +
+// count_r)).  CTA b takes the contiguous range [b chunk, (b + 1) chunk), so a list of
+// many small copies and a few large ones keeps every CTA busy; a thread finds its copy
+// by binary search once and then walks forward.  Destination elements of a copy are
+// consecutive in its column-major index, so writes coalesce wherever the destination is
+// contiguous along the copy's first dimension.
+__global__ void __launch_bounds__(256) block_copy(const BlockCopyDev* list, int n, int64_t total, int64_t chunk,
+                                                  const double* src, double* dst) {
+  const int64_t t0 = (int64_t)blockIdx.x * chunk, t1 = min(total, t0 + chunk);
+  int64_t t = t0 + threadIdx.x;
+  if (t >= t1) return;
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (list[mid].start <= t) lo = mid;
+    else hi = mid - 1;
   }
+  int r = lo;
+  for (; t < t1; t += blockDim.x) {
+    while (r + 1 < n && list[r + 1].start <= t) ++r;
+    const BlockCopyDev& c = list[r];
+    const int64_t e = t - c.start;
+    int64_t so, d;
+    if (c.count < (1ll << 31)) mixed_offsets32(c.idx, (uint32_t)e, so, d);
+    else mixed_offsets(c.idx, e, so, d);
+    dst[c.dst_off + d] = src[c.src_off + so];
+  }
+}
+
+// grid and chunk of a flat copy launch: about 2048 elements per CTA, at most 64 CTAs per SM
+static void block_copy_grid(nd_handle h, int64_t total, int& grid, int64_t& chunk) {
+  const int64_t g = std::max<int64_t>(1, std::min<int64_t>((total + 2047) / 2048, 64ll * h->num_sms));
+  chunk = ((total + g - 1) / g + 255) / 256 * 256;
+  grid = (int)((total + chunk - 1) / chunk);
 }
 
 // Per-block kernels index their block by blockIdx.y (at most 65535): a factorisation
@@ -2409,7 +2433,8 @@ extern "C" nd_status nd_bs_qr_f64(nd_handle h, int32_t nb, const int64_t* rows, 
   return fail_free(st);
 }
 
-// host list -> device form (mixed-radix index per copy); maxc: the largest count
+// host list -> device form (mixed-radix index per copy); maxc: the total element count
+// (each copy's start in the flat element space is the count of the copies before it)
 static nd_status prepare_copies(nd_handle h, int32_t n, const nd_block_copy* list, std::vector<BlockCopyDev>& dl,
                                 int64_t& maxc) {
   dl.assign(n, BlockCopyDev{});
@@ -2428,7 +2453,8 @@ static nd_status prepare_copies(nd_handle h, int32_t n, const nd_block_copy* lis
       d.count *= c.dims[k];
     }
     mixed_simplify(d.idx);
-    maxc = std::max(maxc, d.count);
+    d.start = maxc;                                    // maxc accumulates the flat total
+    maxc += d.count;
   }
   return ND_OK;
 }
@@ -2465,9 +2491,11 @@ extern "C" nd_status nd_block_copy_plan_run(nd_copy_plan p, const double* src, d
   nd_handle h = p->h;
   if (p->n == 0 || p->maxc == 0) return ND_OK;
   if (!src || !dst) return nd_fail(h, ND_ERR_ARG, "block_copy_plan: NULL argument");
-  dim3 grid((unsigned)std::min<int64_t>((p->maxc + 255) / 256, 512), (unsigned)std::min(p->n, 65535));
+  int grid;
+  int64_t chunk;
+  block_copy_grid(h, p->maxc, grid, chunk);
   nd_prof_begin(h, "block_copy");
-  block_copy<<<grid, 256, 0, h->stream>>>(p->list, p->n, src, dst);
+  block_copy<<<grid, 256, 0, h->stream>>>(p->list, p->n, p->maxc, chunk, src, dst);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   return nd_cuda_check(h, cudaGetLastError(), "block_copy");
@@ -2493,9 +2521,11 @@ extern "C" nd_status nd_block_copy_f64(nd_handle h, int32_t n, const nd_block_co
   BlockCopyDev* dd = nullptr;
   ND_CUDA(h, cudaMallocAsync(&dd, n * sizeof(BlockCopyDev), s));
   ND_CUDA(h, cudaMemcpyAsync(dd, dl.data(), n * sizeof(BlockCopyDev), cudaMemcpyHostToDevice, s));
-  dim3 grid((unsigned)std::min<int64_t>((maxc + 255) / 256, 512), (unsigned)std::min(n, 65535));
+  int grid;
+  int64_t chunk;
+  block_copy_grid(h, maxc, grid, chunk);
   nd_prof_begin(h, "block_copy");
-  block_copy<<<grid, 256, 0, s>>>(dd, n, src, dst);
+  block_copy<<<grid, 256, 0, s>>>(dd, n, maxc, chunk, src, dst);
   nd_prof_end(h);
   ND_LAUNCHED(h);
   cudaFreeAsync(dd, s);
